@@ -1,0 +1,415 @@
+#!/usr/bin/env python3
+"""Benchmark of the TAA resolve on the 4K workload (C2: 3840x2160, 64 frames).
+
+A step is one pass of the resolve over the whole 64-frame sequence (64
+launches with ping-pong history).  `value` is Mpx/s with every input already
+resident in HBM; `e2e` is the same metric through the C ABI with host
+buffers: each frame's colour, depth and motion go host->device from pinned
+memory and its screen result comes back device->host inside the timed region.
+Every frame's inputs (500 MB at 4K) are larger than the 129 MB L2, so no L2
+flush is needed between launches.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  Multi-GPU runs are independent replicas: the
+sequence has a frame-to-frame dependence and does not shard.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+for p in (ROOT / "taa-star_gb300", ROOT / "oracle"):
+    sys.path.insert(0, str(p))
+
+METRIC = "4K TAA resolve Mpx/s & HBM GB/s, plain vs FP16/batched on 1 GB300 @ PSNR≥50dB"
+UNIT = "Mpx/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--frames", type=int, default=64)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-forms", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic(form_name: str):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None, None
+    d = json.loads(p.read_text())
+    e = d.get(form_name)
+    if not e:
+        return None, None
+    return e.get("bytes_per_launch_at_4k"), e.get("source")
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                vals = [v.strip() for v in out.stdout.strip().split(",")]
+                if len(vals) == 7:
+                    self.samples.append(vals)
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        import statistics
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+# ------------------------------------------------------------------ reference arm
+def cpu_frames_for_reference(wl, n):
+    """Inputs of the first n+1 frames, rendered on the host by the FP64 scene evaluator."""
+    import numpy as np
+    import oracle as O
+    import taa_abi as T
+    sc = wl.scene()
+    sph = T.synth_spheres(sc)
+    out = []
+    for f in range(n + 1):
+        r = O.synth_frame(sc, sph, f)
+        out.append(dict(color=r["color"].astype(np.float16).astype(np.float32), depth=r["depth"].astype(np.float32),
+                        motion=r["motion"][..., :2].astype(np.float16).astype(np.float32),
+                        jitter=T.synth_jitter(sc, f)[1]))
+    return out
+
+
+def time_oracle(wl, frames, nthreads, budget_s, min_frames=1):
+    """Oracle FP32 resolve over consecutive frames until the time budget is spent."""
+    import numpy as np
+    import oracle as O
+    import taa_abi as T
+    hist = frames[0]["color"].copy()
+    done, t_total = 0, 0.0
+    i = 1
+    while done < min_frames or t_total < budget_s:
+        f = frames[1 + (i - 1) % (len(frames) - 1)]
+        prev = frames[(i - 1) % (len(frames) - 1)]
+        u = T.make_uniforms(wl.parameters(), jitter_ndc=f["jitter"])
+        t0 = time.perf_counter()
+        r = O.resolve(u, f["color"], f["depth"], f["motion"], history=hist, history_depth=prev["depth"],
+                      nthreads=nthreads)
+        t_total += time.perf_counter() - t0
+        hist = r["history"].astype(np.float32)
+        done += 1
+        i += 1
+        if done >= 10000:
+            break
+    return done, t_total
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import workloads as WL
+    wl = WL.c2()
+    n = os.cpu_count() or 1
+    frames = cpu_frames_for_reference(wl, 2)
+    # warm-up frames, then `steps` timed frames (one 4K frame per step)
+    time_oracle(wl, frames, n, 0.0, min_frames=max(1, args.warmup))
+    done, t = time_oracle(wl, frames, n, 0.0, min_frames=args.steps)
+    mpx = wl.pixels * done / t / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": mpx, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t / done * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded analytic scene, rendered on the host)",
+        "config": {"workload": wl.name, "width": wl.width, "height": wl.height, "frames_per_step": 1,
+                   "mode": "Catmull-Rom, YCoCg variance clip gamma 1, clip-fast, alpha 0.1, depth culling, reject outside"},
+        "cpu_baseline": {"value": mpx, "unit": UNIT, "cores": n, "kind": "port",
+                         "sample": f"{done} consecutive 3840x2160 frames of the C2 scene, FP32 oracle restatement of taa.comp, {n} threads"},
+        "e2e": {"value": mpx, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ our arm
+def run_ours(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    if rank == 0 or world == 1:
+        from importlib import util
+        spec = util.spec_from_file_location("taa_lib_build", ROOT / "taa-star_gb300" / "build.py")
+        m = util.module_from_spec(spec)
+        spec.loader.exec_module(m)
+        m.build_library()
+    if world > 1:
+        dist.barrier()
+
+    import taa_abi as T
+    import workloads as WL
+
+    wl = WL.c2()
+    F = args.frames
+    H, W = wl.height, wl.width
+    sc = wl.scene()
+    stream = torch.cuda.current_stream(dev)
+    sid = stream.cuda_stream
+
+    # inputs of the whole sequence, resident in HBM
+    col = torch.empty(F, H, W, 4, dtype=torch.float16, device=dev)
+    dep = torch.empty(F, H, W, dtype=torch.float32, device=dev)
+    mot = torch.empty(F, H, W, 2, dtype=torch.float16, device=dev)
+    for f in range(F):
+        T.synth_render(sc, f, stream=sid, color=col[f], depth=dep[f], motion=mot[f])
+    uniforms = []
+    for f in range(F):
+        uniforms.append(T.make_uniforms(wl.parameters(), jitter_ndc=T.synth_jitter(sc, f)[1],
+                                        mResetHistory=1 if f == 0 else 0))
+    hist = [torch.zeros(H, W, 4, dtype=torch.float32, device=dev) for _ in range(2)]
+    res = torch.empty(H, W, 4, dtype=torch.float16, device=dev)
+    torch.cuda.synchronize()
+
+    def make_ctx(form):
+        c = T.Taa(W, H, form=form)
+        c.set_uniforms(uniforms[1])
+        return c
+
+    def sequence(ctx):
+        for f in range(F):
+            ctx.set_uniforms(uniforms[f])
+            ctx.resolve(stream=sid, color=col[f], depth=dep[f], velocity=mot[f], history=hist[f & 1],
+                        history_depth=dep[f - 1] if f else dep[0], history_out=hist[(f + 1) & 1], result=res)
+
+    def timed(ctx, steps, warmup, sampler=None):
+        for _ in range(warmup):
+            sequence(ctx)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        if sampler:
+            sampler.__enter__()
+        e0.record(stream)
+        for _ in range(steps):
+            sequence(ctx)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if sampler:
+            sampler.__exit__(None, None, None)
+        ms = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+            dist.barrier()
+        return ms
+
+    bpp = wl.bytes_per_pixel(history_bytes=16, motion_bytes=4)
+    launch_bytes = bpp * W * H
+    peak, peak_kind = load_peaks()
+
+    ctx = make_ctx(T.TAA_FORM_AUTO)
+    form_used = ctx.selected_form()
+    form_name = {1: "plain", 2: "tiled", 3: "fp16"}[form_used]
+    sampler = ClockSampler(local)
+    ms = timed(ctx, args.steps, args.warmup, sampler)
+    launches = args.steps * F
+    mpx = world * W * H * F * args.steps / (ms / 1e3) / 1e6
+    avg_launch_s = ms / 1e3 / launches
+    achieved = launch_bytes / avg_launch_s / 1e9
+    traffic, traffic_src = load_traffic(form_name)
+
+    forms = {form_name: {"mpx_s": mpx, "gb_s": achieved, "frac_of_hbm": achieved / peak}}
+    if not args.no_forms:
+        for fid, name in ((T.TAA_FORM_PLAIN, "plain"),):
+            c2 = make_ctx(fid)
+            k = max(2, args.steps // 4)
+            m2 = timed(c2, k, 1)
+            v = world * W * H * F * k / (m2 / 1e3) / 1e6
+            g = launch_bytes / (m2 / 1e3 / (k * F)) / 1e9
+            forms[name] = {"mpx_s": v, "gb_s": g, "frac_of_hbm": g / peak}
+            c2.close()
+
+    # end to end through the C ABI with host buffers (pinned), copies inside the timed region
+    e2e = None
+    if not args.no_e2e:
+        nbuf = 3
+        h_col = col.cpu().pin_memory()
+        h_dep = dep.cpu().pin_memory()
+        h_mot = mot.cpu().pin_memory()
+        h_out = torch.empty(F, H, W, 4, dtype=torch.float16).pin_memory()
+        d_col = [torch.empty(H, W, 4, dtype=torch.float16, device=dev) for _ in range(nbuf)]
+        d_dep = [torch.empty(H, W, dtype=torch.float32, device=dev) for _ in range(nbuf)]
+        d_mot = [torch.empty(H, W, 2, dtype=torch.float16, device=dev) for _ in range(nbuf)]
+        d_res = [torch.empty(H, W, 4, dtype=torch.float16, device=dev) for _ in range(nbuf)]
+        s_in = torch.cuda.Stream(dev)
+        s_out = torch.cuda.Stream(dev)
+        ectx = make_ctx(T.TAA_FORM_AUTO)
+        in_ready = [torch.cuda.Event() for _ in range(nbuf)]
+        done_ev = [torch.cuda.Event() for _ in range(nbuf)]
+        out_done = [torch.cuda.Event() for _ in range(nbuf)]
+
+        def e2e_sequence():
+            for f in range(F):
+                b = f % nbuf
+                with torch.cuda.stream(s_in):
+                    # slot b last held frame f-3: its result must have left the device and the
+                    # resolve of frame f-2 (which read its depth as history depth) must be done
+                    s_in.wait_event(out_done[b])
+                    s_in.wait_event(done_ev[(f - 2) % nbuf])
+                    d_col[b].copy_(h_col[f], non_blocking=True)
+                    d_dep[b].copy_(h_dep[f], non_blocking=True)
+                    d_mot[b].copy_(h_mot[f], non_blocking=True)
+                    in_ready[b].record(s_in)
+                stream.wait_event(in_ready[b])
+                ectx.set_uniforms(uniforms[f])
+                pb = (f - 1) % nbuf
+                ectx.resolve(stream=sid, color=d_col[b], depth=d_dep[b], velocity=d_mot[b], history=hist[f & 1],
+                             history_depth=d_dep[pb] if f else d_dep[b], history_out=hist[(f + 1) & 1],
+                             result=d_res[b])
+                done_ev[b].record(stream)
+                with torch.cuda.stream(s_out):
+                    s_out.wait_event(done_ev[b])
+                    h_out[f].copy_(d_res[b], non_blocking=True)
+                    out_done[b].record(s_out)
+
+        for ev in out_done:
+            ev.record(s_out)
+        e2e_sequence()
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        k = max(2, args.steps // 2)
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(s_in)
+        s_in.wait_stream(stream)
+        for _ in range(k):
+            e2e_sequence()
+        stream.wait_stream(s_out)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        ms_e = t0.elapsed_time(t1)
+        if world > 1:
+            t = torch.tensor([ms_e], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms_e = float(t.item())
+        e2e = {"value": world * W * H * F * k / (ms_e / 1e3) / 1e6, "unit": UNIT,
+               "h2d_bytes_per_step": F * H * W * (8 + 4 + 4), "d2h_bytes_per_step": F * H * W * 8,
+               "note": "pinned host buffers, 3-slot copy/compute/copy pipeline on three streams"}
+        ectx.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        import oracle as O  # the checker; timed here as the CPU baseline only
+        O.load()
+        nthr = os.cpu_count() or 1
+        frames = []
+        for f in range(3):
+            frames.append(dict(color=col[f].float().cpu().numpy(), depth=dep[f].cpu().numpy(),
+                               motion=mot[f].float().cpu().numpy(), jitter=T.synth_jitter(sc, f)[1]))
+        done, t = time_oracle(wl, frames, nthr, args.cpu_seconds)
+        cpu = {"value": wl.pixels * done / t / 1e6, "unit": UNIT, "cores": nthr, "kind": "port",
+               "sample": f"{done} consecutive 3840x2160 frames of the C2 workload through the FP32 oracle "
+                         f"restatement of taa.comp ({t:.1f} s, {nthr} threads)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": mpx, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded analytic scene rendered on the GPU)",
+            "config": {"workload": wl.name, "width": W, "height": H, "frames_per_step": F, "form": form_name,
+                       "history": "RGBA32F", "motion": "RG16F", "bytes_per_px": bpp,
+                       "l2": "no flush: each frame's inputs (500 MB) exceed the 129 MB L2",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "note": f"peak = hbm_gbs of {peak_kind}; achieved = {bpp} B/px x {W}x{H} / avg launch; "
+                                 f"traffic per launch from {traffic_src}"},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": sampler.summary(),
+            "forms": forms,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,185 @@
+/*
+ * taa_gb300.h - C ABI of the GB300-native TAA resolve.
+ *
+ * This library replaces one dispatch of the reference renderer: the compute
+ * pass that source/taa.hpp:1008-1027 records for shaders/taa.comp, plus the
+ * optional sharpen pass that follows it in the same command buffer
+ * (source/taa.hpp:1111-1139, shaders/sharpen.comp and shaders/sharpen_cas.comp),
+ * which this library fuses into the resolve.  Everything else in the
+ * reference (scene rendering, ray tracing, post-process overlay, GUI) stays
+ * outside.
+ *
+ * Conventions
+ *  - All images are headless pitched linear device buffers (no Vulkan images,
+ *    no samplers).  `pitch` is the row stride in bytes.  Every pointer and
+ *    pitch must be a multiple of its texel size, otherwise TAA_E_ALIGN.
+ *  - Texel formats follow the reference (shaders/shader_cpu_common.h:61-76):
+ *    colour RGBA16F, depth D32F, result/debug RGBA16F, segmask R32UI.
+ *    Velocity is RGBA16F in the reference layout (.xy UV-space motion,
+ *    .z depth delta, .w mover id) or RG16F (.xy only; .z and .w read as 0).
+ *    History is RGBA32F (default; an FP32 accumulator) or RGBA16F (reference).
+ *  - Calls are asynchronous on the given CUDA stream (a cudaStream_t passed
+ *    as void*; NULL is the legacy default stream).  No call allocates device
+ *    memory after taa_create and none synchronises the host, so a sequence of
+ *    taa_resolve calls can be captured into a CUDA graph.
+ *  - Return value 0 (TAA_OK) on success, a negative taa_status otherwise; the
+ *    message of the last failure on the calling thread is in taa_last_error().
+ *    The reference has no error path (it asserts, source/taa.hpp:153,237,903).
+ *  - One context per stream; different contexts may be used concurrently.
+ */
+#ifndef TAA_GB300_H
+#define TAA_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+#include "taa_params.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TAA_GB300_ABI_VERSION 1
+
+typedef enum taa_status {
+    TAA_OK            = 0,
+    TAA_E_INVAL       = -1,  /* bad argument: null, size, enum out of range, aliasing */
+    TAA_E_ALIGN       = -2,  /* pointer or pitch not a multiple of the texel size */
+    TAA_E_CUDA        = -3,  /* a CUDA runtime call failed (message in taa_last_error) */
+    TAA_E_TIMEOUT     = -4,  /* a bounded device-side wait gave up */
+    TAA_E_UNSUPPORTED = -5,  /* valid request this build does not implement */
+    TAA_E_NOMEM       = -6   /* allocation failure in taa_create */
+} taa_status;
+
+/* History texel format. */
+#define TAA_HISTORY_RGBA32F 0u
+#define TAA_HISTORY_RGBA16F 1u
+/* Velocity texel format. */
+#define TAA_MOTION_RGBA16F  0u
+#define TAA_MOTION_RG16F    1u
+/* Kernel form. */
+#define TAA_FORM_AUTO   0u  /* fastest form whose precision contract holds for the parameters */
+#define TAA_FORM_PLAIN  1u  /* one thread per pixel, FP32, every parameter honoured */
+#define TAA_FORM_TILED  2u  /* FP32, CTA tile staged in shared memory */
+#define TAA_FORM_FP16   3u  /* packed half2 neighbourhood, clip and sharpen; FP32 history and blend */
+/* Sharpener (taa<CF>::mSharpener, source/taa.hpp:1418). */
+#define TAA_SHARPEN_OFF     0u
+#define TAA_SHARPEN_SIMPLE  1u  /* shaders/sharpen.comp */
+#define TAA_SHARPEN_CAS     2u  /* shaders/sharpen_cas.comp, FidelityFX CAS sharpen-only */
+
+typedef struct taa_ctx taa_ctx;
+
+/* Context description: the image sizes and formats that
+ * taa<CF>::set_source_image_views (source/taa.hpp:263-360) derives from the
+ * views it is given. */
+typedef struct taa_desc_t {
+    uint32_t struct_size;     /* sizeof(taa_desc_t) */
+    int32_t  in_width;        /* source size: colour, depth, velocity, history depth */
+    int32_t  in_height;
+    int32_t  out_width;       /* target size: history, result, debug, segmask */
+    int32_t  out_height;
+    uint32_t history_format;  /* TAA_HISTORY_* */
+    uint32_t motion_format;   /* TAA_MOTION_* */
+    uint32_t form;            /* TAA_FORM_* */
+    uint32_t sharpener;       /* TAA_SHARPEN_* */
+    float    sharpen_factor;  /* mSharpenFactor, default 0.5 (source/taa.hpp:1419) */
+    uint32_t flags;           /* reserved, 0 */
+} taa_desc_t;
+
+/* Per-frame bindings; one field pair per descriptor binding of set 0 in
+ * shaders/taa.comp:24-38 (bound at source/taa.hpp:1009-1025).  Optional
+ * outputs may be NULL; a NULL history reads as zeros (first frame). */
+typedef struct taa_frame_io_t {
+    const void* color;         size_t color_pitch;          /* binding  1 uCurrentFrame    */
+    const void* depth;         size_t depth_pitch;          /* binding  2 uCurrentDepth    */
+    const void* history;       size_t history_pitch;        /* binding  3 uHistoryFrame    */
+    const void* history_depth; size_t history_depth_pitch;  /* binding  4 uHistoryDepth    (depth culling) */
+    void*       result;        size_t result_pitch;         /* binding  5 uResultScreen    (optional) */
+    void*       debug;         size_t debug_pitch;          /* binding  6 uDebug           (optional) */
+    const void* velocity;      size_t velocity_pitch;       /* binding  7 uCurrentVelocity */
+    void*       history_out;   size_t history_out_pitch;    /* binding  8 uResultHistory   */
+    void*       segmask;       size_t segmask_pitch;        /* binding  9 uSegMask         (optional) */
+    const void* material;      size_t material_pitch;       /* binding 10 uCurrentMaterial (optional) */
+    const void* prev_material; size_t prev_material_pitch;  /* binding 11 uPreviousMaterial(optional) */
+    const void* prev_segmask;  size_t prev_segmask_pitch;   /* binding 12 uPreviousSegMask (optional) */
+    const void* uvnrm;         size_t uvnrm_pitch;          /* binding 13 uCurrentUvNrm    (optional) */
+    void*       sharpened;     size_t sharpened_pitch;      /* the sharpen pass's output   (RGBA16F, with a sharpener) */
+} taa_frame_io_t;
+
+/* Jitter options: the debugging knobs of taa<CF>::get_jitter_offset_for_frame
+ * (source/taa.hpp:219-232, members 1404-1407).  Pass NULL for the defaults. */
+typedef struct taa_jitter_opts_t {
+    int32_t fixed_index;      /* mFixedJitterIndex, -1 = off */
+    int32_t slow_motion;      /* mJitterSlowMotion, 1 = off */
+    float   rotate_degrees;   /* mJitterRotateDegrees */
+    float   extra_scale;      /* mJitterExtraScale, 1 = off */
+} taa_jitter_opts_t;
+
+/* ---- library ---------------------------------------------------------- */
+
+/* Version string of the library and its ABI version number. */
+const char* taa_version(int* abi_version);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* taa_last_error(void);
+
+/* ---- host-side helpers (no device work) ------------------------------- */
+
+/* Fill `out` with the reference defaults (source/taa.hpp:31-76). */
+int taa_default_parameters(taa_parameters_t* out);
+
+/* Jitter offset in NDC for a frame, taa<CF>::get_jitter_offset_for_frame
+ * (source/taa.hpp:150-233) with helpers::halton (source/helper_functions.hpp:9-26).
+ * sample_distribution: 0 circular quad, 1 uniform-4 helix, 2 Halton(2,3)x8,
+ * 3 Halton(2,3)x16, 4 regular 16.  in_width/in_height: source resolution.
+ * out_num_samples may be NULL. */
+int taa_get_jitter_offset(int32_t sample_distribution, uint64_t frame_id,
+                          int32_t in_width, int32_t in_height,
+                          const taa_jitter_opts_t* opts,
+                          float out_ndc[2], int32_t* out_num_samples);
+
+/* translate(jitter.x, jitter.y, 0) * proj, taa<CF>::get_jittered_projection_matrix
+ * (source/taa.hpp:243-253).  Column-major 4x4. */
+int taa_jittered_projection(const float proj[16], const float jitter_ndc[2], float out[16]);
+
+/* The two per-frame matrices of taa<CF>::render (source/taa.hpp:993-994),
+ * composed in FP64 and rounded once to FP32:
+ *   inv_view_proj  = inverse(proj_cur * view_cur)
+ *   hist_view_proj = proj_prev * view_prev
+ * All column-major.  Returns TAA_E_INVAL for a singular proj_cur*view_cur. */
+int taa_compose_matrices(const double proj_cur[16], const double view_cur[16],
+                         const double proj_prev[16], const double view_prev[16],
+                         float inv_view_proj[16], float hist_view_proj[16]);
+
+/* FidelityFX CAS constants, CasSetup (shaders/ffx_cas.h:375-394). */
+int taa_cas_setup(float sharpness, float in_w, float in_h, float out_w, float out_h,
+                  uint32_t const0[4], uint32_t const1[4]);
+
+/* ---- context ----------------------------------------------------------- */
+
+/* Create a context for one resolution/format set
+ * (replaces taa<CF>::set_source_image_views + initialize, source/taa.hpp:263,650).
+ * Allocates the small device state it needs; nothing is allocated later. */
+int taa_create(const taa_desc_t* desc, taa_ctx** out_ctx);
+int taa_destroy(taa_ctx* ctx);
+
+/* Copy the uniform block used by the next taa_resolve calls
+ * (replaces mUniformsBuffer[i]->fill, source/taa.hpp:995).  Validates enums. */
+int taa_set_uniforms(taa_ctx* ctx, const taa_uniforms_t* uniforms);
+
+/* Change the sharpener and its strength (source/taa.hpp:961-966). */
+int taa_set_sharpener(taa_ctx* ctx, uint32_t sharpener, float factor);
+
+/* Kernel form actually used for the current uniforms (TAA_FORM_*). */
+int taa_selected_form(const taa_ctx* ctx);
+
+/* Enqueue the resolve (and the fused sharpen when enabled) on `stream`
+ * (replaces the dispatch at source/taa.hpp:1027 and the sharpen dispatch at
+ * source/taa.hpp:1125/1134).  `io->history` and `io->history_out` must not
+ * overlap. */
+int taa_resolve(taa_ctx* ctx, void* stream, const taa_frame_io_t* io);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* TAA_GB300_H */

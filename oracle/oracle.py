@@ -1,0 +1,170 @@
+"""numpy face of the oracle (test infrastructure: the checker, never the product).
+
+Loads ``oracle/_build/liboracle.so`` (built by ``oracle/build_oracle.py``) and wraps
+its entry points for numpy arrays.  Images are (H, W, C) arrays; FP16 inputs
+are widened to float32 exactly before they are handed over.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "liboracle.so"
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            from importlib import util
+            spec = util.spec_from_file_location("build_oracle", HERE / "build_oracle.py")
+            mod = util.module_from_spec(spec)
+            spec.loader.exec_module(mod)
+            mod.build_oracle()
+        lib = C.CDLL(str(LIB_PATH))
+        P = C.POINTER
+        fp, dp, up = P(C.c_float), P(C.c_double), P(C.c_uint32)
+        lib.oracle_resolve.restype = C.c_int
+        lib.oracle_resolve.argtypes = [C.c_int, C.c_void_p] + [C.c_int] * 4 + [fp] * 5 + [up] * 3 + [fp] + \
+                                      [dp] * 3 + [up, C.c_int]
+        lib.oracle_cas.argtypes = [C.c_int, fp, C.c_int, C.c_int, C.c_uint32, dp, C.c_int]
+        lib.oracle_sharpen.argtypes = [C.c_int, fp, C.c_int, C.c_int, C.c_float, dp, C.c_int]
+        lib.oracle_cas_setup.argtypes = [C.c_float] * 5 + [up, up]
+        lib.oracle_cas_setup.restype = None
+        lib.oracle_halton.argtypes = [C.c_int, C.c_int]
+        lib.oracle_halton.restype = C.c_float
+        lib.oracle_jitter_offset.argtypes = [C.c_int, C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float,
+                                             C.c_float, fp, P(C.c_int)]
+        lib.oracle_jitter_offset.restype = None
+        lib.oracle_quantize_half.argtypes = [fp, fp, C.c_size_t]
+        lib.oracle_quantize_half.restype = None
+        lib.oracle_check_div_const.argtypes = [C.c_float, C.c_uint32, C.c_uint32, C.c_int]
+        lib.oracle_check_div_const.restype = C.c_longlong
+        lib.oracle_synth_frame.argtypes = [C.c_void_p, fp, C.c_int, dp, dp, dp, dp, C.c_int]
+        _lib = lib
+    return _lib
+
+
+def _fp(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _up(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_uint32))
+
+
+def _f32(a, ch=None):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if ch is not None and a.ndim == 3 and a.shape[2] < ch:
+        pad = np.zeros(a.shape[:2] + (ch - a.shape[2],), np.float32)
+        a = np.ascontiguousarray(np.concatenate([a, pad], axis=2))
+    return a
+
+
+def _u32(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def nthreads_default() -> int:
+    return max(1, os.cpu_count() or 1)
+
+
+def resolve(uniforms, color, depth, velocity, history=None, history_depth=None, out_size=None, precision=32,
+            material=None, prev_material=None, prev_segmask=None, uvnrm=None, want_debug=False, nthreads=None):
+    """Run the oracle resolve.  Returns dict(history, screen, debug, segmask)
+    of float64 arrays holding the FP32 (precision=32) or FP64 values before
+    any FP16 store."""
+    lib = load()
+    in_h, in_w = color.shape[:2]
+    out_w, out_h = out_size if out_size else (in_w, in_h)
+    col = _f32(color, 4)
+    dep = _f32(depth).reshape(in_h, in_w)
+    vel = _f32(velocity, 4)
+    his = _f32(history, 4)
+    hdp = _f32(history_depth)
+    mat, pmat, pseg = _u32(material), _u32(prev_material), _u32(prev_segmask)
+    nrm = _f32(uvnrm, 4)
+    out_hist = np.zeros((out_h, out_w, 4))
+    out_scr = np.zeros((out_h, out_w, 4))
+    out_dbg = np.zeros((out_h, out_w, 4)) if want_debug else None
+    out_seg = np.zeros((out_h, out_w), np.uint32)
+    rc = lib.oracle_resolve(precision, C.addressof(uniforms), in_w, in_h, out_w, out_h, _fp(col), _fp(dep), _fp(his),
+                            _fp(hdp), _fp(vel), _up(mat), _up(pmat), _up(pseg), _fp(nrm), _dp(out_hist),
+                            _dp(out_scr), _dp(out_dbg), _up(out_seg), nthreads or nthreads_default())
+    if rc != 0:
+        raise ValueError("oracle_resolve rejected its arguments")
+    return dict(history=out_hist, screen=out_scr, debug=out_dbg, segmask=out_seg)
+
+
+def cas(img, peak_bits, precision=32, nthreads=None):
+    lib = load()
+    a = _f32(img, 4)
+    h, w = a.shape[:2]
+    out = np.zeros((h, w, 4))
+    lib.oracle_cas(precision, _fp(a), w, h, peak_bits, _dp(out), nthreads or nthreads_default())
+    return out
+
+
+def sharpen(img, factor, precision=32, nthreads=None):
+    lib = load()
+    a = _f32(img, 4)
+    h, w = a.shape[:2]
+    out = np.zeros((h, w, 4))
+    lib.oracle_sharpen(precision, _fp(a), w, h, factor, _dp(out), nthreads or nthreads_default())
+    return out
+
+
+def cas_setup(sharpness, in_w, in_h, out_w, out_h):
+    c0 = (C.c_uint32 * 4)()
+    c1 = (C.c_uint32 * 4)()
+    load().oracle_cas_setup(sharpness, in_w, in_h, out_w, out_h, c0, c1)
+    return list(c0), list(c1)
+
+
+def halton(i, b):
+    return load().oracle_halton(i, b)
+
+
+def jitter_offset(dist, frame, w, h, fixed_index=-1, slow_motion=1, rotate_degrees=0.0, extra_scale=1.0):
+    out = (C.c_float * 2)()
+    n = C.c_int()
+    load().oracle_jitter_offset(dist, frame, w, h, fixed_index, slow_motion, rotate_degrees, extra_scale, out,
+                                C.byref(n))
+    return (out[0], out[1]), n.value
+
+
+def quantize_half(a):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    out = np.empty_like(a)
+    load().oracle_quantize_half(_fp(a), _fp(out), a.size)
+    return out
+
+
+def check_div_const(d, lo_bits, hi_bits, nthreads=None):
+    return load().oracle_check_div_const(d, lo_bits, hi_bits, nthreads or nthreads_default())
+
+
+def synth_frame(scene, spheres, frame, truth=False, nthreads=None):
+    """FP64 evaluation of the analytic scene; returns dict(color, depth, motion, truth)."""
+    lib = load()
+    w, h = scene.width, scene.height
+    sph = np.ascontiguousarray(spheres, dtype=np.float32)
+    col = np.zeros((h, w, 4))
+    dep = np.zeros((h, w))
+    mot = np.zeros((h, w, 4))
+    tru = np.zeros((h, w, 4)) if truth else None
+    lib.oracle_synth_frame(C.addressof(scene), _fp(sph), frame, _dp(col), _dp(dep), _dp(mot), _dp(tru),
+                           nthreads or nthreads_default())
+    return dict(color=col, depth=dep, motion=mot, truth=tru)

@@ -1,0 +1,570 @@
+// capi.cpp - the C ABI of libtaa_gb300 (include/taa_gb300.h, include/taa_synth.h).
+//
+// Host side of the drop-in: context lifetime, argument validation, kernel
+// form selection, and the small host computations the reference does on the
+// CPU around its dispatch (jitter table, matrix composition, CasSetup).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "../../include/taa_gb300.h"
+#include "../../include/taa_synth.h"
+#include "kernels.h"
+#include "synth_scene.h"
+
+using taa_dev::FrameArgs;
+using taa_dev::Img;
+using taa_dev::ImgW;
+
+struct taa_ctx {
+    taa_desc_t desc;
+    taa_uniforms_t uniforms;
+    bool have_uniforms = false;
+    uint32_t cas_const0[4] = {0, 0, 0, 0};
+    uint32_t cas_const1[4] = {0, 0, 0, 0};
+    int device = 0;
+    // RGBA16F screen image for the plain form's separate sharpen pass when the
+    // caller does not bind a result image; allocated when a sharpener is set.
+    void* scratch_screen = nullptr;
+    size_t scratch_pitch = 0;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+int ok() { return TAA_OK; }
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(TAA_E_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+bool finite(float v) { return std::isfinite(v); }
+
+int check_parameters(const taa_parameters_t& p, int idx) {
+    const float fs[] = {p.mAlpha, p.mUnjitterFactor, p.mVarClipGamma, p.mMinAlpha, p.mMaxAlpha, p.mRejectionAlpha,
+                        p.mNoiseFactor, p.mVelBasedAlphaMax, p.mVelBasedAlphaFactor, p.mRayTraceAugment_WNrm,
+                        p.mRayTraceAugment_WDpt, p.mRayTraceAugment_WMId, p.mRayTraceAugment_WLum,
+                        p.mRayTraceAugment_Thresh, p.mDebugScale, p.mDebugMask[0], p.mDebugMask[1], p.mDebugMask[2],
+                        p.mDebugMask[3]};
+    for (size_t i = 0; i < sizeof fs / sizeof fs[0]; ++i)
+        if (!finite(fs[i])) return fail(TAA_E_INVAL, "param[%d]: float field %zu is not finite", idx, i);
+    return ok();
+}
+
+size_t history_texel(uint32_t fmt) { return fmt == TAA_HISTORY_RGBA32F ? 16 : 8; }
+size_t motion_texel(uint32_t fmt) { return fmt == TAA_MOTION_RGBA16F ? 8 : 4; }
+
+// Validates one binding: alignment, pitch and the byte range it spans.
+int check_image(const char* name, const void* p, size_t pitch, int w, int h, size_t texel, bool required,
+                const char** lo = nullptr, const char** hi = nullptr) {
+    if (!p) {
+        if (required) return fail(TAA_E_INVAL, "%s: required binding is NULL", name);
+        return ok();
+    }
+    if (pitch < (size_t)w * texel) return fail(TAA_E_INVAL, "%s: pitch %zu < width*texel %zu", name, pitch, (size_t)w * texel);
+    if ((uintptr_t)p % texel != 0 || pitch % texel != 0)
+        return fail(TAA_E_ALIGN, "%s: pointer/pitch not a multiple of the %zu-byte texel", name, texel);
+    if (lo) *lo = (const char*)p;
+    if (hi) *hi = (const char*)p + pitch * (size_t)(h - 1) + (size_t)w * texel;
+    return ok();
+}
+
+bool any_param(const taa_uniforms_t& u, int out_w, uint32_t taa_parameters_t::*f) {
+    bool right_used = u.splitScreen && u.splitX < out_w - 1;
+    return u.param[0].*f || (right_used && u.param[1].*f);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* taa_version(int* abi_version) {
+    if (abi_version) *abi_version = TAA_GB300_ABI_VERSION;
+    return "taa_gb300 0.1.0 (sm_103a)";
+}
+
+const char* taa_last_error(void) { return g_last_error.c_str(); }
+
+// source/taa.hpp:31-76
+int taa_default_parameters(taa_parameters_t* o) {
+    if (!o) return fail(TAA_E_INVAL, "taa_default_parameters: out is NULL");
+    std::memset(o, 0, sizeof *o);
+    o->mAlpha = 0.05f;
+    o->mColorClampingOrClipping = 1;
+    o->mUnjitterFactor = 1.0f;
+    o->mVarClipGamma = 1.0f;
+    o->mMinAlpha = 1.0f - 0.97f;
+    o->mMaxAlpha = 1.0f - 0.88f;
+    o->mRejectionAlpha = 1.0f;
+    o->mUseVelocityVectors = 1;
+    o->mNoiseFactor = 1.f / 510.f;
+    o->mVelBasedAlphaMax = 0.2f;
+    o->mVelBasedAlphaFactor = 1.f / 40.f;
+    o->mRayTraceAugmentFlags = 0xffffffffu & ~(TAA_RTFLAG_ALL | TAA_RTFLAG_FXD);
+    o->mRayTraceAugment_WNrm = 0.5f;
+    o->mRayTraceAugment_WDpt = 0.015f;
+    o->mRayTraceAugment_WMId = 0.25f;
+    o->mRayTraceAugment_WLum = 0.5f;
+    o->mRayTraceAugment_Thresh = 0.5f;
+    o->mRayTraceHistoryCount = -1;
+    o->mDebugMask[0] = o->mDebugMask[1] = o->mDebugMask[2] = 1.f;
+    o->mDebugMask[3] = 0.f;
+    o->mDebugScale = 1.0f;
+    return ok();
+}
+
+// helpers::halton (source/helper_functions.hpp:9-17), in float as the reference.
+static float halton_host(int i, int b) {
+    float f = 1.0f, r = 0.0f;
+    while (i > 0) {
+        f = f / (float)b;
+        r = r + f * (float)(i % b);
+        i = i / b;
+    }
+    return r;
+}
+
+// source/taa.hpp:150-233.  The reference fills its tables once from the
+// first resolution it sees (function-local statics); here every call uses
+// the resolution it is given.
+int taa_get_jitter_offset(int32_t dist, uint64_t frame_id, int32_t w, int32_t h, const taa_jitter_opts_t* opts,
+                          float out[2], int32_t* out_n) {
+    if (!out) return fail(TAA_E_INVAL, "taa_get_jitter_offset: out is NULL");
+    if (w <= 0 || h <= 0) return fail(TAA_E_INVAL, "taa_get_jitter_offset: bad resolution %dx%d", w, h);
+    if (dist < 0 || dist > 4) return fail(TAA_E_INVAL, "taa_get_jitter_offset: sample distribution %d not in 0..4", dist);
+    const float sx = 2.0f / (float)w, sy = 2.0f / (float)h;
+    float tx[16], ty[16];
+    int n = 0;
+    if (dist == 0 || dist == 1) {
+        // circular quad / uniform-4 helix, in units of +-0.25 px
+        static const float q[2][4][2] = {{{-.25f, -.25f}, {.25f, -.25f}, {.25f, .25f}, {-.25f, .25f}},
+                                         {{-.25f, -.25f}, {.25f, .25f}, {.25f, -.25f}, {-.25f, .25f}}};
+        for (n = 0; n < 4; ++n) {
+            tx[n] = sx * q[dist][n][0];
+            ty[n] = sy * q[dist][n][1];
+        }
+    } else if (dist == 2 || dist == 3) {
+        int len = dist == 2 ? 8 : 16;
+        for (n = 0; n < len; ++n) {
+            tx[n] = sx * (halton_host(n + 1, 2) - 0.5f);
+            ty[n] = sy * (halton_host(n + 1, 3) - 0.5f);
+        }
+    } else {
+        const float e = 1.f / 8.f;
+        for (int j = 0; j < 4; ++j)
+            for (int i = 0; i < 4; ++i, ++n) {
+                tx[n] = sx * ((float)(2 * i - 3) * e);
+                ty[n] = sy * ((float)(2 * j - 3) * e);
+            }
+    }
+    taa_jitter_opts_t o = {-1, 1, 0.f, 1.f};
+    if (opts) o = *opts;
+    if (o.slow_motion > 1) frame_id /= (uint64_t)o.slow_motion;
+    if (o.fixed_index >= 0) frame_id = (uint64_t)o.fixed_index;
+    float x = tx[frame_id % (uint64_t)n], y = ty[frame_id % (uint64_t)n];
+    if (o.rotate_degrees != 0.f) {
+        float r = o.rotate_degrees * (float)(3.14159265358979323846 / 180.0);
+        float s = std::sin(r), c = std::cos(r);
+        float nx = x * c - y * s, ny = x * s + y * c;
+        x = nx;
+        y = ny;
+    }
+    out[0] = x * o.extra_scale;
+    out[1] = y * o.extra_scale;
+    if (out_n) *out_n = n;
+    return ok();
+}
+
+// glm::translate(vec3(j.x, j.y, 0)) * P (source/taa.hpp:248), column-major.
+int taa_jittered_projection(const float p[16], const float j[2], float out[16]) {
+    if (!p || !j || !out) return fail(TAA_E_INVAL, "taa_jittered_projection: NULL argument");
+    float r[16];
+    for (int c = 0; c < 4; ++c) {
+        // T * column c: rows 0 and 1 gain j * row 3
+        r[c * 4 + 0] = p[c * 4 + 0] + j[0] * p[c * 4 + 3];
+        r[c * 4 + 1] = p[c * 4 + 1] + j[1] * p[c * 4 + 3];
+        r[c * 4 + 2] = p[c * 4 + 2];
+        r[c * 4 + 3] = p[c * 4 + 3];
+    }
+    std::memcpy(out, r, sizeof r);
+    return ok();
+}
+
+static void mat_mul_d(const double* a, const double* b, double* o) {  // column-major o = a*b
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r) {
+            double s = 0.0;
+            for (int k = 0; k < 4; ++k) s += a[k * 4 + r] * b[c * 4 + k];
+            o[c * 4 + r] = s;
+        }
+}
+
+// Gauss-Jordan inverse with partial pivoting; false if singular.
+static bool mat_inv_d(const double* m, double* inv) {
+    double a[4][8];
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) {
+            a[r][c] = m[c * 4 + r];
+            a[r][c + 4] = r == c ? 1.0 : 0.0;
+        }
+    for (int c = 0; c < 4; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < 4; ++r)
+            if (std::fabs(a[r][c]) > std::fabs(a[piv][c])) piv = r;
+        if (!(std::fabs(a[piv][c]) > 1e-300)) return false;
+        if (piv != c)
+            for (int k = 0; k < 8; ++k) std::swap(a[c][k], a[piv][k]);
+        double d = a[c][c];
+        for (int k = 0; k < 8; ++k) a[c][k] /= d;
+        for (int r = 0; r < 4; ++r) {
+            if (r == c) continue;
+            double f = a[r][c];
+            if (f != 0.0)
+                for (int k = 0; k < 8; ++k) a[r][k] -= f * a[c][k];
+        }
+    }
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) inv[c * 4 + r] = a[r][c + 4];
+    return true;
+}
+
+// source/taa.hpp:993-994 in FP64.
+int taa_compose_matrices(const double pc[16], const double vc[16], const double pp[16], const double vp[16],
+                         float inv_vp[16], float hist_vp[16]) {
+    if (!pc || !vc || !pp || !vp || !inv_vp || !hist_vp) return fail(TAA_E_INVAL, "taa_compose_matrices: NULL argument");
+    double cur[16], inv[16], prev[16];
+    mat_mul_d(pc, vc, cur);
+    if (!mat_inv_d(cur, inv)) return fail(TAA_E_INVAL, "taa_compose_matrices: proj_cur*view_cur is singular");
+    mat_mul_d(pp, vp, prev);
+    for (int i = 0; i < 16; ++i) {
+        inv_vp[i] = (float)inv[i];
+        hist_vp[i] = (float)prev[i];
+    }
+    return ok();
+}
+
+static uint32_t fbits(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+}
+
+// CasSetup (shaders/ffx_cas.h:375-394) with ffx_a.h's CPU helpers.
+int taa_cas_setup(float sharpness, float in_w, float in_h, float out_w, float out_h, uint32_t c0[4], uint32_t c1[4]) {
+    if (!c0 || !c1) return fail(TAA_E_INVAL, "taa_cas_setup: NULL argument");
+    c0[0] = fbits(in_w * (1.0f / out_w));
+    c0[1] = fbits(in_h * (1.0f / out_h));
+    c0[2] = fbits(0.5f * in_w * (1.0f / out_w) - 0.5f);
+    c0[3] = fbits(0.5f * in_h * (1.0f / out_h) - 0.5f);
+    float s = sharpness < 0.f ? 0.f : (sharpness > 1.f ? 1.f : sharpness);
+    float sharp = -(1.0f / (5.0f * s + (-8.0f * s + 8.0f)));
+    c1[0] = fbits(sharp);
+    // packed FP16 copy of the sharpness for the packed-math CAS variant:
+    // ffx_a.h's CPU converter truncates the mantissa
+    auto h = [](float f) -> uint32_t {
+        uint32_t u = fbits(f), sg = (u >> 16) & 0x8000u, e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+        if (e < 103u) return sg;
+        if (e < 113u) return sg + (1u << (e - 103u)) + (m >> (126u - e));
+        if (e < 143u) return sg + ((e - 112u) << 10) + (m >> 13);
+        return sg + 0x7bffu;
+    };
+    c1[1] = h(sharp) | (h(0.0f) << 16);
+    c1[2] = fbits(8.0f * in_w * (1.0f / out_w));
+    c1[3] = 0;
+    return ok();
+}
+
+// ---------------------------------------------------------------- context
+
+static int ensure_scratch(taa_ctx* c) {
+    if (c->desc.sharpener == TAA_SHARPEN_OFF || c->scratch_screen) return ok();
+    cudaError_t e = cudaMallocPitch(&c->scratch_screen, &c->scratch_pitch, (size_t)c->desc.out_width * 8,
+                                    (size_t)c->desc.out_height);
+    if (e != cudaSuccess) {
+        c->scratch_screen = nullptr;
+        return e == cudaErrorMemoryAllocation ? fail(TAA_E_NOMEM, "scratch screen image: out of device memory")
+                                              : cuda_fail(e, "cudaMallocPitch");
+    }
+    return ok();
+}
+
+int taa_create(const taa_desc_t* d, taa_ctx** out) {
+    if (!d || !out) return fail(TAA_E_INVAL, "taa_create: NULL argument");
+    *out = nullptr;
+    if (d->struct_size != sizeof(taa_desc_t)) return fail(TAA_E_INVAL, "taa_create: struct_size %u != %zu", d->struct_size, sizeof(taa_desc_t));
+    if (d->in_width <= 0 || d->in_height <= 0 || d->out_width <= 0 || d->out_height <= 0 || d->in_width > 32768 ||
+        d->in_height > 32768 || d->out_width > 32768 || d->out_height > 32768)
+        return fail(TAA_E_INVAL, "taa_create: image sizes must be in 1..32768");
+    if (d->history_format > TAA_HISTORY_RGBA16F) return fail(TAA_E_INVAL, "taa_create: history_format %u", d->history_format);
+    if (d->motion_format > TAA_MOTION_RG16F) return fail(TAA_E_INVAL, "taa_create: motion_format %u", d->motion_format);
+    if (d->form > TAA_FORM_FP16) return fail(TAA_E_INVAL, "taa_create: form %u", d->form);
+    if (d->sharpener > TAA_SHARPEN_CAS) return fail(TAA_E_INVAL, "taa_create: sharpener %u", d->sharpener);
+    if (!finite(d->sharpen_factor)) return fail(TAA_E_INVAL, "taa_create: sharpen_factor not finite");
+    if (d->flags != 0) return fail(TAA_E_INVAL, "taa_create: flags must be 0");
+    taa_ctx* c = new (std::nothrow) taa_ctx();
+    if (!c) return fail(TAA_E_NOMEM, "taa_create: host allocation failed");
+    c->desc = *d;
+    cudaError_t e = cudaGetDevice(&c->device);
+    if (e != cudaSuccess) {
+        delete c;
+        return cuda_fail(e, "cudaGetDevice");
+    }
+    taa_cas_setup(d->sharpen_factor, (float)d->out_width, (float)d->out_height, (float)d->out_width,
+                  (float)d->out_height, c->cas_const0, c->cas_const1);
+    int rc = ensure_scratch(c);
+    if (rc != TAA_OK) {
+        delete c;
+        return rc;
+    }
+    *out = c;
+    return ok();
+}
+
+int taa_destroy(taa_ctx* c) {
+    if (!c) return ok();
+    if (c->scratch_screen) cudaFree(c->scratch_screen);
+    delete c;
+    return ok();
+}
+
+int taa_set_uniforms(taa_ctx* c, const taa_uniforms_t* u) {
+    if (!c || !u) return fail(TAA_E_INVAL, "taa_set_uniforms: NULL argument");
+    for (int i = 0; i < 2; ++i) {
+        int rc = check_parameters(u->param[i], i);
+        if (rc) return rc;
+    }
+    const float m[] = {u->mJitterNdc[0], u->mJitterNdc[1], u->mSinTime[0], u->mCamNearPlane, u->mCamFarPlane};
+    for (float v : m)
+        if (!finite(v)) return fail(TAA_E_INVAL, "taa_set_uniforms: jitter/time/near/far must be finite");
+    for (int i = 0; i < 16; ++i)
+        if (!finite(u->mHistoryViewProjMatrix[i]) || !finite(u->mInverseViewProjMatrix[i]))
+            return fail(TAA_E_INVAL, "taa_set_uniforms: matrices must be finite");
+    c->uniforms = *u;
+    c->have_uniforms = true;
+    return ok();
+}
+
+int taa_set_sharpener(taa_ctx* c, uint32_t sharpener, float factor) {
+    if (!c) return fail(TAA_E_INVAL, "taa_set_sharpener: NULL context");
+    if (sharpener > TAA_SHARPEN_CAS) return fail(TAA_E_INVAL, "taa_set_sharpener: sharpener %u", sharpener);
+    if (!finite(factor)) return fail(TAA_E_INVAL, "taa_set_sharpener: factor not finite");
+    c->desc.sharpener = sharpener;
+    c->desc.sharpen_factor = factor;
+    taa_cas_setup(factor, (float)c->desc.out_width, (float)c->desc.out_height, (float)c->desc.out_width,
+                  (float)c->desc.out_height, c->cas_const0, c->cas_const1);
+    return ensure_scratch(c);
+}
+
+static int select_form(const taa_ctx* c, const taa_frame_io_t* io) {
+    if (c->desc.form == TAA_FORM_PLAIN) return TAA_FORM_PLAIN;
+    const taa_desc_t& d = c->desc;
+    if (!taa_dev::fast_path_supported(c->uniforms, d.in_width, d.in_height, d.out_width, d.out_height))
+        return TAA_FORM_PLAIN;
+    if (io && (io->debug || io->segmask)) return TAA_FORM_PLAIN;
+    return TAA_FORM_TILED;
+}
+
+int taa_selected_form(const taa_ctx* c) {
+    if (!c) return fail(TAA_E_INVAL, "taa_selected_form: NULL context");
+    if (!c->have_uniforms) return fail(TAA_E_INVAL, "taa_selected_form: no uniforms set");
+    return select_form(c, nullptr);
+}
+
+int taa_resolve(taa_ctx* c, void* stream, const taa_frame_io_t* io) {
+    if (!c || !io) return fail(TAA_E_INVAL, "taa_resolve: NULL argument");
+    if (!c->have_uniforms) return fail(TAA_E_INVAL, "taa_resolve: taa_set_uniforms was not called");
+    const taa_desc_t& d = c->desc;
+    const taa_uniforms_t& U = c->uniforms;
+    const int iw = d.in_width, ih = d.in_height, ow = d.out_width, oh = d.out_height;
+    const size_t ht = history_texel(d.history_format), mt = motion_texel(d.motion_format);
+    const char *hlo = nullptr, *hhi = nullptr, *olo = nullptr, *ohi = nullptr;
+    int rc;
+    if ((rc = check_image("color", io->color, io->color_pitch, iw, ih, 8, true))) return rc;
+    if ((rc = check_image("depth", io->depth, io->depth_pitch, iw, ih, 4, true))) return rc;
+    if ((rc = check_image("velocity", io->velocity, io->velocity_pitch, iw, ih, mt, true))) return rc;
+    if ((rc = check_image("history", io->history, io->history_pitch, ow, oh, ht, false, &hlo, &hhi))) return rc;
+    if ((rc = check_image("history_out", io->history_out, io->history_out_pitch, ow, oh, ht, true, &olo, &ohi))) return rc;
+    bool depth_cull = any_param(U, ow, &taa_parameters_t::mDepthCulling);
+    if ((rc = check_image("history_depth", io->history_depth, io->history_depth_pitch, iw, ih, 4, depth_cull))) return rc;
+    if ((rc = check_image("result", io->result, io->result_pitch, ow, oh, 8, false))) return rc;
+    if ((rc = check_image("debug", io->debug, io->debug_pitch, ow, oh, 8, false))) return rc;
+    if ((rc = check_image("segmask", io->segmask, io->segmask_pitch, ow, oh, 4, false))) return rc;
+    if ((rc = check_image("material", io->material, io->material_pitch, iw, ih, 4, false))) return rc;
+    if ((rc = check_image("prev_material", io->prev_material, io->prev_material_pitch, iw, ih, 4, false))) return rc;
+    if ((rc = check_image("prev_segmask", io->prev_segmask, io->prev_segmask_pitch, ow, oh, 4, false))) return rc;
+    if ((rc = check_image("uvnrm", io->uvnrm, io->uvnrm_pitch, iw, ih, 16, false))) return rc;
+    bool sharpen = d.sharpener != TAA_SHARPEN_OFF;
+    if ((rc = check_image("sharpened", io->sharpened, io->sharpened_pitch, ow, oh, 8, sharpen))) return rc;
+    if (hlo && hlo < ohi && olo < hhi) return fail(TAA_E_INVAL, "taa_resolve: history and history_out overlap");
+
+    FrameArgs a{};
+    a.color = Img{(const char*)io->color, io->color_pitch, iw, ih};
+    a.depth = Img{(const char*)io->depth, io->depth_pitch, iw, ih};
+    a.history = Img{(const char*)io->history, io->history_pitch, ow, oh};
+    a.history_depth = Img{(const char*)io->history_depth, io->history_depth_pitch, iw, ih};
+    a.velocity = Img{(const char*)io->velocity, io->velocity_pitch, iw, ih};
+    a.material = Img{(const char*)io->material, io->material_pitch, iw, ih};
+    a.prev_material = Img{(const char*)io->prev_material, io->prev_material_pitch, iw, ih};
+    a.prev_segmask = Img{(const char*)io->prev_segmask, io->prev_segmask_pitch, ow, oh};
+    a.uvnrm = Img{(const char*)io->uvnrm, io->uvnrm_pitch, iw, ih};
+    a.result = ImgW{(char*)io->result, io->result_pitch};
+    a.debug = ImgW{(char*)io->debug, io->debug_pitch};
+    a.history_out = ImgW{(char*)io->history_out, io->history_out_pitch};
+    a.segmask = ImgW{(char*)io->segmask, io->segmask_pitch};
+    a.sharpened = ImgW{(char*)io->sharpened, io->sharpened_pitch};
+    a.out_w = ow;
+    a.out_h = oh;
+    a.inv_out_w = 1.0f / (float)ow;
+    a.inv_out_h = 1.0f / (float)oh;
+    a.cas_peak_bits = c->cas_const1[0];
+    a.sharpen_factor = d.sharpen_factor;
+
+    cudaStream_t s = (cudaStream_t)stream;
+    int form = select_form(c, io);
+    cudaError_t e;
+    if (form == TAA_FORM_PLAIN) {
+        if (sharpen && !a.result.p) a.result = ImgW{(char*)c->scratch_screen, c->scratch_pitch};
+        e = taa_dev::launch_resolve_plain(U, a, (int)d.history_format, d.motion_format == TAA_MOTION_RGBA16F ? 4 : 2, s);
+        if (e == cudaSuccess && sharpen) e = taa_dev::launch_sharpen((int)d.sharpener, a, s);
+    } else {
+        taa_dev::FastKey k;
+        k.form = form;
+        k.history_fmt = (int)d.history_format;
+        k.motion_ch = d.motion_format == TAA_MOTION_RGBA16F ? 4 : 2;
+        k.interp = U.param[0].mInterpolationMode;
+        k.sharpen = (int)d.sharpener;
+        e = taa_dev::launch_resolve_fast(k, U, a, s);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "taa_resolve launch");
+    return ok();
+}
+
+// ---------------------------------------------------------------- synthetic scene
+
+int taa_synth_default_scene(taa_synth_scene_t* o, int32_t w, int32_t h, uint64_t seed) {
+    if (!o) return fail(TAA_E_INVAL, "taa_synth_default_scene: NULL");
+    if (w <= 0 || h <= 0) return fail(TAA_E_INVAL, "taa_synth_default_scene: bad size");
+    std::memset(o, 0, sizeof *o);
+    o->struct_size = sizeof *o;
+    o->width = w;
+    o->height = h;
+    o->seed = seed;
+    o->num_spheres = 32;
+    o->radius_min = 20.f;
+    o->radius_max = 120.f;
+    o->sphere_speed_max = 6.f;
+    o->spin_max = 0.f;
+    o->cam_v0[0] = 3.f;
+    o->checker_period = 7.3f;
+    o->firefly_fraction = 0.01f;
+    o->firefly_max = 64.f;
+    o->jitter_phase = 0;
+    o->jitter_enabled = 1;
+    return ok();
+}
+
+static int check_scene(const taa_synth_scene_t* s) {
+    if (!s) return fail(TAA_E_INVAL, "synth: NULL scene");
+    if (s->struct_size != sizeof(taa_synth_scene_t)) return fail(TAA_E_INVAL, "synth: struct_size mismatch");
+    if (s->width <= 0 || s->height <= 0) return fail(TAA_E_INVAL, "synth: bad size");
+    if (s->num_spheres < 0 || s->num_spheres > TAA_SYNTH_MAX_SPHERES) return fail(TAA_E_INVAL, "synth: num_spheres");
+    if (!(s->checker_period > 0.f)) return fail(TAA_E_INVAL, "synth: checker_period");
+    return ok();
+}
+
+int taa_synth_spheres(const taa_synth_scene_t* s, float* t, int32_t cap) {
+    int rc = check_scene(s);
+    if (rc) return rc;
+    if (!t || cap < s->num_spheres) return fail(TAA_E_INVAL, "synth: sphere table too small");
+    uint64_t st = s->seed ^ 0xA0761D6478BD642Full;
+    auto uni = [&]() {
+        st += 0x9E3779B97F4A7C15ull;
+        return (double)(taa_synth::mix64(st) >> 11) * (1.0 / 9007199254740992.0);
+    };
+    for (int i = 0; i < s->num_spheres; ++i) {
+        float* p = t + i * TAA_SYNTH_SPHERE_FLOATS;
+        p[0] = (float)(uni() * s->width);
+        p[1] = (float)(uni() * s->height);
+        p[2] = (float)(s->radius_min + uni() * (s->radius_max - s->radius_min));
+        p[3] = (float)(50.0 + uni() * 350.0);
+        p[4] = (float)uni();
+        p[5] = (float)uni();
+        p[6] = (float)uni();
+        p[7] = (float)((2.0 * uni() - 1.0) * s->sphere_speed_max);
+        p[8] = (float)((2.0 * uni() - 1.0) * s->sphere_speed_max);
+        p[9] = (float)((2.0 * uni() - 1.0) * s->spin_max);
+        p[10] = p[2] / 3.0f;
+        p[11] = 0.f;
+    }
+    return ok();
+}
+
+int taa_synth_jitter(const taa_synth_scene_t* s, int32_t frame, float px[2], float ndc[2]) {
+    int rc = check_scene(s);
+    if (rc) return rc;
+    float jx, jy;
+    taa_synth::jitter_px(*s, frame, jx, jy);
+    if (px) {
+        px[0] = jx;
+        px[1] = jy;
+    }
+    if (ndc) {
+        ndc[0] = 2.0f * jx / (float)s->width;
+        ndc[1] = 2.0f * jy / (float)s->height;
+    }
+    return ok();
+}
+
+int taa_synth_camera(const taa_synth_scene_t* s, int32_t frame, double proj[16], double view[16]) {
+    int rc = check_scene(s);
+    if (rc) return rc;
+    if (!proj || !view) return fail(TAA_E_INVAL, "synth: NULL matrix");
+    using namespace taa_synth;
+    std::memset(proj, 0, 16 * sizeof(double));
+    std::memset(view, 0, 16 * sizeof(double));
+    // clip = (2f/W X, 2f/H Y, A Z + B, Z); ndc.z = A + B/Z is the depth the renderer writes
+    proj[0] = 2.0 * kFocal / s->width;
+    proj[5] = 2.0 * kFocal / s->height;
+    proj[10] = kFar / (kFar - kNear);
+    proj[11] = 1.0;
+    proj[14] = -kFar * kNear / (kFar - kNear);
+    // the backdrop moves by -cam(t) px at depth kBackdropZ: camera at cam(t)*Z/f
+    double t = frame;
+    double cx = (double)s->cam_v0[0] * t + 0.5 * (double)s->cam_accel[0] * t * t;
+    double cy = (double)s->cam_v0[1] * t + 0.5 * (double)s->cam_accel[1] * t * t;
+    view[0] = view[5] = view[10] = view[15] = 1.0;
+    view[12] = -cx * kBackdropZ / kFocal;
+    view[13] = -cy * kBackdropZ / kFocal;
+    return ok();
+}
+
+int taa_synth_render(const taa_synth_scene_t* s, int32_t frame, void* stream, const taa_synth_frame_t* out) {
+    int rc = check_scene(s);
+    if (rc) return rc;
+    if (!out) return fail(TAA_E_INVAL, "synth: NULL output");
+    if (out->motion && out->motion_channels != 2 && out->motion_channels != 4)
+        return fail(TAA_E_INVAL, "synth: motion_channels must be 2 or 4");
+    static thread_local float table[TAA_SYNTH_MAX_SPHERES * TAA_SYNTH_SPHERE_FLOATS];
+    taa_synth_spheres(s, table, TAA_SYNTH_MAX_SPHERES);
+    cudaError_t e = taa_dev::launch_synth(*s, table, frame, *out, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "taa_synth_render launch");
+    return ok();
+}
+
+}  // extern "C"

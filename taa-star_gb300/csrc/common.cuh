@@ -1,0 +1,140 @@
+// common.cuh - device-side helpers shared by the resolve kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+#include "../../include/taa_params.h"
+
+namespace taa_dev {
+
+// A pitched device image.
+struct Img {
+    const char* p;
+    size_t pitch;
+    int w, h;
+};
+struct ImgW {
+    char* p;
+    size_t pitch;
+};
+
+// Everything one resolve launch needs besides the uniform block.
+struct FrameArgs {
+    Img color;          // RGBA16F, source size
+    Img depth;          // D32F, source size
+    Img history;        // RGBA32F or RGBA16F, target size (p == nullptr reads zeros)
+    Img history_depth;  // D32F, source size
+    Img velocity;       // RG16F or RGBA16F, source size
+    Img material;       // R32UI
+    Img prev_material;  // R32UI
+    Img prev_segmask;   // R32UI
+    Img uvnrm;          // RGBA32F
+    ImgW result;        // RGBA16F, target size
+    ImgW debug;         // RGBA16F
+    ImgW history_out;   // RGBA32F or RGBA16F
+    ImgW segmask;       // R32UI
+    ImgW sharpened;     // RGBA16F
+    int out_w, out_h;
+    float inv_out_w, inv_out_h;  // correctly rounded 1/out size
+    uint32_t cas_peak_bits;      // CasSetup const1.x
+    float sharpen_factor;
+};
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// GLSL min/max on finite values.
+__device__ __forceinline__ float gmax(float a, float b) { return a < b ? b : a; }
+__device__ __forceinline__ float gmin(float a, float b) { return b < a ? b : a; }
+__device__ __forceinline__ float gclamp(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
+
+// ivec2(float) made total (NaN -> large negative, clamped by the caller).
+__device__ __forceinline__ int trunc_index(float t) {
+    if (!(t > -1e9f)) return -1000000000;
+    if (t > 1e9f) return 1000000000;
+    return (int)t;
+}
+
+template <class T> __device__ __forceinline__ const T* texel_ptr(const Img& im, int x, int y) {
+    return reinterpret_cast<const T*>(im.p + (size_t)y * im.pitch) + x;
+}
+
+__device__ __forceinline__ float4 half4_to_float4(uint2 v) {
+    __half2 a = *reinterpret_cast<__half2*>(&v.x);
+    __half2 b = *reinterpret_cast<__half2*>(&v.y);
+    float2 fa = __half22float2(a), fb = __half22float2(b);
+    return make_float4(fa.x, fa.y, fb.x, fb.y);
+}
+__device__ __forceinline__ uint2 float4_to_half4(float4 v) {
+    __half2 a = __floats2half2_rn(v.x, v.y);
+    __half2 b = __floats2half2_rn(v.z, v.w);
+    uint2 r;
+    r.x = *reinterpret_cast<uint32_t*>(&a);
+    r.y = *reinterpret_cast<uint32_t*>(&b);
+    return r;
+}
+
+// RGBA16F texel (clamped to the image).
+__device__ __forceinline__ float4 fetch_rgba16f(const Img& im, int x, int y) {
+    x = clampi(x, 0, im.w - 1);
+    y = clampi(y, 0, im.h - 1);
+    return half4_to_float4(__ldg(texel_ptr<uint2>(im, x, y)));
+}
+__device__ __forceinline__ float fetch_r32f(const Img& im, int x, int y) {
+    x = clampi(x, 0, im.w - 1);
+    y = clampi(y, 0, im.h - 1);
+    return __ldg(texel_ptr<float>(im, x, y));
+}
+__device__ __forceinline__ uint32_t fetch_r32u(const Img& im, int x, int y) {
+    if (!im.p) return 0u;
+    x = clampi(x, 0, im.w - 1);
+    y = clampi(y, 0, im.h - 1);
+    return __ldg(texel_ptr<uint32_t>(im, x, y));
+}
+__device__ __forceinline__ float4 fetch_rgba32f(const Img& im, int x, int y) {
+    if (!im.p) return make_float4(0.f, 0.f, 0.f, 0.f);
+    x = clampi(x, 0, im.w - 1);
+    y = clampi(y, 0, im.h - 1);
+    return __ldg(texel_ptr<float4>(im, x, y));
+}
+// Velocity with 2 or 4 channels (missing channels read 0).
+template <int MC> __device__ __forceinline__ float4 fetch_velocity(const Img& im, int x, int y) {
+    x = clampi(x, 0, im.w - 1);
+    y = clampi(y, 0, im.h - 1);
+    if (MC == 4) return half4_to_float4(__ldg(texel_ptr<uint2>(im, x, y)));
+    uint32_t v = __ldg(texel_ptr<uint32_t>(im, x, y));
+    float2 f = __half22float2(*reinterpret_cast<__half2*>(&v));
+    return make_float4(f.x, f.y, 0.f, 0.f);
+}
+// History texel in either format (null history reads zeros).
+template <int HF> __device__ __forceinline__ float4 fetch_history(const Img& im, int x, int y) {
+    if (!im.p) return make_float4(0.f, 0.f, 0.f, 0.f);
+    x = clampi(x, 0, im.w - 1);
+    y = clampi(y, 0, im.h - 1);
+    if (HF == 0) return __ldg(texel_ptr<float4>(im, x, y));
+    return half4_to_float4(__ldg(texel_ptr<uint2>(im, x, y)));
+}
+
+template <class T> __device__ __forceinline__ T* texel_ptr_w(const ImgW& im, int x, int y) {
+    return reinterpret_cast<T*>(im.p + (size_t)y * im.pitch) + x;
+}
+__device__ __forceinline__ void store_rgba16f(const ImgW& im, int x, int y, float4 v) {
+    *texel_ptr_w<uint2>(im, x, y) = float4_to_half4(v);
+}
+template <int HF> __device__ __forceinline__ void store_history(const ImgW& im, int x, int y, float4 v) {
+    if (HF == 0) *texel_ptr_w<float4>(im, x, y) = v;
+    else *texel_ptr_w<uint2>(im, x, y) = float4_to_half4(v);
+}
+
+// Correctly rounded x / d for a constant divisor d with precomputed
+// rd = RN(1/d): one product and one FMA-based residual correction
+// (P. Markstein, "Computation of elementary functions on the IBM RISC
+// System/6000 processor", IBM J. Res. Dev. 34(1), 1990).  The identity is
+// checked exhaustively against IEEE division on the CPU for the divisors the
+// kernels use.
+__device__ __forceinline__ float div_const_rn(float x, float d, float rd) {
+    float q = __fmul_rn(x, rd);
+    float r = __fmaf_rn(-d, q, x);
+    return __fmaf_rn(r, rd, q);
+}
+
+}  // namespace taa_dev

@@ -1,0 +1,37 @@
+// kernels.h - launchers of the device kernels (internal to the library).
+#pragma once
+#include <cuda_runtime.h>
+#include "common.cuh"
+#include "../../include/taa_synth.h"
+
+namespace taa_dev {
+
+// Plain FP32 resolve (resolve_plain.cu).
+cudaError_t launch_resolve_plain(const taa_uniforms_t& U, const FrameArgs& a, int history_format,
+                                 int motion_channels, cudaStream_t stream);
+
+// Parameters the fast forms specialise on at compile time; everything else in
+// the parameter block stays a runtime value.
+struct FastKey {
+    int form;          // TAA_FORM_TILED or TAA_FORM_FP16
+    int history_fmt;   // 0 RGBA32F, 1 RGBA16F
+    int motion_ch;     // 2 or 4
+    int interp;        // 0 bilinear, 1 b-spline, 2 Catmull-Rom
+    int sharpen;       // 0 off, 1 simple, 2 CAS (fused epilogue)
+};
+
+// True when the fast forms implement every feature the uniforms ask for.
+bool fast_path_supported(const taa_uniforms_t& U, int in_w, int in_h, int out_w, int out_h);
+
+// Tiled FP32 / FP16 resolve, optionally with the fused sharpen (resolve_fast.cu).
+cudaError_t launch_resolve_fast(const FastKey& key, const taa_uniforms_t& U, const FrameArgs& a,
+                                cudaStream_t stream);
+
+// Standalone sharpen passes on an RGBA16F image (used after the plain form).
+cudaError_t launch_sharpen(int sharpener, const FrameArgs& a, cudaStream_t stream);
+
+// Synthetic renderer (synth.cu).
+cudaError_t launch_synth(const taa_synth_scene_t& s, const float* host_spheres, int frame,
+                         const taa_synth_frame_t& out, cudaStream_t stream);
+
+}  // namespace taa_dev

@@ -1,0 +1,298 @@
+"""ctypes binding of libtaa_gb300 (include/taa_gb300.h, include/taa_synth.h).
+
+This is the Python face of the C ABI, used by the tests and the benchmark.
+It mirrors the structs byte for byte and adds a thin ``Taa`` context wrapper
+that accepts torch CUDA tensors for the per-frame bindings.  It never falls
+back to anything: if the shared library is missing, loading raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "_build" / "libtaa_gb300.so"
+
+TAA_OK = 0
+TAA_E_INVAL = -1
+TAA_E_ALIGN = -2
+TAA_E_CUDA = -3
+TAA_E_TIMEOUT = -4
+TAA_E_UNSUPPORTED = -5
+TAA_E_NOMEM = -6
+
+TAA_HISTORY_RGBA32F = 0
+TAA_HISTORY_RGBA16F = 1
+TAA_MOTION_RGBA16F = 0
+TAA_MOTION_RG16F = 1
+TAA_FORM_AUTO, TAA_FORM_PLAIN, TAA_FORM_TILED, TAA_FORM_FP16 = 0, 1, 2, 3
+TAA_SHARPEN_OFF, TAA_SHARPEN_SIMPLE, TAA_SHARPEN_CAS = 0, 1, 2
+
+RTFLAG = dict(OUT=0x1, DIS=0x2, NRM=0x4, DPT=0x8, MID=0x10, LUM=0x20, CNT=0x40, ALL=0x80, FXD=0x100, FXA=0x200)
+
+_PARAM_FIELDS = [
+    ("mAlpha", "f"), ("mColorClampingOrClipping", "i"), ("mDepthCulling", "u"), ("mUnjitterNeighbourhood", "u"),
+    ("mUnjitterCurrentSample", "u"), ("mUnjitterFactor", "f"), ("mPassThrough", "u"), ("mUseYCoCg", "u"),
+    ("mShrinkChromaAxis", "u"), ("mVarianceClipping", "u"), ("mShapedNeighbourhood", "u"),
+    ("mLumaWeightingLottes", "u"), ("mVarClipGamma", "f"), ("mMinAlpha", "f"), ("mMaxAlpha", "f"),
+    ("mRejectionAlpha", "f"), ("mRejectOutside", "u"), ("mUseVelocityVectors", "i"), ("mVelocitySampleMode", "i"),
+    ("mInterpolationMode", "i"), ("mToneMapLumaKaris", "u"), ("mAddNoise", "u"), ("mNoiseFactor", "f"),
+    ("mReduceBlendNearClamp", "u"), ("mDynamicAntiGhosting", "u"), ("mVelBasedAlpha", "u"),
+    ("mVelBasedAlphaMax", "f"), ("mVelBasedAlphaFactor", "f"), ("mRayTraceAugment", "u"),
+    ("mRayTraceAugmentFlags", "u"), ("mRayTraceAugment_WNrm", "f"), ("mRayTraceAugment_WDpt", "f"),
+    ("mRayTraceAugment_WMId", "f"), ("mRayTraceAugment_WLum", "f"), ("mRayTraceAugment_Thresh", "f"),
+    ("mRayTraceHistoryCount", "i"), ("mDebugMask", "f4"), ("mDebugMode", "i"), ("mDebugScale", "f"),
+    ("mDebugCenter", "u"), ("mDebugToScreenOutput", "u"),
+]
+_CT = {"f": C.c_float, "i": C.c_int32, "u": C.c_uint32, "f4": C.c_float * 4}
+PARAM_NAMES = [n for n, _ in _PARAM_FIELDS]
+
+
+class Parameters(C.Structure):
+    """taa<CF>::Parameters (source/taa.hpp:30-77), 176 bytes."""
+    _fields_ = [(n, _CT[t]) for n, t in _PARAM_FIELDS]
+
+
+class Uniforms(C.Structure):
+    """taa<CF>::uniforms_for_taa (source/taa.hpp:113-129), 544 bytes."""
+    _fields_ = [
+        ("mHistoryViewProjMatrix", C.c_float * 16), ("mInverseViewProjMatrix", C.c_float * 16),
+        ("param", Parameters * 2), ("mJitterNdc", C.c_float * 4), ("mSinTime", C.c_float * 4),
+        ("splitScreen", C.c_uint32), ("splitX", C.c_int32), ("mUpsampling", C.c_uint32),
+        ("mBypassHistoryUpdate", C.c_uint32), ("mResetHistory", C.c_uint32), ("mCamNearPlane", C.c_float),
+        ("mCamFarPlane", C.c_float), ("pad1", C.c_float),
+    ]
+
+
+class Desc(C.Structure):
+    _fields_ = [
+        ("struct_size", C.c_uint32), ("in_width", C.c_int32), ("in_height", C.c_int32), ("out_width", C.c_int32),
+        ("out_height", C.c_int32), ("history_format", C.c_uint32), ("motion_format", C.c_uint32),
+        ("form", C.c_uint32), ("sharpener", C.c_uint32), ("sharpen_factor", C.c_float), ("flags", C.c_uint32),
+    ]
+
+
+_IO_NAMES = ["color", "depth", "history", "history_depth", "result", "debug", "velocity", "history_out", "segmask",
+             "material", "prev_material", "prev_segmask", "uvnrm", "sharpened"]
+
+
+class FrameIO(C.Structure):
+    _fields_ = [f for n in _IO_NAMES for f in ((n, C.c_void_p), (n + "_pitch", C.c_size_t))]
+
+
+class JitterOpts(C.Structure):
+    _fields_ = [("fixed_index", C.c_int32), ("slow_motion", C.c_int32), ("rotate_degrees", C.c_float),
+                ("extra_scale", C.c_float)]
+
+
+class SynthScene(C.Structure):
+    _fields_ = [
+        ("struct_size", C.c_uint32), ("width", C.c_int32), ("height", C.c_int32), ("seed", C.c_uint64),
+        ("num_spheres", C.c_int32), ("radius_min", C.c_float), ("radius_max", C.c_float),
+        ("sphere_speed_max", C.c_float), ("spin_max", C.c_float), ("cam_v0", C.c_float * 2),
+        ("cam_accel", C.c_float * 2), ("checker_period", C.c_float), ("firefly_fraction", C.c_float),
+        ("firefly_max", C.c_float), ("jitter_phase", C.c_int32), ("jitter_enabled", C.c_int32),
+    ]
+
+
+class SynthFrame(C.Structure):
+    _fields_ = [("color", C.c_void_p), ("color_pitch", C.c_size_t), ("depth", C.c_void_p),
+                ("depth_pitch", C.c_size_t), ("motion", C.c_void_p), ("motion_pitch", C.c_size_t),
+                ("motion_channels", C.c_int32), ("truth", C.c_void_p), ("truth_pitch", C.c_size_t)]
+
+
+SYNTH_MAX_SPHERES = 256
+SYNTH_SPHERE_FLOATS = 12
+
+assert C.sizeof(Parameters) == 176 and C.sizeof(Uniforms) == 544
+
+# Every symbol include/taa_gb300.h and include/taa_synth.h declare.
+EXPORTS = ["taa_version", "taa_last_error", "taa_default_parameters", "taa_get_jitter_offset",
+           "taa_jittered_projection", "taa_compose_matrices", "taa_cas_setup", "taa_create", "taa_destroy",
+           "taa_set_uniforms", "taa_set_sharpener", "taa_selected_form", "taa_resolve",
+           "taa_synth_default_scene", "taa_synth_spheres", "taa_synth_jitter", "taa_synth_camera",
+           "taa_synth_render"]
+
+_lib = None
+
+
+def load(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Load the shared library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise FileNotFoundError(f"{p} is missing: build it with taa-star_gb300/build.py")
+    lib = C.CDLL(str(p))
+    P = C.POINTER
+    sig = {
+        "taa_version": (C.c_char_p, [P(C.c_int)]),
+        "taa_last_error": (C.c_char_p, []),
+        "taa_default_parameters": (C.c_int, [P(Parameters)]),
+        "taa_get_jitter_offset": (C.c_int, [C.c_int32, C.c_uint64, C.c_int32, C.c_int32, P(JitterOpts),
+                                            P(C.c_float), P(C.c_int32)]),
+        "taa_jittered_projection": (C.c_int, [P(C.c_float), P(C.c_float), P(C.c_float)]),
+        "taa_compose_matrices": (C.c_int, [P(C.c_double)] * 4 + [P(C.c_float)] * 2),
+        "taa_cas_setup": (C.c_int, [C.c_float] * 5 + [P(C.c_uint32)] * 2),
+        "taa_create": (C.c_int, [P(Desc), P(C.c_void_p)]),
+        "taa_destroy": (C.c_int, [C.c_void_p]),
+        "taa_set_uniforms": (C.c_int, [C.c_void_p, P(Uniforms)]),
+        "taa_set_sharpener": (C.c_int, [C.c_void_p, C.c_uint32, C.c_float]),
+        "taa_selected_form": (C.c_int, [C.c_void_p]),
+        "taa_resolve": (C.c_int, [C.c_void_p, C.c_void_p, P(FrameIO)]),
+        "taa_synth_default_scene": (C.c_int, [P(SynthScene), C.c_int32, C.c_int32, C.c_uint64]),
+        "taa_synth_spheres": (C.c_int, [P(SynthScene), P(C.c_float), C.c_int32]),
+        "taa_synth_jitter": (C.c_int, [P(SynthScene), C.c_int32, P(C.c_float), P(C.c_float)]),
+        "taa_synth_camera": (C.c_int, [P(SynthScene), C.c_int32, P(C.c_double), P(C.c_double)]),
+        "taa_synth_render": (C.c_int, [P(SynthScene), C.c_int32, C.c_void_p, P(SynthFrame)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class TaaError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{code}: {msg}")
+        self.code = code
+
+
+def check(rc: int) -> int:
+    if rc < 0:
+        raise TaaError(rc, load().taa_last_error().decode())
+    return rc
+
+
+def default_parameters() -> Parameters:
+    p = Parameters()
+    check(load().taa_default_parameters(C.byref(p)))
+    return p
+
+
+def identity16():
+    return (C.c_float * 16)(*[1.0 if i % 5 == 0 else 0.0 for i in range(16)])
+
+
+def make_uniforms(p0: Parameters, p1: Parameters | None = None, jitter_ndc=(0.0, 0.0), **kw) -> Uniforms:
+    u = Uniforms()
+    u.mHistoryViewProjMatrix = identity16()
+    u.mInverseViewProjMatrix = identity16()
+    u.param[0] = p0
+    u.param[1] = p1 if p1 is not None else p0
+    u.mJitterNdc[0], u.mJitterNdc[1] = jitter_ndc
+    u.mCamNearPlane = 0.1
+    u.mCamFarPlane = 1000.0
+    for k, v in kw.items():
+        if k in ("mHistoryViewProjMatrix", "mInverseViewProjMatrix"):
+            setattr(u, k, (C.c_float * 16)(*[float(x) for x in v]))
+        else:
+            setattr(u, k, v)
+    return u
+
+
+def tensor_ptr_pitch(t) -> tuple[int, int]:
+    """Device pointer and row pitch in bytes of an (H, W, ...) tensor with contiguous rows."""
+    return int(t.data_ptr()), int(t.stride(0) * t.element_size())
+
+
+class Taa:
+    """One resolve context (taa_create ... taa_destroy)."""
+
+    def __init__(self, in_w, in_h, out_w=None, out_h=None, history_format=TAA_HISTORY_RGBA32F,
+                 motion_format=TAA_MOTION_RG16F, form=TAA_FORM_AUTO, sharpener=TAA_SHARPEN_OFF, sharpen_factor=0.5):
+        self.lib = load()
+        d = Desc(C.sizeof(Desc), in_w, in_h, out_w or in_w, out_h or in_h, history_format, motion_format, form,
+                 sharpener, sharpen_factor, 0)
+        h = C.c_void_p()
+        check(self.lib.taa_create(C.byref(d), C.byref(h)))
+        self.handle = h
+        self.desc = d
+
+    def close(self):
+        if self.handle:
+            self.lib.taa_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_uniforms(self, u: Uniforms):
+        check(self.lib.taa_set_uniforms(self.handle, C.byref(u)))
+
+    def set_sharpener(self, mode: int, factor: float):
+        check(self.lib.taa_set_sharpener(self.handle, mode, factor))
+
+    def selected_form(self) -> int:
+        return check(self.lib.taa_selected_form(self.handle))
+
+    def resolve(self, stream: int = 0, **bindings):
+        """bindings: name=tensor (or None) for the names of taa_frame_io_t."""
+        io = FrameIO()
+        for name, t in bindings.items():
+            if name not in _IO_NAMES:
+                raise KeyError(name)
+            if t is None:
+                continue
+            p, pitch = tensor_ptr_pitch(t)
+            setattr(io, name, p)
+            setattr(io, name + "_pitch", pitch)
+        check(self.lib.taa_resolve(self.handle, C.c_void_p(stream), C.byref(io)))
+
+
+def synth_default_scene(w, h, seed) -> SynthScene:
+    s = SynthScene()
+    check(load().taa_synth_default_scene(C.byref(s), w, h, seed))
+    return s
+
+
+def synth_spheres(scene: SynthScene):
+    import numpy as np
+    buf = (C.c_float * (SYNTH_MAX_SPHERES * SYNTH_SPHERE_FLOATS))()
+    check(load().taa_synth_spheres(C.byref(scene), buf, SYNTH_MAX_SPHERES))
+    return np.frombuffer(buf, dtype=np.float32).reshape(SYNTH_MAX_SPHERES, SYNTH_SPHERE_FLOATS)[
+        : scene.num_spheres].copy()
+
+
+def synth_jitter(scene: SynthScene, frame: int):
+    px = (C.c_float * 2)()
+    ndc = (C.c_float * 2)()
+    check(load().taa_synth_jitter(C.byref(scene), frame, px, ndc))
+    return (px[0], px[1]), (ndc[0], ndc[1])
+
+
+def synth_camera(scene: SynthScene, frame: int):
+    import numpy as np
+    p = (C.c_double * 16)()
+    v = (C.c_double * 16)()
+    check(load().taa_synth_camera(C.byref(scene), frame, p, v))
+    return np.array(p[:]), np.array(v[:])
+
+
+def compose_matrices(pc, vc, pp, vp):
+    import numpy as np
+    arr = [(C.c_double * 16)(*[float(x) for x in m]) for m in (pc, vc, pp, vp)]
+    inv = (C.c_float * 16)()
+    hist = (C.c_float * 16)()
+    check(load().taa_compose_matrices(*arr, inv, hist))
+    return np.array(inv[:], dtype=np.float32), np.array(hist[:], dtype=np.float32)
+
+
+def synth_render(scene: SynthScene, frame: int, stream: int = 0, color=None, depth=None, motion=None, truth=None):
+    f = SynthFrame()
+    for name, t in (("color", color), ("depth", depth), ("motion", motion), ("truth", truth)):
+        if t is not None:
+            p, pitch = tensor_ptr_pitch(t)
+            setattr(f, name, p)
+            setattr(f, name + "_pitch", pitch)
+    if motion is not None:
+        f.motion_channels = int(motion.shape[-1])
+    check(load().taa_synth_render(C.byref(scene), frame, C.c_void_p(stream), C.byref(f)))

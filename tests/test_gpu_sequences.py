@@ -1,0 +1,92 @@
+"""Whole-sequence parity at the benchmark sizes (run with -m gpu).
+
+Frames come from the GPU renderer; every frame's resolve is checked against
+the FP32 oracle fed the same history the GPU form was fed (per-frame error),
+and the error against the FP64 oracle is reported.  At 4K a subset of frames
+is checked so the suite stays within minutes.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+import taa_abi as T
+import workloads as WL
+from helpers import max_rel
+
+pytestmark = pytest.mark.gpu
+
+
+def render(wl, sc, f, dev, motion_ch=2):
+    H, W = wl.height, wl.width
+    col = torch.empty(H, W, 4, dtype=torch.float16, device=dev)
+    dep = torch.empty(H, W, dtype=torch.float32, device=dev)
+    mot = torch.empty(H, W, motion_ch, dtype=torch.float16, device=dev)
+    T.synth_render(sc, f, color=col, depth=dep, motion=mot)
+    return col, dep, mot
+
+
+def run_sequence(dev, wl, frames, check_frames, form=T.TAA_FORM_TILED, fp64_report=None):
+    sc = wl.scene()
+    H, W = wl.height, wl.width
+    ctx = T.Taa(W, H, form=form)
+    hist = torch.zeros(H, W, 4, dtype=torch.float32, device=dev)
+    hout = torch.empty_like(hist)
+    res = torch.empty(H, W, 4, dtype=torch.float16, device=dev)
+    prev_dep = None
+    errs = []
+    for f in range(frames):
+        col, dep, mot = render(wl, sc, f, dev)
+        jit = T.synth_jitter(sc, f)[1]
+        u = T.make_uniforms(wl.parameters(), jitter_ndc=jit, mResetHistory=1 if f == 0 else 0)
+        ctx.set_uniforms(u)
+        pd = prev_dep if prev_dep is not None else dep
+        ctx.resolve(color=col, depth=dep, velocity=mot, history=hist, history_depth=pd, history_out=hout, result=res)
+        torch.cuda.synchronize()
+        if f in check_frames:
+            args = (u, col.float().cpu().numpy(), dep.cpu().numpy(), mot.float().cpu().numpy())
+            kw = dict(history=hist.cpu().numpy(), history_depth=pd.cpu().numpy())
+            ref = O.resolve(*args, **kw)
+            got = hout.cpu().numpy()[..., :3]
+            err = max_rel(got, ref["history"][..., :3])
+            errs.append(err)
+            assert err <= 1e-4, (f, err)
+            if fp64_report is not None:
+                r64 = O.resolve(*args, precision=64, **kw)
+                fp64_report.append(max_rel(got, r64["history"][..., :3]))
+        hist, hout = hout, hist
+        prev_dep = dep
+    ctx.close()
+    return errs
+
+
+def test_c1_720p_sixteen_frames(cuda):
+    rep = []
+    errs = run_sequence(cuda, WL.c1(), 16, set(range(16)), fp64_report=rep)
+    print("C1 per-frame max rel vs FP32 oracle:", max(errs), " vs FP64:", max(rep))
+    assert max(rep) < 2e-3
+
+
+def test_c1_720p_plain_form(cuda):
+    run_sequence(cuda, WL.c1(), 6, {1, 5}, form=T.TAA_FORM_PLAIN)
+
+
+def test_c2_4k_frames(cuda):
+    wl = WL.c2()
+    rep = []
+    errs = run_sequence(cuda, wl, 6, {1, 5}, fp64_report=rep)
+    print("C2 per-frame max rel vs FP32 oracle:", max(errs), " vs FP64:", max(rep))
+
+
+def test_4k_constant_image_is_a_fixed_point(cuda):
+    H, W = 2160, 3840
+    ctx = T.Taa(W, H)
+    ctx.set_uniforms(T.make_uniforms(WL.base_parameters(mDepthCulling=1, mRejectOutside=1)))
+    col = torch.full((H, W, 4), 0.75, dtype=torch.float16, device=cuda)
+    dep = torch.full((H, W), 0.5, dtype=torch.float32, device=cuda)
+    mot = torch.zeros(H, W, 2, dtype=torch.float16, device=cuda)
+    hist = torch.full((H, W, 4), 0.75, dtype=torch.float32, device=cuda)
+    out = torch.empty_like(hist)
+    ctx.resolve(color=col, depth=dep, velocity=mot, history=hist, history_depth=dep, history_out=out)
+    torch.cuda.synchronize()
+    assert torch.allclose(out[..., :3], hist[..., :3], rtol=2e-7, atol=0)
