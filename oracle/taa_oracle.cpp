@@ -352,21 +352,22 @@ template <class R> struct Resolver {
         weights(fy, wy);
         int kx = trunc_index(std::floor(itx - R(0.5)));
         int ky = trunc_index(std::floor(ity - R(0.5)));
+        // rows first, then columns, each a fused multiply-add chain from zero
         V4<R> acc{R(0), R(0), R(0), R(0)};
         for (int j = 0; j < 4; ++j) {
             V4<R> row{R(0), R(0), R(0), R(0)};
             int yy = ky - 1 + j;
             for (int i = 0; i < 4; ++i) {
                 V4<R> s = fetch<R>(t, kx - 1 + i, yy);
-                row.x = row.x + wx[i] * s.x;
-                row.y = row.y + wx[i] * s.y;
-                row.z = row.z + wx[i] * s.z;
-                row.w = row.w + wx[i] * s.w;
+                row.x = std::fma(wx[i], s.x, row.x);
+                row.y = std::fma(wx[i], s.y, row.y);
+                row.z = std::fma(wx[i], s.z, row.z);
+                row.w = std::fma(wx[i], s.w, row.w);
             }
-            acc.x = acc.x + wy[j] * row.x;
-            acc.y = acc.y + wy[j] * row.y;
-            acc.z = acc.z + wy[j] * row.z;
-            acc.w = acc.w + wy[j] * row.w;
+            acc.x = std::fma(wy[j], row.x, acc.x);
+            acc.y = std::fma(wy[j], row.y, acc.y);
+            acc.z = std::fma(wy[j], row.z, acc.z);
+            acc.w = std::fma(wy[j], row.w, acc.w);
         }
         return acc;
     }

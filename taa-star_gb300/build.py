@@ -1,9 +1,9 @@
 """Build recipe for libtaa_gb300.so (sm_103a), in-tree, without cmake.
 
 Every translation unit is compiled by nvcc in parallel and linked into
-``taa-star_gb300/_build/libtaa_gb300.so``.  The plain form's unit is compiled
-with ``-fmad=false`` so that it rounds operation for operation like the FP32
-oracle; the others may contract to FMA.
+``taa-star_gb300/_build/libtaa_gb300.so``.  The resolve units are compiled
+with ``-fmad=false`` so that they round operation for operation like the FP32
+oracle (their sources place explicit FMAs where the oracle has them).
 
 Usage: ``python taa-star_gb300/build.py`` or ``build_library()`` from Python.
 """
@@ -29,7 +29,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", str(ROO
 # unit -> extra flags
 UNITS = {
     "resolve_plain.cu": ["-fmad=false"],
-    "resolve_fast.cu": [],
+    "resolve_fast.cu": ["-fmad=false"],
     "synth.cu": [],
     "capi.cpp": [],
 }

@@ -13,9 +13,11 @@
 // the simple sharpener to the tile from there, so the unsharpened image never
 // goes to HBM.
 //
-// Arithmetic follows the oracle's FP32 order at the two places where FP32
-// cancellation would amplify a difference (the neighbourhood moments and the
-// history position); elsewhere the compiler may contract to FMA.
+// This translation unit is compiled with -fmad=false: every operation rounds
+// as the FP32 oracle's does, with fused multiply-adds only where the oracle
+// has them (moments, Catmull-Rom accumulation) or where fusing provably
+// cannot change a result (products by powers of two), so the tiled form gives
+// the oracle's bits.
 #include "common.cuh"
 #include "sharpen.cuh"
 #include "kernels.h"
@@ -53,16 +55,20 @@ __device__ __forceinline__ float4 to_working(float4 c, bool tonemap, bool ycocg)
         c.z = c.z / l;
     }
     if (ycocg) {
-        // the products by powers of two are exact, so contraction cannot change the sums
-        float y = .25f * c.x + .5f * c.y + .25f * c.z;
-        float co = .5f * c.x - .5f * c.z;
-        float cg = -.25f * c.x + .5f * c.y - .25f * c.z;
+        // the products by powers of two are exact, so a fused form rounds like
+        // the separate multiply and add of the oracle
+        float y = __fmaf_rn(.25f, c.z, __fmaf_rn(.25f, c.x, .5f * c.y));
+        float co = __fmaf_rn(-.5f, c.z, .5f * c.x);
+        float cg = __fmaf_rn(-.25f, c.z, __fmaf_rn(-.25f, c.x, .5f * c.y));
         return make_float4(y, co, cg, 0.f);
     }
     return make_float4(c.x, c.y, c.z, 0.f);
 }
 
-template <int INTERP, int HF>
+// History sample in the oracle's FP32 order (the Catmull-Rom accumulation is
+// its fused multiply-add chain).  The alpha channel carries the dynamic
+// anti-ghosting mask, which these forms do not read.
+template <int INTERP, int HF, bool WANT_ALPHA = false>
 __device__ __forceinline__ float4 sample_history(const Img& h, float u, float v) {
     if (INTERP == 2) {
         // 16-tap Catmull-Rom, separable rows (taa.comp:441-514)
@@ -102,15 +108,15 @@ __device__ __forceinline__ float4 sample_history(const Img& h, float u, float v)
                 float4 s;
                 if (HF == 0) s = __ldg(reinterpret_cast<const float4*>(rowp) + xs[i]);
                 else s = half4_to_float4(__ldg(reinterpret_cast<const uint2*>(rowp) + xs[i]));
-                r.x += wx[i] * s.x;
-                r.y += wx[i] * s.y;
-                r.z += wx[i] * s.z;
-                r.w += wx[i] * s.w;
+                r.x = __fmaf_rn(wx[i], s.x, r.x);
+                r.y = __fmaf_rn(wx[i], s.y, r.y);
+                r.z = __fmaf_rn(wx[i], s.z, r.z);
+                if (WANT_ALPHA) r.w = __fmaf_rn(wx[i], s.w, r.w);
             }
-            acc.x += wy[j] * r.x;
-            acc.y += wy[j] * r.y;
-            acc.z += wy[j] * r.z;
-            acc.w += wy[j] * r.w;
+            acc.x = __fmaf_rn(wy[j], r.x, acc.x);
+            acc.y = __fmaf_rn(wy[j], r.y, acc.y);
+            acc.z = __fmaf_rn(wy[j], r.z, acc.z);
+            if (WANT_ALPHA) acc.w = __fmaf_rn(wy[j], r.w, acc.w);
         }
         return acc;
     } else {

@@ -6,8 +6,9 @@
 // at a by-construction texel centre is that texel; elsewhere exact-weight
 // bilinear; the 9-tap Catmull-Rom is its 16-tap equivalent).  This
 // translation unit is compiled with -fmad=false and uses explicit FMAs only
-// where the oracle does (the second-moment chain), so on the same inputs it
-// rounds like the FP32 oracle operation for operation.  It is the reference
+// where the oracle does (the second-moment chain and the Catmull-Rom
+// accumulation), so on the same inputs it rounds like the FP32 oracle
+// operation for operation.  It is the reference
 // form the tiled and FP16 forms are measured against.
 #include "common.cuh"
 #include "kernels.h"
@@ -288,15 +289,15 @@ struct PlainResolver {
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 float4 s = his(kx - 1 + i, ky - 1 + j);
-                row.x = row.x + wx[i] * s.x;
-                row.y = row.y + wx[i] * s.y;
-                row.z = row.z + wx[i] * s.z;
-                row.w = row.w + wx[i] * s.w;
+                row.x = __fmaf_rn(wx[i], s.x, row.x);
+                row.y = __fmaf_rn(wx[i], s.y, row.y);
+                row.z = __fmaf_rn(wx[i], s.z, row.z);
+                row.w = __fmaf_rn(wx[i], s.w, row.w);
             }
-            acc.x = acc.x + wy[j] * row.x;
-            acc.y = acc.y + wy[j] * row.y;
-            acc.z = acc.z + wy[j] * row.z;
-            acc.w = acc.w + wy[j] * row.w;
+            acc.x = __fmaf_rn(wy[j], row.x, acc.x);
+            acc.y = __fmaf_rn(wy[j], row.y, acc.y);
+            acc.z = __fmaf_rn(wy[j], row.z, acc.z);
+            acc.w = __fmaf_rn(wy[j], row.w, acc.w);
         }
         return acc;
     }

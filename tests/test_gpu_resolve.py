@@ -1,10 +1,11 @@
 """GPU parity of the resolve forms against the oracle (run with -m gpu).
 
-* plain form  : rounds like the FP32 oracle operation for operation -> equal bits
-                on the configurations without transcendental functions.
-* tiled form  : FP32 with FMA contraction -> within 1e-4 relative (floor 1e-3)
-                of the FP32 oracle on the history accumulator; screen within one
-                FP16 ulp of the oracle's value rounded to FP16.
+* plain and tiled forms: both round like the FP32 oracle operation for
+                operation (no FMA contraction; explicit FMAs where the oracle
+                has them), so the FP32 history accumulator has the oracle's
+                bits; the contract they are held to is 1e-4 relative (floor
+                1e-3), and the screen is within one FP16 ulp of the oracle's
+                value rounded to FP16.
 * fused sharpen: the tiled form with CAS / simple sharpen in its epilogue matches
                 the oracle's two separate passes (TAA -> FP16 store -> sharpen).
 """
@@ -74,6 +75,7 @@ def test_tiled_and_plain_match_oracle(cuda, mode, size):
         out = gpu_resolve(ctx, cuda, fr[1]["color"], fr[1]["depth"], fr[1]["motion"], hist, fr[0]["depth"])
         err = max_rel(out["history_out"][..., :3], ref["history"][..., :3])
         assert err <= REL_TOL, (form, err)
+        np.testing.assert_array_equal(out["history_out"], ref["history"].astype(np.float32), err_msg=str(form))
         assert screen_ok(out["result"][..., :3], ref["screen"][..., :3]), form
         ctx.close()
 
@@ -235,8 +237,12 @@ def test_gpu_renderer_matches_fp64_scene(cuda):
         ref = O.synth_frame(sc, sph, f, truth=True)
         c = col.float().cpu().numpy()
         qc = ref["color"].astype(np.float16).astype(np.float32)
+        # FP32 evaluation flips the FP16 rounding of values near a rounding
+        # boundary, and discontinuities (checker edges, silhouettes) of
+        # samples within FP32 error of an edge
         exact = np.mean(np.all(c == qc, axis=-1))
-        assert exact > 0.99, exact
+        near = np.mean(np.all(np.abs(c - ref["color"]) <= 1.01 * half_ulp(ref["color"]), axis=-1))
+        assert exact > 0.95 and near > 0.995, (exact, near)
         d = dep.cpu().numpy()
         assert np.mean(np.abs(d - ref["depth"]) < 1e-6) > 0.99
         m = mot.float().cpu().numpy()
