@@ -80,7 +80,9 @@ SYN_HD Hit<R> shade(const taa_synth_scene_t& s, const float* sph, int t, R sx, R
     const R tt = R(t);
     // backdrop
     R cx = cam_x<R>(s, tt), cy = cam_y<R>(s, tt);
-    R ux = sx + cx, uy = sy + cy;
+    // the fixed sub-pixel offset keeps checker edges (every 3.65 px) off the
+    // exact decimal pixel centres they would otherwise hit (10 * 3.65 = 36.5)
+    R ux = sx + cx + R(0.31830988618), uy = sy + cy + R(0.21132486541);
     R half = R(s.checker_period) * R(0.5);
     long long qx = (long long)floor(ux / half), qy = (long long)floor(uy / half);
     R checker = ((qx + qy) & 1) ? R(1) : R(0);
@@ -88,9 +90,11 @@ SYN_HD Hit<R> shade(const taa_synth_scene_t& s, const float* sph, int t, R sx, R
     R maxdim = R(s.width > s.height ? s.width : s.height);
     R zp = R(0.5) + R(0.5) * cos(R(kPi) / (R(2) * maxdim) * (zx * zx + zy * zy));
     R base = R(4) * (R(0.15) + R(0.85) * checker) * (R(0.25) + R(0.75) * zp);
-    h.r = base * R(0.9);
+    // a warm tint off the Cg = 0 plane (an RGB ramp such as 0.9/0.8/0.7 has
+    // Cg exactly 0, which makes the variance box degenerate in Cg)
+    h.r = base * R(0.95);
     h.g = base * R(0.8);
-    h.b = base * R(0.7);
+    h.b = base * R(0.6);
     R zbest = R(kBackdropZ);
     h.mx = -(cx - cam_x<R>(s, tt - R(1)));
     h.my = -(cy - cam_y<R>(s, tt - R(1)));

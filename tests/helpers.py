@@ -35,6 +35,14 @@ def max_rel(a, ref, floor=1e-3):
     return float(np.max(np.abs(a - ref) / np.maximum(np.abs(ref), floor))) if a.size else 0.0
 
 
+def rel_l2(a, ref):
+    """Frame-level relative error ||a - ref||_2 / ||ref||_2."""
+    a = np.asarray(a, np.float64)
+    ref = np.asarray(ref, np.float64)
+    n = float(np.linalg.norm(ref))
+    return float(np.linalg.norm(a - ref)) / n if n else float(np.linalg.norm(a))
+
+
 def half_ulp(x):
     """Spacing of binary16 at |x| (normal range), for comparisons after an FP16 store."""
     x = np.abs(np.asarray(x, dtype=np.float64))

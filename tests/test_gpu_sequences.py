@@ -1,9 +1,14 @@
 """Whole-sequence parity at the benchmark sizes (run with -m gpu).
 
-Frames come from the GPU renderer; every frame's resolve is checked against
-the FP32 oracle fed the same history the GPU form was fed (per-frame error),
-and the error against the FP64 oracle is reported.  At 4K a subset of frames
-is checked so the suite stays within minutes.
+Frames come from the GPU renderer; every checked frame's resolve is compared
+with the FP32 oracle fed the same history the GPU form was fed: the FP32
+forms must give its bits.  Against the FP64 oracle (the error truth) the
+frame-level relative L2 error must stay within 1e-4 and the PSNR (peak = the
+frame's largest HDR value) above 50 dB.  Per-pixel FP32-vs-FP64 differences
+are larger in a few pixels because the reference algorithm amplifies FP32
+rounding (the variance of a flat neighbourhood, taa.comp:270, and the
+max-ratio clip toward a near-degenerate box, taa.comp:335-340).  At 4K a
+subset of frames is checked so the suite stays within minutes.
 """
 import numpy as np
 import pytest
@@ -12,7 +17,7 @@ import torch
 import oracle as O
 import taa_abi as T
 import workloads as WL
-from helpers import max_rel
+from helpers import max_rel, psnr, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -47,13 +52,14 @@ def run_sequence(dev, wl, frames, check_frames, form=T.TAA_FORM_TILED, fp64_repo
             args = (u, col.float().cpu().numpy(), dep.cpu().numpy(), mot.float().cpu().numpy())
             kw = dict(history=hist.cpu().numpy(), history_depth=pd.cpu().numpy())
             ref = O.resolve(*args, **kw)
-            got = hout.cpu().numpy()[..., :3]
-            err = max_rel(got, ref["history"][..., :3])
+            got = hout.cpu().numpy()
+            err = max_rel(got[..., :3], ref["history"][..., :3])
             errs.append(err)
-            assert err <= 1e-4, (f, err)
+            np.testing.assert_array_equal(got, ref["history"].astype(np.float32), err_msg=f"frame {f}")
             if fp64_report is not None:
                 r64 = O.resolve(*args, precision=64, **kw)
-                fp64_report.append(max_rel(got, r64["history"][..., :3]))
+                h64 = r64["history"][..., :3]
+                fp64_report.append((rel_l2(got[..., :3], h64), psnr(got[..., :3], h64)))
         hist, hout = hout, hist
         prev_dep = dep
     ctx.close()
@@ -63,8 +69,9 @@ def run_sequence(dev, wl, frames, check_frames, form=T.TAA_FORM_TILED, fp64_repo
 def test_c1_720p_sixteen_frames(cuda):
     rep = []
     errs = run_sequence(cuda, WL.c1(), 16, set(range(16)), fp64_report=rep)
-    print("C1 per-frame max rel vs FP32 oracle:", max(errs), " vs FP64:", max(rep))
-    assert max(rep) < 2e-3
+    print("C1 per-frame max rel vs FP32 oracle:", max(errs), " vs FP64 (relL2, PSNR):", rep)
+    assert max(r for r, _ in rep) <= 1e-4
+    assert min(p for _, p in rep) >= 50.0
 
 
 def test_c1_720p_plain_form(cuda):
@@ -75,7 +82,9 @@ def test_c2_4k_frames(cuda):
     wl = WL.c2()
     rep = []
     errs = run_sequence(cuda, wl, 6, {1, 5}, fp64_report=rep)
-    print("C2 per-frame max rel vs FP32 oracle:", max(errs), " vs FP64:", max(rep))
+    print("C2 per-frame max rel vs FP32 oracle:", max(errs), " vs FP64 (relL2, PSNR):", rep)
+    assert max(r for r, _ in rep) <= 1e-4
+    assert min(p for _, p in rep) >= 50.0
 
 
 def test_4k_constant_image_is_a_fixed_point(cuda):
