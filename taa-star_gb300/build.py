@@ -30,6 +30,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", str(ROO
 UNITS = {
     "resolve_plain.cu": ["-fmad=false"],
     "resolve_fast.cu": ["-fmad=false"],
+    "resolve_tiled.cu": ["-fmad=false"],
     "synth.cu": [],
     "capi.cpp": [],
 }

@@ -443,13 +443,18 @@ int taa_resolve(taa_ctx* c, void* stream, const taa_frame_io_t* io) {
         e = taa_dev::launch_resolve_plain(U, a, (int)d.history_format, d.motion_format == TAA_MOTION_RGBA16F ? 4 : 2, s);
         if (e == cudaSuccess && sharpen) e = taa_dev::launch_sharpen((int)d.sharpener, a, s);
     } else {
-        taa_dev::FastKey k;
-        k.form = form;
-        k.history_fmt = (int)d.history_format;
-        k.motion_ch = d.motion_format == TAA_MOTION_RGBA16F ? 4 : 2;
-        k.interp = U.param[0].mInterpolationMode;
-        k.sharpen = (int)d.sharpener;
-        e = taa_dev::launch_resolve_fast(k, U, a, s);
+        const int mc = d.motion_format == TAA_MOTION_RGBA16F ? 4 : 2;
+        if (!sharpen) {
+            e = taa_dev::launch_resolve_tiled((int)d.history_format, mc, U.param[0].mInterpolationMode, U, a, s);
+        } else {
+            taa_dev::FastKey k;
+            k.form = form;
+            k.history_fmt = (int)d.history_format;
+            k.motion_ch = mc;
+            k.interp = U.param[0].mInterpolationMode;
+            k.sharpen = (int)d.sharpener;
+            e = taa_dev::launch_resolve_fast(k, U, a, s);
+        }
     }
     if (e != cudaSuccess) return cuda_fail(e, "taa_resolve launch");
     return ok();
