@@ -286,7 +286,7 @@ def run_ours(args):
 
     forms = {form_name: {"mpx_s": mpx, "gb_s": achieved, "frac_of_hbm": achieved / peak}}
     if not args.no_forms:
-        for fid, name in ((T.TAA_FORM_PLAIN, "plain"),):
+        for fid, name in ((T.TAA_FORM_PLAIN, "plain"), (T.TAA_FORM_FP16, "fp16")):
             c2 = make_ctx(fid)
             k = max(2, args.steps // 4)
             m2 = timed(c2, k, 1)

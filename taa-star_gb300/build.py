@@ -1,9 +1,10 @@
 """Build recipe for libtaa_gb300.so (sm_103a), in-tree, without cmake.
 
 Every translation unit is compiled by nvcc in parallel and linked into
-``taa-star_gb300/_build/libtaa_gb300.so``.  The resolve units are compiled
-with ``-fmad=false`` so that they round operation for operation like the FP32
-oracle (their sources place explicit FMAs where the oracle has them).
+``taa-star_gb300/_build/libtaa_gb300.so``.  The FP32 resolve units are
+compiled with ``-fmad=false`` so that they round operation for operation like
+the FP32 oracle (their sources place explicit FMAs where the oracle has them);
+the FP16 form's unit may contract to FMA.
 
 Usage: ``python taa-star_gb300/build.py`` or ``build_library()`` from Python.
 """
@@ -31,6 +32,7 @@ UNITS = {
     "resolve_plain.cu": ["-fmad=false"],
     "resolve_fast.cu": ["-fmad=false"],
     "resolve_tiled.cu": ["-fmad=false"],
+    "resolve_half.cu": [],
     "synth.cu": [],
     "capi.cpp": [],
 }

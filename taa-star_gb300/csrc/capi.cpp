@@ -371,12 +371,17 @@ int taa_set_sharpener(taa_ctx* c, uint32_t sharpener, float factor) {
     return ensure_scratch(c);
 }
 
+// AUTO picks the tiled FP32 form (bit-identical to the plain form); the FP16
+// form is used only when asked for, since its error contract is looser.
+// Parameters the tiled forms do not implement fall back to the plain form;
+// the FP16 form with a fused sharpener runs as the tiled FP32 form.
 static int select_form(const taa_ctx* c, const taa_frame_io_t* io) {
     if (c->desc.form == TAA_FORM_PLAIN) return TAA_FORM_PLAIN;
     const taa_desc_t& d = c->desc;
     if (!taa_dev::fast_path_supported(c->uniforms, d.in_width, d.in_height, d.out_width, d.out_height))
         return TAA_FORM_PLAIN;
     if (io && (io->debug || io->segmask)) return TAA_FORM_PLAIN;
+    if (d.form == TAA_FORM_FP16 && d.sharpener == TAA_SHARPEN_OFF) return TAA_FORM_FP16;
     return TAA_FORM_TILED;
 }
 
@@ -444,7 +449,9 @@ int taa_resolve(taa_ctx* c, void* stream, const taa_frame_io_t* io) {
         if (e == cudaSuccess && sharpen) e = taa_dev::launch_sharpen((int)d.sharpener, a, s);
     } else {
         const int mc = d.motion_format == TAA_MOTION_RGBA16F ? 4 : 2;
-        if (!sharpen) {
+        if (form == TAA_FORM_FP16) {
+            e = taa_dev::launch_resolve_half((int)d.history_format, mc, U.param[0].mInterpolationMode, U, a, s);
+        } else if (!sharpen) {
             e = taa_dev::launch_resolve_tiled((int)d.history_format, mc, U.param[0].mInterpolationMode, U, a, s);
         } else {
             taa_dev::FastKey k;

@@ -27,9 +27,12 @@ bool fast_path_supported(const taa_uniforms_t& U, int in_w, int in_h, int out_w,
 cudaError_t launch_resolve_fast(const FastKey& key, const taa_uniforms_t& U, const FrameArgs& a,
                                 cudaStream_t stream);
 
-// Latency-hiding tiled FP32 resolve without a fused sharpener (resolve_tiled.cu).
+// Tiled resolve without a fused sharpener: exact FP32 (resolve_tiled.cu) and
+// packed FP16 neighbourhood (resolve_half.cu), sharing tiled_skeleton.cuh.
 cudaError_t launch_resolve_tiled(int history_fmt, int motion_ch, int interp, const taa_uniforms_t& U,
                                  const FrameArgs& a, cudaStream_t stream);
+cudaError_t launch_resolve_half(int history_fmt, int motion_ch, int interp, const taa_uniforms_t& U,
+                                const FrameArgs& a, cudaStream_t stream);
 
 // Standalone sharpen passes on an RGBA16F image (used after the plain form).
 cudaError_t launch_sharpen(int sharpener, const FrameArgs& a, cudaStream_t stream);

@@ -1,0 +1,286 @@
+// tiled_skeleton.cuh - the CTA structure shared by the tiled FP32 and FP16 resolve forms.
+//
+// One 256-thread CTA resolves a 32x8 tile, one pixel per thread:
+//   1. each thread requests its pixel's velocity and depth, one or two texels
+//      of the tile's source colour plus 1-pixel halo, and the velocity of the
+//      tile's reference pixel (the same address for the whole CTA);
+//   2. the reference pixel's history position fixes a window of history
+//      texels - its Catmull-Rom taps widened by the tile and a margin of
+//      WIN_MARGIN pixels of motion difference - which the CTA copies into
+//      shared memory with cp.async (each texel crosses L1 once per tile
+//      instead of once per tap); the window is indexed by unclamped texel
+//      coordinates and stores the edge-clamped texel at every position, so a
+//      pixel's 16 taps are 4x4 consecutive window entries read with immediate
+//      offsets from one base;
+//   3. while the window is in flight the staged colour gives the 3x3 box
+//      (the arithmetic policy decides how: exact FP32 or packed FP16);
+//   4. a pixel whose taps fall inside the window reads them from shared
+//      memory, any other pixel (motion differing from the reference pixel's
+//      by more than the margin) reads them from global memory; then
+//      rejection, rectification and blend finish the pixel.
+//
+// The arithmetic lives in a policy class `Pol` so that the exact FP32 form
+// (compiled with -fmad=false, bit-identical to the oracle) and the FP16 form
+// share the memory pipeline.
+#pragma once
+#include <atomic>
+
+#include "common.cuh"
+
+namespace taa_dev {
+namespace tiled {
+
+constexpr int TX = 32, TY = 8, NT = TX * TY;
+constexpr int SX = TX + 2, SY = TY + 2, NS = SX * SY;  // staged colour with halo
+constexpr int WIN_MARGIN = 3;                          // motion difference (px) the window absorbs
+constexpr int WW = TX + 3 + 2 * WIN_MARGIN;            // history window width  (texels)
+constexpr int WH = TY + 3 + 2 * WIN_MARGIN;            // history window height (texels)
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* dst_smem, const void* src) {
+    if (BYTES == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_addr(dst_smem)), "l"(src) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(smem_addr(dst_smem)), "l"(src), "n"(BYTES)
+                     : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Compile-time view of the parameter block: Hot = the benchmark mode (variance
+// clip in YCoCg, clip towards the box centre, velocity for every pixel, simple
+// velocity sampling, no tonemap / luma weighting / near-clamp reduction).
+template <bool Hot> struct Mode {
+    const taa_parameters_t& P;
+    __device__ bool ycocg() const { return Hot || P.mUseYCoCg; }
+    __device__ bool tonemap() const { return !Hot && P.mToneMapLumaKaris; }
+    __device__ bool variance() const { return Hot || P.mVarianceClipping; }
+    __device__ bool shaped() const { return !Hot && P.mShapedNeighbourhood; }
+    __device__ bool shrink() const { return !Hot && P.mUseYCoCg && P.mShrinkChromaAxis; }
+    __device__ int clip() const { return Hot ? 2 : P.mColorClampingOrClipping; }
+    __device__ int use_velocity() const { return Hot ? 2 : P.mUseVelocityVectors; }
+    __device__ int velocity_sample() const { return Hot ? 0 : P.mVelocitySampleMode; }
+    __device__ bool vel_alpha() const { return !Hot && P.mVelBasedAlpha; }
+    __device__ bool lottes() const { return !Hot && P.mLumaWeightingLottes; }
+    __device__ bool near_clamp() const { return !Hot && P.mReduceBlendNearClamp; }
+};
+
+inline bool is_hot(const taa_parameters_t& P) {
+    return P.mUseYCoCg && !P.mToneMapLumaKaris && P.mVarianceClipping && !P.mShrinkChromaAxis &&
+           P.mColorClampingOrClipping == 2 && P.mUseVelocityVectors == 2 && P.mVelocitySampleMode == 0 &&
+           !P.mVelBasedAlpha && !P.mLumaWeightingLottes && !P.mReduceBlendNearClamp;
+}
+
+struct C3 { float x, y, z; };
+
+// History filter taps: up to 16 texels (clamped coordinates) with weights.
+// INTERP 2: 4x4 separable Catmull-Rom; 0: one bilinear 2x2; 1: four bilinear
+// 2x2 sets combined with the "b-spline" weights.
+struct Taps {
+    int xs[4], ys[4];  // clamped texel coordinates
+    float wx[4], wy[4];
+    int ux, uy;        // unclamped coordinate of the first tap
+};
+
+template <class Pol, int INTERP> struct HistoryTaps {
+    Taps t[INTERP == 1 ? 4 : 1];
+    float s0[2], s1[2];  // b-spline combination weights
+
+    __device__ __forceinline__ void setup(float u, float v, int w, int h) {
+        if (INTERP == 2) {
+            Pol::catmullrom_taps(u, v, w, h, t[0]);
+        } else if (INTERP == 0) {
+            Pol::bilinear_taps(u, v, w, h, t[0]);
+        } else {
+            float t0[2], t1[2];
+            Pol::bspline_positions(u, v, w, h, s0, s1, t0, t1);
+            Pol::bilinear_taps(t0[0], t0[1], w, h, t[0]);
+            Pol::bilinear_taps(t1[0], t0[1], w, h, t[1]);
+            Pol::bilinear_taps(t0[0], t1[1], w, h, t[2]);
+            Pol::bilinear_taps(t1[0], t1[1], w, h, t[3]);
+        }
+    }
+};
+
+template <int HF> struct HistTexel;
+template <> struct HistTexel<0> { using T = float4; static constexpr int B = 16; };
+template <> struct HistTexel<1> { using T = uint2; static constexpr int B = 8; };
+
+template <int HF> __device__ __forceinline__ float4 to_f4(float4 v) { return v; }
+template <int HF> __device__ __forceinline__ float4 to_f4(uint2 v) { return half4_to_float4(v); }
+
+// History position of pixel (cx, cy) (taa.comp:391-438).
+template <class Pol, int MC, bool HOT>
+__device__ __forceinline__ void history_position(const taa_uniforms_t& U, const FrameArgs& a, const Mode<HOT>& M,
+                                                 int cx, int cy, float4 vs, float depth, float u, float v, float& hu,
+                                                 float& hv, float& ehd) {
+    const bool can = !(M.use_velocity() == 0 || (M.use_velocity() == 1 && vs.w < 0.5f));
+    if (can) {
+        if (M.velocity_sample() == 2) {
+            int bdx = -1, bdy = -1;
+            float dc = fetch_r32f(a.depth, cx - 1, cy - 1);
+#pragma unroll
+            for (int k = 1; k < 9; ++k) {
+                int dx = k % 3 - 1, dy = k / 3 - 1;
+                float d = fetch_r32f(a.depth, cx + dx, cy + dy);
+                if (d < dc) { bdx = dx; bdy = dy; dc = d; }
+            }
+            vs = fetch_velocity<MC>(a.velocity, cx + bdx, cy + bdy);
+        }
+        hu = u - vs.x;
+        hv = v - vs.y;
+        ehd = depth - vs.z;
+    } else {
+        Pol::reproject(U, u, v, depth, hu, hv, ehd);
+    }
+}
+
+// The resolve kernel.  Pol provides the working colour format and the box,
+// tap, filter and finishing arithmetic (see resolve_tiled.cu, resolve_half.cu).
+template <class Pol, int HF, int MC, int INTERP, bool HOT>
+__global__ void __launch_bounds__(NT, 4) resolve_tile(const taa_uniforms_t U, const FrameArgs a) {
+    using HT = typename HistTexel<HF>::T;
+    using Staged = typename Pol::Staged;
+    __shared__ Staged s_col[NS];
+    __shared__ HT s_win[WW * WH];
+
+    const taa_parameters_t& P = U.param[0];
+    const Mode<HOT> M{P};
+    const int tid = threadIdx.x;
+    const int lx = tid % TX, ly = tid / TX;
+    const int W = a.out_w, H = a.out_h;
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+    const int x = x0 + lx, y = y0 + ly;
+    const bool inside = x < W && y < H;
+    const int cx = min(x, W - 1), cy = min(y, H - 1);
+    // the tile's reference pixel (its centre, clamped into the image)
+    const int rx = min(x0 + TX / 2, W - 1), ry = min(y0 + TY / 2, H - 1);
+
+    // 1. own depth and velocity, the reference pixel's, staged colour texels
+    float depth = __ldg(texel_ptr<float>(a.depth, cx, cy));
+    float4 vs = fetch_velocity<MC>(a.velocity, cx, cy);
+    float rdepth = __ldg(texel_ptr<float>(a.depth, rx, ry));
+    float4 rvs = fetch_velocity<MC>(a.velocity, rx, ry);
+    uint2 st0, st1 = make_uint2(0u, 0u);
+    {
+        int sy = tid / SX, sx = tid - sy * SX;
+        st0 = __ldg(texel_ptr<uint2>(a.color, clampi(x0 - 1 + sx, 0, W - 1), clampi(y0 - 1 + sy, 0, H - 1)));
+        if (tid + NT < NS) {
+            int i = tid + NT, sy1 = i / SX, sx1 = i - sy1 * SX;
+            st1 = __ldg(texel_ptr<uint2>(a.color, clampi(x0 - 1 + sx1, 0, W - 1), clampi(y0 - 1 + sy1, 0, H - 1)));
+        }
+    }
+
+    // 2. the reference pixel's taps place the history window; copy it in flight
+    const Img& hi = a.history;
+    const bool have_hist = hi.p != nullptr;
+    const bool windowed = have_hist && INTERP != 1;
+    int wx0 = 0, wy0 = 0;
+    if (windowed) {
+        float ru = div_const_rn((float)rx + 0.5f, (float)W, a.inv_out_w);
+        float rv = div_const_rn((float)ry + 0.5f, (float)H, a.inv_out_h);
+        float rhu, rhv, rehd;
+        history_position<Pol, MC, HOT>(U, a, M, rx, ry, rvs, rdepth, ru, rv, rhu, rhv, rehd);
+        Taps rt;
+        if (INTERP == 2) Pol::catmullrom_taps(rhu, rhv, hi.w, hi.h, rt);
+        else Pol::bilinear_taps(rhu, rhv, hi.w, hi.h, rt);
+        // the reference pixel sits at (TX/2, TY/2) of the tile
+        wx0 = rt.ux - (rx - x0) - WIN_MARGIN;
+        wy0 = rt.uy - (ry - y0) - WIN_MARGIN;
+        const int lane = tid & 31, warp = tid >> 5;
+        for (int r = warp; r < WH; r += NT / 32) {
+            const int gy = clampi(wy0 + r, 0, hi.h - 1);
+            const char* row = hi.p + (size_t)gy * hi.pitch;
+            for (int c = lane; c < WW; c += 32)
+                cp_async<HistTexel<HF>::B>(&s_win[r * WW + c],
+                                           row + (size_t)clampi(wx0 + c, 0, hi.w - 1) * HistTexel<HF>::B);
+        }
+    }
+    cp_async_commit();
+
+    // own history position and taps
+    float u = div_const_rn((float)cx + 0.5f, (float)W, a.inv_out_w);
+    float v = div_const_rn((float)cy + 0.5f, (float)H, a.inv_out_h);
+    float hu, hv, ehd;
+    history_position<Pol, MC, HOT>(U, a, M, cx, cy, vs, depth, u, v, hu, hv, ehd);
+    HistoryTaps<Pol, INTERP> taps;
+    taps.setup(hu, hv, hi.w, hi.h);
+    float prev_depth = 0.f;
+    const bool depth_cull = P.mDepthCulling != 0;
+    if (depth_cull && a.history_depth.p) {
+        int tx_ = clampi(trunc_index(hu * (float)a.color.w), 0, a.color.w - 1);
+        int ty_ = clampi(trunc_index(hv * (float)a.color.h), 0, a.color.h - 1);
+        prev_depth = __ldg(texel_ptr<float>(a.history_depth, tx_, ty_));
+    }
+
+    // 3. staged colour in the policy's working format, then the 3x3 box
+    const bool tm = M.tonemap(), yc = M.ycocg();
+    s_col[tid] = Pol::stage(st0, tm, yc);
+    if (tid + NT < NS) s_col[tid + NT] = Pol::stage(st1, tm, yc);
+    __syncthreads();
+    typename Pol::Box box;
+    Pol::template box<HOT>(&s_col[(ly + 1) * SX + lx + 1], SX, M, P.mVarClipGamma, box);
+    if (Pol::kExactCentre) Pol::centre_colour(box, a.color, cx, cy, tm, yc);
+
+    cp_async_wait_all();
+    __syncthreads();
+    if (!inside) return;
+
+    // 4. history sample: from the window when all taps fall inside it
+    float4 hraw = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (have_hist) {
+        const int span = INTERP == 2 ? 4 : 2;
+        const int bx = taps.t[0].ux - wx0, by = taps.t[0].uy - wy0;
+        const bool in_win = windowed && bx >= 0 && by >= 0 && bx + span <= WW && by + span <= WH;
+        if (in_win) {
+            const HT* base = &s_win[by * WW + bx];
+            hraw = Pol::template filter_window<INTERP, HF>(taps, base, WW);
+        } else {
+            hraw = Pol::template filter<INTERP>(taps, [&](int tx_, int ty_) { return fetch_history<HF>(hi, tx_, ty_); });
+        }
+    }
+
+    bool rejected = false;
+    if (P.mRejectOutside && (hu < 0.f || hv < 0.f || hu >= 1.f || hv >= 1.f)) rejected = true;
+    if (depth_cull) {
+        float hd = prev_depth;
+        if (fabsf(hd - ehd) > 0.1f * (1.0f - hd)) rejected = true;
+    }
+    float4 o = Pol::template finish<HOT>(U, P, M, box, hraw, u, v, hu, hv, rejected);
+    store_history<HF>(a.history_out, x, y, make_float4(o.x, o.y, o.z, 0.f));
+    if (a.result.p) {
+        if (tm) o = Pol::un_tonemap(o);
+        store_rgba16f(a.result, x, y, make_float4(o.x, o.y, o.z, 1.0f));
+    }
+}
+
+template <class Pol, int HF, int MC, int INTERP, bool HOT>
+cudaError_t launch_tile(const taa_uniforms_t& U, const FrameArgs& a, cudaStream_t s) {
+    dim3 grid((a.out_w + TX - 1) / TX, (a.out_h + TY - 1) / TY);
+    resolve_tile<Pol, HF, MC, INTERP, HOT><<<grid, NT, 0, s>>>(U, a);
+    return cudaGetLastError();
+}
+
+template <class Pol, int HF, int MC>
+cudaError_t launch_interp(int interp, const taa_uniforms_t& U, const FrameArgs& a, cudaStream_t s) {
+    const bool hot = is_hot(U.param[0]);
+    switch (interp) {
+        case 0: return hot ? launch_tile<Pol, HF, MC, 0, true>(U, a, s) : launch_tile<Pol, HF, MC, 0, false>(U, a, s);
+        case 1: return hot ? launch_tile<Pol, HF, MC, 1, true>(U, a, s) : launch_tile<Pol, HF, MC, 1, false>(U, a, s);
+        default: return hot ? launch_tile<Pol, HF, MC, 2, true>(U, a, s) : launch_tile<Pol, HF, MC, 2, false>(U, a, s);
+    }
+}
+
+template <class Pol>
+cudaError_t launch_form(int history_fmt, int motion_ch, int interp, const taa_uniforms_t& U, const FrameArgs& a,
+                        cudaStream_t s) {
+    if (history_fmt == 0)
+        return motion_ch == 4 ? launch_interp<Pol, 0, 4>(interp, U, a, s) : launch_interp<Pol, 0, 2>(interp, U, a, s);
+    return motion_ch == 4 ? launch_interp<Pol, 1, 4>(interp, U, a, s) : launch_interp<Pol, 1, 2>(interp, U, a, s);
+}
+
+}  // namespace tiled
+}  // namespace taa_dev

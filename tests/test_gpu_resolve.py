@@ -17,7 +17,7 @@ import pytest
 import oracle as O
 import taa_abi as T
 import workloads as WL
-from helpers import cpu_frames, gpu_resolve, half_ulp, max_rel
+from helpers import cpu_frames, gpu_resolve, half_ulp, max_rel, psnr, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -249,3 +249,26 @@ def test_gpu_renderer_matches_fp64_scene(cuda):
         assert np.mean(np.all(np.abs(m - ref["motion"].astype(np.float16)) <= 2 * half_ulp(ref["motion"]), -1)) > 0.99
         t = tru.cpu().numpy()
         assert np.mean(np.abs(t - ref["truth"]) <= 1e-3 * np.maximum(1, np.abs(ref["truth"]))) > 0.99
+
+
+FP16_MODES = ["base", "c2", "bilinear", "bspline", "clamp_rgb", "clip_slow_shaped", "shrink_chroma",
+              "tonemap_lottes", "reduce_blend_velalpha", "closest_velocity"]
+
+
+@pytest.mark.parametrize("mode", FP16_MODES)
+def test_fp16_form_frame_error_vs_fp64(cuda, mode):
+    """The FP16 form's contract: per frame, relative L2 error <= 1e-3 and
+    PSNR >= 50 dB against the FP64 oracle fed the same history."""
+    w, h = 96, 64
+    wl = WL.small(w, h, frames=2, params=MODES[mode])
+    fr = cpu_frames(wl, range(2))
+    hist = np.ascontiguousarray(fr[0]["color"].astype(np.float32))
+    u = T.make_uniforms(wl.parameters(), jitter_ndc=fr[1]["jitter"])
+    ref = oracle_for(u, fr[1], fr[0], hist, precision=64)
+    ctx = T.Taa(w, h, form=T.TAA_FORM_FP16)
+    ctx.set_uniforms(u)
+    assert ctx.selected_form() == T.TAA_FORM_FP16
+    out = gpu_resolve(ctx, cuda, fr[1]["color"], fr[1]["depth"], fr[1]["motion"], hist, fr[0]["depth"])
+    got, want = out["history_out"][..., :3], ref["history"][..., :3]
+    assert rel_l2(got, want) <= 1e-3, rel_l2(got, want)
+    assert psnr(got, want) >= 50.0
