@@ -47,11 +47,10 @@ __device__ __forceinline__ float gmax(float a, float b) { return a < b ? b : a; 
 __device__ __forceinline__ float gmin(float a, float b) { return b < a ? b : a; }
 __device__ __forceinline__ float gclamp(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
 
-// ivec2(float) made total (NaN -> large negative, clamped by the caller).
+// ivec2(float) made total: truncation toward zero of t held in [-1e9, 1e9]
+// (NaN gives -1e9); the caller clamps the index to the image.
 __device__ __forceinline__ int trunc_index(float t) {
-    if (!(t > -1e9f)) return -1000000000;
-    if (t > 1e9f) return 1000000000;
-    return (int)t;
+    return __float2int_rz(fminf(fmaxf(t, -1e9f), 1e9f));
 }
 
 template <class T> __device__ __forceinline__ const T* texel_ptr(const Img& im, int x, int y) {

@@ -31,6 +31,10 @@ namespace taa_dev {
 namespace tiled {
 
 constexpr int TX = 32, TY = 8, NT = TX * TY;
+// resident CTAs per SM the register budget is sized for (a tuning constant)
+#ifndef TAA_TILE_MIN_BLOCKS
+#define TAA_TILE_MIN_BLOCKS 6
+#endif
 constexpr int SX = TX + 2, SY = TY + 2, NS = SX * SY;  // staged colour with halo
 constexpr int WIN_MARGIN = 3;                          // motion difference (px) the window absorbs
 constexpr int WW = TX + 3 + 2 * WIN_MARGIN;            // history window width  (texels)
@@ -141,7 +145,7 @@ __device__ __forceinline__ void history_position(const taa_uniforms_t& U, const 
 // The resolve kernel.  Pol provides the working colour format and the box,
 // tap, filter and finishing arithmetic (see resolve_tiled.cu, resolve_half.cu).
 template <class Pol, int HF, int MC, int INTERP, bool HOT>
-__global__ void __launch_bounds__(NT, 4) resolve_tile(const taa_uniforms_t U, const FrameArgs a) {
+__global__ void __launch_bounds__(NT, TAA_TILE_MIN_BLOCKS) resolve_tile(const taa_uniforms_t U, const FrameArgs a) {
     using HT = typename HistTexel<HF>::T;
     using Staged = typename Pol::Staged;
     __shared__ Staged s_col[NS];
@@ -180,16 +184,17 @@ __global__ void __launch_bounds__(NT, 4) resolve_tile(const taa_uniforms_t U, co
     const bool windowed = have_hist && INTERP != 1;
     int wx0 = 0, wy0 = 0;
     if (windowed) {
+        // only the first tap's integer coordinate of the reference pixel is needed
         float ru = div_const_rn((float)rx + 0.5f, (float)W, a.inv_out_w);
         float rv = div_const_rn((float)ry + 0.5f, (float)H, a.inv_out_h);
         float rhu, rhv, rehd;
         history_position<Pol, MC, HOT>(U, a, M, rx, ry, rvs, rdepth, ru, rv, rhu, rhv, rehd);
-        Taps rt;
-        if (INTERP == 2) Pol::catmullrom_taps(rhu, rhv, hi.w, hi.h, rt);
-        else Pol::bilinear_taps(rhu, rhv, hi.w, hi.h, rt);
-        // the reference pixel sits at (TX/2, TY/2) of the tile
-        wx0 = rt.ux - (rx - x0) - WIN_MARGIN;
-        wy0 = rt.uy - (ry - y0) - WIN_MARGIN;
+        const int k0 = INTERP == 2 ? 1 : 0;  // Catmull-Rom starts one texel before floor(p - 0.5)
+        int rux = trunc_index(floorf(rhu * (float)hi.w - 0.5f)) - k0;
+        int ruy = trunc_index(floorf(rhv * (float)hi.h - 0.5f)) - k0;
+        // the reference pixel sits at (rx - x0, ry - y0) in the tile
+        wx0 = rux - (rx - x0) - WIN_MARGIN;
+        wy0 = ruy - (ry - y0) - WIN_MARGIN;
         const int lane = tid & 31, warp = tid >> 5;
         for (int r = warp; r < WH; r += NT / 32) {
             const int gy = clampi(wy0 + r, 0, hi.h - 1);
