@@ -1,0 +1,77 @@
+"""Builds oracle/_ref: the reference's own code for the resolve path, compiled here.
+
+Test infrastructure: these libraries pin the oracle's restatement; nothing in
+the product loads them, and they exist only where the reference tree is
+present (they are not built on the GPU machine).
+
+  * libtaa_ref32.so / libtaa_ref64.so - shaders/taa.comp and
+    shaders/sharpen.comp compiled as C++ through oracle/ref_shim/glsl_shim.hpp
+    with REAL = float / double.  The shader text is copied into oracle/_ref
+    with three mechanical rewrites only: the `#version` and `#extension` lines
+    are dropped (C++ has no such directives) and `out T name` / `inout T name`
+    parameters become `T &name` (C++ spells out-parameters as references).
+  * libcas_ref.so - CasSetup from shaders/ffx_cas.h with ffx_a.h's CPU path
+    (A_CPU), exactly as source/taa.hpp:15-19 compiles it.
+"""
+from __future__ import annotations
+
+import re
+import shutil
+import subprocess
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent
+REF = Path("/root/reference")
+SHADERS = REF / "shaders"
+OUT = HERE / "_ref"
+SHIM = HERE / "ref_shim"
+
+
+def available() -> bool:
+    return (SHADERS / "taa.comp").exists() and (SHADERS / "ffx_cas.h").exists()
+
+
+def rewrite(src: Path, dst: Path) -> None:
+    text = src.read_text()
+    lines = [ln for ln in text.splitlines() if not re.match(r"\s*#\s*(version|extension)\b", ln)]
+    text = "\n".join(lines) + "\n"
+    text = re.sub(r"\b(?:inout|out)\s+(\w+)\s+(\w+)\b", r"\1 &\2", text)
+    dst.write_text(text)
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference build failed:\n" + " ".join(map(str, cmd)) + "\n" + r.stdout + r.stderr)
+
+
+def build(force: bool = False):
+    if not available():
+        return None
+    OUT.mkdir(exist_ok=True)
+    taa = OUT / "taa_comp.glsl.inc"
+    sharpen = OUT / "sharpen_comp.glsl.inc"
+    rewrite(SHADERS / "taa.comp", taa)
+    rewrite(SHADERS / "sharpen.comp", sharpen)
+    cxx = shutil.which("g++") or "c++"
+    common = [cxx, "-O1", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+              "-Wno-pedantic", "-I", str(SHIM), "-I", str(SHADERS), "-I", str(ROOT / "include"),
+              f'-DTAA_COMP_SOURCE="{taa}"', f'-DSHARPEN_SOURCE="{sharpen}"', str(SHIM / "taa_ref_main.cpp")]
+    libs = {}
+    for name, flags in (("libtaa_ref32.so", ["-DREAL=float", "-fsingle-precision-constant"]),
+                        ("libtaa_ref64.so", ["-DREAL=double"])):
+        lib = OUT / name
+        if force or not lib.exists() or lib.stat().st_mtime < max(p.stat().st_mtime for p in SHIM.iterdir()):
+            _run([*common, *flags, "-o", str(lib)])
+        libs[name] = lib
+    cas = OUT / "libcas_ref.so"
+    if force or not cas.exists():
+        _run([cxx, "-O1", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-I", str(SHADERS),
+              str(SHIM / "cas_setup_ref.cpp"), "-o", str(cas)])
+    libs["libcas_ref.so"] = cas
+    return libs
+
+
+if __name__ == "__main__":
+    print(build(force=True))
