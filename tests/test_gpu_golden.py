@@ -50,15 +50,16 @@ def gpu(key, form, dev):
              prev_segmask=t(g("prev_segmask").view(np.int32), torch.int32), uvnrm=t(g("uvnrm"), torch.float32),
              history_out=torch.full((oh, ow, 4), float("nan"), device=dev),
              result=torch.full((oh, ow, 4), float("nan"), dtype=torch.float16, device=dev),
-             # a debug binding routes the call to the plain form, so only that form gets one
+             # debug and segmask bindings route a call to the plain form, so only that form gets them
              debug=torch.full((oh, ow, 4), float("nan"), dtype=torch.float16, device=dev)
              if form == T.TAA_FORM_PLAIN else None,
-             segmask=torch.zeros((oh, ow), dtype=torch.int32, device=dev))
+             segmask=torch.zeros((oh, ow), dtype=torch.int32, device=dev) if form == T.TAA_FORM_PLAIN else None)
     used = ctx.selected_form()
     ctx.resolve(**b)
     torch.cuda.synchronize()
     ctx.close()
-    return used, b["history_out"].cpu().numpy(), b["segmask"].cpu().numpy().view(np.uint32)
+    seg = b["segmask"].cpu().numpy().view(np.uint32) if b["segmask"] is not None else None
+    return used, b["history_out"].cpu().numpy(), seg
 
 
 def oracle32(key):
