@@ -26,6 +26,13 @@ CASES = [str(c) for c in FIX["cases"]]
 TRANSCENDENTAL = ("noise", "segmask_all_tests", "segmask_no_history_count", "segmask_fixed_border", "debug_8")
 
 
+def rel_bound(key):
+    # taa.comp:551-556 hashes with fract(sin(x) * 43758.5453): one ulp of sin
+    # moves the noise anywhere within its amplitude (2 * mNoiseFactor = 2/510),
+    # so CUDA's and libm's sinf differ by up to that much per pixel
+    return 3e-3 if key.endswith(":noise") else 1e-5
+
+
 def uniforms_of(key):
     u = T.Uniforms()
     C.memmove(C.addressof(u), FIX[f"{key}/uniforms"].tobytes(), C.sizeof(u))
@@ -77,7 +84,7 @@ def test_plain_form_on_reference_fixtures(cuda, key):
     assert used == T.TAA_FORM_PLAIN
     ref32 = FIX[f"{key}/ref32_history"].astype(np.float64)
     rel = np.linalg.norm(hist - ref32) / max(np.linalg.norm(ref32), 1e-30)
-    assert rel <= 1e-5, rel
+    assert rel <= rel_bound(key), rel
     name = key.split(":")[1]
     if name.startswith("segmask"):
         assert np.mean(seg == FIX[f"{key}/ref64_segmask"]) >= 0.99
@@ -90,6 +97,6 @@ def test_tiled_form_on_reference_fixtures(cuda, key):
     used, hist, _ = gpu(key, T.TAA_FORM_TILED, cuda)
     ref32 = FIX[f"{key}/ref32_history"].astype(np.float64)
     rel = np.linalg.norm(hist - ref32) / max(np.linalg.norm(ref32), 1e-30)
-    assert rel <= 1e-5, (used, rel)
+    assert rel <= rel_bound(key), (used, rel)
     if used == T.TAA_FORM_TILED:
         np.testing.assert_array_equal(hist, oracle32(key)["history"].astype(np.float32))
