@@ -1,0 +1,35 @@
+"""The C++ mirror of taa<CF> (taa-star_gb300/taa.hpp): it compiles against the
+C ABI (CPU) and drives a short synthetic sequence on the GPU (-m gpu)."""
+import subprocess
+from pathlib import Path
+
+import pytest
+
+import build as lib_build
+
+ROOT = Path(__file__).resolve().parent.parent
+SRC = ROOT / "taa-star_gb300" / "examples" / "sequence.cpp"
+
+
+def compile_example(tmp_path):
+    lib = lib_build.build_library()
+    exe = tmp_path / "sequence"
+    cmd = [lib_build.nvcc(), "-std=c++17", "-O2", "-x", "cu", str(SRC), "-o", str(exe), "-L", str(lib.parent),
+           "-ltaa_gb300", f"-Xlinker=-rpath,{lib.parent}"]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    return exe
+
+
+def test_mirror_compiles(built, tmp_path):
+    assert compile_example(tmp_path).exists()
+
+
+@pytest.mark.gpu
+def test_mirror_runs_a_sequence(cuda, tmp_path):
+    exe = compile_example(tmp_path)
+    r = subprocess.run([str(exe), "160", "96", "6"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = [l for l in r.stdout.splitlines() if l.startswith("frame")]
+    assert len(lines) == 6
+    means = [float(l.split()[-1]) for l in lines]
+    assert all(0.0 < m < 64.0 for m in means)
