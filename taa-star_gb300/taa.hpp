@@ -205,6 +205,7 @@ template <size_t CF> class taa {
             io.sharpened = mSharpened[cur].ptr;
             io.sharpened_pitch = mSharpened[cur].pitch;
         }
+        mShowSharpened[cur] = mSharpener != TAA_SHARPEN_OFF;
         cudaEventRecord(mT0, stream);
         check(taa_resolve(mCtx, stream, &io));
         cudaEventRecord(mT1, stream);
@@ -222,7 +223,7 @@ template <size_t CF> class taa {
 
     // the image to show for a frame: the sharpened one with a sharpener (taa.hpp:1137)
     const Image& result(uint64_t frameId) const {
-        return mSharpener != TAA_SHARPEN_OFF && mHaveHistory ? mSharpened[frameId % CF] : mResult[frameId % CF];
+        return mShowSharpened[frameId % CF] ? mSharpened[frameId % CF] : mResult[frameId % CF];
     }
     const Image& history(uint64_t frameId) const { return mHistory[frameId % CF]; }
     taa_ctx* context() const { return mCtx; }
@@ -233,6 +234,7 @@ template <size_t CF> class taa {
             throw std::runtime_error("taa: cudaMallocPitch failed");
     }
     void copy_source(size_t cur, cudaStream_t s) {
+        mShowSharpened[cur] = false;  // nothing was sharpened for this frame
         if (mUpsampling) return;  // the reference blits with scaling; a headless caller reads the source itself
         cudaMemcpy2DAsync(mResult[cur].ptr, mResult[cur].pitch, mSrcColor[cur].ptr, mSrcColor[cur].pitch,
                           (size_t)mOut[0] * 8, (size_t)mOut[1], cudaMemcpyDeviceToDevice, s);
@@ -264,6 +266,7 @@ template <size_t CF> class taa {
     bool mOldParamsValid = false;
     bool mHaveHistory = false;
     bool mFirstResolve = true;
+    std::array<bool, CF> mShowSharpened{};
     uint32_t mCtxSharpener = TAA_SHARPEN_OFF;
     float mCtxSharpenFactor = 0.5f;
     cudaEvent_t mT0 = nullptr, mT1 = nullptr;

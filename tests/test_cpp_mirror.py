@@ -32,4 +32,4 @@ def test_mirror_runs_a_sequence(cuda, tmp_path):
     lines = [l for l in r.stdout.splitlines() if l.startswith("frame")]
     assert len(lines) == 6
     means = [float(l.split()[-1]) for l in lines]
-    assert all(0.0 < m < 64.0 for m in means)
+    assert all(0.0 < m < 64.0 for m in means), r.stdout
