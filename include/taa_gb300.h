@@ -178,6 +178,35 @@ int taa_selected_form(const taa_ctx* ctx);
  * overlap. */
 int taa_resolve(taa_ctx* ctx, void* stream, const taa_frame_io_t* io);
 
+/* Largest out_width * out_height that taa_resolve_static_scratch accepts when
+ * it needs its buffer: one 3840x2160 RGBA16F screen image, 66,355,200 bytes
+ * per device, set aside when the CUDA runtime loads the library's device code. */
+#define TAA_STATIC_SCRATCH_MAX_TEXELS (3840 * 2160)
+
+/* taa_resolve with the given sharpener, for callers that may not allocate
+ * device memory.  No counterpart in the reference: it exists for hosts that
+ * own every byte of device memory themselves - an engine that sizes one pool
+ * at load time and hands out only images from it (or images imported from
+ * Vulkan), or a frame loop where cudaMalloc/cudaFree would stall or
+ * synchronise the device.  taa_create with TAA_SHARPEN_OFF allocates no device
+ * memory; with a sharpener it allocates the screen image that the plain form
+ * hands from its resolve to its sharpen pass when io->result is NULL.  Create
+ * the context with TAA_SHARPEN_OFF and name the sharpener here instead: when
+ * the call runs the plain form with a sharpener and no result binding, that
+ * screen image lives in a fixed buffer inside the library, and nothing is
+ * allocated.  Otherwise the call is taa_resolve with the sharpener given.
+ *  - The first call on each device looks the buffer up (cudaGetSymbolAddress,
+ *    on the current device); make it before any stream capture.
+ *  - The buffer holds TAA_STATIC_SCRATCH_MAX_TEXELS texels: a call that needs
+ *    it for a larger output returns TAA_E_INVAL (bind io->result instead).
+ *  - One buffer per device: calls that overlap on the same device (two
+ *    streams, or two host threads) race on it.  Calls queued on one stream
+ *    do not.
+ *  - Nothing needs to start at zero: the resolve writes the whole screen image
+ *    before the sharpen pass reads it. */
+int taa_resolve_static_scratch(taa_ctx* ctx, void* stream, const taa_frame_io_t* io,
+                               uint32_t sharpener, float factor);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

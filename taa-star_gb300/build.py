@@ -34,6 +34,7 @@ UNITS = {
     "resolve_tiled.cu": ["-fmad=false"],
     "resolve_half.cu": [],
     "synth.cu": [],
+    "static_scratch.cu": [],
     "capi.cpp": [],
 }
 

@@ -467,6 +467,39 @@ int taa_resolve(taa_ctx* c, void* stream, const taa_frame_io_t* io) {
     return ok();
 }
 
+// taa_resolve on a copy of the context that carries the given sharpener and,
+// where the plain form needs a screen image between its two passes, the
+// library's fixed buffer (static_scratch.cu) instead of an allocated one.
+int taa_resolve_static_scratch(taa_ctx* c, void* stream, const taa_frame_io_t* io, uint32_t sharpener, float factor) {
+    if (!c || !io) return fail(TAA_E_INVAL, "taa_resolve_static_scratch: NULL argument");
+    if (!c->have_uniforms) return fail(TAA_E_INVAL, "taa_resolve_static_scratch: taa_set_uniforms was not called");
+    if (sharpener > TAA_SHARPEN_CAS) return fail(TAA_E_INVAL, "taa_resolve_static_scratch: sharpener %u", sharpener);
+    if (!finite(factor)) return fail(TAA_E_INVAL, "taa_resolve_static_scratch: factor not finite");
+    taa_ctx v = *c;
+    const int ow = v.desc.out_width, oh = v.desc.out_height;
+    v.desc.sharpener = sharpener;
+    v.desc.sharpen_factor = factor;
+    taa_cas_setup(factor, (float)ow, (float)oh, (float)ow, (float)oh, v.cas_const0, v.cas_const1);
+    v.scratch_screen = nullptr;
+    v.scratch_pitch = 0;
+    if (sharpener != TAA_SHARPEN_OFF && !io->result && select_form(&v, io) == TAA_FORM_PLAIN) {
+        const size_t texels = (size_t)ow * (size_t)oh;
+        if (texels > (size_t)TAA_STATIC_SCRATCH_MAX_TEXELS)
+            return fail(TAA_E_INVAL,
+                        "taa_resolve_static_scratch: a %dx%d screen image (%zu texels) exceeds the static buffer "
+                        "of %d texels; bind io->result or use taa_resolve",
+                        ow, oh, texels, TAA_STATIC_SCRATCH_MAX_TEXELS);
+        void* p = nullptr;
+        size_t bytes = 0;
+        cudaError_t e = taa_dev::static_screen_scratch(&p, &bytes);
+        if (e != cudaSuccess) return cuda_fail(e, "taa_resolve_static_scratch: cudaGetSymbolAddress");
+        if (bytes < texels * 8) return fail(TAA_E_INVAL, "taa_resolve_static_scratch: static buffer too small");
+        v.scratch_screen = p;
+        v.scratch_pitch = (size_t)ow * 8;
+    }
+    return taa_resolve(&v, stream, io);
+}
+
 // ---------------------------------------------------------------- synthetic scene
 
 int taa_synth_default_scene(taa_synth_scene_t* o, int32_t w, int32_t h, uint64_t seed) {

@@ -37,6 +37,10 @@ cudaError_t launch_resolve_half(int history_fmt, int motion_ch, int interp, cons
 // Standalone sharpen passes on an RGBA16F image (used after the plain form).
 cudaError_t launch_sharpen(int sharpener, const FrameArgs& a, cudaStream_t stream);
 
+// Device address and size of the fixed screen buffer of static_scratch.cu on
+// the current device (looked up once per device).
+cudaError_t static_screen_scratch(void** address, size_t* bytes);
+
 // Synthetic renderer (synth.cu).
 cudaError_t launch_synth(const taa_synth_scene_t& s, const float* host_spheres, int frame,
                          const taa_synth_frame_t& out, cudaStream_t stream);

@@ -111,6 +111,7 @@ assert C.sizeof(Parameters) == 176 and C.sizeof(Uniforms) == 544
 EXPORTS = ["taa_version", "taa_last_error", "taa_default_parameters", "taa_get_jitter_offset",
            "taa_jittered_projection", "taa_compose_matrices", "taa_cas_setup", "taa_create", "taa_destroy",
            "taa_set_uniforms", "taa_set_sharpener", "taa_selected_form", "taa_resolve",
+           "taa_resolve_static_scratch",
            "taa_synth_default_scene", "taa_synth_spheres", "taa_synth_jitter", "taa_synth_camera",
            "taa_synth_render"]
 
@@ -142,6 +143,7 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
         "taa_set_sharpener": (C.c_int, [C.c_void_p, C.c_uint32, C.c_float]),
         "taa_selected_form": (C.c_int, [C.c_void_p]),
         "taa_resolve": (C.c_int, [C.c_void_p, C.c_void_p, P(FrameIO)]),
+        "taa_resolve_static_scratch": (C.c_int, [C.c_void_p, C.c_void_p, P(FrameIO), C.c_uint32, C.c_float]),
         "taa_synth_default_scene": (C.c_int, [P(SynthScene), C.c_int32, C.c_int32, C.c_uint64]),
         "taa_synth_spheres": (C.c_int, [P(SynthScene), P(C.c_float), C.c_int32]),
         "taa_synth_jitter": (C.c_int, [P(SynthScene), C.c_int32, P(C.c_float), P(C.c_float)]),
