@@ -20,8 +20,9 @@
  *    History is RGBA32F (default; an FP32 accumulator) or RGBA16F (reference).
  *  - Calls are asynchronous on the given CUDA stream (a cudaStream_t passed
  *    as void*; NULL is the legacy default stream).  No call allocates device
- *    memory after taa_create and none synchronises the host, so a sequence of
- *    taa_resolve calls can be captured into a CUDA graph.
+ *    memory after taa_create and no resolve call synchronises the host (only
+ *    taa_device_status waits for the device), so a sequence of taa_resolve
+ *    calls can be captured into a CUDA graph.
  *  - Return value 0 (TAA_OK) on success, a negative taa_status otherwise; the
  *    message of the last failure on the calling thread is in taa_last_error().
  *    The reference has no error path (it asserts, source/taa.hpp:153,237,903).
@@ -177,6 +178,16 @@ int taa_selected_form(const taa_ctx* ctx);
  * source/taa.hpp:1125/1134).  `io->history` and `io->history_out` must not
  * overlap. */
 int taa_resolve(taa_ctx* ctx, void* stream, const taa_frame_io_t* io);
+
+/* Bits of the device status word (taa_device_status). */
+#define TAA_DEVICE_WINDOW_TIMEOUT 0x1u /* a history-window copy did not land within its bounded wait */
+
+/* Read (and with clear != 0, reset) the device status word of the current
+ * device.  Kernels never spin without bound: a wait that gives up sets a bit
+ * here and leaves the affected pixels unwritten instead of hanging.  This
+ * call waits for the device (a synchronous read); it has no counterpart in
+ * the reference, whose shaders do not wait. */
+int taa_device_status(uint32_t* bits, int clear);
 
 /* Largest out_width * out_height that taa_resolve_static_scratch accepts when
  * it needs its buffer: one 3840x2160 RGBA16F screen image, 66,355,200 bytes

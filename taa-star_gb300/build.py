@@ -35,6 +35,7 @@ UNITS = {
     "resolve_half.cu": [],
     "synth.cu": [],
     "static_scratch.cu": [],
+    "device_state.cu": [],
     "capi.cpp": [],
 }
 
@@ -82,7 +83,8 @@ def build_library(force: bool = False, verbose: bool = False, ptxas_info: bool =
                 print(" ".join(cmd), file=sys.stderr)
         list(ex.map(_run, jobs))
     if force or jobs or not LIB.exists():
-        _run([cc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart_static", "-lrt", "-ldl", "-lpthread"])
+        _run([cc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart_static", "-lrt", "-ldl", "-lpthread",
+              "-Xlinker", "--no-undefined"])
     return LIB
 
 

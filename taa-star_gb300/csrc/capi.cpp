@@ -439,6 +439,9 @@ int taa_resolve(taa_ctx* c, void* stream, const taa_frame_io_t* io) {
     a.inv_out_h = 1.0f / (float)oh;
     a.cas_peak_bits = c->cas_const1[0];
     a.sharpen_factor = d.sharpen_factor;
+    a.neg_zero2 = taa_dev::kNegZeroPair;
+    cudaError_t se = taa_dev::device_status_word(&a.status);
+    if (se != cudaSuccess) return cuda_fail(se, "taa_resolve: device status word");
 
     cudaStream_t s = (cudaStream_t)stream;
     int form = select_form(c, io);
@@ -498,6 +501,22 @@ int taa_resolve_static_scratch(taa_ctx* c, void* stream, const taa_frame_io_t* i
         v.scratch_pitch = (size_t)ow * 8;
     }
     return taa_resolve(&v, stream, io);
+}
+
+int taa_device_status(uint32_t* bits, int clear) {
+    if (!bits) return fail(TAA_E_INVAL, "taa_device_status: NULL argument");
+    unsigned int* w = nullptr;
+    cudaError_t e = taa_dev::device_status_word(&w);
+    if (e != cudaSuccess) return cuda_fail(e, "taa_device_status: device status word");
+    unsigned int v = 0;
+    e = cudaMemcpy(&v, w, sizeof v, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "taa_device_status: read");
+    if (clear && v) {
+        e = cudaMemset(w, 0, sizeof v);
+        if (e != cudaSuccess) return cuda_fail(e, "taa_device_status: clear");
+    }
+    *bits = v;
+    return ok();
 }
 
 // ---------------------------------------------------------------- synthetic scene

@@ -38,7 +38,12 @@ struct FrameArgs {
     float inv_out_w, inv_out_h;  // correctly rounded 1/out size
     uint32_t cas_peak_bits;      // CasSetup const1.x
     float sharpen_factor;
+    unsigned int* status;        // device status word (bounded waits that gave up set bits)
+    uint64_t neg_zero2;          // the FP32 pair (-0.0, -0.0), opaque to the compiler (f32x2.cuh)
 };
+
+// Bits of the device status word.
+constexpr unsigned int kStatusWindowTimeout = 1u;  // a history-window copy did not complete in time
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 

@@ -1,7 +1,9 @@
 // kernels.h - launchers of the device kernels (internal to the library).
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include "common.cuh"
+#include "f32x2.cuh"
 #include "../../include/taa_synth.h"
 
 namespace taa_dev {
@@ -40,6 +42,13 @@ cudaError_t launch_sharpen(int sharpener, const FrameArgs& a, cudaStream_t strea
 // Device address and size of the fixed screen buffer of static_scratch.cu on
 // the current device (looked up once per device).
 cudaError_t static_screen_scratch(void** address, size_t* bytes);
+
+// Address of the device status word on the current device (device_state.cu).
+cudaError_t device_status_word(unsigned int** out);
+
+// Tensor map of a history image for box_w x box_h texel window copies;
+// false when the image cannot be a TMA source (alignment, driver entry point).
+bool encode_history_map(const Img& history, int history_fmt, int box_w, int box_h, CUtensorMap* map);
 
 // Synthetic renderer (synth.cu).
 cudaError_t launch_synth(const taa_synth_scene_t& s, const float* host_spheres, int frame,

@@ -18,19 +18,18 @@
 // and PSNR), not bit parity.
 #include <cuda_fp16.h>
 
-#include "tiled_skeleton.cuh"
+#include "history_filter.cuh"
 #include "kernels.h"
 
 namespace taa_dev {
 namespace {
 
 using tiled::C3;
-using tiled::Taps;
 
 __device__ __forceinline__ __half2 u2h(uint32_t v) { return *reinterpret_cast<__half2*>(&v); }
 __device__ __forceinline__ uint32_t h2u(__half2 v) { return *reinterpret_cast<uint32_t*>(&v); }
 
-struct HalfPol {
+struct HalfPol : tiled::HistoryFilter {
     using Staged = uint2;  // (Y, Co), (Cg, 0) as half2 - or (R, G), (B, 0)
     struct Box {
         __half2 c0a, c0b, lo_a, lo_b, hi_a, hi_b, ct_a, ct_b;
@@ -73,7 +72,8 @@ struct HalfPol {
     }
 
     template <bool HOT>
-    static __device__ __forceinline__ void box(const uint2* nb, int ns, const tiled::Mode<HOT>& M, float g, Box& b) {
+    static __device__ __forceinline__ void box(const uint2* nb, int ns, const tiled::Mode<HOT>& M, float g, Box& b,
+                                               f2 /*unused*/) {
         const int off[8] = {-ns - 1, -ns, -ns + 1, -1, 1, ns - 1, ns, ns + 1};
         const uint2 cc = nb[0];
         const __half2 c0a = u2h(cc.x), c0b = u2h(cc.y);
@@ -178,138 +178,6 @@ struct HalfPol {
         hu = (hs[0] * r) * 0.5f + 0.5f;
         hv = (hs[1] * r) * 0.5f + 0.5f;
         ehd = hs[2] * r;
-    }
-
-    static __device__ __forceinline__ void catmullrom_taps(float u, float v, int w, int h, Taps& t) {
-        float itx = u * (float)w, ity = v * (float)h;
-        float bx = floorf(itx - 0.5f), by = floorf(ity - 0.5f);
-        float fx = itx - (bx + 0.5f), fy = ity - (by + 0.5f);
-        {
-            float f2 = fx * fx, f3 = f2 * fx;
-            t.wx[0] = -0.5f * f3 + f2 - 0.5f * fx;
-            t.wx[1] = 1.5f * f3 - 2.5f * f2 + 1.0f;
-            t.wx[2] = -1.5f * f3 + 2.0f * f2 + 0.5f * fx;
-            t.wx[3] = 0.5f * f3 - 0.5f * f2;
-        }
-        {
-            float f2 = fy * fy, f3 = f2 * fy;
-            t.wy[0] = -0.5f * f3 + f2 - 0.5f * fy;
-            t.wy[1] = 1.5f * f3 - 2.5f * f2 + 1.0f;
-            t.wy[2] = -1.5f * f3 + 2.0f * f2 + 0.5f * fy;
-            t.wy[3] = 0.5f * f3 - 0.5f * f2;
-        }
-        int kx = trunc_index(bx), ky = trunc_index(by);
-        t.ux = kx - 1;
-        t.uy = ky - 1;
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            t.xs[i] = clampi(kx - 1 + i, 0, w - 1);
-            t.ys[i] = clampi(ky - 1 + i, 0, h - 1);
-        }
-    }
-    static __device__ __forceinline__ void bilinear_taps(float u, float v, int w, int h, Taps& t) {
-        float px = u * (float)w - 0.5f, py = v * (float)h - 0.5f;
-        float fx0 = floorf(px), fy0 = floorf(py);
-        float fx = px - fx0, fy = py - fy0;
-        if (!(fx == fx)) fx = 0.f;
-        if (!(fy == fy)) fy = 0.f;
-        int x0 = trunc_index(fx0), y0 = trunc_index(fy0);
-        t.ux = x0;
-        t.uy = y0;
-        t.xs[0] = clampi(x0, 0, w - 1);
-        t.xs[1] = clampi(x0 + 1 < x0 ? x0 : x0 + 1, 0, w - 1);
-        t.ys[0] = clampi(y0, 0, h - 1);
-        t.ys[1] = clampi(y0 + 1 < y0 ? y0 : y0 + 1, 0, h - 1);
-        t.wx[0] = 1.0f - fx;
-        t.wx[1] = fx;
-        t.wy[0] = 1.0f - fy;
-        t.wy[1] = fy;
-    }
-    static __device__ __forceinline__ void bspline_positions(float u, float v, int w, int h, float s0[2], float s1[2],
-                                                             float t0[2], float t1[2]) {
-        float it[2] = {u * (float)w, v * (float)h};
-        float inv[2] = {1.0f / (float)w, 1.0f / (float)h};
-#pragma unroll
-        for (int k = 0; k < 2; ++k) {
-            float tc = floorf(it[k] - 0.5f) + 0.5f;
-            float f = it[k] - tc, f2 = f * f, f3 = f2 * f;
-            float w0 = f2 - 0.5f * (f3 + f);
-            float w1 = 1.5f * f3 - 2.5f * f2 + 1.0f;
-            float w3 = 0.5f * (f3 - f2);
-            float w2 = 1.0f - w0 - w1 - w3;
-            s0[k] = w0 + w1;
-            s1[k] = w2 + w3;
-            t0[k] = (tc - 1.0f + w1 / (w0 + w1)) * inv[k];
-            t1[k] = (tc + 1.0f + w3 / (w2 + w3)) * inv[k];
-        }
-    }
-    template <class F>
-    static __device__ __forceinline__ float4 bil(const Taps& t, F&& texel) {
-        float4 A = texel(t.xs[0], t.ys[0]), B = texel(t.xs[1], t.ys[0]);
-        float4 C = texel(t.xs[0], t.ys[1]), D = texel(t.xs[1], t.ys[1]);
-        float gx = t.wx[0], fx = t.wx[1], gy = t.wy[0], fy = t.wy[1];
-        float4 tt = make_float4(A.x * gx + B.x * fx, A.y * gx + B.y * fx, A.z * gx + B.z * fx, 0.f);
-        float4 bb = make_float4(C.x * gx + D.x * fx, C.y * gx + D.y * fx, C.z * gx + D.z * fx, 0.f);
-        return make_float4(tt.x * gy + bb.x * fy, tt.y * gy + bb.y * fy, tt.z * gy + bb.z * fy, 0.f);
-    }
-    // the same filter reading 4x4 (or 2x2) consecutive window entries
-    template <int INTERP, int HF, class HT>
-    static __device__ __forceinline__ float4 filter_window(const tiled::HistoryTaps<HalfPol, INTERP>& h, const HT* base,
-                                                           int stride) {
-        const Taps& t = h.t[0];
-        auto at = [&](int i, int j) { return tiled::to_f4<HF>(base[j * stride + i]); };
-        if (INTERP == 2) {
-            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                float rx = 0.f, ry = 0.f, rz = 0.f;
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    float4 s = at(i, j);
-                    rx = __fmaf_rn(t.wx[i], s.x, rx);
-                    ry = __fmaf_rn(t.wx[i], s.y, ry);
-                    rz = __fmaf_rn(t.wx[i], s.z, rz);
-                }
-                acc.x = __fmaf_rn(t.wy[j], rx, acc.x);
-                acc.y = __fmaf_rn(t.wy[j], ry, acc.y);
-                acc.z = __fmaf_rn(t.wy[j], rz, acc.z);
-            }
-            return acc;
-        }
-        float4 A = at(0, 0), B = at(1, 0), C = at(0, 1), D = at(1, 1);
-        float gx = t.wx[0], fx = t.wx[1], gy = t.wy[0], fy = t.wy[1];
-        float4 tt = make_float4(A.x * gx + B.x * fx, A.y * gx + B.y * fx, A.z * gx + B.z * fx, 0.f);
-        float4 bb = make_float4(C.x * gx + D.x * fx, C.y * gx + D.y * fx, C.z * gx + D.z * fx, 0.f);
-        return make_float4(tt.x * gy + bb.x * fy, tt.y * gy + bb.y * fy, tt.z * gy + bb.z * fy, 0.f);
-    }
-
-    template <int INTERP, class F>
-    static __device__ __forceinline__ float4 filter(const tiled::HistoryTaps<HalfPol, INTERP>& h, F&& texel) {
-        if (INTERP == 2) {
-            const Taps& t = h.t[0];
-            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                float rx = 0.f, ry = 0.f, rz = 0.f;
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    float4 s = texel(t.xs[i], t.ys[j]);
-                    rx = __fmaf_rn(t.wx[i], s.x, rx);
-                    ry = __fmaf_rn(t.wx[i], s.y, ry);
-                    rz = __fmaf_rn(t.wx[i], s.z, rz);
-                }
-                acc.x = __fmaf_rn(t.wy[j], rx, acc.x);
-                acc.y = __fmaf_rn(t.wy[j], ry, acc.y);
-                acc.z = __fmaf_rn(t.wy[j], rz, acc.z);
-            }
-            return acc;
-        }
-        if (INTERP == 0) return bil(h.t[0], texel);
-        float4 A = bil(h.t[0], texel), B = bil(h.t[1], texel), C = bil(h.t[2], texel), D = bil(h.t[3], texel);
-        const float *s0 = h.s0, *s1 = h.s1;
-        return make_float4((A.x * s0[0] + B.x * s1[0]) * s0[1] + (C.x * s0[0] + D.x * s1[0]) * s1[1],
-                           (A.y * s0[0] + B.y * s1[0]) * s0[1] + (C.y * s0[0] + D.y * s1[0]) * s1[1],
-                           (A.z * s0[0] + B.z * s1[0]) * s0[1] + (C.z * s0[0] + D.z * s1[0]) * s1[1], 0.f);
     }
 
     template <bool HOT>

@@ -6,16 +6,16 @@
 // second-moment chain, the Catmull-Rom accumulation) or where fusing provably
 // cannot change a result (products by powers of two), so the tiled form gives
 // the oracle's bits - the same bits as the plain form.
-#include "tiled_skeleton.cuh"
+#include "f32x2.cuh"
+#include "history_filter.cuh"
 #include "kernels.h"
 
 namespace taa_dev {
 namespace {
 
 using tiled::C3;
-using tiled::Taps;
 
-struct ExactF32 {
+struct ExactF32 : tiled::HistoryFilter {
     using Staged = float4;
     struct Box {
         C3 c0, mn, mx, ct;
@@ -45,30 +45,44 @@ struct ExactF32 {
 
     // taa.comp:259-319 on the staged neighbourhood (nb points at the centre)
     template <bool HOT>
-    static __device__ __forceinline__ void box(const float4* nb, int ns, const tiled::Mode<HOT>& M, float g, Box& b) {
+    static __device__ __forceinline__ void box(const float4* nb, int ns, const tiled::Mode<HOT>& M, float g, Box& b,
+                                               f2 z) {
         auto ld = [&](int o) { float4 t = nb[o]; return C3{t.x, t.y, t.z}; };
         const C3 c0 = ld(0), c1 = ld(-ns - 1), c2 = ld(-ns), c3 = ld(-ns + 1), c4 = ld(-1), c5 = ld(1),
                  c6 = ld(ns - 1), c7 = ld(ns), c8 = ld(ns + 1);
         b.c0 = c0;
         b.ct = c0;
         if (M.variance()) {
-            const float N = 9.0f, rN = 1.0f / 9.0f;
-            auto ch = [&](float p0, float p1, float p2, float p3, float p4, float p5, float p6, float p7, float p8,
-                          float& lo, float& hi, float& mean) {
-                float m1 = p0 + p1 + p2 + p3 + p4 + p5 + p6 + p7 + p8;
-                float m2 = __fmul_rn(p0, p0);
-                m2 = __fmaf_rn(p1, p1, m2); m2 = __fmaf_rn(p2, p2, m2); m2 = __fmaf_rn(p3, p3, m2);
-                m2 = __fmaf_rn(p4, p4, m2); m2 = __fmaf_rn(p5, p5, m2); m2 = __fmaf_rn(p6, p6, m2);
-                m2 = __fmaf_rn(p7, p7, m2); m2 = __fmaf_rn(p8, p8, m2);
-                mean = div_const_rn(m1, N, rN);
-                float var = __fmaf_rn(-mean, mean, div_const_rn(m2, N, rN));
-                float s = g * sqrtf(gmax(0.f, var));
-                lo = mean - s;
-                hi = mean + s;
-            };
-            ch(c0.x, c1.x, c2.x, c3.x, c4.x, c5.x, c6.x, c7.x, c8.x, b.mn.x, b.mx.x, b.ct.x);
-            ch(c0.y, c1.y, c2.y, c3.y, c4.y, c5.y, c6.y, c7.y, c8.y, b.mn.y, b.mx.y, b.ct.y);
-            ch(c0.z, c1.z, c2.z, c3.z, c4.z, c5.z, c6.z, c7.z, c8.z, b.mn.z, b.mx.z, b.ct.z);
+            // per channel: m1 = p0 + ... + p8 in tap order, m2 = p0^2 then FMAs,
+            // mean = m1 / 9, var = m2 / 9 - mean^2 (one FMA); the channels run
+            // two at a time as (Y, Co) and (Cg, 0) pairs
+            const int off[9] = {0, -ns - 1, -ns, -ns + 1, -1, 1, ns - 1, ns, ns + 1};
+            f2 pa[9], pb[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) load_pairs(&nb[off[k]], pa[k], pb[k]);
+            f2 m1a = add2(pa[0], pa[1]), m1b = add2(pb[0], pb[1]);
+            f2 m2a = mul2(pa[0], pa[0], z), m2b = mul2(pb[0], pb[0], z);
+            m2a = fma2(pa[1], pa[1], m2a);
+            m2b = fma2(pb[1], pb[1], m2b);
+#pragma unroll
+            for (int k = 2; k < 9; ++k) {
+                m1a = add2(m1a, pa[k]);
+                m1b = add2(m1b, pb[k]);
+                m2a = fma2(pa[k], pa[k], m2a);
+                m2b = fma2(pb[k], pb[k], m2b);
+            }
+            const f2 nN = dup(-9.0f), rN = dup(1.0f / 9.0f);
+            const f2 mean_a = div_const_rn2(m1a, nN, rN, z), mean_b = div_const_rn2(m1b, nN, rN, z);
+            const f2 var_a = fma2(neg2(mean_a), mean_a, div_const_rn2(m2a, nN, rN, z));
+            const f2 var_b = fma2(neg2(mean_b), mean_b, div_const_rn2(m2b, nN, rN, z));
+            const f2 gg = dup(g);
+            const f2 s_a = mul2(gg, pk(sqrtf(gmax(0.f, f2lo(var_a))), sqrtf(gmax(0.f, f2hi(var_a)))), z);
+            const f2 s_b = mul2(gg, pk(sqrtf(gmax(0.f, f2lo(var_b))), 0.f), z);
+            const f2 lo_a = sub2(mean_a, s_a), hi_a = add2(mean_a, s_a);
+            const f2 lo_b = sub2(mean_b, s_b), hi_b = add2(mean_b, s_b);
+            b.mn = {f2lo(lo_a), f2hi(lo_a), f2lo(lo_b)};
+            b.mx = {f2lo(hi_a), f2hi(hi_a), f2lo(hi_b)};
+            b.ct = {f2lo(mean_a), f2hi(mean_a), f2lo(mean_b)};
         } else {
             auto mn9 = [](float a0, float a1, float a2, float a3, float a4, float a5, float a6, float a7, float a8) {
                 return gmin(gmin(gmin(gmin(gmin(gmin(gmin(gmin(a0, a1), a2), a3), a4), a5), a6), a7), a8);
@@ -117,141 +131,55 @@ struct ExactF32 {
         ehd = hs[2] / hs[3];
     }
 
-    // taa.comp:441-514 as the 16-tap form
-    static __device__ __forceinline__ void catmullrom_taps(float u, float v, int w, int h, Taps& t) {
-        float itx = u * (float)w, ity = v * (float)h;
-        float bx = floorf(itx - 0.5f), by = floorf(ity - 0.5f);
-        float fx = itx - (bx + 0.5f), fy = ity - (by + 0.5f);
-        {
-            float f2 = fx * fx, f3 = f2 * fx;
-            t.wx[0] = -0.5f * f3 + f2 - 0.5f * fx;
-            t.wx[1] = 1.5f * f3 - 2.5f * f2 + 1.0f;
-            t.wx[2] = -1.5f * f3 + 2.0f * f2 + 0.5f * fx;
-            t.wx[3] = 0.5f * f3 - 0.5f * f2;
-        }
-        {
-            float f2 = fy * fy, f3 = f2 * fy;
-            t.wy[0] = -0.5f * f3 + f2 - 0.5f * fy;
-            t.wy[1] = 1.5f * f3 - 2.5f * f2 + 1.0f;
-            t.wy[2] = -1.5f * f3 + 2.0f * f2 + 0.5f * fy;
-            t.wy[3] = 0.5f * f3 - 0.5f * f2;
-        }
-        int kx = trunc_index(bx), ky = trunc_index(by);
-        t.ux = kx - 1;
-        t.uy = ky - 1;
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            t.xs[i] = clampi(kx - 1 + i, 0, w - 1);
-            t.ys[i] = clampi(ky - 1 + i, 0, h - 1);
-        }
-    }
-    // exact-weight bilinear (taa.comp:546)
-    static __device__ __forceinline__ void bilinear_taps(float u, float v, int w, int h, Taps& t) {
-        float px = u * (float)w - 0.5f, py = v * (float)h - 0.5f;
-        float fx0 = floorf(px), fy0 = floorf(py);
-        float fx = px - fx0, fy = py - fy0;
-        if (!(fx == fx)) fx = 0.f;
-        if (!(fy == fy)) fy = 0.f;
-        int x0 = trunc_index(fx0), y0 = trunc_index(fy0);
-        t.ux = x0;
-        t.uy = y0;
-        t.xs[0] = clampi(x0, 0, w - 1);
-        t.xs[1] = clampi(x0 + 1 < x0 ? x0 : x0 + 1, 0, w - 1);
-        t.ys[0] = clampi(y0, 0, h - 1);
-        t.ys[1] = clampi(y0 + 1 < y0 ? y0 : y0 + 1, 0, h - 1);
-        t.wx[0] = 1.0f - fx;
-        t.wx[1] = fx;
-        t.wy[0] = 1.0f - fy;
-        t.wy[1] = fy;
-    }
-    // taa.comp:517-537: positions and combination weights of the four bilinear taps
-    static __device__ __forceinline__ void bspline_positions(float u, float v, int w, int h, float s0[2], float s1[2],
-                                                             float t0[2], float t1[2]) {
-        float it[2] = {u * (float)w, v * (float)h};
-        float inv[2] = {1.0f / (float)w, 1.0f / (float)h};
-#pragma unroll
-        for (int k = 0; k < 2; ++k) {
-            float tc = floorf(it[k] - 0.5f) + 0.5f;
-            float f = it[k] - tc, f2 = f * f, f3 = f2 * f;
-            float w0 = f2 - 0.5f * (f3 + f);
-            float w1 = 1.5f * f3 - 2.5f * f2 + 1.0f;
-            float w3 = 0.5f * (f3 - f2);
-            float w2 = 1.0f - w0 - w1 - w3;
-            s0[k] = w0 + w1;
-            s1[k] = w2 + w3;
-            t0[k] = (tc - 1.0f + w1 / (w0 + w1)) * inv[k];
-            t1[k] = (tc + 1.0f + w3 / (w2 + w3)) * inv[k];
-        }
+    // taa.comp:441-514: the x and y axes of the Catmull-Rom weights as pairs
+    static __device__ __forceinline__ void catmullrom_taps(float u, float v, int w, int h, tiled::Taps& t, f2 z) {
+        const f2 it = mul2(pk(u, v), pk((float)w, (float)h), z);
+        const f2 half = dup(0.5f);
+        const f2 bf = pk(floorf(f2lo(it) - 0.5f), floorf(f2hi(it) - 0.5f));
+        const f2 f = sub2(it, add2(bf, half));
+        const f2 f2_ = mul2(f, f, z), f3 = mul2(f2_, f, z);
+        const f2 hf = mul2(half, f, z);
+        const f2 w0 = sub2(add2(mul2(dup(-0.5f), f3, z), f2_), hf);
+        const f2 w1 = add2(sub2(mul2(dup(1.5f), f3, z), mul2(dup(2.5f), f2_, z)), dup(1.0f));
+        const f2 w2 = add2(add2(mul2(dup(-1.5f), f3, z), mul2(dup(2.0f), f2_, z)), hf);
+        const f2 w3 = sub2(mul2(half, f3, z), mul2(half, f2_, z));
+        t.wx[0] = f2lo(w0); t.wy[0] = f2hi(w0);
+        t.wx[1] = f2lo(w1); t.wy[1] = f2hi(w1);
+        t.wx[2] = f2lo(w2); t.wy[2] = f2hi(w2);
+        t.wx[3] = f2lo(w3); t.wy[3] = f2hi(w3);
+        t.ux = trunc_index(f2lo(bf)) - 1;
+        t.uy = trunc_index(f2hi(bf)) - 1;
     }
 
-    template <class F>
-    static __device__ __forceinline__ float4 bil(const Taps& t, F&& texel) {
-        float4 A = texel(t.xs[0], t.ys[0]), B = texel(t.xs[1], t.ys[0]);
-        float4 C = texel(t.xs[0], t.ys[1]), D = texel(t.xs[1], t.ys[1]);
-        float gx = t.wx[0], fx = t.wx[1], gy = t.wy[0], fy = t.wy[1];
-        float4 tt = make_float4(A.x * gx + B.x * fx, A.y * gx + B.y * fx, A.z * gx + B.z * fx, 0.f);
-        float4 bb = make_float4(C.x * gx + D.x * fx, C.y * gx + D.y * fx, C.z * gx + D.z * fx, 0.f);
-        return make_float4(tt.x * gy + bb.x * fy, tt.y * gy + bb.y * fy, tt.z * gy + bb.z * fy, 0.f);
-    }
-
-    // the same filter reading 4x4 (or 2x2) consecutive window entries
-    template <int INTERP, int HF, class HT>
-    static __device__ __forceinline__ float4 filter_window(const tiled::HistoryTaps<ExactF32, INTERP>& h, const HT* base,
-                                                           int stride) {
-        const Taps& t = h.t[0];
-        auto at = [&](int i, int j) { return tiled::to_f4<HF>(base[j * stride + i]); };
-        if (INTERP == 2) {
-            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    // the window filter with each tap as two pairs (x, y), (z, w): a row sums
+    // its four taps, then the rows are summed, both with one FMA per step
+    template <int INTERP, int HF, class Taps_, class HT>
+    static __device__ __forceinline__ float4 filter_window(const Taps_& h, const HT* base, int stride) {
+        if constexpr (INTERP == 2 && HF == 0) {
+            const tiled::Taps& t = h.t[0];
+            const f2 zero = dup(0.f);
+            f2 wxd[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) wxd[i] = dup(t.wx[i]);
+            f2 acc_xy = zero, acc_zw = zero;
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                float rx = 0.f, ry = 0.f, rz = 0.f;
+                f2 r_xy = zero, r_zw = zero;
 #pragma unroll
                 for (int i = 0; i < 4; ++i) {
-                    float4 s = at(i, j);
-                    rx = __fmaf_rn(t.wx[i], s.x, rx);
-                    ry = __fmaf_rn(t.wx[i], s.y, ry);
-                    rz = __fmaf_rn(t.wx[i], s.z, rz);
+                    f2 s_xy, s_zw;
+                    load_pairs(&base[j * stride + i], s_xy, s_zw);
+                    r_xy = fma2(wxd[i], s_xy, r_xy);
+                    r_zw = fma2(wxd[i], s_zw, r_zw);
                 }
-                acc.x = __fmaf_rn(t.wy[j], rx, acc.x);
-                acc.y = __fmaf_rn(t.wy[j], ry, acc.y);
-                acc.z = __fmaf_rn(t.wy[j], rz, acc.z);
+                const f2 wyd = dup(t.wy[j]);
+                acc_xy = fma2(wyd, r_xy, acc_xy);
+                acc_zw = fma2(wyd, r_zw, acc_zw);
             }
-            return acc;
+            return make_float4(f2lo(acc_xy), f2hi(acc_xy), f2lo(acc_zw), 0.f);
+        } else {
+            return tiled::HistoryFilter::filter_window<INTERP, HF>(h, base, stride);
         }
-        float4 A = at(0, 0), B = at(1, 0), C = at(0, 1), D = at(1, 1);
-        float gx = t.wx[0], fx = t.wx[1], gy = t.wy[0], fy = t.wy[1];
-        float4 tt = make_float4(A.x * gx + B.x * fx, A.y * gx + B.y * fx, A.z * gx + B.z * fx, 0.f);
-        float4 bb = make_float4(C.x * gx + D.x * fx, C.y * gx + D.y * fx, C.z * gx + D.z * fx, 0.f);
-        return make_float4(tt.x * gy + bb.x * fy, tt.y * gy + bb.y * fy, tt.z * gy + bb.z * fy, 0.f);
-    }
-
-    template <int INTERP, class F>
-    static __device__ __forceinline__ float4 filter(const tiled::HistoryTaps<ExactF32, INTERP>& h, F&& texel) {
-        if (INTERP == 2) {
-            const Taps& t = h.t[0];
-            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                float rx = 0.f, ry = 0.f, rz = 0.f;
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    float4 s = texel(t.xs[i], t.ys[j]);
-                    rx = __fmaf_rn(t.wx[i], s.x, rx);
-                    ry = __fmaf_rn(t.wx[i], s.y, ry);
-                    rz = __fmaf_rn(t.wx[i], s.z, rz);
-                }
-                acc.x = __fmaf_rn(t.wy[j], rx, acc.x);
-                acc.y = __fmaf_rn(t.wy[j], ry, acc.y);
-                acc.z = __fmaf_rn(t.wy[j], rz, acc.z);
-            }
-            return acc;
-        }
-        if (INTERP == 0) return bil(h.t[0], texel);
-        float4 A = bil(h.t[0], texel), B = bil(h.t[1], texel), C = bil(h.t[2], texel), D = bil(h.t[3], texel);
-        const float *s0 = h.s0, *s1 = h.s1;
-        return make_float4((A.x * s0[0] + B.x * s1[0]) * s0[1] + (C.x * s0[0] + D.x * s1[0]) * s1[1],
-                           (A.y * s0[0] + B.y * s1[0]) * s0[1] + (C.y * s0[0] + D.y * s1[0]) * s1[1],
-                           (A.z * s0[0] + B.z * s1[0]) * s0[1] + (C.z * s0[0] + D.z * s1[0]) * s1[1], 0.f);
     }
 
     // taa.comp:825-900: rectification and blend; returns the RGB result

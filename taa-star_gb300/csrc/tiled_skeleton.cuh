@@ -1,31 +1,40 @@
 // tiled_skeleton.cuh - the CTA structure shared by the tiled FP32 and FP16 resolve forms.
 //
 // One 256-thread CTA resolves a 32x8 tile, one pixel per thread:
-//   1. each thread requests its pixel's velocity and depth, one or two texels
-//      of the tile's source colour plus 1-pixel halo, and the velocity of the
-//      tile's reference pixel (the same address for the whole CTA);
-//   2. the reference pixel's history position fixes a window of history
-//      texels - its Catmull-Rom taps widened by the tile and a margin of
-//      WIN_MARGIN pixels of motion difference - which the CTA copies into
-//      shared memory with cp.async (each texel crosses L1 once per tile
-//      instead of once per tap); the window is indexed by unclamped texel
-//      coordinates and stores the edge-clamped texel at every position, so a
-//      pixel's 16 taps are 4x4 consecutive window entries read with immediate
-//      offsets from one base;
+//   1. each thread requests its pixel's velocity and depth and one or two
+//      texels of the tile's source colour plus 1-pixel halo; warp 0 alone
+//      reads the velocity of the tile's reference pixel and places the
+//      history window: the reference pixel's Catmull-Rom taps widened by the
+//      tile and a margin of WIN_MARGIN pixels of motion difference;
+//   2. a window that lies inside the history image is copied into shared
+//      memory by one TMA tensor copy (cp.async.bulk.tensor) that thread 0
+//      issues on an mbarrier; a window that crosses the image border is
+//      copied by all threads with cp.async, edge-clamping each texel.  Either
+//      way the window is indexed by unclamped texel coordinates, so a
+//      pixel's 16 taps are 4x4 consecutive entries read from one base;
 //   3. while the window is in flight the staged colour gives the 3x3 box
 //      (the arithmetic policy decides how: exact FP32 or packed FP16);
 //   4. a pixel whose taps fall inside the window reads them from shared
 //      memory, any other pixel (motion differing from the reference pixel's
-//      by more than the margin) reads them from global memory; then
-//      rejection, rectification and blend finish the pixel.
+//      by more than the margin) reads them from global memory with clamped
+//      coordinates; then rejection, rectification and blend finish the pixel.
+//
+// The wait for the TMA copy polls its mbarrier a bounded number of times; a
+// copy that has not landed by then sets kStatusWindowTimeout in the device
+// status word, and the CTA waits a second bounded while for the copy before
+// it leaves.
 //
 // The arithmetic lives in a policy class `Pol` so that the exact FP32 form
 // (compiled with -fmad=false, bit-identical to the oracle) and the FP16 form
 // share the memory pipeline.
 #pragma once
-#include <atomic>
+#include <cuda.h>
+
+#include <cstring>
 
 #include "common.cuh"
+#include "f32x2.cuh"
+#include "kernels.h"
 
 namespace taa_dev {
 namespace tiled {
@@ -39,6 +48,15 @@ constexpr int SX = TX + 2, SY = TY + 2, NS = SX * SY;  // staged colour with hal
 constexpr int WIN_MARGIN = 3;                          // motion difference (px) the window absorbs
 constexpr int WW = TX + 3 + 2 * WIN_MARGIN;            // history window width  (texels)
 constexpr int WH = TY + 3 + 2 * WIN_MARGIN;            // history window height (texels)
+// Stored window width: RGBA16F windows start on an even texel (a TMA copy of
+// half texels starts on a 16-byte boundary), so they are one texel wider.
+template <int HF> struct Win {
+    static constexpr int W = HF == 0 ? WW : WW + 1;
+    static constexpr int ALIGN = HF == 0 ? 1 : 2;
+};
+// Polls of the window's mbarrier before the wait gives up (each poll may
+// suspend the thread for a while in hardware): far above any real copy time.
+constexpr uint32_t kWaitPolls = 1u << 22;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -53,6 +71,47 @@ __device__ __forceinline__ void cp_async(void* dst_smem, const void* src) {
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// mbarrier and TMA tensor copies (PTX ISA: mbarrier, cp.async.bulk.tensor).
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    // the barrier's initialisation becomes visible to the TMA unit (async proxy)
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+// Bounded wait for phase `parity` of the barrier: false after kWaitPolls polls.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    for (uint32_t i = 0; i < kWaitPolls; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(bar))
+        : "memory");
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int c0, int c1, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+        "[%4];\n" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_addr(bar))
+        : "memory");
+}
 
 // Compile-time view of the parameter block: Hot = the benchmark mode (variance
 // clip in YCoCg, clip towards the box centre, velocity for every pixel, simple
@@ -84,18 +143,20 @@ struct C3 { float x, y, z; };
 // INTERP 2: 4x4 separable Catmull-Rom; 0: one bilinear 2x2; 1: four bilinear
 // 2x2 sets combined with the "b-spline" weights.
 struct Taps {
-    int xs[4], ys[4];  // clamped texel coordinates
     float wx[4], wy[4];
-    int ux, uy;        // unclamped coordinate of the first tap
+    int ux, uy;  // unclamped coordinate of the first tap
+    // clamped coordinate of tap i (global reads only; the window holds clamped texels)
+    __device__ __forceinline__ int xs(int i, int w) const { return clampi(ux + i, 0, w - 1); }
+    __device__ __forceinline__ int ys(int j, int h) const { return clampi(uy + j, 0, h - 1); }
 };
 
 template <class Pol, int INTERP> struct HistoryTaps {
     Taps t[INTERP == 1 ? 4 : 1];
     float s0[2], s1[2];  // b-spline combination weights
 
-    __device__ __forceinline__ void setup(float u, float v, int w, int h) {
+    __device__ __forceinline__ void setup(float u, float v, int w, int h, f2 z) {
         if (INTERP == 2) {
-            Pol::catmullrom_taps(u, v, w, h, t[0]);
+            Pol::catmullrom_taps(u, v, w, h, t[0], z);
         } else if (INTERP == 0) {
             Pol::bilinear_taps(u, v, w, h, t[0]);
         } else {
@@ -144,12 +205,18 @@ __device__ __forceinline__ void history_position(const taa_uniforms_t& U, const 
 
 // The resolve kernel.  Pol provides the working colour format and the box,
 // tap, filter and finishing arithmetic (see resolve_tiled.cu, resolve_half.cu).
+// `hmap` is the history image's tensor map (box Win<HF>::W x WH texels) when
+// `tma_ok`; otherwise every window is copied with cp.async.
 template <class Pol, int HF, int MC, int INTERP, bool HOT>
-__global__ void __launch_bounds__(NT, TAA_TILE_MIN_BLOCKS) resolve_tile(const taa_uniforms_t U, const FrameArgs a) {
+__global__ void __launch_bounds__(NT, TAA_TILE_MIN_BLOCKS)
+    resolve_tile(const taa_uniforms_t U, const FrameArgs a, const __grid_constant__ CUtensorMap hmap, const int tma_ok) {
     using HT = typename HistTexel<HF>::T;
     using Staged = typename Pol::Staged;
+    constexpr int WWS = Win<HF>::W;
     __shared__ Staged s_col[NS];
-    __shared__ HT s_win[WW * WH];
+    __shared__ __align__(128) HT s_win[WWS * WH];
+    __shared__ uint64_t s_bar;
+    __shared__ int s_org[3];  // window origin x, y and how it is copied (1 TMA, 2 cp.async)
 
     const taa_parameters_t& P = U.param[0];
     const Mode<HOT> M{P};
@@ -160,14 +227,10 @@ __global__ void __launch_bounds__(NT, TAA_TILE_MIN_BLOCKS) resolve_tile(const ta
     const int x = x0 + lx, y = y0 + ly;
     const bool inside = x < W && y < H;
     const int cx = min(x, W - 1), cy = min(y, H - 1);
-    // the tile's reference pixel (its centre, clamped into the image)
-    const int rx = min(x0 + TX / 2, W - 1), ry = min(y0 + TY / 2, H - 1);
 
-    // 1. own depth and velocity, the reference pixel's, staged colour texels
+    // 1. own depth and velocity, staged colour texels
     float depth = __ldg(texel_ptr<float>(a.depth, cx, cy));
     float4 vs = fetch_velocity<MC>(a.velocity, cx, cy);
-    float rdepth = __ldg(texel_ptr<float>(a.depth, rx, ry));
-    float4 rvs = fetch_velocity<MC>(a.velocity, rx, ry);
     uint2 st0, st1 = make_uint2(0u, 0u);
     {
         int sy = tid / SX, sx = tid - sy * SX;
@@ -178,41 +241,49 @@ __global__ void __launch_bounds__(NT, TAA_TILE_MIN_BLOCKS) resolve_tile(const ta
         }
     }
 
-    // 2. the reference pixel's taps place the history window; copy it in flight
+    // 2. warp 0 places the history window at the tile's reference pixel (its
+    //    centre, clamped into the image) and thread 0 starts the TMA copy
     const Img& hi = a.history;
     const bool have_hist = hi.p != nullptr;
     const bool windowed = have_hist && INTERP != 1;
-    int wx0 = 0, wy0 = 0;
-    if (windowed) {
-        // only the first tap's integer coordinate of the reference pixel is needed
+    if (windowed && tid < 32) {
+        const int rx = min(x0 + TX / 2, W - 1), ry = min(y0 + TY / 2, H - 1);
+        const float rdepth = __ldg(texel_ptr<float>(a.depth, rx, ry));
+        const float4 rvs = fetch_velocity<MC>(a.velocity, rx, ry);
         float ru = div_const_rn((float)rx + 0.5f, (float)W, a.inv_out_w);
         float rv = div_const_rn((float)ry + 0.5f, (float)H, a.inv_out_h);
         float rhu, rhv, rehd;
         history_position<Pol, MC, HOT>(U, a, M, rx, ry, rvs, rdepth, ru, rv, rhu, rhv, rehd);
         const int k0 = INTERP == 2 ? 1 : 0;  // Catmull-Rom starts one texel before floor(p - 0.5)
-        int rux = trunc_index(floorf(rhu * (float)hi.w - 0.5f)) - k0;
-        int ruy = trunc_index(floorf(rhv * (float)hi.h - 0.5f)) - k0;
-        // the reference pixel sits at (rx - x0, ry - y0) in the tile
-        wx0 = rux - (rx - x0) - WIN_MARGIN;
-        wy0 = ruy - (ry - y0) - WIN_MARGIN;
-        const int lane = tid & 31, warp = tid >> 5;
-        for (int r = warp; r < WH; r += NT / 32) {
-            const int gy = clampi(wy0 + r, 0, hi.h - 1);
-            const char* row = hi.p + (size_t)gy * hi.pitch;
-            for (int c = lane; c < WW; c += 32)
-                cp_async<HistTexel<HF>::B>(&s_win[r * WW + c],
-                                           row + (size_t)clampi(wx0 + c, 0, hi.w - 1) * HistTexel<HF>::B);
+        const int rux = trunc_index(floorf(rhu * (float)hi.w - 0.5f)) - k0;
+        const int ruy = trunc_index(floorf(rhv * (float)hi.h - 0.5f)) - k0;
+        // the reference pixel sits at (rx - x0, ry - y0) in the tile; floor to the stored alignment
+        const int wx0 = (rux - (rx - x0) - WIN_MARGIN) & ~(Win<HF>::ALIGN - 1);
+        const int wy0 = ruy - (ry - y0) - WIN_MARGIN;
+        const bool interior = wx0 >= 0 && wy0 >= 0 && wx0 <= hi.w - WWS && wy0 <= hi.h - WH;
+        const int mode = tma_ok && interior ? 1 : 2;
+        if (tid == 0) {
+            s_org[0] = wx0;
+            s_org[1] = wy0;
+            s_org[2] = mode;
+            if (mode == 1) {
+                mbar_init(&s_bar, 1);
+                mbar_expect_tx(&s_bar, (uint32_t)sizeof(s_win));
+                if (HF == 0) tma_load_3d(s_win, &hmap, 0, wx0, wy0, &s_bar);
+                else tma_load_2d(s_win, &hmap, 4 * wx0, wy0, &s_bar);
+            }
         }
     }
-    cp_async_commit();
 
-    // own history position and taps
-    float u = div_const_rn((float)cx + 0.5f, (float)W, a.inv_out_w);
-    float v = div_const_rn((float)cy + 0.5f, (float)H, a.inv_out_h);
+    // own history position and taps; (u, v) = (texel + 0.5) / size, correctly rounded, as a pair
+    const f2 z{a.neg_zero2};
+    const f2 uv = div_const_rn2(add2(pk((float)cx, (float)cy), dup(0.5f)), pk(-(float)W, -(float)H),
+                                pk(a.inv_out_w, a.inv_out_h), z);
+    float u = f2lo(uv), v = f2hi(uv);
     float hu, hv, ehd;
     history_position<Pol, MC, HOT>(U, a, M, cx, cy, vs, depth, u, v, hu, hv, ehd);
     HistoryTaps<Pol, INTERP> taps;
-    taps.setup(hu, hv, hi.w, hi.h);
+    taps.setup(hu, hv, hi.w, hi.h, z);
     float prev_depth = 0.f;
     const bool depth_cull = P.mDepthCulling != 0;
     if (depth_cull && a.history_depth.p) {
@@ -221,17 +292,44 @@ __global__ void __launch_bounds__(NT, TAA_TILE_MIN_BLOCKS) resolve_tile(const ta
         prev_depth = __ldg(texel_ptr<float>(a.history_depth, tx_, ty_));
     }
 
-    // 3. staged colour in the policy's working format, then the 3x3 box
+    // 3. staged colour in the policy's working format
     const bool tm = M.tonemap(), yc = M.ycocg();
     s_col[tid] = Pol::stage(st0, tm, yc);
     if (tid + NT < NS) s_col[tid + NT] = Pol::stage(st1, tm, yc);
     __syncthreads();
+    int wx0 = 0, wy0 = 0, mode = 0;
+    if (windowed) {
+        wx0 = s_org[0];
+        wy0 = s_org[1];
+        mode = s_org[2];
+    }
+    if (mode == 2) {
+        // a window across the image border: every texel edge-clamped
+        const int lane = tid & 31, warp = tid >> 5;
+        for (int r = warp; r < WH; r += NT / 32) {
+            const int gy = clampi(wy0 + r, 0, hi.h - 1);
+            const char* row = hi.p + (size_t)gy * hi.pitch;
+            for (int c = lane; c < WWS; c += 32)
+                cp_async<HistTexel<HF>::B>(&s_win[r * WWS + c],
+                                           row + (size_t)clampi(wx0 + c, 0, hi.w - 1) * HistTexel<HF>::B);
+        }
+        cp_async_commit();
+    }
+    // the 3x3 box while the window is in flight
     typename Pol::Box box;
-    Pol::template box<HOT>(&s_col[(ly + 1) * SX + lx + 1], SX, M, P.mVarClipGamma, box);
+    Pol::template box<HOT>(&s_col[(ly + 1) * SX + lx + 1], SX, M, P.mVarClipGamma, box, z);
     if (Pol::kExactCentre) Pol::centre_colour(box, a.color, cx, cy, tm, yc);
 
-    cp_async_wait_all();
-    __syncthreads();
+    if (mode == 1) {
+        if (!mbar_wait_bounded(&s_bar, 0)) {
+            atomicOr(a.status, kStatusWindowTimeout);
+            mbar_wait_bounded(&s_bar, 0);  // the copy may still land in this CTA's memory
+            return;
+        }
+    } else if (mode == 2) {
+        cp_async_wait_all();
+        __syncthreads();
+    }
     if (!inside) return;
 
     // 4. history sample: from the window when all taps fall inside it
@@ -239,12 +337,13 @@ __global__ void __launch_bounds__(NT, TAA_TILE_MIN_BLOCKS) resolve_tile(const ta
     if (have_hist) {
         const int span = INTERP == 2 ? 4 : 2;
         const int bx = taps.t[0].ux - wx0, by = taps.t[0].uy - wy0;
-        const bool in_win = windowed && bx >= 0 && by >= 0 && bx + span <= WW && by + span <= WH;
+        const bool in_win = windowed && bx >= 0 && by >= 0 && bx + span <= WWS && by + span <= WH;
         if (in_win) {
-            const HT* base = &s_win[by * WW + bx];
-            hraw = Pol::template filter_window<INTERP, HF>(taps, base, WW);
+            const HT* base = &s_win[by * WWS + bx];
+            hraw = Pol::template filter_window<INTERP, HF>(taps, base, WWS);
         } else {
-            hraw = Pol::template filter<INTERP>(taps, [&](int tx_, int ty_) { return fetch_history<HF>(hi, tx_, ty_); });
+            hraw = Pol::template filter<INTERP>(taps, hi.w, hi.h,
+                                                [&](int tx_, int ty_) { return fetch_history<HF>(hi, tx_, ty_); });
         }
     }
 
@@ -265,10 +364,13 @@ __global__ void __launch_bounds__(NT, TAA_TILE_MIN_BLOCKS) resolve_tile(const ta
 template <class Pol, int HF, int MC, int INTERP, bool HOT>
 cudaError_t launch_tile(const taa_uniforms_t& U, const FrameArgs& a, cudaStream_t s) {
     dim3 grid((a.out_w + TX - 1) / TX, (a.out_h + TY - 1) / TY);
-    resolve_tile<Pol, HF, MC, INTERP, HOT><<<grid, NT, 0, s>>>(U, a);
+    CUtensorMap map;
+    std::memset(&map, 0, sizeof map);
+    const int tma_ok = INTERP != 1 && a.history.p && a.history.w >= Win<HF>::W && a.history.h >= WH &&
+                       encode_history_map(a.history, HF, Win<HF>::W, WH, &map);
+    resolve_tile<Pol, HF, MC, INTERP, HOT><<<grid, NT, 0, s>>>(U, a, map, tma_ok);
     return cudaGetLastError();
 }
-
 template <class Pol, int HF, int MC>
 cudaError_t launch_interp(int interp, const taa_uniforms_t& U, const FrameArgs& a, cudaStream_t s) {
     const bool hot = is_hot(U.param[0]);

@@ -111,7 +111,7 @@ assert C.sizeof(Parameters) == 176 and C.sizeof(Uniforms) == 544
 EXPORTS = ["taa_version", "taa_last_error", "taa_default_parameters", "taa_get_jitter_offset",
            "taa_jittered_projection", "taa_compose_matrices", "taa_cas_setup", "taa_create", "taa_destroy",
            "taa_set_uniforms", "taa_set_sharpener", "taa_selected_form", "taa_resolve",
-           "taa_resolve_static_scratch",
+           "taa_resolve_static_scratch", "taa_device_status",
            "taa_synth_default_scene", "taa_synth_spheres", "taa_synth_jitter", "taa_synth_camera",
            "taa_synth_render"]
 
@@ -144,6 +144,7 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
         "taa_selected_form": (C.c_int, [C.c_void_p]),
         "taa_resolve": (C.c_int, [C.c_void_p, C.c_void_p, P(FrameIO)]),
         "taa_resolve_static_scratch": (C.c_int, [C.c_void_p, C.c_void_p, P(FrameIO), C.c_uint32, C.c_float]),
+        "taa_device_status": (C.c_int, [P(C.c_uint32), C.c_int]),
         "taa_synth_default_scene": (C.c_int, [P(SynthScene), C.c_int32, C.c_int32, C.c_uint64]),
         "taa_synth_spheres": (C.c_int, [P(SynthScene), P(C.c_float), C.c_int32]),
         "taa_synth_jitter": (C.c_int, [P(SynthScene), C.c_int32, P(C.c_float), P(C.c_float)]),
@@ -169,6 +170,13 @@ def check(rc: int) -> int:
     if rc < 0:
         raise TaaError(rc, load().taa_last_error().decode())
     return rc
+
+
+def device_status(clear: bool = True) -> int:
+    """The device status word (TAA_DEVICE_* bits); waits for the device."""
+    bits = C.c_uint32()
+    check(load().taa_device_status(C.byref(bits), int(clear)))
+    return bits.value
 
 
 def default_parameters() -> Parameters:

@@ -273,3 +273,19 @@ def test_fp16_form_frame_error_vs_fp64(cuda, mode):
     got, want = out["history_out"][..., :3], ref["history"][..., :3]
     assert rel_l2(got, want) <= 1e-2, rel_l2(got, want)
     assert psnr(got, want) >= 50.0
+
+def test_device_status_stays_clear(cuda):
+    # the tiled forms wait on their history-window copy with a bounded poll;
+    # in a normal run no wait gives up, so no status bit is set
+    T.device_status(clear=True)
+    w, h = 256, 96
+    wl = WL.small(w, h, frames=2)
+    fr = cpu_frames(wl, range(2))
+    u = T.make_uniforms(wl.parameters(), jitter_ndc=fr[1]["jitter"])
+    hist = fr[0]["color"].astype(np.float32)
+    for form in (T.TAA_FORM_TILED, T.TAA_FORM_FP16):
+        ctx = T.Taa(w, h, form=form)
+        ctx.set_uniforms(u)
+        gpu_resolve(ctx, cuda, fr[1]["color"], fr[1]["depth"], fr[1]["motion"], hist, fr[0]["depth"])
+        ctx.close()
+    assert T.device_status(clear=True) == 0
