@@ -37,6 +37,7 @@ struct HalfPol : tiled::HistoryFilter {
     };
     // the blend takes the current colour in FP32 from the source texel
     static constexpr bool kExactCentre = true;
+    static __device__ __forceinline__ C3 centre(const Box& b, const uint2*) { return b.cur; }
     static __device__ __forceinline__ void centre_colour(Box& b, const Img& color, int cx, int cy, bool tonemap,
                                                          bool ycocg) {
         float4 c = half4_to_float4(__ldg(texel_ptr<uint2>(color, cx, cy)));
@@ -182,7 +183,7 @@ struct HalfPol : tiled::HistoryFilter {
 
     template <bool HOT>
     static __device__ __forceinline__ float4 finish(const taa_uniforms_t& U, const taa_parameters_t& P,
-                                                    const tiled::Mode<HOT>& M, const Box& b, float4 hraw, float u,
+                                                    const tiled::Mode<HOT>& M, const Box& b, const C3& c0, float4 hraw, float u,
                                                     float v, float hu, float hv, bool rejected) {
         const bool yc = M.ycocg();
         C3 hc{hraw.x, hraw.y, hraw.z};
@@ -228,7 +229,6 @@ struct HalfPol : tiled::HistoryFilter {
                 hc = {ct.x + r.x, ct.y + r.y, ct.z + r.z};
             }
         }
-        const C3 c0 = b.cur;
         float alpha = P.mAlpha;
         if (rejected) {
             alpha = P.mRejectionAlpha;

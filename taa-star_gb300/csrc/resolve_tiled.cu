@@ -18,8 +18,14 @@ using tiled::C3;
 struct ExactF32 : tiled::HistoryFilter {
     using Staged = float4;
     struct Box {
-        C3 c0, mn, mx, ct;
+        C3 mn, mx, ct;
     };
+    // the current colour for the blend: the staged centre texel, read again
+    // when it is needed rather than held in registers across the window wait
+    static __device__ __forceinline__ C3 centre(const Box&, const float4* staged_centre) {
+        const float4 t = *staged_centre;
+        return C3{t.x, t.y, t.z};
+    }
     // the staged centre texel already is the exact current colour
     static constexpr bool kExactCentre = false;
     static __device__ __forceinline__ void centre_colour(Box&, const Img&, int, int, bool, bool) {}
@@ -50,26 +56,23 @@ struct ExactF32 : tiled::HistoryFilter {
         auto ld = [&](int o) { float4 t = nb[o]; return C3{t.x, t.y, t.z}; };
         const C3 c0 = ld(0), c1 = ld(-ns - 1), c2 = ld(-ns), c3 = ld(-ns + 1), c4 = ld(-1), c5 = ld(1),
                  c6 = ld(ns - 1), c7 = ld(ns), c8 = ld(ns + 1);
-        b.c0 = c0;
         b.ct = c0;
         if (M.variance()) {
             // per channel: m1 = p0 + ... + p8 in tap order, m2 = p0^2 then FMAs,
             // mean = m1 / 9, var = m2 / 9 - mean^2 (one FMA); the channels run
             // two at a time as (Y, Co) and (Cg, 0) pairs
             const int off[9] = {0, -ns - 1, -ns, -ns + 1, -1, 1, ns - 1, ns, ns + 1};
-            f2 pa[9], pb[9];
+            f2 pa, pb, m1a, m1b, m2a, m2b;
+            load_pairs(&nb[0], m1a, m1b);
+            m2a = mul2(m1a, m1a, z);
+            m2b = mul2(m1b, m1b, z);
 #pragma unroll
-            for (int k = 0; k < 9; ++k) load_pairs(&nb[off[k]], pa[k], pb[k]);
-            f2 m1a = add2(pa[0], pa[1]), m1b = add2(pb[0], pb[1]);
-            f2 m2a = mul2(pa[0], pa[0], z), m2b = mul2(pb[0], pb[0], z);
-            m2a = fma2(pa[1], pa[1], m2a);
-            m2b = fma2(pb[1], pb[1], m2b);
-#pragma unroll
-            for (int k = 2; k < 9; ++k) {
-                m1a = add2(m1a, pa[k]);
-                m1b = add2(m1b, pb[k]);
-                m2a = fma2(pa[k], pa[k], m2a);
-                m2b = fma2(pb[k], pb[k], m2b);
+            for (int k = 1; k < 9; ++k) {
+                load_pairs(&nb[off[k]], pa, pb);
+                m1a = add2(m1a, pa);
+                m1b = add2(m1b, pb);
+                m2a = fma2(pa, pa, m2a);
+                m2b = fma2(pb, pb, m2b);
             }
             const f2 nN = dup(-9.0f), rN = dup(1.0f / 9.0f);
             const f2 mean_a = div_const_rn2(m1a, nN, rN, z), mean_b = div_const_rn2(m1b, nN, rN, z);
@@ -185,7 +188,7 @@ struct ExactF32 : tiled::HistoryFilter {
     // taa.comp:825-900: rectification and blend; returns the RGB result
     template <bool HOT>
     static __device__ __forceinline__ float4 finish(const taa_uniforms_t& U, const taa_parameters_t& P,
-                                                    const tiled::Mode<HOT>& M, const Box& b, float4 hraw, float u,
+                                                    const tiled::Mode<HOT>& M, const Box& b, const C3& c0, float4 hraw, float u,
                                                     float v, float hu, float hv, bool rejected) {
         const bool yc = M.ycocg();
         C3 hc{hraw.x, hraw.y, hraw.z};
@@ -233,7 +236,7 @@ struct ExactF32 : tiled::HistoryFilter {
             }
             auto lum = [&](C3 c) { return yc ? c.x : .25f * c.x + .5f * c.y + .25f * c.z; };
             if (M.lottes()) {
-                float lc = lum(b.c0), lh = lum(hc);
+                float lc = lum(c0), lh = lum(hc);
                 float w = 1.0f - fabsf(lc - lh) / gmax(gmax(lc, lh), 0.2f);
                 float ww = w * w;
                 alpha = P.mMaxAlpha * (1.0f - ww) + P.mMinAlpha * ww;
@@ -247,7 +250,6 @@ struct ExactF32 : tiled::HistoryFilter {
         }
         if (U.mResetHistory) alpha = 1.0f;
         float t = 1.0f - alpha;
-        const C3& c0 = b.c0;
         C3 o{hc.x * t + c0.x * alpha, hc.y * t + c0.y * alpha, hc.z * t + c0.z * alpha};
         if (yc) {
             float tmp = o.x - o.z;

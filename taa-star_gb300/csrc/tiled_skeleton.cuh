@@ -282,8 +282,6 @@ __global__ void __launch_bounds__(NT, TAA_TILE_MIN_BLOCKS)
     float u = f2lo(uv), v = f2hi(uv);
     float hu, hv, ehd;
     history_position<Pol, MC, HOT>(U, a, M, cx, cy, vs, depth, u, v, hu, hv, ehd);
-    HistoryTaps<Pol, INTERP> taps;
-    taps.setup(hu, hv, hi.w, hi.h, z);
     float prev_depth = 0.f;
     const bool depth_cull = P.mDepthCulling != 0;
     if (depth_cull && a.history_depth.p) {
@@ -332,9 +330,19 @@ __global__ void __launch_bounds__(NT, TAA_TILE_MIN_BLOCKS)
     }
     if (!inside) return;
 
+    // rejection (taa.comp:787-823) first, so its inputs die before the filter
+    bool rejected = false;
+    if (P.mRejectOutside && (hu < 0.f || hv < 0.f || hu >= 1.f || hv >= 1.f)) rejected = true;
+    if (depth_cull) {
+        float hd = prev_depth;
+        if (fabsf(hd - ehd) > 0.1f * (1.0f - hd)) rejected = true;
+    }
+
     // 4. history sample: from the window when all taps fall inside it
     float4 hraw = make_float4(0.f, 0.f, 0.f, 0.f);
     if (have_hist) {
+        HistoryTaps<Pol, INTERP> taps;
+        taps.setup(hu, hv, hi.w, hi.h, z);
         const int span = INTERP == 2 ? 4 : 2;
         const int bx = taps.t[0].ux - wx0, by = taps.t[0].uy - wy0;
         const bool in_win = windowed && bx >= 0 && by >= 0 && bx + span <= WWS && by + span <= WH;
@@ -347,13 +355,8 @@ __global__ void __launch_bounds__(NT, TAA_TILE_MIN_BLOCKS)
         }
     }
 
-    bool rejected = false;
-    if (P.mRejectOutside && (hu < 0.f || hv < 0.f || hu >= 1.f || hv >= 1.f)) rejected = true;
-    if (depth_cull) {
-        float hd = prev_depth;
-        if (fabsf(hd - ehd) > 0.1f * (1.0f - hd)) rejected = true;
-    }
-    float4 o = Pol::template finish<HOT>(U, P, M, box, hraw, u, v, hu, hv, rejected);
+    const C3 c0 = Pol::centre(box, &s_col[(ly + 1) * SX + lx + 1]);
+    float4 o = Pol::template finish<HOT>(U, P, M, box, c0, hraw, u, v, hu, hv, rejected);
     store_history<HF>(a.history_out, x, y, make_float4(o.x, o.y, o.z, 0.f));
     if (a.result.p) {
         if (tm) o = Pol::un_tonemap(o);
