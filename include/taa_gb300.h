@@ -179,6 +179,55 @@ int taa_selected_form(const taa_ctx* ctx);
  * overlap. */
 int taa_resolve(taa_ctx* ctx, void* stream, const taa_frame_io_t* io);
 
+/* ---- batches: many views in one persistent launch --------------------------
+ * No counterpart in the reference, which resolves one view per dispatch
+ * (source/taa.hpp:1027).  A batch holds up to TAA_BATCH_MAX_VIEWS views of any
+ * sizes that share the motion format, the interpolation mode and the
+ * parameter mode (all views either in the benchmark mode - YCoCg variance
+ * clip towards the box centre, velocity for every pixel - or all not); each
+ * view keeps RGBA32F history, has equal source and target sizes and no
+ * sharpener, and is resolved with the same bits as its own taa_resolve in
+ * TAA_FORM_TILED.  Per-view arguments (uniform block, bindings, history
+ * tensor maps) live in TAA_BATCH_SLOTS device slots: taa_batch_prepare fills
+ * a slot, taa_batch_launch resolves every view of a prepared slot with one
+ * launch (a persistent grid of SM count x CTAs per SM taking tiles from a job
+ * list, or one CTA per tile, as tuned) and does no host work besides it, so a sequence of launches
+ * on prepared slots can be captured into a CUDA graph. */
+typedef struct taa_batch taa_batch;
+#define TAA_BATCH_MAX_VIEWS 255
+#define TAA_BATCH_SLOTS 4
+/* Job orders. */
+#define TAA_SCHEDULE_VIEW_ORDER    0  /* views in the given order, each tile by tile, row by row */
+#define TAA_SCHEDULE_LARGEST_FIRST 1  /* views by decreasing pixel count */
+#define TAA_SCHEDULE_INTERLEAVED   2  /* one tile of each view in turn */
+#define TAA_BATCH_CTA_PER_TILE    -1  /* taa_batch_tuning_t.ctas_per_sm: a grid of one CTA per tile */
+typedef struct taa_batch_tuning_t {
+    int32_t tile_w, tile_h;  /* 32x8, 16x16, 32x16, 16x8 or 8x8 pixels */
+    int32_t schedule;        /* TAA_SCHEDULE_* */
+    int32_t ctas_per_sm;     /* persistent grid = SM count x this; 0 = as many as fit;
+                                TAA_BATCH_CTA_PER_TILE = one CTA per tile instead */
+    float   ms;              /* one launch, as measured by taa_batch_autotune (0 otherwise) */
+} taa_batch_tuning_t;
+
+/* Create a batch for n views; allocates its device slots and job list. */
+int taa_batch_create(const taa_desc_t* descs, int32_t n, taa_batch** out_batch);
+int taa_batch_destroy(taa_batch* batch);
+/* The uniform block of one view for the next taa_batch_prepare. */
+int taa_batch_set_uniforms(taa_batch* batch, int32_t view, const taa_uniforms_t* uniforms);
+/* Validate the n bindings in ios[] (as taa_resolve does) and copy every
+ * view's arguments into slot `slot` on `stream`.  Waits on the host only while
+ * the slot's previous copy is still in flight. */
+int taa_batch_prepare(taa_batch* batch, void* stream, int32_t slot, const taa_frame_io_t* ios);
+/* Resolve every view of a prepared slot on `stream` (one launch). */
+int taa_batch_launch(taa_batch* batch, void* stream, int32_t slot);
+/* Time every tile shape and job order, each with a persistent grid and with
+ * one CTA per tile, on a prepared slot (reps launches each,
+ * which rewrite the slot's outputs with the same values), keep the fastest
+ * and return it.  Synchronises the stream. */
+int taa_batch_autotune(taa_batch* batch, void* stream, int32_t slot, int32_t reps, taa_batch_tuning_t* best);
+int taa_batch_get_tuning(const taa_batch* batch, taa_batch_tuning_t* out);
+int taa_batch_set_tuning(taa_batch* batch, const taa_batch_tuning_t* tuning);
+
 /* Bits of the device status word (taa_device_status). */
 #define TAA_DEVICE_WINDOW_TIMEOUT 0x1u /* a history-window copy did not land within its bounded wait */
 

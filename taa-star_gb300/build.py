@@ -33,10 +33,12 @@ UNITS = {
     "resolve_fast.cu": ["-fmad=false"],
     "resolve_tiled.cu": ["-fmad=false"],
     "resolve_half.cu": [],
+    "batch_tiled.cu": ["-fmad=false"],
     "synth.cu": [],
     "static_scratch.cu": [],
     "device_state.cu": [],
     "capi.cpp": [],
+    "batch_api.cpp": [],
 }
 
 

@@ -14,6 +14,7 @@
 
 #include "../../include/taa_gb300.h"
 #include "../../include/taa_synth.h"
+#include "host_util.h"
 #include "kernels.h"
 #include "synth_scene.h"
 
@@ -34,11 +35,10 @@ struct taa_ctx {
     size_t scratch_pitch = 0;
 };
 
-namespace {
+namespace taa_host {
 
 thread_local std::string g_last_error;
 
-int fail(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
 int fail(int code, const char* fmt, ...) {
     char buf[512];
     va_list ap;
@@ -90,7 +90,94 @@ bool any_param(const taa_uniforms_t& u, int out_w, uint32_t taa_parameters_t::*f
     return u.param[0].*f || (right_used && u.param[1].*f);
 }
 
-}  // namespace
+// Validates a context description (sizes, enums).
+int check_desc(const taa_desc_t& d, const char* who) {
+    if (d.struct_size != sizeof(taa_desc_t)) return fail(TAA_E_INVAL, "%s: struct_size %u != %zu", who, d.struct_size, sizeof(taa_desc_t));
+    if (d.in_width <= 0 || d.in_height <= 0 || d.out_width <= 0 || d.out_height <= 0 || d.in_width > 32768 ||
+        d.in_height > 32768 || d.out_width > 32768 || d.out_height > 32768)
+        return fail(TAA_E_INVAL, "%s: image sizes must be in 1..32768", who);
+    if (d.history_format > TAA_HISTORY_RGBA16F) return fail(TAA_E_INVAL, "%s: history_format %u", who, d.history_format);
+    if (d.motion_format > TAA_MOTION_RG16F) return fail(TAA_E_INVAL, "%s: motion_format %u", who, d.motion_format);
+    if (d.form > TAA_FORM_FP16) return fail(TAA_E_INVAL, "%s: form %u", who, d.form);
+    if (d.sharpener > TAA_SHARPEN_CAS) return fail(TAA_E_INVAL, "%s: sharpener %u", who, d.sharpener);
+    if (!finite(d.sharpen_factor)) return fail(TAA_E_INVAL, "%s: sharpen_factor not finite", who);
+    if (d.flags != 0) return fail(TAA_E_INVAL, "%s: flags must be 0", who);
+    return ok();
+}
+
+// Validates a uniform block (finite floats).
+int check_uniforms(const taa_uniforms_t& u, const char* who) {
+    for (int i = 0; i < 2; ++i) {
+        int rc = check_parameters(u.param[i], i);
+        if (rc) return rc;
+    }
+    const float m[] = {u.mJitterNdc[0], u.mJitterNdc[1], u.mSinTime[0], u.mCamNearPlane, u.mCamFarPlane};
+    for (float v : m)
+        if (!finite(v)) return fail(TAA_E_INVAL, "%s: jitter/time/near/far must be finite", who);
+    for (int i = 0; i < 16; ++i)
+        if (!finite(u.mHistoryViewProjMatrix[i]) || !finite(u.mInverseViewProjMatrix[i]))
+            return fail(TAA_E_INVAL, "%s: matrices must be finite", who);
+    return ok();
+}
+
+// Validates one frame's bindings against a description (sizes, formats,
+// alignment, aliasing) and fills the kernel arguments.
+int frame_args(const taa_desc_t& d, const taa_uniforms_t& U, uint32_t cas_peak_bits, const taa_frame_io_t* io,
+               const char* who, FrameArgs* out) {
+    const int iw = d.in_width, ih = d.in_height, ow = d.out_width, oh = d.out_height;
+    const size_t ht = history_texel(d.history_format), mt = motion_texel(d.motion_format);
+    const char *hlo = nullptr, *hhi = nullptr, *olo = nullptr, *ohi = nullptr;
+    int rc;
+    if ((rc = check_image("color", io->color, io->color_pitch, iw, ih, 8, true))) return rc;
+    if ((rc = check_image("depth", io->depth, io->depth_pitch, iw, ih, 4, true))) return rc;
+    if ((rc = check_image("velocity", io->velocity, io->velocity_pitch, iw, ih, mt, true))) return rc;
+    if ((rc = check_image("history", io->history, io->history_pitch, ow, oh, ht, false, &hlo, &hhi))) return rc;
+    if ((rc = check_image("history_out", io->history_out, io->history_out_pitch, ow, oh, ht, true, &olo, &ohi))) return rc;
+    bool depth_cull = any_param(U, ow, &taa_parameters_t::mDepthCulling);
+    if ((rc = check_image("history_depth", io->history_depth, io->history_depth_pitch, iw, ih, 4, depth_cull))) return rc;
+    if ((rc = check_image("result", io->result, io->result_pitch, ow, oh, 8, false))) return rc;
+    if ((rc = check_image("debug", io->debug, io->debug_pitch, ow, oh, 8, false))) return rc;
+    if ((rc = check_image("segmask", io->segmask, io->segmask_pitch, ow, oh, 4, false))) return rc;
+    if ((rc = check_image("material", io->material, io->material_pitch, iw, ih, 4, false))) return rc;
+    if ((rc = check_image("prev_material", io->prev_material, io->prev_material_pitch, iw, ih, 4, false))) return rc;
+    if ((rc = check_image("prev_segmask", io->prev_segmask, io->prev_segmask_pitch, ow, oh, 4, false))) return rc;
+    if ((rc = check_image("uvnrm", io->uvnrm, io->uvnrm_pitch, iw, ih, 16, false))) return rc;
+    const bool sharpen = d.sharpener != TAA_SHARPEN_OFF;
+    if ((rc = check_image("sharpened", io->sharpened, io->sharpened_pitch, ow, oh, 8, sharpen))) return rc;
+    if (hlo && hlo < ohi && olo < hhi) return fail(TAA_E_INVAL, "%s: history and history_out overlap", who);
+
+    FrameArgs& a = *out;
+    a = FrameArgs{};
+    a.color = Img{(const char*)io->color, io->color_pitch, iw, ih};
+    a.depth = Img{(const char*)io->depth, io->depth_pitch, iw, ih};
+    a.history = Img{(const char*)io->history, io->history_pitch, ow, oh};
+    a.history_depth = Img{(const char*)io->history_depth, io->history_depth_pitch, iw, ih};
+    a.velocity = Img{(const char*)io->velocity, io->velocity_pitch, iw, ih};
+    a.material = Img{(const char*)io->material, io->material_pitch, iw, ih};
+    a.prev_material = Img{(const char*)io->prev_material, io->prev_material_pitch, iw, ih};
+    a.prev_segmask = Img{(const char*)io->prev_segmask, io->prev_segmask_pitch, ow, oh};
+    a.uvnrm = Img{(const char*)io->uvnrm, io->uvnrm_pitch, iw, ih};
+    a.result = ImgW{(char*)io->result, io->result_pitch};
+    a.debug = ImgW{(char*)io->debug, io->debug_pitch};
+    a.history_out = ImgW{(char*)io->history_out, io->history_out_pitch};
+    a.segmask = ImgW{(char*)io->segmask, io->segmask_pitch};
+    a.sharpened = ImgW{(char*)io->sharpened, io->sharpened_pitch};
+    a.out_w = ow;
+    a.out_h = oh;
+    a.inv_out_w = 1.0f / (float)ow;
+    a.inv_out_h = 1.0f / (float)oh;
+    a.cas_peak_bits = cas_peak_bits;
+    a.sharpen_factor = d.sharpen_factor;
+    a.neg_zero2 = taa_dev::kNegZeroPair;
+    cudaError_t se = taa_dev::device_status_word(&a.status);
+    if (se != cudaSuccess) return cuda_fail(se, "device status word");
+    return ok();
+
+}
+
+}  // namespace taa_host
+
+using namespace taa_host;
 
 extern "C" {
 
@@ -307,16 +394,8 @@ static int ensure_scratch(taa_ctx* c) {
 int taa_create(const taa_desc_t* d, taa_ctx** out) {
     if (!d || !out) return fail(TAA_E_INVAL, "taa_create: NULL argument");
     *out = nullptr;
-    if (d->struct_size != sizeof(taa_desc_t)) return fail(TAA_E_INVAL, "taa_create: struct_size %u != %zu", d->struct_size, sizeof(taa_desc_t));
-    if (d->in_width <= 0 || d->in_height <= 0 || d->out_width <= 0 || d->out_height <= 0 || d->in_width > 32768 ||
-        d->in_height > 32768 || d->out_width > 32768 || d->out_height > 32768)
-        return fail(TAA_E_INVAL, "taa_create: image sizes must be in 1..32768");
-    if (d->history_format > TAA_HISTORY_RGBA16F) return fail(TAA_E_INVAL, "taa_create: history_format %u", d->history_format);
-    if (d->motion_format > TAA_MOTION_RG16F) return fail(TAA_E_INVAL, "taa_create: motion_format %u", d->motion_format);
-    if (d->form > TAA_FORM_FP16) return fail(TAA_E_INVAL, "taa_create: form %u", d->form);
-    if (d->sharpener > TAA_SHARPEN_CAS) return fail(TAA_E_INVAL, "taa_create: sharpener %u", d->sharpener);
-    if (!finite(d->sharpen_factor)) return fail(TAA_E_INVAL, "taa_create: sharpen_factor not finite");
-    if (d->flags != 0) return fail(TAA_E_INVAL, "taa_create: flags must be 0");
+    int rc0 = check_desc(*d, "taa_create");
+    if (rc0) return rc0;
     taa_ctx* c = new (std::nothrow) taa_ctx();
     if (!c) return fail(TAA_E_NOMEM, "taa_create: host allocation failed");
     c->desc = *d;
@@ -345,16 +424,8 @@ int taa_destroy(taa_ctx* c) {
 
 int taa_set_uniforms(taa_ctx* c, const taa_uniforms_t* u) {
     if (!c || !u) return fail(TAA_E_INVAL, "taa_set_uniforms: NULL argument");
-    for (int i = 0; i < 2; ++i) {
-        int rc = check_parameters(u->param[i], i);
-        if (rc) return rc;
-    }
-    const float m[] = {u->mJitterNdc[0], u->mJitterNdc[1], u->mSinTime[0], u->mCamNearPlane, u->mCamFarPlane};
-    for (float v : m)
-        if (!finite(v)) return fail(TAA_E_INVAL, "taa_set_uniforms: jitter/time/near/far must be finite");
-    for (int i = 0; i < 16; ++i)
-        if (!finite(u->mHistoryViewProjMatrix[i]) || !finite(u->mInverseViewProjMatrix[i]))
-            return fail(TAA_E_INVAL, "taa_set_uniforms: matrices must be finite");
+    int rc0 = check_uniforms(*u, "taa_set_uniforms");
+    if (rc0) return rc0;
     c->uniforms = *u;
     c->have_uniforms = true;
     return ok();
@@ -396,52 +467,10 @@ int taa_resolve(taa_ctx* c, void* stream, const taa_frame_io_t* io) {
     if (!c->have_uniforms) return fail(TAA_E_INVAL, "taa_resolve: taa_set_uniforms was not called");
     const taa_desc_t& d = c->desc;
     const taa_uniforms_t& U = c->uniforms;
-    const int iw = d.in_width, ih = d.in_height, ow = d.out_width, oh = d.out_height;
-    const size_t ht = history_texel(d.history_format), mt = motion_texel(d.motion_format);
-    const char *hlo = nullptr, *hhi = nullptr, *olo = nullptr, *ohi = nullptr;
-    int rc;
-    if ((rc = check_image("color", io->color, io->color_pitch, iw, ih, 8, true))) return rc;
-    if ((rc = check_image("depth", io->depth, io->depth_pitch, iw, ih, 4, true))) return rc;
-    if ((rc = check_image("velocity", io->velocity, io->velocity_pitch, iw, ih, mt, true))) return rc;
-    if ((rc = check_image("history", io->history, io->history_pitch, ow, oh, ht, false, &hlo, &hhi))) return rc;
-    if ((rc = check_image("history_out", io->history_out, io->history_out_pitch, ow, oh, ht, true, &olo, &ohi))) return rc;
-    bool depth_cull = any_param(U, ow, &taa_parameters_t::mDepthCulling);
-    if ((rc = check_image("history_depth", io->history_depth, io->history_depth_pitch, iw, ih, 4, depth_cull))) return rc;
-    if ((rc = check_image("result", io->result, io->result_pitch, ow, oh, 8, false))) return rc;
-    if ((rc = check_image("debug", io->debug, io->debug_pitch, ow, oh, 8, false))) return rc;
-    if ((rc = check_image("segmask", io->segmask, io->segmask_pitch, ow, oh, 4, false))) return rc;
-    if ((rc = check_image("material", io->material, io->material_pitch, iw, ih, 4, false))) return rc;
-    if ((rc = check_image("prev_material", io->prev_material, io->prev_material_pitch, iw, ih, 4, false))) return rc;
-    if ((rc = check_image("prev_segmask", io->prev_segmask, io->prev_segmask_pitch, ow, oh, 4, false))) return rc;
-    if ((rc = check_image("uvnrm", io->uvnrm, io->uvnrm_pitch, iw, ih, 16, false))) return rc;
-    bool sharpen = d.sharpener != TAA_SHARPEN_OFF;
-    if ((rc = check_image("sharpened", io->sharpened, io->sharpened_pitch, ow, oh, 8, sharpen))) return rc;
-    if (hlo && hlo < ohi && olo < hhi) return fail(TAA_E_INVAL, "taa_resolve: history and history_out overlap");
-
+    const bool sharpen = d.sharpener != TAA_SHARPEN_OFF;
     FrameArgs a{};
-    a.color = Img{(const char*)io->color, io->color_pitch, iw, ih};
-    a.depth = Img{(const char*)io->depth, io->depth_pitch, iw, ih};
-    a.history = Img{(const char*)io->history, io->history_pitch, ow, oh};
-    a.history_depth = Img{(const char*)io->history_depth, io->history_depth_pitch, iw, ih};
-    a.velocity = Img{(const char*)io->velocity, io->velocity_pitch, iw, ih};
-    a.material = Img{(const char*)io->material, io->material_pitch, iw, ih};
-    a.prev_material = Img{(const char*)io->prev_material, io->prev_material_pitch, iw, ih};
-    a.prev_segmask = Img{(const char*)io->prev_segmask, io->prev_segmask_pitch, ow, oh};
-    a.uvnrm = Img{(const char*)io->uvnrm, io->uvnrm_pitch, iw, ih};
-    a.result = ImgW{(char*)io->result, io->result_pitch};
-    a.debug = ImgW{(char*)io->debug, io->debug_pitch};
-    a.history_out = ImgW{(char*)io->history_out, io->history_out_pitch};
-    a.segmask = ImgW{(char*)io->segmask, io->segmask_pitch};
-    a.sharpened = ImgW{(char*)io->sharpened, io->sharpened_pitch};
-    a.out_w = ow;
-    a.out_h = oh;
-    a.inv_out_w = 1.0f / (float)ow;
-    a.inv_out_h = 1.0f / (float)oh;
-    a.cas_peak_bits = c->cas_const1[0];
-    a.sharpen_factor = d.sharpen_factor;
-    a.neg_zero2 = taa_dev::kNegZeroPair;
-    cudaError_t se = taa_dev::device_status_word(&a.status);
-    if (se != cudaSuccess) return cuda_fail(se, "taa_resolve: device status word");
+    int rc = frame_args(d, U, c->cas_const1[0], io, "taa_resolve", &a);
+    if (rc) return rc;
 
     cudaStream_t s = (cudaStream_t)stream;
     int form = select_form(c, io);

@@ -42,6 +42,20 @@ struct FrameArgs {
     uint64_t neg_zero2;          // the FP32 pair (-0.0, -0.0), opaque to the compiler (f32x2.cuh)
 };
 
+// A view of a batch, in device memory: its uniform block and images.
+struct __align__(16) BatchView {
+    taa_uniforms_t U;
+    FrameArgs a;
+};
+// A batch job names a view and one tile of it: view (8 bits), tile row and
+// tile column (12 bits each).
+__host__ __device__ constexpr uint32_t make_job(int view, int tile_x, int tile_y) {
+    return ((uint32_t)view << 24) | ((uint32_t)tile_y << 12) | (uint32_t)tile_x;
+}
+__host__ __device__ constexpr int job_view(uint32_t j) { return (int)(j >> 24); }
+__host__ __device__ constexpr int job_tile_y(uint32_t j) { return (int)((j >> 12) & 0xfffu); }
+__host__ __device__ constexpr int job_tile_x(uint32_t j) { return (int)(j & 0xfffu); }
+
 // Bits of the device status word.
 constexpr unsigned int kStatusWindowTimeout = 1u;  // a history-window copy did not complete in time
 

@@ -50,6 +50,26 @@ cudaError_t device_status_word(unsigned int** out);
 // false when the image cannot be a TMA source (alignment, driver entry point).
 bool encode_history_map(const Img& history, int history_fmt, int box_w, int box_h, CUtensorMap* map);
 
+// The batched persistent resolve (batch_tiled.cu).
+struct BatchKey {
+    int shape;        // tile shape id: 0 32x8, 1 16x16, 2 32x16, 3 16x8, 4 8x8
+    int history_fmt;  // 0 (RGBA32F) only
+    int motion_ch;    // 2 or 4
+    int interp;       // 0 bilinear or 2 Catmull-Rom
+    int hot;          // the benchmark-mode specialisation (tiled::is_hot)
+};
+struct BatchShapeInfo {
+    int tile_w, tile_h, threads;
+    int win_w, win_h;  // history window (texels) = the TMA box
+};
+constexpr int kBatchShapes = 5;
+bool batch_shape_info(int shape, int history_fmt, BatchShapeInfo* out);
+cudaError_t batch_occupancy(const BatchKey& k, int* ctas_per_sm);
+cudaError_t launch_batch(const BatchKey& k, const BatchView* views, const CUtensorMap* maps, const int* tma_ok,
+                         const uint32_t* jobs, int njobs, int grid, cudaStream_t stream);
+// True when the parameters select the benchmark-mode specialisation.
+bool hot_parameters(const taa_parameters_t& P);
+
 // Synthetic renderer (synth.cu).
 cudaError_t launch_synth(const taa_synth_scene_t& s, const float* host_spheres, int frame,
                          const taa_synth_frame_t& out, cudaStream_t stream);

@@ -39,19 +39,32 @@
 namespace taa_dev {
 namespace tiled {
 
-constexpr int TX = 32, TY = 8, NT = TX * TY;
-// resident CTAs per SM the register budget is sized for (a tuning constant)
+// resident threads per SM the register budget of a tile kernel is sized for
+// (a tuning constant: 6 CTAs of 256 threads)
 #ifndef TAA_TILE_MIN_BLOCKS
 #define TAA_TILE_MIN_BLOCKS 6
 #endif
-constexpr int SX = TX + 2, SY = TY + 2, NS = SX * SY;  // staged colour with halo
-constexpr int WIN_MARGIN = 3;                          // motion difference (px) the window absorbs
-constexpr int WW = TX + 3 + 2 * WIN_MARGIN;            // history window width  (texels)
-constexpr int WH = TY + 3 + 2 * WIN_MARGIN;            // history window height (texels)
+constexpr int WIN_MARGIN = 3;  // motion difference (px) the history window absorbs
+
+// A tile shape: TX x TY pixels, one per thread, staged with a 1-pixel halo;
+// its history window spans the reference pixel's Catmull-Rom taps widened by
+// the tile and WIN_MARGIN on each side.
+template <int TX_, int TY_> struct Shape {
+    static constexpr int TX = TX_, TY = TY_, NT = TX * TY;
+    static constexpr int SX = TX + 2, SY = TY + 2, NS = SX * SY;
+    static constexpr int WW = TX + 3 + 2 * WIN_MARGIN;
+    static constexpr int WH = TY + 3 + 2 * WIN_MARGIN;
+    static constexpr int MIN_BLOCKS =
+        TAA_TILE_MIN_BLOCKS * 256 / NT < 1 ? 1 : (TAA_TILE_MIN_BLOCKS * 256 / NT > 32 ? 32 : TAA_TILE_MIN_BLOCKS * 256 / NT);
+    static_assert(NT % 32 == 0 && NT <= 1024, "whole warps");
+    static_assert(NS <= 2 * NT, "each thread stages at most two colour texels");
+};
+using DefaultShape = Shape<32, 8>;
+
 // Stored window width: RGBA16F windows start on an even texel (a TMA copy of
-// half texels starts on a 16-byte boundary), so they are one texel wider.
-template <int HF> struct Win {
-    static constexpr int W = HF == 0 ? WW : WW + 1;
+// half texels starts on a 16-byte boundary), so their width is even.
+template <class S, int HF> struct Win {
+    static constexpr int W = HF == 0 ? S::WW : S::WW + (S::WW & 1);
     static constexpr int ALIGN = HF == 0 ? 1 : 2;
 };
 // Polls of the window's mbarrier before the wait gives up (each poll may
@@ -203,27 +216,38 @@ __device__ __forceinline__ void history_position(const taa_uniforms_t& U, const 
     }
 }
 
-// The resolve kernel.  Pol provides the working colour format and the box,
-// tap, filter and finishing arithmetic (see resolve_tiled.cu, resolve_half.cu).
-// `hmap` is the history image's tensor map (box Win<HF>::W x WH texels) when
-// `tma_ok`; otherwise every window is copied with cp.async.
-template <class Pol, int HF, int MC, int INTERP, bool HOT>
-__global__ void __launch_bounds__(NT, TAA_TILE_MIN_BLOCKS)
-    resolve_tile(const taa_uniforms_t U, const FrameArgs a, const __grid_constant__ CUtensorMap hmap, const int tma_ok) {
+// Shared memory of one tile.
+template <class Pol, class S, int HF> struct TileSmem {
+    typename Pol::Staged col[S::NS];
+    alignas(128) typename HistTexel<HF>::T win[Win<S, HF>::W * S::WH];
+    uint64_t bar;  // completion of the window's TMA copy
+    int org[3];    // window origin x, y and how it is copied (1 TMA, 2 cp.async)
+    int abort;     // a persistent CTA stops after this tile (a window wait gave up)
+};
+
+// One tile of the resolve: pixels (tile_x * TX + i, tile_y * TY + j).  Pol
+// provides the working colour format and the box, tap, filter and finishing
+// arithmetic (policy_f32.cuh, resolve_half.cu).  `hmap` is the history image's
+// tensor map (box Win::W x WH texels) when `tma_ok`; otherwise every window is
+// copied with cp.async.  `sm.bar` is initialised by the caller; `phase` is the
+// barrier phase the next TMA copy completes.  A wait that gives up sets the
+// status bit and leaves the tile's pixels unwritten; in a persistent loop
+// (PERSIST) it also sets sm.abort, which the caller reads after the barrier
+// that separates tiles, so the whole CTA stops together.
+template <class Pol, class S, int HF, int MC, int INTERP, bool HOT, bool PERSIST>
+__device__ __forceinline__ void tile_body(const taa_uniforms_t& U, const FrameArgs& a, const CUtensorMap* hmap,
+                                          bool tma_ok, int tile_x, int tile_y, TileSmem<Pol, S, HF>& sm,
+                                          uint32_t& phase) {
     using HT = typename HistTexel<HF>::T;
-    using Staged = typename Pol::Staged;
-    constexpr int WWS = Win<HF>::W;
-    __shared__ Staged s_col[NS];
-    __shared__ __align__(128) HT s_win[WWS * WH];
-    __shared__ uint64_t s_bar;
-    __shared__ int s_org[3];  // window origin x, y and how it is copied (1 TMA, 2 cp.async)
+    constexpr int TX = S::TX, TY = S::TY, NT = S::NT, SX = S::SX, NS = S::NS, WH = S::WH;
+    constexpr int WWS = Win<S, HF>::W;
 
     const taa_parameters_t& P = U.param[0];
     const Mode<HOT> M{P};
     const int tid = threadIdx.x;
     const int lx = tid % TX, ly = tid / TX;
     const int W = a.out_w, H = a.out_h;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+    const int x0 = tile_x * TX, y0 = tile_y * TY;
     const int x = x0 + lx, y = y0 + ly;
     const bool inside = x < W && y < H;
     const int cx = min(x, W - 1), cy = min(y, H - 1);
@@ -258,24 +282,23 @@ __global__ void __launch_bounds__(NT, TAA_TILE_MIN_BLOCKS)
         const int rux = trunc_index(floorf(rhu * (float)hi.w - 0.5f)) - k0;
         const int ruy = trunc_index(floorf(rhv * (float)hi.h - 0.5f)) - k0;
         // the reference pixel sits at (rx - x0, ry - y0) in the tile; floor to the stored alignment
-        const int wx0 = (rux - (rx - x0) - WIN_MARGIN) & ~(Win<HF>::ALIGN - 1);
+        const int wx0 = (rux - (rx - x0) - WIN_MARGIN) & ~(Win<S, HF>::ALIGN - 1);
         const int wy0 = ruy - (ry - y0) - WIN_MARGIN;
         const bool interior = wx0 >= 0 && wy0 >= 0 && wx0 <= hi.w - WWS && wy0 <= hi.h - WH;
         const int mode = tma_ok && interior ? 1 : 2;
         if (tid == 0) {
-            s_org[0] = wx0;
-            s_org[1] = wy0;
-            s_org[2] = mode;
+            sm.org[0] = wx0;
+            sm.org[1] = wy0;
+            sm.org[2] = mode;
             if (mode == 1) {
-                mbar_init(&s_bar, 1);
-                mbar_expect_tx(&s_bar, (uint32_t)sizeof(s_win));
-                if (HF == 0) tma_load_3d(s_win, &hmap, 0, wx0, wy0, &s_bar);
-                else tma_load_2d(s_win, &hmap, 4 * wx0, wy0, &s_bar);
+                mbar_expect_tx(&sm.bar, (uint32_t)sizeof(sm.win));
+                if (HF == 0) tma_load_3d(sm.win, hmap, 0, wx0, wy0, &sm.bar);
+                else tma_load_2d(sm.win, hmap, 4 * wx0, wy0, &sm.bar);
             }
         }
     }
 
-    // own history position and taps; (u, v) = (texel + 0.5) / size, correctly rounded, as a pair
+    // own history position; (u, v) = (texel + 0.5) / size, correctly rounded, as a pair
     const f2 z{a.neg_zero2};
     const f2 uv = div_const_rn2(add2(pk((float)cx, (float)cy), dup(0.5f)), pk(-(float)W, -(float)H),
                                 pk(a.inv_out_w, a.inv_out_h), z);
@@ -292,14 +315,14 @@ __global__ void __launch_bounds__(NT, TAA_TILE_MIN_BLOCKS)
 
     // 3. staged colour in the policy's working format
     const bool tm = M.tonemap(), yc = M.ycocg();
-    s_col[tid] = Pol::stage(st0, tm, yc);
-    if (tid + NT < NS) s_col[tid + NT] = Pol::stage(st1, tm, yc);
+    sm.col[tid] = Pol::stage(st0, tm, yc);
+    if (tid + NT < NS) sm.col[tid + NT] = Pol::stage(st1, tm, yc);
     __syncthreads();
     int wx0 = 0, wy0 = 0, mode = 0;
     if (windowed) {
-        wx0 = s_org[0];
-        wy0 = s_org[1];
-        mode = s_org[2];
+        wx0 = sm.org[0];
+        wy0 = sm.org[1];
+        mode = sm.org[2];
     }
     if (mode == 2) {
         // a window across the image border: every texel edge-clamped
@@ -308,70 +331,132 @@ __global__ void __launch_bounds__(NT, TAA_TILE_MIN_BLOCKS)
             const int gy = clampi(wy0 + r, 0, hi.h - 1);
             const char* row = hi.p + (size_t)gy * hi.pitch;
             for (int c = lane; c < WWS; c += 32)
-                cp_async<HistTexel<HF>::B>(&s_win[r * WWS + c],
+                cp_async<HistTexel<HF>::B>(&sm.win[r * WWS + c],
                                            row + (size_t)clampi(wx0 + c, 0, hi.w - 1) * HistTexel<HF>::B);
         }
         cp_async_commit();
     }
     // the 3x3 box while the window is in flight
     typename Pol::Box box;
-    Pol::template box<HOT>(&s_col[(ly + 1) * SX + lx + 1], SX, M, P.mVarClipGamma, box, z);
+    Pol::template box<HOT>(&sm.col[(ly + 1) * SX + lx + 1], SX, M, P.mVarClipGamma, box, z);
     if (Pol::kExactCentre) Pol::centre_colour(box, a.color, cx, cy, tm, yc);
 
+    bool landed = true;
     if (mode == 1) {
-        if (!mbar_wait_bounded(&s_bar, 0)) {
+        landed = mbar_wait_bounded(&sm.bar, phase & 1u);
+        if (!landed) {
             atomicOr(a.status, kStatusWindowTimeout);
-            mbar_wait_bounded(&s_bar, 0);  // the copy may still land in this CTA's memory
-            return;
+            mbar_wait_bounded(&sm.bar, phase & 1u);  // the copy may still land in this CTA's memory
+            if (PERSIST) sm.abort = 1;
         }
+        phase ^= 1u;
     } else if (mode == 2) {
         cp_async_wait_all();
         __syncthreads();
     }
-    if (!inside) return;
+    if (inside && landed) {
+        // rejection (taa.comp:787-823) first, so its inputs die before the filter
+        bool rejected = false;
+        if (P.mRejectOutside && (hu < 0.f || hv < 0.f || hu >= 1.f || hv >= 1.f)) rejected = true;
+        if (depth_cull) {
+            float hd = prev_depth;
+            if (fabsf(hd - ehd) > 0.1f * (1.0f - hd)) rejected = true;
+        }
 
-    // rejection (taa.comp:787-823) first, so its inputs die before the filter
-    bool rejected = false;
-    if (P.mRejectOutside && (hu < 0.f || hv < 0.f || hu >= 1.f || hv >= 1.f)) rejected = true;
-    if (depth_cull) {
-        float hd = prev_depth;
-        if (fabsf(hd - ehd) > 0.1f * (1.0f - hd)) rejected = true;
-    }
+        // 4. history sample: from the window when all taps fall inside it
+        float4 hraw = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (have_hist) {
+            HistoryTaps<Pol, INTERP> taps;
+            taps.setup(hu, hv, hi.w, hi.h, z);
+            const int span = INTERP == 2 ? 4 : 2;
+            const int bx = taps.t[0].ux - wx0, by = taps.t[0].uy - wy0;
+            const bool in_win = windowed && bx >= 0 && by >= 0 && bx + span <= WWS && by + span <= WH;
+            if (in_win) {
+                const HT* base = &sm.win[by * WWS + bx];
+                hraw = Pol::template filter_window<INTERP, HF>(taps, base, WWS);
+            } else {
+                hraw = Pol::template filter<INTERP>(
+                    taps, hi.w, hi.h, [&](int tx_, int ty_) { return fetch_history<HF>(hi, tx_, ty_); });
+            }
+        }
 
-    // 4. history sample: from the window when all taps fall inside it
-    float4 hraw = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (have_hist) {
-        HistoryTaps<Pol, INTERP> taps;
-        taps.setup(hu, hv, hi.w, hi.h, z);
-        const int span = INTERP == 2 ? 4 : 2;
-        const int bx = taps.t[0].ux - wx0, by = taps.t[0].uy - wy0;
-        const bool in_win = windowed && bx >= 0 && by >= 0 && bx + span <= WWS && by + span <= WH;
-        if (in_win) {
-            const HT* base = &s_win[by * WWS + bx];
-            hraw = Pol::template filter_window<INTERP, HF>(taps, base, WWS);
-        } else {
-            hraw = Pol::template filter<INTERP>(taps, hi.w, hi.h,
-                                                [&](int tx_, int ty_) { return fetch_history<HF>(hi, tx_, ty_); });
+        const C3 c0 = Pol::centre(box, &sm.col[(ly + 1) * SX + lx + 1]);
+        float4 o = Pol::template finish<HOT>(U, P, M, box, c0, hraw, u, v, hu, hv, rejected);
+        store_history<HF>(a.history_out, x, y, make_float4(o.x, o.y, o.z, 0.f));
+        if (a.result.p) {
+            if (tm) o = Pol::un_tonemap(o);
+            store_rgba16f(a.result, x, y, make_float4(o.x, o.y, o.z, 1.0f));
         }
     }
+}
 
-    const C3 c0 = Pol::centre(box, &s_col[(ly + 1) * SX + lx + 1]);
-    float4 o = Pol::template finish<HOT>(U, P, M, box, c0, hraw, u, v, hu, hv, rejected);
-    store_history<HF>(a.history_out, x, y, make_float4(o.x, o.y, o.z, 0.f));
-    if (a.result.p) {
-        if (tm) o = Pol::un_tonemap(o);
-        store_rgba16f(a.result, x, y, make_float4(o.x, o.y, o.z, 1.0f));
+// One view, one CTA per tile.
+template <class Pol, class S, int HF, int MC, int INTERP, bool HOT>
+__global__ void __launch_bounds__(S::NT, S::MIN_BLOCKS)
+    resolve_tile(const taa_uniforms_t U, const FrameArgs a, const __grid_constant__ CUtensorMap hmap, const int tma_ok) {
+    __shared__ TileSmem<Pol, S, HF> sm;
+    if (threadIdx.x == 0) mbar_init(&sm.bar, 1);
+    uint32_t phase = 0;
+    tile_body<Pol, S, HF, MC, INTERP, HOT, false>(U, a, &hmap, tma_ok != 0, blockIdx.x, blockIdx.y, sm, phase);
+}
+
+// Resident CTAs per SM the batch kernels' register budget is sized for.
+#ifndef TAA_BATCH_MIN_BLOCKS
+#define TAA_BATCH_MIN_BLOCKS 5
+#endif
+template <class S> constexpr int batch_min_blocks() {
+    return TAA_BATCH_MIN_BLOCKS * 256 / S::NT < 1 ? 1
+                                                  : (TAA_BATCH_MIN_BLOCKS * 256 / S::NT > 32 ? 32
+                                                                                             : TAA_BATCH_MIN_BLOCKS * 256 / S::NT);
+}
+
+// Many views in one launch: each CTA takes jobs blockIdx.x, blockIdx.x +
+// gridDim.x, ... from the schedule's job list (BatchView and the job encoding
+// are in common.cuh) - a persistent loop when the grid is smaller than the
+// list.  A view's arguments are copied into shared memory when a CTA's job
+// moves to another view.  maps[v] is view v's history tensor map for this tile
+// shape, usable when tma_ok[v].
+template <class Pol, class S, int HF, int MC, int INTERP, bool HOT>
+__global__ void __launch_bounds__(S::NT, batch_min_blocks<S>())
+    resolve_batch(const BatchView* __restrict__ views, const CUtensorMap* __restrict__ maps,
+                  const int* __restrict__ tma_ok, const uint32_t* __restrict__ jobs, const int njobs) {
+    __shared__ TileSmem<Pol, S, HF> sm;
+    __shared__ __align__(16) BatchView s_view;
+    static_assert(sizeof(BatchView) % 16 == 0, "copied as 16-byte words");
+    constexpr int kWords = (int)(sizeof(BatchView) / 16);
+    if (threadIdx.x == 0) {
+        mbar_init(&sm.bar, 1);
+        sm.abort = 0;
+    }
+    uint32_t phase = 0;
+    int cur_view = -1;
+    for (int j = blockIdx.x; j < njobs; j += gridDim.x) {
+        const uint32_t job = __ldg(jobs + j);
+        const int vi = job_view(job);
+        if (vi != cur_view) {
+            const uint4* src = reinterpret_cast<const uint4*>(views + vi);
+            for (int w = threadIdx.x; w < kWords; w += S::NT) reinterpret_cast<uint4*>(&s_view)[w] = __ldg(src + w);
+            if (threadIdx.x == 0)
+                asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;\n" ::"l"(maps + vi) : "memory");
+            cur_view = vi;
+            __syncthreads();
+        }
+        tile_body<Pol, S, HF, MC, INTERP, HOT, true>(s_view.U, s_view.a, maps + vi, __ldg(tma_ok + vi) != 0,
+                                                     job_tile_x(job), job_tile_y(job), sm, phase);
+        __syncthreads();  // the next tile reuses the shared memory
+        if (sm.abort) return;
     }
 }
 
 template <class Pol, int HF, int MC, int INTERP, bool HOT>
 cudaError_t launch_tile(const taa_uniforms_t& U, const FrameArgs& a, cudaStream_t s) {
-    dim3 grid((a.out_w + TX - 1) / TX, (a.out_h + TY - 1) / TY);
+    using S = DefaultShape;
+    dim3 grid((a.out_w + S::TX - 1) / S::TX, (a.out_h + S::TY - 1) / S::TY);
     CUtensorMap map;
     std::memset(&map, 0, sizeof map);
-    const int tma_ok = INTERP != 1 && a.history.p && a.history.w >= Win<HF>::W && a.history.h >= WH &&
-                       encode_history_map(a.history, HF, Win<HF>::W, WH, &map);
-    resolve_tile<Pol, HF, MC, INTERP, HOT><<<grid, NT, 0, s>>>(U, a, map, tma_ok);
+    const int tma_ok = INTERP != 1 && a.history.p && a.history.w >= Win<S, HF>::W && a.history.h >= S::WH &&
+                       encode_history_map(a.history, HF, Win<S, HF>::W, S::WH, &map);
+    resolve_tile<Pol, S, HF, MC, INTERP, HOT><<<grid, S::NT, 0, s>>>(U, a, map, tma_ok);
     return cudaGetLastError();
 }
 template <class Pol, int HF, int MC>

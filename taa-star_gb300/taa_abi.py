@@ -86,6 +86,16 @@ class JitterOpts(C.Structure):
                 ("extra_scale", C.c_float)]
 
 
+class BatchTuning(C.Structure):
+    _fields_ = [("tile_w", C.c_int32), ("tile_h", C.c_int32), ("schedule", C.c_int32), ("ctas_per_sm", C.c_int32),
+                ("ms", C.c_float)]
+
+
+TAA_SCHEDULE_VIEW_ORDER, TAA_SCHEDULE_LARGEST_FIRST, TAA_SCHEDULE_INTERLEAVED = 0, 1, 2
+BATCH_SLOTS = 4
+TAA_BATCH_CTA_PER_TILE = -1
+
+
 class SynthScene(C.Structure):
     _fields_ = [
         ("struct_size", C.c_uint32), ("width", C.c_int32), ("height", C.c_int32), ("seed", C.c_uint64),
@@ -111,7 +121,9 @@ assert C.sizeof(Parameters) == 176 and C.sizeof(Uniforms) == 544
 EXPORTS = ["taa_version", "taa_last_error", "taa_default_parameters", "taa_get_jitter_offset",
            "taa_jittered_projection", "taa_compose_matrices", "taa_cas_setup", "taa_create", "taa_destroy",
            "taa_set_uniforms", "taa_set_sharpener", "taa_selected_form", "taa_resolve",
-           "taa_resolve_static_scratch", "taa_device_status",
+           "taa_resolve_static_scratch", "taa_device_status", "taa_batch_create", "taa_batch_destroy",
+           "taa_batch_set_uniforms", "taa_batch_prepare", "taa_batch_launch", "taa_batch_autotune",
+           "taa_batch_get_tuning", "taa_batch_set_tuning",
            "taa_synth_default_scene", "taa_synth_spheres", "taa_synth_jitter", "taa_synth_camera",
            "taa_synth_render"]
 
@@ -145,6 +157,14 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
         "taa_resolve": (C.c_int, [C.c_void_p, C.c_void_p, P(FrameIO)]),
         "taa_resolve_static_scratch": (C.c_int, [C.c_void_p, C.c_void_p, P(FrameIO), C.c_uint32, C.c_float]),
         "taa_device_status": (C.c_int, [P(C.c_uint32), C.c_int]),
+        "taa_batch_create": (C.c_int, [P(Desc), C.c_int32, P(C.c_void_p)]),
+        "taa_batch_destroy": (C.c_int, [C.c_void_p]),
+        "taa_batch_set_uniforms": (C.c_int, [C.c_void_p, C.c_int32, P(Uniforms)]),
+        "taa_batch_prepare": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, P(FrameIO)]),
+        "taa_batch_launch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
+        "taa_batch_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, P(BatchTuning)]),
+        "taa_batch_get_tuning": (C.c_int, [C.c_void_p, P(BatchTuning)]),
+        "taa_batch_set_tuning": (C.c_int, [C.c_void_p, P(BatchTuning)]),
         "taa_synth_default_scene": (C.c_int, [P(SynthScene), C.c_int32, C.c_int32, C.c_uint64]),
         "taa_synth_spheres": (C.c_int, [P(SynthScene), P(C.c_float), C.c_int32]),
         "taa_synth_jitter": (C.c_int, [P(SynthScene), C.c_int32, P(C.c_float), P(C.c_float)]),
@@ -256,6 +276,70 @@ class Taa:
             setattr(io, name, p)
             setattr(io, name + "_pitch", pitch)
         check(self.lib.taa_resolve(self.handle, C.c_void_p(stream), C.byref(io)))
+
+
+def frame_io(**bindings) -> FrameIO:
+    """A taa_frame_io_t from name=tensor (or None) bindings."""
+    io = FrameIO()
+    for name, t in bindings.items():
+        if name not in _IO_NAMES:
+            raise KeyError(name)
+        if t is None:
+            continue
+        p, pitch = tensor_ptr_pitch(t)
+        setattr(io, name, p)
+        setattr(io, name + "_pitch", pitch)
+    return io
+
+
+class Batch:
+    """A batch of views resolved by one persistent launch (taa_batch_*)."""
+
+    def __init__(self, sizes, motion_format=TAA_MOTION_RG16F):
+        self.lib = load()
+        self.n = len(sizes)
+        descs = (Desc * self.n)()
+        for i, (w, h) in enumerate(sizes):
+            descs[i] = Desc(C.sizeof(Desc), w, h, w, h, TAA_HISTORY_RGBA32F, motion_format, TAA_FORM_AUTO,
+                            TAA_SHARPEN_OFF, 0.5, 0)
+        h = C.c_void_p()
+        check(self.lib.taa_batch_create(descs, self.n, C.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            self.lib.taa_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_uniforms(self, view: int, u: Uniforms):
+        check(self.lib.taa_batch_set_uniforms(self.handle, view, C.byref(u)))
+
+    def prepare(self, slot: int, views: list[dict], stream: int = 0):
+        ios = (FrameIO * self.n)(*[frame_io(**v) for v in views])
+        check(self.lib.taa_batch_prepare(self.handle, C.c_void_p(stream), slot, ios))
+
+    def launch(self, slot: int, stream: int = 0):
+        check(self.lib.taa_batch_launch(self.handle, C.c_void_p(stream), slot))
+
+    def autotune(self, slot: int, reps: int = 3, stream: int = 0) -> BatchTuning:
+        t = BatchTuning()
+        check(self.lib.taa_batch_autotune(self.handle, C.c_void_p(stream), slot, reps, C.byref(t)))
+        return t
+
+    def tuning(self) -> BatchTuning:
+        t = BatchTuning()
+        check(self.lib.taa_batch_get_tuning(self.handle, C.byref(t)))
+        return t
+
+    def set_tuning(self, tile_w, tile_h, schedule, ctas_per_sm=0):
+        t = BatchTuning(tile_w, tile_h, schedule, ctas_per_sm, 0.0)
+        check(self.lib.taa_batch_set_tuning(self.handle, C.byref(t)))
 
 
 def synth_default_scene(w, h, seed) -> SynthScene:

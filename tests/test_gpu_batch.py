@@ -1,0 +1,150 @@
+"""The batched resolve (taa_batch_*) against per-view taa_resolve (run with -m gpu).
+
+A batch resolves views of different sizes in one persistent launch; every
+view must get exactly the bits its own taa_resolve gives in the tiled FP32
+form, whatever tile shape and job order the batch runs with, when the launch
+is replayed from a CUDA graph, and after taa_batch_autotune has picked its
+configuration.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+import taa_abi as T
+import workloads as WL
+from helpers import cpu_frames, to_dev
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [(70, 41), (17, 9), (256, 96), (33, 31), (128, 72), (64, 36)]
+SHAPES = [(32, 8), (16, 16), (32, 16), (16, 8), (8, 8)]
+
+
+def make_views(dev, sizes, params=None, motion_channels=2):
+    views = []
+    for i, (w, h) in enumerate(sizes):
+        wl = WL.small(w, h, frames=2, seed=20 + i, params=params or {})
+        fr = cpu_frames(wl, range(2), motion_channels=motion_channels)
+        u = T.make_uniforms(wl.parameters(), jitter_ndc=fr[1]["jitter"])
+        b = dict(color=to_dev(fr[1]["color"], torch.float16, dev), depth=to_dev(fr[1]["depth"], torch.float32, dev),
+                 velocity=to_dev(fr[1]["motion"], torch.float16, dev),
+                 history=to_dev(fr[0]["color"].astype(np.float32), torch.float32, dev),
+                 history_depth=to_dev(fr[0]["depth"], torch.float32, dev),
+                 history_out=torch.full((h, w, 4), float("nan"), device=dev),
+                 result=torch.full((h, w, 4), float("nan"), dtype=torch.float16, device=dev))
+        views.append(dict(size=(w, h), u=u, b=b))
+    return views
+
+
+def reference(views, motion_format):
+    out = []
+    for v in views:
+        w, h = v["size"]
+        ctx = T.Taa(w, h, motion_format=motion_format, form=T.TAA_FORM_TILED)
+        ctx.set_uniforms(v["u"])
+        b = dict(v["b"])
+        b["history_out"] = torch.full_like(b["history_out"], float("nan"))
+        b["result"] = torch.full_like(b["result"], float("nan"))
+        ctx.resolve(**b)
+        torch.cuda.synchronize()
+        out.append((b["history_out"].cpu().numpy(), b["result"].float().cpu().numpy()))
+        ctx.close()
+    return out
+
+
+def reset_outputs(views):
+    for v in views:
+        v["b"]["history_out"].fill_(float("nan"))
+        v["b"]["result"].fill_(float("nan"))
+
+
+def check_equal(views, ref):
+    torch.cuda.synchronize()
+    for v, (h_ref, r_ref) in zip(views, ref):
+        np.testing.assert_array_equal(v["b"]["history_out"].cpu().numpy(), h_ref, err_msg=str(v["size"]))
+        np.testing.assert_array_equal(v["b"]["result"].float().cpu().numpy(), r_ref, err_msg=str(v["size"]))
+
+
+def make_batch(views, motion_format):
+    batch = T.Batch([v["size"] for v in views], motion_format=motion_format)
+    for i, v in enumerate(views):
+        batch.set_uniforms(i, v["u"])
+    batch.prepare(0, [v["b"] for v in views])
+    return batch
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+@pytest.mark.parametrize("schedule", [T.TAA_SCHEDULE_VIEW_ORDER, T.TAA_SCHEDULE_LARGEST_FIRST,
+                                      T.TAA_SCHEDULE_INTERLEAVED])
+def test_batch_equals_per_view_resolve(cuda, shape, schedule):
+    views = make_views(cuda, SIZES)
+    ref = reference(views, T.TAA_MOTION_RG16F)
+    batch = make_batch(views, T.TAA_MOTION_RG16F)
+    for grid_mode in (0, T.TAA_BATCH_CTA_PER_TILE, 1):
+        batch.set_tuning(shape[0], shape[1], schedule, grid_mode)
+        reset_outputs(views)
+        batch.launch(0)
+        check_equal(views, ref)
+    batch.close()
+
+
+@pytest.mark.parametrize("mode", ["bilinear_clamp", "rgba16f_motion"])
+def test_batch_other_modes(cuda, mode):
+    params = dict(mInterpolationMode=0, mColorClampingOrClipping=1) if mode == "bilinear_clamp" else {}
+    mc, mf = (4, T.TAA_MOTION_RGBA16F) if mode == "rgba16f_motion" else (2, T.TAA_MOTION_RG16F)
+    views = make_views(cuda, SIZES[:4], params=params, motion_channels=mc)
+    ref = reference(views, mf)
+    batch = make_batch(views, mf)
+    for shape in ((16, 16), (8, 8)):
+        batch.set_tuning(shape[0], shape[1], T.TAA_SCHEDULE_INTERLEAVED)
+        reset_outputs(views)
+        batch.launch(0)
+        check_equal(views, ref)
+    batch.close()
+
+
+def test_autotune_then_graph_replay(cuda):
+    views = make_views(cuda, SIZES)
+    ref = reference(views, T.TAA_MOTION_RG16F)
+    batch = make_batch(views, T.TAA_MOTION_RG16F)
+    best = batch.autotune(0, reps=2)
+    assert (best.tile_w, best.tile_h) in SHAPES and best.ms > 0
+    t = batch.tuning()
+    assert (t.tile_w, t.tile_h, t.schedule) == (best.tile_w, best.tile_h, best.schedule)
+    reset_outputs(views)
+    batch.launch(0)
+    check_equal(views, ref)
+    # the launch captured into a CUDA graph, replayed
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        batch.launch(0, stream=torch.cuda.current_stream().cuda_stream)
+    reset_outputs(views)
+    torch.cuda.synchronize()
+    g.replay()
+    check_equal(views, ref)
+    reset_outputs(views)
+    g.replay()
+    check_equal(views, ref)
+    assert T.device_status(clear=True) == 0
+    batch.close()
+
+
+def test_batch_rejects_what_it_does_not_run(cuda):
+    lib = T.load()
+    d = (T.Desc * 2)()
+    d[0] = T.Desc(C.sizeof(T.Desc), 64, 32, 64, 32, T.TAA_HISTORY_RGBA32F, T.TAA_MOTION_RG16F, 0, 0, 0.5, 0)
+    d[1] = T.Desc(C.sizeof(T.Desc), 64, 32, 64, 32, T.TAA_HISTORY_RGBA32F, T.TAA_MOTION_RGBA16F, 0, 0, 0.5, 0)
+    h = C.c_void_p()
+    assert lib.taa_batch_create(d, 2, C.byref(h)) == T.TAA_E_UNSUPPORTED  # mixed motion formats
+    d[1] = T.Desc(C.sizeof(T.Desc), 32, 16, 64, 32, T.TAA_HISTORY_RGBA32F, T.TAA_MOTION_RG16F, 0, 0, 0.5, 0)
+    assert lib.taa_batch_create(d, 2, C.byref(h)) == T.TAA_E_UNSUPPORTED  # upsampling
+    d[1] = T.Desc(C.sizeof(T.Desc), 64, 32, 64, 32, T.TAA_HISTORY_RGBA16F, T.TAA_MOTION_RG16F, 0, 0, 0.5, 0)
+    assert lib.taa_batch_create(d, 2, C.byref(h)) == T.TAA_E_UNSUPPORTED  # RGBA16F history
+    batch = T.Batch([(64, 32), (32, 16)])
+    assert lib.taa_batch_launch(batch.handle, None, 0) == T.TAA_E_INVAL  # slot never prepared
+    bad = T.BatchTuning(24, 8, 0, 0, 0.0)
+    assert lib.taa_batch_set_tuning(batch.handle, C.byref(bad)) == T.TAA_E_INVAL
+    batch.close()
