@@ -43,7 +43,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--profile", choices=["tiled", "fp16", "plain", "batch48"],
+                    help="a small case for ncu: a few launches of one form on 4K frames (no JSON line)")
     return ap.parse_args()
 
 
@@ -189,6 +192,60 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------ our arm
+def time_batch(T, WL, dev, stream, sid, world, args, peak, single_mpx):
+    """48 views of the C4 sizes resolved by one batched launch per step; the
+    batch is autotuned first (tile shape, job order, grid).  Returns its Mpx/s,
+    GB/s and the per-pixel ratio to the single-4K number."""
+    import torch
+    import torch.distributed as dist
+
+    views = WL.c4_views()
+    npx = sum(v.width * v.height for v in views)
+    bufs = []
+    for v in views:
+        sc, w, h = v.scene(), v.width, v.height
+        col = [torch.empty(h, w, 4, dtype=torch.float16, device=dev) for _ in range(2)]
+        dep = [torch.empty(h, w, dtype=torch.float32, device=dev) for _ in range(2)]
+        mot = [torch.empty(h, w, 2, dtype=torch.float16, device=dev) for _ in range(2)]
+        for f in range(2):
+            T.synth_render(sc, f, stream=sid, color=col[f], depth=dep[f], motion=mot[f])
+        u = T.make_uniforms(v.parameters(), jitter_ndc=T.synth_jitter(sc, 1)[1])
+        bufs.append(dict(u=u, b=dict(color=col[1], depth=dep[1], velocity=mot[1], history=col[0].float(),
+                                     history_depth=dep[0], history_out=torch.empty(h, w, 4, device=dev),
+                                     result=torch.empty(h, w, 4, dtype=torch.float16, device=dev))))
+    torch.cuda.synchronize()
+    batch = T.Batch([(v.width, v.height) for v in views])
+    for i, b in enumerate(bufs):
+        batch.set_uniforms(i, b["u"])
+    batch.prepare(0, [b["b"] for b in bufs], stream=sid)
+    best = batch.autotune(0, reps=3, stream=sid)
+    for _ in range(args.warmup):
+        batch.launch(0, stream=sid)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    k = max(3, args.steps)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(k):
+        batch.launch(0, stream=sid)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    batch.close()
+    mpx = world * npx * k / (ms / 1e3) / 1e6
+    gbs = views[0].bytes_per_pixel(history_bytes=16, motion_bytes=4) * npx / (ms / 1e3 / k) / 1e9
+    return {"mpx_s": mpx, "gb_s": gbs, "frac_of_hbm": gbs / peak, "views": len(views), "pixels": npx,
+            "per_pixel_vs_single_4k": (mpx / world) / single_mpx,
+            "tuning": {"tile": [best.tile_w, best.tile_h], "schedule": best.schedule,
+                       "grid": "one CTA per tile" if best.ctas_per_sm == T.TAA_BATCH_CTA_PER_TILE else "persistent"},
+            "launches_per_step": 1}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -294,6 +351,10 @@ def run_ours(args):
             g = launch_bytes / (m2 / 1e3 / (k * F)) / 1e9
             forms[name] = {"mpx_s": v, "gb_s": g, "frac_of_hbm": g / peak}
             c2.close()
+
+    # the 48-view batch (C4 sizes, log-uniform 320x180 .. 3840x2160): one launch per step
+    if not args.no_batch:
+        forms["batch48"] = time_batch(T, WL, dev, stream, sid, world, args, peak, mpx / world)
 
     # end to end through the C ABI with host buffers (pinned), copies inside the timed region
     e2e = None
@@ -404,8 +465,49 @@ def run_ours(args):
     return 0
 
 
+def run_profile_case(args):
+    """A few launches of one form on 3 frames of the 4K workload (or one batch
+    of the C4 views), for an ncu capture: about 1 GB on the device."""
+    import torch
+    import taa_abi as T
+    import workloads as WL
+    from importlib import util
+    spec = util.spec_from_file_location("taa_lib_build", ROOT / "taa-star_gb300" / "build.py")
+    m = util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    m.build_library()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    sid = stream.cuda_stream
+    if args.profile == "batch48":
+        args.steps, args.warmup = 3, 1
+        print(json.dumps(time_batch(T, WL, dev, stream, sid, 1, args, 1.0, 1.0)))
+        return 0
+    wl = WL.c2()
+    H, W, F = wl.height, wl.width, 3
+    sc = wl.scene()
+    col = torch.empty(F, H, W, 4, dtype=torch.float16, device=dev)
+    dep = torch.empty(F, H, W, dtype=torch.float32, device=dev)
+    mot = torch.empty(F, H, W, 2, dtype=torch.float16, device=dev)
+    for f in range(F):
+        T.synth_render(sc, f, stream=sid, color=col[f], depth=dep[f], motion=mot[f])
+    hist = [torch.zeros(H, W, 4, dtype=torch.float32, device=dev) for _ in range(2)]
+    res = torch.empty(H, W, 4, dtype=torch.float16, device=dev)
+    form = {"tiled": T.TAA_FORM_TILED, "fp16": T.TAA_FORM_FP16, "plain": T.TAA_FORM_PLAIN}[args.profile]
+    ctx = T.Taa(W, H, form=form)
+    for f in range(1, F):
+        ctx.set_uniforms(T.make_uniforms(wl.parameters(), jitter_ndc=T.synth_jitter(sc, f)[1]))
+        ctx.resolve(stream=sid, color=col[f], depth=dep[f], velocity=mot[f], history=hist[f & 1],
+                    history_depth=dep[f - 1], history_out=hist[(f + 1) & 1], result=res)
+    torch.cuda.synchronize()
+    ctx.close()
+    return 0
+
+
 def main():
     args = parse()
+    if args.profile:
+        return run_profile_case(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)
