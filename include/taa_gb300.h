@@ -62,6 +62,7 @@ typedef enum taa_status {
 #define TAA_FORM_PLAIN  1u  /* one thread per pixel, FP32, every parameter honoured */
 #define TAA_FORM_TILED  2u  /* FP32, CTA tile staged in shared memory */
 #define TAA_FORM_FP16   3u  /* packed half2 neighbourhood, clip and sharpen; FP32 history and blend */
+#define TAA_FORM_LEARNED 4u /* blend weight and clip-box scale from a per-pixel MLP (taa_set_mlp) */
 /* Sharpener (taa<CF>::mSharpener, source/taa.hpp:1418). */
 #define TAA_SHARPEN_OFF     0u
 #define TAA_SHARPEN_SIMPLE  1u  /* shaders/sharpen.comp */
@@ -227,6 +228,73 @@ int taa_batch_launch(taa_batch* batch, void* stream, int32_t slot);
 int taa_batch_autotune(taa_batch* batch, void* stream, int32_t slot, int32_t reps, taa_batch_tuning_t* best);
 int taa_batch_get_tuning(const taa_batch* batch, taa_batch_tuning_t* out);
 int taa_batch_set_tuning(taa_batch* batch, const taa_batch_tuning_t* tuning);
+
+/* ---- the learned rectifier (TAA_FORM_LEARNED) -----------------------------
+ * No counterpart in the reference.  A per-pixel MLP (32 features -> 32 -> 32
+ * -> 2, ReLU; FP16 weights, FP32 accumulation on the tensor cores) predicts
+ * the blend weight (sigmoid of output 0) and the scale of the variance clip
+ * box (2 to the power of output 1) from the pixel's 3x3 mean, standard
+ * deviation, minimum and maximum, history, current colour, velocity length
+ * and depth difference (all in YCoCg, normalised by the mean luma).  Where the
+ * scale leaves [0.5, 2] the pixel falls back to the plain variance clip with
+ * mAlpha; rejected pixels blend with mRejectionAlpha as in the shader.  The
+ * form runs YCoCg variance clipping with Catmull-Rom history, RGBA32F
+ * history, equal source and target sizes and no sharpener. */
+typedef struct taa_mlp_weights_t {
+    float w1[32 * 32], b1[32];  /* layer 1, row-major [out][in] */
+    float w2[32 * 32], b2[32];  /* layer 2 */
+    float w3[2 * 32], b3[2];    /* output layer: blend weight, log2 box scale */
+} taa_mlp_weights_t;
+
+/* One training record: a pixel of a collected frame. */
+typedef struct taa_mlp_record_t {
+    uint16_t features[32];      /* FP16 bits, as the network reads them */
+    float mean[3], sigma[3];    /* 3x3 variance box, YCoCg */
+    float history[3], current[3];
+    float truth[3];             /* RGB, 64-spp ground truth */
+    float gamma, alpha_fixed;   /* mVarClipGamma; the blend weight when bit 0 of flags is set */
+    uint32_t flags;             /* bit 0: rejected or reset (the network does not choose alpha) */
+    float pad[2];
+} taa_mlp_record_t;
+
+/* Random starting weights (uniform, Glorot scale; seeded) whose outputs
+ * start near alpha0 and box scale 1. */
+int taa_mlp_init_weights(taa_mlp_weights_t* w, uint64_t seed, float alpha0);
+/* Upload the weights of a TAA_FORM_LEARNED context (waits for the copy). */
+int taa_set_mlp(taa_ctx* ctx, const taa_mlp_weights_t* w);
+/* The network alone: n rows of 32 FP32 features (device memory) -> n x 2
+ * FP32 outputs (device memory), with the context's weights. */
+int taa_mlp_forward(taa_ctx* ctx, void* stream, const float* features, float* outputs, int32_t n);
+
+/* Training: records are collected while frames are resolved with the plain
+ * variance clip, then the network is trained on them with Adam by the
+ * library's tensor-core forward and backward kernels. */
+typedef struct taa_mlp_trainer taa_mlp_trainer;
+int taa_mlp_trainer_create(int32_t capacity, taa_mlp_trainer** out);
+int taa_mlp_trainer_destroy(taa_mlp_trainer* tr);
+/* Resolve one frame with the plain variance clip (like taa_resolve on `ctx`,
+ * which must fit the learned form) and append a record for each pixel whose
+ * hash of (seed, x, y) falls in the given fraction; `truth` is the frame's
+ * RGBA32F ground truth (device memory, target size). */
+int taa_mlp_collect(taa_mlp_trainer* tr, taa_ctx* ctx, void* stream, const taa_frame_io_t* io, const void* truth,
+                    size_t truth_pitch, float fraction, uint32_t seed);
+/* Records collected so far (capped at the capacity); waits for the device. */
+int taa_mlp_record_count(taa_mlp_trainer* tr, int32_t* count);
+/* Copy records [first, first + count) to host memory; waits for the device. */
+int taa_mlp_records(taa_mlp_trainer* tr, int32_t first, int32_t count, taa_mlp_record_t* out);
+/* Sums over records [first, first + count) of the loss and of its gradient
+ * with respect to every weight (taa_mlp_weights_t layout).  The loss of a
+ * record: its resolved RGB (variance clip with the predicted box scale, blend
+ * with the predicted weight) against the ground truth, both through
+ * x / (1 + |x|), squared and summed over the channels.  Waits for the device. */
+int taa_mlp_gradients(taa_mlp_trainer* tr, const taa_mlp_weights_t* w, int32_t first, int32_t count,
+                      taa_mlp_weights_t* grad, float* loss_sum);
+/* `steps` Adam steps (learning rate lr) on batches of `batch` records drawn
+ * without replacement from a seeded shuffle, starting from *w; the trained
+ * weights are written back to *w, and the mean loss of the first and last
+ * batch to *loss_first / *loss_last.  Waits for the device. */
+int taa_mlp_train(taa_mlp_trainer* tr, taa_mlp_weights_t* w, int32_t steps, int32_t batch, float lr, uint64_t seed,
+                  float* loss_first, float* loss_last);
 
 /* Bits of the device status word (taa_device_status). */
 #define TAA_DEVICE_WINDOW_TIMEOUT 0x1u /* a history-window copy did not land within its bounded wait */

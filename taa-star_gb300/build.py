@@ -34,11 +34,13 @@ UNITS = {
     "resolve_tiled.cu": ["-fmad=false"],
     "resolve_half.cu": [],
     "batch_tiled.cu": ["-fmad=false"],
+    "learned.cu": ["-fmad=false"],
     "synth.cu": [],
     "static_scratch.cu": [],
     "device_state.cu": [],
     "capi.cpp": [],
     "batch_api.cpp": [],
+    "learned_api.cpp": [],
 }
 
 

@@ -22,19 +22,6 @@ using taa_dev::FrameArgs;
 using taa_dev::Img;
 using taa_dev::ImgW;
 
-struct taa_ctx {
-    taa_desc_t desc;
-    taa_uniforms_t uniforms;
-    bool have_uniforms = false;
-    uint32_t cas_const0[4] = {0, 0, 0, 0};
-    uint32_t cas_const1[4] = {0, 0, 0, 0};
-    int device = 0;
-    // RGBA16F screen image for the plain form's separate sharpen pass when the
-    // caller does not bind a result image; allocated when a sharpener is set.
-    void* scratch_screen = nullptr;
-    size_t scratch_pitch = 0;
-};
-
 namespace taa_host {
 
 thread_local std::string g_last_error;
@@ -98,7 +85,7 @@ int check_desc(const taa_desc_t& d, const char* who) {
         return fail(TAA_E_INVAL, "%s: image sizes must be in 1..32768", who);
     if (d.history_format > TAA_HISTORY_RGBA16F) return fail(TAA_E_INVAL, "%s: history_format %u", who, d.history_format);
     if (d.motion_format > TAA_MOTION_RG16F) return fail(TAA_E_INVAL, "%s: motion_format %u", who, d.motion_format);
-    if (d.form > TAA_FORM_FP16) return fail(TAA_E_INVAL, "%s: form %u", who, d.form);
+    if (d.form > TAA_FORM_LEARNED) return fail(TAA_E_INVAL, "%s: form %u", who, d.form);
     if (d.sharpener > TAA_SHARPEN_CAS) return fail(TAA_E_INVAL, "%s: sharpener %u", who, d.sharpener);
     if (!finite(d.sharpen_factor)) return fail(TAA_E_INVAL, "%s: sharpen_factor not finite", who);
     if (d.flags != 0) return fail(TAA_E_INVAL, "%s: flags must be 0", who);
@@ -173,6 +160,19 @@ int frame_args(const taa_desc_t& d, const taa_uniforms_t& U, uint32_t cas_peak_b
     if (se != cudaSuccess) return cuda_fail(se, "device status word");
     return ok();
 
+}
+
+int learned_supported(const taa_desc_t& d, const taa_uniforms_t& U, const taa_frame_io_t* io, const char* who) {
+    const taa_parameters_t& P = U.param[0];
+    if (d.history_format != TAA_HISTORY_RGBA32F || d.sharpener != TAA_SHARPEN_OFF)
+        return fail(TAA_E_UNSUPPORTED, "%s: the learned form keeps RGBA32F history and has no sharpener", who);
+    if (!taa_dev::fast_path_supported(U, d.in_width, d.in_height, d.out_width, d.out_height))
+        return fail(TAA_E_UNSUPPORTED, "%s: these parameters need the plain form", who);
+    if (!P.mUseYCoCg || P.mToneMapLumaKaris || P.mInterpolationMode != 2)
+        return fail(TAA_E_UNSUPPORTED, "%s: the learned form works in YCoCg without tonemapping, Catmull-Rom history", who);
+    if (io && (io->debug || io->segmask))
+        return fail(TAA_E_UNSUPPORTED, "%s: debug and segmask outputs run with the plain form", who);
+    return TAA_OK;
 }
 
 }  // namespace taa_host
@@ -407,8 +407,14 @@ int taa_create(const taa_desc_t* d, taa_ctx** out) {
     taa_cas_setup(d->sharpen_factor, (float)d->out_width, (float)d->out_height, (float)d->out_width,
                   (float)d->out_height, c->cas_const0, c->cas_const1);
     int rc = ensure_scratch(c);
+    if (rc == TAA_OK && d->form == TAA_FORM_LEARNED) {
+        e = cudaMalloc(&c->mlp_weights, sizeof(float) * (size_t)taa_dev::learned_param_count());
+        if (e == cudaSuccess) e = cudaMalloc(&c->mlp_blob, (size_t)taa_dev::learned_blob_bytes());
+        if (e != cudaSuccess) rc = e == cudaErrorMemoryAllocation ? fail(TAA_E_NOMEM, "taa_create: out of device memory")
+                                                                  : cuda_fail(e, "taa_create: network buffers");
+    }
     if (rc != TAA_OK) {
-        delete c;
+        taa_destroy(c);
         return rc;
     }
     *out = c;
@@ -418,6 +424,8 @@ int taa_create(const taa_desc_t* d, taa_ctx** out) {
 int taa_destroy(taa_ctx* c) {
     if (!c) return ok();
     if (c->scratch_screen) cudaFree(c->scratch_screen);
+    if (c->mlp_weights) cudaFree(c->mlp_weights);
+    if (c->mlp_blob) cudaFree(c->mlp_blob);
     delete c;
     return ok();
 }
@@ -448,6 +456,7 @@ int taa_set_sharpener(taa_ctx* c, uint32_t sharpener, float factor) {
 // the FP16 form with a fused sharpener runs as the tiled FP32 form.
 static int select_form(const taa_ctx* c, const taa_frame_io_t* io) {
     if (c->desc.form == TAA_FORM_PLAIN) return TAA_FORM_PLAIN;
+    if (c->desc.form == TAA_FORM_LEARNED) return TAA_FORM_LEARNED;
     const taa_desc_t& d = c->desc;
     if (!taa_dev::fast_path_supported(c->uniforms, d.in_width, d.in_height, d.out_width, d.out_height))
         return TAA_FORM_PLAIN;
@@ -475,7 +484,12 @@ int taa_resolve(taa_ctx* c, void* stream, const taa_frame_io_t* io) {
     cudaStream_t s = (cudaStream_t)stream;
     int form = select_form(c, io);
     cudaError_t e;
-    if (form == TAA_FORM_PLAIN) {
+    if (form == TAA_FORM_LEARNED) {
+        if (!c->have_mlp) return fail(TAA_E_INVAL, "taa_resolve: the learned form has no weights (taa_set_mlp)");
+        if ((rc = learned_supported(d, U, io, "taa_resolve"))) return rc;
+        e = taa_dev::launch_resolve_learned((int)d.history_format, d.motion_format == TAA_MOTION_RGBA16F ? 4 : 2,
+                                            false, U, a, c->mlp_blob, nullptr, nullptr, 0, 0, 0.f, Img{}, s);
+    } else if (form == TAA_FORM_PLAIN) {
         if (sharpen && !a.result.p) a.result = ImgW{(char*)c->scratch_screen, c->scratch_pitch};
         e = taa_dev::launch_resolve_plain(U, a, (int)d.history_format, d.motion_format == TAA_MOTION_RGBA16F ? 4 : 2, s);
         if (e == cudaSuccess && sharpen) e = taa_dev::launch_sharpen((int)d.sharpener, a, s);
@@ -530,6 +544,21 @@ int taa_resolve_static_scratch(taa_ctx* c, void* stream, const taa_frame_io_t* i
         v.scratch_pitch = (size_t)ow * 8;
     }
     return taa_resolve(&v, stream, io);
+}
+
+int taa_set_mlp(taa_ctx* c, const taa_mlp_weights_t* w) {
+    if (!c || !w) return fail(TAA_E_INVAL, "taa_set_mlp: NULL argument");
+    if (c->desc.form != TAA_FORM_LEARNED || !c->mlp_blob)
+        return fail(TAA_E_INVAL, "taa_set_mlp: the context was not created with TAA_FORM_LEARNED");
+    const float* p = reinterpret_cast<const float*>(w);
+    for (int i = 0; i < taa_dev::learned_param_count(); ++i)
+        if (!finite(p[i])) return fail(TAA_E_INVAL, "taa_set_mlp: weight %d is not finite", i);
+    cudaError_t e = cudaMemcpy(c->mlp_weights, w, sizeof(taa_mlp_weights_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = taa_dev::launch_mlp_build_blob(c->mlp_weights, c->mlp_blob, nullptr);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(nullptr);
+    if (e != cudaSuccess) return cuda_fail(e, "taa_set_mlp");
+    c->have_mlp = true;
+    return ok();
 }
 
 int taa_device_status(uint32_t* bits, int clear) {

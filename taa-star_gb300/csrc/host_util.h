@@ -5,6 +5,25 @@
 #include "../../include/taa_gb300.h"
 #include "kernels.h"
 
+// A resolve context (taa_create): the description, the uniform block of the
+// next resolves, CasSetup constants and the few device buffers it owns.
+struct taa_ctx {
+    taa_desc_t desc;
+    taa_uniforms_t uniforms;
+    bool have_uniforms = false;
+    uint32_t cas_const0[4] = {0, 0, 0, 0};
+    uint32_t cas_const1[4] = {0, 0, 0, 0};
+    int device = 0;
+    // RGBA16F screen image for the plain form's separate sharpen pass when the
+    // caller does not bind a result image; allocated when a sharpener is set.
+    void* scratch_screen = nullptr;
+    size_t scratch_pitch = 0;
+    // the learned form's weights (TAA_FORM_LEARNED): FP32 masters and the FP16 blob
+    float* mlp_weights = nullptr;
+    char* mlp_blob = nullptr;
+    bool have_mlp = false;
+};
+
 namespace taa_host {
 
 // Records the message of a failing call (taa_last_error) and returns `code`.
@@ -18,5 +37,8 @@ int check_uniforms(const taa_uniforms_t& u, const char* who);
 // alignment, aliasing) and fills the kernel arguments.
 int frame_args(const taa_desc_t& d, const taa_uniforms_t& U, uint32_t cas_peak_bits, const taa_frame_io_t* io,
                const char* who, taa_dev::FrameArgs* out);
+// Whether the learned form runs these parameters and bindings (TAA_OK, or a
+// TAA_E_UNSUPPORTED failure naming what it does not run).
+int learned_supported(const taa_desc_t& d, const taa_uniforms_t& U, const taa_frame_io_t* io, const char* who);
 
 }  // namespace taa_host

@@ -70,6 +70,22 @@ cudaError_t launch_batch(const BatchKey& k, const BatchView* views, const CUtens
 // True when the parameters select the benchmark-mode specialisation.
 bool hot_parameters(const taa_parameters_t& P);
 
+// The learned rectifier (learned.cu).
+size_t learned_record_bytes();
+int learned_param_count();
+int learned_blob_bytes();
+cudaError_t launch_mlp_build_blob(const float* weights, char* blob, cudaStream_t s);
+cudaError_t launch_mlp_forward(const char* blob, const float* feat, float* out, int n, unsigned int* status,
+                               cudaStream_t s);
+cudaError_t launch_mlp_train(const char* blob, const void* records, const uint32_t* order, int first, int count,
+                             float* grads, unsigned int* status, int grid, cudaStream_t s);
+cudaError_t launch_mlp_adam(float* weights, float* m, float* v, float* grads, int step, float lr, char* blob,
+                            cudaStream_t s);
+cudaError_t launch_resolve_learned(int history_fmt, int motion_ch, bool collect, const taa_uniforms_t& U,
+                                   const FrameArgs& a, const char* blob, void* records, uint32_t* count,
+                                   uint32_t capacity, uint32_t seed, float sample_fraction, const Img& truth,
+                                   cudaStream_t s);
+
 // Synthetic renderer (synth.cu).
 cudaError_t launch_synth(const taa_synth_scene_t& s, const float* host_spheres, int frame,
                          const taa_synth_frame_t& out, cudaStream_t stream);

@@ -1,0 +1,187 @@
+// learned.cuh - the learned history rectifier: a per-pixel MLP
+// (32 features -> 32 -> 32 -> 2, ReLU) that predicts the blend weight and the
+// scale of the variance clip box, run on the tensor cores (tcgen05.cuh).
+//
+// Features (taa.comp's own quantities, in YCoCg, normalised by the 3x3 mean
+// luma): the 3x3 mean, standard deviation, minimum and maximum; the filtered
+// history; the current colour; the history's deviation from the mean in
+// standard deviations; velocity length; depth difference against the
+// culling threshold; the rejection flag; the clip ratio of the plain box;
+// log luma; the box's luma range; current minus mean; history minus current
+// luma; a constant.  Outputs: alpha = sigmoid(o0), box scale s = 2^o1.  The
+// rectified pixel is the variance clip of taa.comp:323-345 with the box
+// mean +- s * gamma * sigma and the blend taa.comp:900 with alpha; a rejected
+// pixel (taa.comp:787-823) blends with the rejection alpha as the shader does;
+// a scale outside [0.5, 2] falls back to the plain variance clip and alpha.
+#pragma once
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "tcgen05.cuh"
+
+namespace taa_dev {
+namespace learned {
+
+constexpr int kIn = 32, kHid = 32, kOut = 2, kOutPad = 16;
+constexpr int kRows = 128;  // pixels per tensor-core block (the MMA's M)
+
+// The weights as FP32 masters (row-major [out][in]), the layout of
+// taa_mlp_weights_t (include/taa_gb300.h).
+struct Weights {
+    float w1[kHid * kIn], b1[kHid];
+    float w2[kHid * kHid], b2[kHid];
+    float w3[kOut * kHid], b3[kOut];
+};
+
+// The device blob the kernels copy into shared memory: FP16 weights in the
+// canonical K-major layout as MMA B operands ([N rows][K columns]), and the
+// transposes the backward pass multiplies by, then FP32 biases.
+struct Blob {
+    static constexpr int W1 = 0;                       // [32 hid][32 in]
+    static constexpr int W2 = W1 + kHid * kIn * 2;     // [32 hid][32 hid]
+    static constexpr int W3 = W2 + kHid * kHid * 2;    // [16 out (2 used)][32 hid]
+    static constexpr int W3T = W3 + kOutPad * kHid * 2;  // [32 hid][16 out (2 used)]
+    static constexpr int W2T = W3T + kHid * kOutPad * 2;  // [32 in of layer 2][32 out of layer 2]
+    static constexpr int W1T = W2T + kHid * kHid * 2;     // unused by the kernels; keeps the pattern
+    static constexpr int B1 = W2T + kHid * kHid * 2;      // float[32]
+    static constexpr int B2 = B1 + kHid * 4;
+    static constexpr int B3 = B2 + kHid * 4;              // float[2] (+2 pad)
+    static constexpr int INFER_BYTES = W3T;                // W1, W2, W3 are all inference reads ...
+    static constexpr int BYTES = B3 + 16;                  // ... plus the biases at the end
+};
+static_assert(Blob::BYTES % 16 == 0, "blob copied as 16-byte words");
+
+// Features of one pixel (see the file comment).  All colours YCoCg.
+struct FeatureIn {
+    float mean[3], sigma[3], mn[3], mx[3], hist[3], cur[3];
+    float vel_px;      // velocity length in pixels
+    float depth_rel;   // (previous depth - expected depth) / (0.1 * (1 - previous depth)), 0 without culling
+    bool rejected;
+};
+
+__device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
+
+__device__ __forceinline__ void features(const FeatureIn& p, float (&f)[kIn]) {
+    const float inv = 1.0f / (fmaxf(p.mean[0], 0.f) + 0.05f);
+    float ma = 0.f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        f[0 + c] = p.mean[c] * inv;
+        f[3 + c] = p.sigma[c] * inv;
+        f[6 + c] = p.mn[c] * inv;
+        f[9 + c] = p.mx[c] * inv;
+        f[12 + c] = p.hist[c] * inv;
+        f[15 + c] = p.cur[c] * inv;
+        const float dev = (p.hist[c] - p.mean[c]) / (p.sigma[c] + 1e-3f / inv);
+        f[18 + c] = clampf(dev, -8.f, 8.f) * 0.25f;
+        ma = fmaxf(ma, fabsf(p.hist[c] - p.mean[c]) / (p.sigma[c] + 1e-7f));
+        f[27 + c] = (p.cur[c] - p.mean[c]) * inv;
+    }
+    f[21] = fminf(p.vel_px, 64.f) * (1.f / 16.f);
+    f[22] = clampf(p.depth_rel, -8.f, 8.f) * 0.125f;
+    f[23] = p.rejected ? 1.f : 0.f;
+    f[24] = fminf(ma, 8.f) * 0.125f;
+    f[25] = log2f(fmaxf(p.mean[0], 0.f) + 1e-3f) * 0.125f;
+    f[26] = (p.mx[0] - p.mn[0]) * inv;
+    f[30] = (p.hist[0] - p.cur[0]) * inv;
+    f[31] = 1.f;
+#pragma unroll
+    for (int i = 0; i < kIn; ++i) f[i] = clampf(f[i], -60000.f, 60000.f);  // finite in FP16
+}
+
+// The network's outputs turned into the blend weight and the box scale.
+__device__ __forceinline__ float out_alpha(float o0) { return 1.0f / (1.0f + __expf(-o0)); }
+__device__ __forceinline__ float out_scale(float o1) { return exp2f(o1); }
+
+// Variance clip towards the mean with the box mean +- e (e = s*gamma*sigma +
+// 1e-7, taa.comp:323-345), then the blend (taa.comp:900).  YCoCg in and out.
+__device__ __forceinline__ void rectify_blend(const float (&mean)[3], const float (&e)[3], const float (&hist)[3],
+                                              const float (&cur)[3], float alpha, float (&out)[3]) {
+    float d[3], ma = 0.f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        d[c] = hist[c] - mean[c];
+        ma = fmaxf(ma, fabsf(d[c] / e[c]));
+    }
+    const float k = ma > 1.f ? 1.f / ma : 1.f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float hc = mean[c] + d[c] * k;
+        out[c] = hc * (1.f - alpha) + cur[c] * alpha;
+    }
+}
+
+// Writes one pixel's 32 FP16 values as row r of a canonical [128][32] A tile.
+__device__ __forceinline__ void store_row(char* tile, int r, const float (&v)[32]) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        __half2 h0 = __floats2half2_rn(v[8 * j + 0], v[8 * j + 1]), h1 = __floats2half2_rn(v[8 * j + 2], v[8 * j + 3]);
+        __half2 h2 = __floats2half2_rn(v[8 * j + 4], v[8 * j + 5]), h3 = __floats2half2_rn(v[8 * j + 6], v[8 * j + 7]);
+        uint4 w;
+        w.x = *reinterpret_cast<uint32_t*>(&h0);
+        w.y = *reinterpret_cast<uint32_t*>(&h1);
+        w.z = *reinterpret_cast<uint32_t*>(&h2);
+        w.w = *reinterpret_cast<uint32_t*>(&h3);
+        *reinterpret_cast<uint4*>(tile + tc::canon(r, 8 * j, 32)) = w;
+    }
+}
+// Reads row r of a canonical [128][32] FP16 tile as floats.
+__device__ __forceinline__ void load_row(const char* tile, int r, float (&v)[32]) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        uint4 w = *reinterpret_cast<const uint4*>(tile + tc::canon(r, 8 * j, 32));
+        const uint32_t u[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            float2 f = __half22float2(*reinterpret_cast<const __half2*>(&u[q]));
+            v[8 * j + 2 * q] = f.x;
+            v[8 * j + 2 * q + 1] = f.y;
+        }
+    }
+}
+
+// Polls of an MMA-completion barrier before a wait gives up.
+constexpr uint32_t kMmaPolls = 1u << 22;
+__device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity) {
+    for (uint32_t i = 0; i < kMmaPolls; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(tc::saddr(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// All threads: make this CTA's shared-memory writes visible to the tensor
+// core and order them before the MMAs one thread issues next.
+__device__ __forceinline__ void sync_for_mma() {
+    tc::fence_smem_to_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+}
+
+// One dense layer for `nblocks` blocks of 128 rows: D[b] = A[b] . W^T with
+// K = 32 (two MMAs per block) and N = n; thread 0 issues, everyone waits.
+// Returns false if the wait gave up.
+__device__ __forceinline__ bool layer(char* const* a_tiles, const char* w, int n, uint32_t tmem, int nblocks,
+                                      uint64_t* bar, uint32_t& phase) {
+    if (threadIdx.x == 0) {
+        const uint32_t idesc = tc::idesc_f16(128, n);
+        for (int b = 0; b < nblocks; ++b)
+            for (int ks = 0; ks < 2; ++ks)
+                tc::mma_f16(tmem + (uint32_t)(b * 32), tc::smem_desc(a_tiles[b] + ks * 256, 128, 512),
+                            tc::smem_desc(w + ks * 256, 128, 512), idesc, ks > 0);
+        tc::commit(bar);
+    }
+    const bool ok = wait_bar(bar, phase);
+    phase ^= 1u;
+    tc::fence_after_sync();
+    return ok;
+}
+
+}  // namespace learned
+}  // namespace taa_dev

@@ -234,10 +234,10 @@ template <class Pol, class S, int HF> struct TileSmem {
 // status bit and leaves the tile's pixels unwritten; in a persistent loop
 // (PERSIST) it also sets sm.abort, which the caller reads after the barrier
 // that separates tiles, so the whole CTA stops together.
-template <class Pol, class S, int HF, int MC, int INTERP, bool HOT, bool PERSIST>
+template <class Pol, class S, int HF, int MC, int INTERP, bool HOT, bool PERSIST, class Fin>
 __device__ __forceinline__ void tile_body(const taa_uniforms_t& U, const FrameArgs& a, const CUtensorMap* hmap,
                                           bool tma_ok, int tile_x, int tile_y, TileSmem<Pol, S, HF>& sm,
-                                          uint32_t& phase) {
+                                          uint32_t& phase, Fin& fin) {
     using HT = typename HistTexel<HF>::T;
     constexpr int TX = S::TX, TY = S::TY, NT = S::NT, SX = S::SX, NS = S::NS, WH = S::WH;
     constexpr int WWS = Win<S, HF>::W;
@@ -354,17 +354,17 @@ __device__ __forceinline__ void tile_body(const taa_uniforms_t& U, const FrameAr
         cp_async_wait_all();
         __syncthreads();
     }
-    if (inside && landed) {
-        // rejection (taa.comp:787-823) first, so its inputs die before the filter
-        bool rejected = false;
-        if (P.mRejectOutside && (hu < 0.f || hv < 0.f || hu >= 1.f || hv >= 1.f)) rejected = true;
-        if (depth_cull) {
-            float hd = prev_depth;
-            if (fabsf(hd - ehd) > 0.1f * (1.0f - hd)) rejected = true;
-        }
-
-        // 4. history sample: from the window when all taps fall inside it
-        float4 hraw = make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool valid = inside && landed;
+    // rejection (taa.comp:787-823) first, so its inputs die before the filter
+    bool rejected = false;
+    if (P.mRejectOutside && (hu < 0.f || hv < 0.f || hu >= 1.f || hv >= 1.f)) rejected = true;
+    if (depth_cull) {
+        float hd = prev_depth;
+        if (fabsf(hd - ehd) > 0.1f * (1.0f - hd)) rejected = true;
+    }
+    // 4. history sample: from the window when all taps fall inside it
+    float4 hraw = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (valid) {
         if (have_hist) {
             HistoryTaps<Pol, INTERP> taps;
             taps.setup(hu, hv, hi.w, hi.h, z);
@@ -379,8 +379,23 @@ __device__ __forceinline__ void tile_body(const taa_uniforms_t& U, const FrameAr
                     taps, hi.w, hi.h, [&](int tx_, int ty_) { return fetch_history<HF>(hi, tx_, ty_); });
             }
         }
+    }
+    // 5. rectification, blend and stores: every thread of the CTA calls the
+    //    finisher (valid says whether its pixel is in the image and resolved)
+    const C3 c0 = Pol::centre(box, &sm.col[(ly + 1) * SX + lx + 1]);
+    Fin::template run<Pol, HF, HOT>(U, a, P, M, box, c0, hraw, u, v, hu, hv, ehd, prev_depth, rejected, valid, x, y,
+                                    tm, fin);
+}
 
-        const C3 c0 = Pol::centre(box, &sm.col[(ly + 1) * SX + lx + 1]);
+// The finisher of the plain tiled forms: the policy's rectification and
+// blend (taa.comp:825-900), then the history and screen stores.
+struct StoreFinish {
+    template <class Pol, int HF, bool HOT>
+    static __device__ __forceinline__ void run(const taa_uniforms_t& U, const FrameArgs& a, const taa_parameters_t& P,
+                                               const Mode<HOT>& M, const typename Pol::Box& box, const C3& c0,
+                                               float4 hraw, float u, float v, float hu, float hv, float, float,
+                                               bool rejected, bool valid, int x, int y, bool tm, StoreFinish&) {
+        if (!valid) return;
         float4 o = Pol::template finish<HOT>(U, P, M, box, c0, hraw, u, v, hu, hv, rejected);
         store_history<HF>(a.history_out, x, y, make_float4(o.x, o.y, o.z, 0.f));
         if (a.result.p) {
@@ -388,7 +403,7 @@ __device__ __forceinline__ void tile_body(const taa_uniforms_t& U, const FrameAr
             store_rgba16f(a.result, x, y, make_float4(o.x, o.y, o.z, 1.0f));
         }
     }
-}
+};
 
 // One view, one CTA per tile.
 template <class Pol, class S, int HF, int MC, int INTERP, bool HOT>
@@ -397,7 +412,8 @@ __global__ void __launch_bounds__(S::NT, S::MIN_BLOCKS)
     __shared__ TileSmem<Pol, S, HF> sm;
     if (threadIdx.x == 0) mbar_init(&sm.bar, 1);
     uint32_t phase = 0;
-    tile_body<Pol, S, HF, MC, INTERP, HOT, false>(U, a, &hmap, tma_ok != 0, blockIdx.x, blockIdx.y, sm, phase);
+    StoreFinish fin;
+    tile_body<Pol, S, HF, MC, INTERP, HOT, false>(U, a, &hmap, tma_ok != 0, blockIdx.x, blockIdx.y, sm, phase, fin);
 }
 
 // Resident CTAs per SM the batch kernels' register budget is sized for.
@@ -441,8 +457,9 @@ __global__ void __launch_bounds__(S::NT, batch_min_blocks<S>())
             cur_view = vi;
             __syncthreads();
         }
+        StoreFinish fin;
         tile_body<Pol, S, HF, MC, INTERP, HOT, true>(s_view.U, s_view.a, maps + vi, __ldg(tma_ok + vi) != 0,
-                                                     job_tile_x(job), job_tile_y(job), sm, phase);
+                                                     job_tile_x(job), job_tile_y(job), sm, phase, fin);
         __syncthreads();  // the next tile reuses the shared memory
         if (sm.abort) return;
     }

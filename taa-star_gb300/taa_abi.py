@@ -26,7 +26,7 @@ TAA_HISTORY_RGBA32F = 0
 TAA_HISTORY_RGBA16F = 1
 TAA_MOTION_RGBA16F = 0
 TAA_MOTION_RG16F = 1
-TAA_FORM_AUTO, TAA_FORM_PLAIN, TAA_FORM_TILED, TAA_FORM_FP16 = 0, 1, 2, 3
+TAA_FORM_AUTO, TAA_FORM_PLAIN, TAA_FORM_TILED, TAA_FORM_FP16, TAA_FORM_LEARNED = 0, 1, 2, 3, 4
 TAA_SHARPEN_OFF, TAA_SHARPEN_SIMPLE, TAA_SHARPEN_CAS = 0, 1, 2
 
 RTFLAG = dict(OUT=0x1, DIS=0x2, NRM=0x4, DPT=0x8, MID=0x10, LUM=0x20, CNT=0x40, ALL=0x80, FXD=0x100, FXA=0x200)
@@ -91,6 +91,17 @@ class BatchTuning(C.Structure):
                 ("ms", C.c_float)]
 
 
+class MlpWeights(C.Structure):
+    _fields_ = [("w1", C.c_float * 1024), ("b1", C.c_float * 32), ("w2", C.c_float * 1024), ("b2", C.c_float * 32),
+                ("w3", C.c_float * 64), ("b3", C.c_float * 2)]
+
+
+class MlpRecord(C.Structure):
+    _fields_ = [("features", C.c_uint16 * 32), ("mean", C.c_float * 3), ("sigma", C.c_float * 3),
+                ("history", C.c_float * 3), ("current", C.c_float * 3), ("truth", C.c_float * 3),
+                ("gamma", C.c_float), ("alpha_fixed", C.c_float), ("flags", C.c_uint32), ("pad", C.c_float * 2)]
+
+
 TAA_SCHEDULE_VIEW_ORDER, TAA_SCHEDULE_LARGEST_FIRST, TAA_SCHEDULE_INTERLEAVED = 0, 1, 2
 BATCH_SLOTS = 4
 TAA_BATCH_CTA_PER_TILE = -1
@@ -123,7 +134,9 @@ EXPORTS = ["taa_version", "taa_last_error", "taa_default_parameters", "taa_get_j
            "taa_set_uniforms", "taa_set_sharpener", "taa_selected_form", "taa_resolve",
            "taa_resolve_static_scratch", "taa_device_status", "taa_batch_create", "taa_batch_destroy",
            "taa_batch_set_uniforms", "taa_batch_prepare", "taa_batch_launch", "taa_batch_autotune",
-           "taa_batch_get_tuning", "taa_batch_set_tuning",
+           "taa_batch_get_tuning", "taa_batch_set_tuning", "taa_mlp_init_weights", "taa_set_mlp", "taa_mlp_forward",
+           "taa_mlp_trainer_create", "taa_mlp_trainer_destroy", "taa_mlp_collect", "taa_mlp_record_count",
+           "taa_mlp_records", "taa_mlp_gradients", "taa_mlp_train",
            "taa_synth_default_scene", "taa_synth_spheres", "taa_synth_jitter", "taa_synth_camera",
            "taa_synth_render"]
 
@@ -165,6 +178,18 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
         "taa_batch_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, P(BatchTuning)]),
         "taa_batch_get_tuning": (C.c_int, [C.c_void_p, P(BatchTuning)]),
         "taa_batch_set_tuning": (C.c_int, [C.c_void_p, P(BatchTuning)]),
+        "taa_mlp_init_weights": (C.c_int, [P(MlpWeights), C.c_uint64, C.c_float]),
+        "taa_set_mlp": (C.c_int, [C.c_void_p, P(MlpWeights)]),
+        "taa_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32]),
+        "taa_mlp_trainer_create": (C.c_int, [C.c_int32, P(C.c_void_p)]),
+        "taa_mlp_trainer_destroy": (C.c_int, [C.c_void_p]),
+        "taa_mlp_collect": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, P(FrameIO), C.c_void_p, C.c_size_t,
+                                      C.c_float, C.c_uint32]),
+        "taa_mlp_record_count": (C.c_int, [C.c_void_p, P(C.c_int32)]),
+        "taa_mlp_records": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, P(MlpRecord)]),
+        "taa_mlp_gradients": (C.c_int, [C.c_void_p, P(MlpWeights), C.c_int32, C.c_int32, P(MlpWeights), P(C.c_float)]),
+        "taa_mlp_train": (C.c_int, [C.c_void_p, P(MlpWeights), C.c_int32, C.c_int32, C.c_float, C.c_uint64,
+                                    P(C.c_float), P(C.c_float)]),
         "taa_synth_default_scene": (C.c_int, [P(SynthScene), C.c_int32, C.c_int32, C.c_uint64]),
         "taa_synth_spheres": (C.c_int, [P(SynthScene), P(C.c_float), C.c_int32]),
         "taa_synth_jitter": (C.c_int, [P(SynthScene), C.c_int32, P(C.c_float), P(C.c_float)]),
@@ -261,6 +286,13 @@ class Taa:
     def set_sharpener(self, mode: int, factor: float):
         check(self.lib.taa_set_sharpener(self.handle, mode, factor))
 
+    def set_mlp(self, w: MlpWeights):
+        check(self.lib.taa_set_mlp(self.handle, C.byref(w)))
+
+    def mlp_forward(self, features, outputs, stream: int = 0):
+        check(self.lib.taa_mlp_forward(self.handle, C.c_void_p(stream), C.c_void_p(features.data_ptr()),
+                                       C.c_void_p(outputs.data_ptr()), int(features.shape[0])))
+
     def selected_form(self) -> int:
         return check(self.lib.taa_selected_form(self.handle))
 
@@ -340,6 +372,74 @@ class Batch:
     def set_tuning(self, tile_w, tile_h, schedule, ctas_per_sm=0):
         t = BatchTuning(tile_w, tile_h, schedule, ctas_per_sm, 0.0)
         check(self.lib.taa_batch_set_tuning(self.handle, C.byref(t)))
+
+
+def mlp_init_weights(seed: int = 1, alpha0: float = 0.1) -> MlpWeights:
+    w = MlpWeights()
+    check(load().taa_mlp_init_weights(C.byref(w), seed, alpha0))
+    return w
+
+
+def mlp_to_numpy(w: MlpWeights) -> dict:
+    import numpy as np
+    return dict(w1=np.ctypeslib.as_array(w.w1).reshape(32, 32).astype(np.float64), b1=np.ctypeslib.as_array(w.b1).astype(np.float64),
+                w2=np.ctypeslib.as_array(w.w2).reshape(32, 32).astype(np.float64), b2=np.ctypeslib.as_array(w.b2).astype(np.float64),
+                w3=np.ctypeslib.as_array(w.w3).reshape(2, 32).astype(np.float64), b3=np.ctypeslib.as_array(w.b3).astype(np.float64))
+
+
+class MlpTrainer:
+    """Record collection and training of the learned rectifier (taa_mlp_*)."""
+
+    def __init__(self, capacity: int):
+        self.lib = load()
+        h = C.c_void_p()
+        check(self.lib.taa_mlp_trainer_create(capacity, C.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            self.lib.taa_mlp_trainer_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def collect(self, ctx: "Taa", truth, fraction: float, seed: int, stream: int = 0, **bindings):
+        io = frame_io(**bindings)
+        p, pitch = tensor_ptr_pitch(truth)
+        check(self.lib.taa_mlp_collect(self.handle, ctx.handle, C.c_void_p(stream), C.byref(io), C.c_void_p(p), pitch,
+                                       fraction, seed))
+
+    def count(self) -> int:
+        n = C.c_int32()
+        check(self.lib.taa_mlp_record_count(self.handle, C.byref(n)))
+        return n.value
+
+    def records(self, first: int, count: int):
+        import numpy as np
+        buf = (MlpRecord * count)()
+        check(self.lib.taa_mlp_records(self.handle, first, count, buf))
+        raw = np.frombuffer(buf, dtype=np.uint8).reshape(count, C.sizeof(MlpRecord))
+        f32 = raw.view(np.float32)
+        return dict(features=raw[:, :64].copy().view(np.float16).astype(np.float64),
+                    mean=f32[:, 16:19].astype(np.float64), sigma=f32[:, 19:22].astype(np.float64),
+                    history=f32[:, 22:25].astype(np.float64), current=f32[:, 25:28].astype(np.float64),
+                    truth=f32[:, 28:31].astype(np.float64), gamma=f32[:, 31].astype(np.float64),
+                    alpha_fixed=f32[:, 32].astype(np.float64), flags=raw.view(np.uint32)[:, 33].copy())
+
+    def gradients(self, w: MlpWeights, first: int, count: int):
+        g = MlpWeights()
+        loss = C.c_float()
+        check(self.lib.taa_mlp_gradients(self.handle, C.byref(w), first, count, C.byref(g), C.byref(loss)))
+        return g, loss.value
+
+    def train(self, w: MlpWeights, steps: int, batch: int, lr: float, seed: int = 1):
+        lf, ll = C.c_float(), C.c_float()
+        check(self.lib.taa_mlp_train(self.handle, C.byref(w), steps, batch, lr, seed, C.byref(lf), C.byref(ll)))
+        return lf.value, ll.value
 
 
 def synth_default_scene(w, h, seed) -> SynthScene:
