@@ -240,6 +240,9 @@ int taa_batch_set_tuning(taa_batch* batch, const taa_batch_tuning_t* tuning);
  * mAlpha; rejected pixels blend with mRejectionAlpha as in the shader.  The
  * form runs YCoCg variance clipping with Catmull-Rom history, RGBA32F
  * history, equal source and target sizes and no sharpener. */
+/* Input 31 and hidden unit 31 of each layer are the constant 1 that carries
+ * the next layer's bias: rows 31 of w1 and w2, columns 31 of w1, w2 and w3,
+ * b1[31] and b2[31] are not weights (ignored; their gradients are zero). */
 typedef struct taa_mlp_weights_t {
     float w1[32 * 32], b1[32];  /* layer 1, row-major [out][in] */
     float w2[32 * 32], b2[32];  /* layer 2 */
@@ -285,11 +288,12 @@ int taa_mlp_records(taa_mlp_trainer* tr, int32_t first, int32_t count, taa_mlp_r
 /* Sums over records [first, first + count) of the loss and of its gradient
  * with respect to every weight (taa_mlp_weights_t layout).  The loss of a
  * record: its resolved RGB (variance clip with the predicted box scale, blend
- * with the predicted weight) against the ground truth, both through
- * x / (1 + |x|), squared and summed over the channels.  Waits for the device. */
+ * with the predicted weight) minus the ground truth, squared and summed over
+ * the channels.  Waits for the device. */
 int taa_mlp_gradients(taa_mlp_trainer* tr, const taa_mlp_weights_t* w, int32_t first, int32_t count,
                       taa_mlp_weights_t* grad, float* loss_sum);
-/* `steps` Adam steps (learning rate lr) on batches of `batch` records drawn
+/* `steps` Adam steps (learning rate lr, cosine-decayed to lr / 10 over the
+ * run) on batches of `batch` records drawn
  * without replacement from a seeded shuffle, starting from *w; the trained
  * weights are written back to *w, and the mean loss of the first and last
  * batch to *loss_first / *loss_last.  Waits for the device. */

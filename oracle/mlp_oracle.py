@@ -12,8 +12,9 @@ tensor-core kernels (taa-star_gb300/csrc/learned.cu, learned.cuh):
   (weights, inputs, activations, back-propagated gradients), so the sums can
   be compared tightly with the kernels' FP32 accumulation;
 * ``loss_and_output_grad`` - the loss of one record (its rectified, blended
-  RGB against the ground truth through x / (1 + |x|)) and its derivative with
-  respect to the two network outputs (learned.cu ``record_loss``);
+  RGB against the ground truth, squared, in linear space as the library is
+  built by default) and its derivative with respect to the two network
+  outputs (learned.cu ``record_loss``);
 * ``gradients_exact`` - the same gradients without any FP16 rounding, which
   the tests hold against central differences.
 """
@@ -22,6 +23,7 @@ from __future__ import annotations
 import numpy as np
 
 LN2 = 0.69314718055994531
+PENALTY = 1.0  # weight of the pull on a log2 box scale outside [-1, 1] (learned.cu kPenalty)
 
 
 def half(x):
@@ -55,38 +57,51 @@ def features(mean, sigma, mn, mx, hist, cur, vel_px, depth_rel, rejected):
     return np.clip(f, -60000.0, 60000.0)
 
 
-def _w16(w, rounded):
-    r = half if rounded else (lambda a: np.asarray(a, np.float64))
-    return {k: (r(v) if k.startswith("w") else np.asarray(v, np.float64)) for k, v in w.items()}
+CONST = 31  # input 31 and hidden unit 31 of each layer are the constant 1
+
+
+def effective(w):
+    """The matrices the kernels multiply by: biases in column 31, the constant
+    unit in row 31 of layers 1 and 2 (learned.cu eff1, eff2, eff3)."""
+    e1 = np.array(w["w1"], np.float64).reshape(32, 32).copy()
+    e2 = np.array(w["w2"], np.float64).reshape(32, 32).copy()
+    e3 = np.array(w["w3"], np.float64).reshape(2, 32).copy()
+    e1[:, CONST] = w["b1"]
+    e2[:, CONST] = w["b2"]
+    e3[:, CONST] = w["b3"]
+    for e in (e1, e2):
+        e[CONST, :] = 0.0
+        e[CONST, CONST] = 1.0
+    return dict(w1=e1, w2=e2, w3=e3)
 
 
 def forward(w, f, rounded=True):
     """Outputs [n, 2] and the activations the backward pass needs."""
     r = half if rounded else (lambda a: np.asarray(a, np.float64))
-    q = _w16(w, rounded)
+    q = {k: r(v) for k, v in effective(w).items()}
     x = r(f)
-    h1 = r(np.maximum(x @ q["w1"].T + q["b1"], 0.0))
-    h2 = r(np.maximum(h1 @ q["w2"].T + q["b2"], 0.0))
-    o = h2 @ q["w3"].T + q["b3"]
+    h1 = np.maximum(r(x @ q["w1"].T), 0.0)
+    h2 = np.maximum(r(h1 @ q["w2"].T), 0.0)
+    o = h2 @ q["w3"].T
     return o, dict(x=x, h1=h1, h2=h2, q=q)
 
 
 def _g(x):
-    return x / (1.0 + np.abs(x))
+    return np.asarray(x, np.float64)
 
 
 def _dg(x):
-    return 1.0 / (1.0 + np.abs(x)) ** 2
+    return np.ones_like(np.asarray(x, np.float64))
 
 
 def loss_and_output_grad(rec, o):
     """Loss per record and d loss / d outputs [n, 2] (learned.cu record_loss)."""
     o0, o1 = o[:, 0], o[:, 1]
     fixed = (rec["flags"] & 1) != 0
-    alpha = np.where(fixed, rec["alpha_fixed"], 1.0 / (1.0 + np.exp(-o0)))
     s = np.exp2(o1)
-    s_in = (s > 0.5) & (s < 2.0)
-    sc = np.clip(s, 0.5, 2.0)
+    s_in = (s >= 0.5) & (s <= 2.0)
+    alpha = np.where(fixed | ~s_in, rec["alpha_fixed"], 1.0 / (1.0 + np.exp(-o0)))
+    sc = np.where(s_in, s, 1.0)
     mean, sigma, hist, cur, gt = rec["mean"], rec["sigma"], rec["history"], rec["current"], rec["truth"]
     g = rec["gamma"][:, None]
     e = sc[:, None] * g * sigma + 1e-7
@@ -109,8 +124,12 @@ def loss_and_output_grad(rec, o):
     sk = sigma[np.arange(len(k)), k]
     dsc = np.where(clipped, np.sum(dout * (1.0 - alpha[:, None]) * d, axis=1) * (rec["gamma"] * sk /
                                                                                    np.where(clipped, dk, 1.0)), 0.0)
-    d0 = np.where(fixed, 0.0, dalpha * alpha * (1.0 - alpha))
+    d0 = np.where(fixed | ~s_in, 0.0, dalpha * alpha * (1.0 - alpha))
     d1 = np.where(s_in, dsc * s * LN2, 0.0)
+    # outside the trusted scale range: the plain result and a penalty pulling o1 back
+    over = np.abs(o1) - 1.0
+    loss = loss + np.where(s_in, 0.0, PENALTY * over * over)
+    d1 = np.where(s_in, d1, 2.0 * PENALTY * over * np.sign(o1))
     return loss, np.stack([d0, d1], axis=1)
 
 
@@ -123,7 +142,17 @@ def gradients(w, rec, rounded=True):
     q, x, h1, h2 = act["q"], act["x"], act["h1"], act["h2"]
     g2 = np.where(h2 > 0, r(do @ q["w3"]), 0.0)
     g1 = np.where(h1 > 0, r(g2 @ q["w2"]), 0.0)
-    grad = dict(w3=do.T @ h2, b3=do.sum(0), w2=g2.T @ h1, b2=g2.sum(0), w1=g1.T @ x, b1=g1.sum(0))
+    d1, d2, d3 = g1.T @ x, g2.T @ h1, do.T @ h2
+    # gradients of the effective matrices -> of the masters (learned.cu map_grads)
+    grad = dict(b1=d1[:, CONST].copy(), b2=d2[:, CONST].copy(), b3=d3[:, CONST].copy())
+    grad["b1"][CONST] = 0.0
+    grad["b2"][CONST] = 0.0
+    for k, d in (("w1", d1), ("w2", d2), ("w3", d3)):
+        d = d.copy()
+        d[:, CONST] = 0.0
+        if k != "w3":
+            d[CONST, :] = 0.0
+        grad[k] = d
     return float(loss.sum()), grad
 
 

@@ -75,6 +75,7 @@ size_t learned_record_bytes();
 int learned_param_count();
 int learned_blob_bytes();
 cudaError_t launch_mlp_build_blob(const float* weights, char* blob, cudaStream_t s);
+cudaError_t launch_mlp_map_grads(float* grads, cudaStream_t s);
 cudaError_t launch_mlp_forward(const char* blob, const float* feat, float* out, int n, unsigned int* status,
                                cudaStream_t s);
 cudaError_t launch_mlp_train(const char* blob, const void* records, const uint32_t* order, int first, int count,

@@ -78,52 +78,84 @@ struct LearnedPol : tiled::ExactF32 {
 
 // ---------------------------------------------------------------- shared memory
 
-// A tile's network state: its two 128-row blocks' activation tiles, the
-// weights and biases, the barrier of the MMAs and the TMEM base.
-struct NetSmem {
-    alignas(128) char a[3][2][kRows * kIn * 2];  // features, layer-1 and layer-2 activations
-    alignas(128) char blob[Blob::BYTES];
-    uint64_t bar;
+// A CTA's network state: NB activation tiles for each of its two 128-row
+// blocks (2: features and layer 2 share one, layer 1 the other; 3: the
+// training pass keeps both layers), the weights (the first BLOB bytes of the
+// blob), the barrier of the MMAs and the TMEM base.
+template <int NB, int BLOB> struct NetSmem {
+    alignas(128) char a[NB][2][kRows * kIn * 2];
+    alignas(128) char blob[BLOB];
+    uint64_t bar;      // MMA completion, whole-CTA forward and training
+    uint64_t bar_wg[2];  // MMA completion of each warpgroup's block (inference)
     uint32_t tmem;
 };
+using InferSmem = NetSmem<2, Blob::INFER_BYTES>;
 
-__device__ __forceinline__ void copy_blob(char* dst, const char* src) {
-    for (int w = threadIdx.x; w < Blob::BYTES / 16; w += blockDim.x)
+__device__ __forceinline__ void copy_blob(char* dst, const char* src, int bytes) {
+    for (int w = threadIdx.x; w < bytes / 16; w += blockDim.x)
         reinterpret_cast<uint4*>(dst)[w] = __ldg(reinterpret_cast<const uint4*>(src) + w);
 }
 
 // The network on the features in a[0][*]; thread t (block t / 128, row t % 128)
 // ends with its outputs.  All threads of the CTA call it.  False if a wait
 // gave up (the outputs are then meaningless).
-__device__ __forceinline__ bool forward(NetSmem& s, int nblocks, uint32_t& phase, float& o0, float& o1) {
+// Inference: each warpgroup runs the network on its own 128-row block, with
+// its own barrier and MMA-issuing thread, so the two halves of a tile do not
+// wait for each other.
+template <int NB, int BLOB>
+__device__ __forceinline__ bool forward_group(NetSmem<NB, BLOB>& s, uint32_t& phase, float& o0, float& o1) {
+    const int wg = threadIdx.x >> 7, row = threadIdx.x & 127;
+    const bool issuer = row == 0;
+    const uint32_t cols = s.tmem + (uint32_t)(wg * 32);
+    const uint32_t lane_cols = cols + ((uint32_t)((threadIdx.x >> 5) & 3) * 32u << 16);
+    constexpr int L2 = NB == 2 ? 0 : 2;
+    uint64_t* bar = &s.bar_wg[wg];
+    bool ok = true;
+    float acc[32];
+    sync_group_for_mma(wg);
+    ok &= layer_block(s.a[0][wg], s.blob + Blob::W1, kHid, cols, issuer, bar, phase);
+    tc::ld32(lane_cols, acc);
+    store_row_relu(s.a[1][wg], row, acc);
+    sync_group_for_mma(wg);
+    ok &= layer_block(s.a[1][wg], s.blob + Blob::W2, kHid, cols, issuer, bar, phase);
+    tc::ld32(lane_cols, acc);
+    store_row_relu(s.a[L2][wg], row, acc);
+    sync_group_for_mma(wg);
+    ok &= layer_block(s.a[L2][wg], s.blob + Blob::W3, kOutPad, cols, issuer, bar, phase);
+    float o[16];
+    tc::ld16(lane_cols, o);
+    o0 = o[0];
+    o1 = o[1];
+    tc::fence_before_sync();
+    return ok;
+}
+
+// The biases ride in column 31 of each matrix (input 31 and hidden unit 31
+// are the constant 1), so a layer is the MMA and the ReLU of its FP16 output.
+template <int NB, int BLOB>
+__device__ __forceinline__ bool forward(NetSmem<NB, BLOB>& s, int nblocks, uint32_t& phase, float& o0, float& o1) {
     const int blk = threadIdx.x >> 7, row = threadIdx.x & 127;
     const uint32_t lane_cols = s.tmem + ((uint32_t)((threadIdx.x >> 5) & 3) * 32u << 16) + (uint32_t)(blk * 32);
-    const float* b1 = reinterpret_cast<const float*>(s.blob + Blob::B1);
-    const float* b2 = reinterpret_cast<const float*>(s.blob + Blob::B2);
-    const float* b3 = reinterpret_cast<const float*>(s.blob + Blob::B3);
+    constexpr int L2 = NB == 2 ? 0 : 2;  // where layer 2's activations go
     char* t0[2] = {s.a[0][0], s.a[0][1]};
     char* t1[2] = {s.a[1][0], s.a[1][1]};
-    char* t2[2] = {s.a[2][0], s.a[2][1]};
+    char* t2[2] = {s.a[L2][0], s.a[L2][1]};
     bool ok = true;
     float acc[32];
     sync_for_mma();
     ok &= layer(t0, s.blob + Blob::W1, kHid, s.tmem, nblocks, &s.bar, phase);
     tc::ld32(lane_cols, acc);
-#pragma unroll
-    for (int i = 0; i < 32; ++i) acc[i] = fmaxf(acc[i] + b1[i], 0.f);
-    store_row(s.a[1][blk], row, acc);
+    store_row_relu(s.a[1][blk], row, acc);
     sync_for_mma();
     ok &= layer(t1, s.blob + Blob::W2, kHid, s.tmem, nblocks, &s.bar, phase);
     tc::ld32(lane_cols, acc);
-#pragma unroll
-    for (int i = 0; i < 32; ++i) acc[i] = fmaxf(acc[i] + b2[i], 0.f);
-    store_row(s.a[2][blk], row, acc);
+    store_row_relu(s.a[L2][blk], row, acc);
     sync_for_mma();
     ok &= layer(t2, s.blob + Blob::W3, kOutPad, s.tmem, nblocks, &s.bar, phase);
     float o[16];
     tc::ld16(lane_cols, o);
-    o0 = o[0] + b3[0];
-    o1 = o[1] + b3[1];
+    o0 = o[0];
+    o1 = o[1];
     tc::fence_before_sync();
     return ok;
 }
@@ -151,7 +183,7 @@ struct CollectArgs {
 };
 
 template <bool COLLECT> struct LearnedFinish {
-    NetSmem* net;
+    InferSmem* net;
     uint32_t phase;
     CollectArgs col;
 
@@ -217,10 +249,10 @@ template <bool COLLECT> struct LearnedFinish {
                 }
             }
         } else {
-            NetSmem& s = *self.net;
+            InferSmem& s = *self.net;
             store_row(s.a[0][threadIdx.x >> 7], threadIdx.x & 127, f);
             float o0 = 0.f, o1 = 0.f;
-            const bool ok = forward(s, 2, self.phase, o0, o1);
+            const bool ok = forward_group(s, self.phase, o0, o1);
             if (!ok && threadIdx.x == 0) atomicOr(a.status, kStatusWindowTimeout);
             alpha = out_alpha(o0);
             scale = out_scale(o1);
@@ -246,18 +278,21 @@ template <bool COLLECT> struct LearnedFinish {
 using S = tiled::DefaultShape;
 
 template <int HF, int MC, bool COLLECT>
-__global__ void __launch_bounds__(S::NT, 3)
+__global__ void __launch_bounds__(S::NT, 4)
     resolve_learned(const taa_uniforms_t U, const FrameArgs a, const __grid_constant__ CUtensorMap hmap,
                     const int tma_ok, const char* __restrict__ blob, const CollectArgs col) {
     __shared__ tiled::TileSmem<LearnedPol, S, HF> sm;
     extern __shared__ __align__(128) char dyn[];
-    NetSmem& net = *reinterpret_cast<NetSmem*>(dyn);
+    InferSmem& net = *reinterpret_cast<InferSmem*>(dyn);
     if (threadIdx.x == 0) {
         tiled::mbar_init(&sm.bar, 1);
-        if (!COLLECT) tiled::mbar_init(&net.bar, 1);
+        if (!COLLECT) {
+            tiled::mbar_init(&net.bar_wg[0], 1);
+            tiled::mbar_init(&net.bar_wg[1], 1);
+        }
     }
     if (!COLLECT) {
-        copy_blob(net.blob, blob);
+        copy_blob(net.blob, blob, Blob::INFER_BYTES);
         if (threadIdx.x < 32) tc::tmem_alloc(&net.tmem, 64);
     }
     tc::fence_before_sync();
@@ -279,9 +314,9 @@ __global__ void __launch_bounds__(S::NT, 3)
 __global__ void __launch_bounds__(128) mlp_forward(const char* __restrict__ blob, const float* __restrict__ feat,
                                                    float* __restrict__ out, int n, unsigned int* status) {
     extern __shared__ __align__(128) char dyn[];
-    NetSmem& net = *reinterpret_cast<NetSmem*>(dyn);
+    InferSmem& net = *reinterpret_cast<InferSmem*>(dyn);
     if (threadIdx.x == 0) tiled::mbar_init(&net.bar, 1);
-    copy_blob(net.blob, blob);
+    copy_blob(net.blob, blob, Blob::INFER_BYTES);
     if (threadIdx.x < 32) tc::tmem_alloc(&net.tmem, 32);
     tc::fence_before_sync();
     __syncthreads();
@@ -312,20 +347,30 @@ __global__ void __launch_bounds__(128) mlp_forward(const char* __restrict__ blob
 constexpr int kParams = (int)(sizeof(Weights) / sizeof(float));
 constexpr int kGradFloats = kParams + 2;
 
-__device__ __forceinline__ float tonemap_g(float x) { return x / (1.f + fabsf(x)); }
+// The space the loss compares colours in: linear (TAA_MLP_LOSS 1, the space
+// the PSNR against the ground truth is measured in) or compressed by
+// x / (1 + |x|) (TAA_MLP_LOSS 0).
+#ifndef TAA_MLP_LOSS
+#define TAA_MLP_LOSS 1
+#endif
+__device__ __forceinline__ float tonemap_g(float x) { return TAA_MLP_LOSS ? x : x / (1.f + fabsf(x)); }
 __device__ __forceinline__ float tonemap_dg(float x) {
     const float d = 1.f + fabsf(x);
-    return 1.f / (d * d);
+    return TAA_MLP_LOSS ? 1.f : 1.f / (d * d);
 }
 
 // Loss of one record and its gradient with respect to the two outputs
 // (see the C ABI's taa_mlp_gradients for the definition).
+// As in inference, a box scale outside [0.5, 2] falls back to the plain
+// variance clip (scale 1, the record's plain alpha) and passes no gradient;
+// a penalty kPenalty * (|o1| - 1)^2 pulls such an output back into range.
+constexpr float kPenalty = 1.0f;
 __device__ __forceinline__ float record_loss(const Record& r, float o0, float o1, float& d0, float& d1) {
     const bool fixed_alpha = r.flags & 1u;
-    const float alpha = fixed_alpha ? r.alpha_fixed : out_alpha(o0);
     const float s = out_scale(o1);
-    const bool s_in = s > 0.5f && s < 2.0f;
-    const float sc = fminf(fmaxf(s, 0.5f), 2.0f);
+    const bool s_in = s >= 0.5f && s <= 2.0f;
+    const float alpha = (fixed_alpha || !s_in) ? r.alpha_fixed : out_alpha(o0);
+    const float sc = s_in ? s : 1.0f;
     float e[3], dd[3], ma = 0.f;
     int k = 0;
     for (int c = 0; c < 3; ++c) {
@@ -359,18 +404,22 @@ __device__ __forceinline__ float record_loss(const Record& r, float o0, float o1
         // hc = mean + d * e_k / |d_k| when clipped: d(hc)/d(sc) = d * gamma * sigma_k / |d_k|
         if (clipped) dsc += dout[c] * (1.f - alpha) * dd[c] * (r.gamma * r.sigma[k] / fabsf(dd[k]));
     }
-    d0 = fixed_alpha ? 0.f : dalpha * alpha * (1.f - alpha);
+    d0 = (fixed_alpha || !s_in) ? 0.f : dalpha * alpha * (1.f - alpha);
     d1 = s_in ? dsc * s * 0.69314718055994531f : 0.f;
+    if (!s_in) {
+        const float over = fabsf(o1) - 1.f;
+        loss += kPenalty * over * over;
+        d1 = 2.f * kPenalty * over * (o1 > 0.f ? 1.f : -1.f);
+    }
     return loss;
 }
 
 struct TrainSmem {
-    NetSmem net;
+    NetSmem<3, Blob::BYTES> net;
     alignas(128) char g3[kRows * 16 * 2];      // dLoss/dOutputs, [128][16] (2 used)
     alignas(128) char g2[kRows * kHid * 2];    // dLoss/dH2 after the ReLU mask
     alignas(128) char at[128 * kRows * 2];     // a gradient, transposed: [128 (32 or 2 used)][128 pixels]
     alignas(128) char bt[kHid * kRows * 2];    // an activation, transposed: [32][128 pixels]
-    float db[kHid + kHid + kOut];              // bias gradients of this CTA
     float loss;
     float count;
 };
@@ -413,8 +462,7 @@ __global__ void __launch_bounds__(128) mlp_train(const char* __restrict__ blob, 
         s.loss = 0.f;
         s.count = 0.f;
     }
-    for (int i = t; i < kHid + kHid + kOut; i += 128) s.db[i] = 0.f;
-    copy_blob(s.net.blob, blob);
+    copy_blob(s.net.blob, blob, Blob::BYTES);
     for (int w = t; w < (int)sizeof(s.at) / 16; w += 128) reinterpret_cast<uint4*>(s.at)[w] = make_uint4(0, 0, 0, 0);
     for (int w = t; w < (int)sizeof(s.g3) / 16; w += 128) reinterpret_cast<uint4*>(s.g3)[w] = make_uint4(0, 0, 0, 0);
     if (t < 32) tc::tmem_alloc(&s.net.tmem, 128);
@@ -461,18 +509,6 @@ __global__ void __launch_bounds__(128) mlp_train(const char* __restrict__ blob, 
 #pragma unroll
         for (int i = 0; i < 32; ++i) g[i] = h2[i] > 0.f ? __half2float(__float2half_rn(g[i])) : 0.f;
         store_row(s.g2, t, g);
-        // bias gradients of layers 3 and 2
-        {
-            const float v3[2] = {d0, d1};
-            for (int o = 0; o < 2; ++o) {
-                const float w = warp_sum(v3[o]);
-                if ((t & 31) == 0) atomicAdd(&s.db[2 * kHid + o], w);
-            }
-            for (int o = 0; o < kHid; ++o) {
-                const float w = warp_sum(g[o]);
-                if ((t & 31) == 0) atomicAdd(&s.db[kHid + o], w);
-            }
-        }
         // dW3 += dO^T . H2 and dW2 += dH2^T . H1 (transposed copies, then K = 128 pixels)
         {
             const float v3[2] = {d0, d1};
@@ -493,10 +529,6 @@ __global__ void __launch_bounds__(128) mlp_train(const char* __restrict__ blob, 
             tc::ld32(s.net.tmem + lane, g);
 #pragma unroll
             for (int i = 0; i < 32; ++i) g[i] = h1[i] > 0.f ? __half2float(__float2half_rn(g[i])) : 0.f;
-            for (int o = 0; o < kHid; ++o) {
-                const float w = warp_sum(g[o]);
-                if ((t & 31) == 0) atomicAdd(&s.db[o], w);
-            }
             tc::fence_before_sync();
             __syncthreads();
             store_col(s.at, t, g, kHid);
@@ -526,11 +558,6 @@ __global__ void __launch_bounds__(128) mlp_train(const char* __restrict__ blob, 
         for (int i = 0; i < kIn; ++i) atomicAdd(&grads[offsetof(Weights, w1) / 4 + t * kIn + i], acc[i]);
     }
     __syncthreads();
-    for (int i = t; i < kHid; i += 128) {
-        atomicAdd(&grads[offsetof(Weights, b1) / 4 + i], s.db[i]);
-        atomicAdd(&grads[offsetof(Weights, b2) / 4 + i], s.db[kHid + i]);
-    }
-    if (t < kOut) atomicAdd(&grads[offsetof(Weights, b3) / 4 + t], s.db[2 * kHid + t]);
     if (t == 0) {
         atomicAdd(&grads[kParams], s.loss);
         atomicAdd(&grads[kParams + 1], s.count);
@@ -541,6 +568,21 @@ __global__ void __launch_bounds__(128) mlp_train(const char* __restrict__ blob, 
     if (t < 32) tc::tmem_free(s.net.tmem, 128);
 }
 
+// The effective matrices of the FP32 masters: column 31 carries the bias,
+// rows 31 of layers 1 and 2 make the constant unit.
+__device__ __forceinline__ float eff1(const Weights& w, int h, int x) {
+    if (h == kConst) return x == kConst ? 1.f : 0.f;
+    return x == kConst ? w.b1[h] : w.w1[h * kIn + x];
+}
+__device__ __forceinline__ float eff2(const Weights& w, int o, int x) {
+    if (o == kConst) return x == kConst ? 1.f : 0.f;
+    return x == kConst ? w.b2[o] : w.w2[o * kHid + x];
+}
+__device__ __forceinline__ float eff3(const Weights& w, int o, int x) {
+    if (o >= kOut) return 0.f;
+    return x == kConst ? w.b3[o] : w.w3[o * kHid + x];
+}
+
 // The FP16 blob from FP32 master weights.
 __device__ __forceinline__ void build_blob(const Weights& w, char* blob, int t, int nt) {
     auto put = [&](int base, int r, int k, int K, float v) {
@@ -548,36 +590,48 @@ __device__ __forceinline__ void build_blob(const Weights& w, char* blob, int t, 
     };
     for (int i = t; i < kHid * kIn; i += nt) {
         const int h = i / kIn, x = i % kIn;
-        put(Blob::W1, h, x, kIn, w.w1[i]);
-    }
-    for (int i = t; i < kHid * kHid; i += nt) {
-        const int o = i / kHid, x = i % kHid;
-        put(Blob::W2, o, x, kHid, w.w2[i]);
-        put(Blob::W2T, x, o, kHid, w.w2[i]);
+        put(Blob::W1, h, x, kIn, eff1(w, h, x));
+        put(Blob::W2, h, x, kHid, eff2(w, h, x));
+        put(Blob::W2T, x, h, kHid, eff2(w, h, x));
     }
     for (int i = t; i < kOutPad * kHid; i += nt) {
         const int o = i / kHid, h = i % kHid;
-        const float v = o < kOut ? w.w3[o * kHid + h] : 0.f;
-        put(Blob::W3, o, h, kHid, v);
-        put(Blob::W3T, h, o, kOutPad, v);
+        put(Blob::W3, o, h, kHid, eff3(w, o, h));
+        put(Blob::W3T, h, o, kOutPad, eff3(w, o, h));
     }
-    float* b = reinterpret_cast<float*>(blob + Blob::B1);
+}
+
+// Gradients of the effective matrices -> gradients of the masters: column 31
+// is the bias, the constant rows and the unused columns have none.
+__device__ __forceinline__ void map_grads(float* g, int t, int nt) {
+    Weights& G = *reinterpret_cast<Weights*>(g);
     for (int i = t; i < kHid; i += nt) {
-        b[i] = w.b1[i];
-        reinterpret_cast<float*>(blob + Blob::B2)[i] = w.b2[i];
+        G.b1[i] = i == kConst ? 0.f : G.w1[i * kIn + kConst];
+        G.b2[i] = i == kConst ? 0.f : G.w2[i * kHid + kConst];
     }
-    for (int i = t; i < 4; i += nt) reinterpret_cast<float*>(blob + Blob::B3)[i] = i < kOut ? w.b3[i] : 0.f;
+    for (int i = t; i < kOut; i += nt) G.b3[i] = G.w3[i * kHid + kConst];
+    __syncthreads();
+    for (int i = t; i < kHid; i += nt) {
+        G.w1[i * kIn + kConst] = 0.f;
+        G.w2[i * kHid + kConst] = 0.f;
+        G.w1[kConst * kIn + i] = 0.f;
+        G.w2[kConst * kHid + i] = 0.f;
+    }
+    for (int i = t; i < kOut; i += nt) G.w3[i * kHid + kConst] = 0.f;
+    __syncthreads();
 }
 
 __global__ void mlp_build_blob(const Weights* w, char* blob) { build_blob(*w, blob, threadIdx.x, blockDim.x); }
+__global__ void mlp_map_grads(float* grads) { map_grads(grads, threadIdx.x, blockDim.x); }
 
 // Adam on the FP32 masters from the summed gradients (divided by the record
 // count), then the blob; the gradient buffer is cleared for the next step.
 __global__ void mlp_adam(Weights* w, float* m, float* v, float* grads, int step, float lr, char* blob) {
-    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;  // lr is this step's rate (the host decays it)
     const float n = fmaxf(grads[kParams + 1], 1.f);
     float* p = reinterpret_cast<float*>(w);
     const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+    map_grads(grads, threadIdx.x, blockDim.x);
     for (int i = threadIdx.x; i < kParams; i += blockDim.x) {
         const float g = grads[i] / n;
         m[i] = b1 * m[i] + (1.f - b1) * g;
@@ -600,6 +654,11 @@ size_t learned_record_bytes() { return sizeof(Record); }
 int learned_param_count() { return learned::kParams; }
 int learned_blob_bytes() { return learned::Blob::BYTES; }
 
+cudaError_t launch_mlp_map_grads(float* grads, cudaStream_t s) {
+    learned::mlp_map_grads<<<1, 256, 0, s>>>(grads);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_mlp_build_blob(const float* weights, char* blob, cudaStream_t s) {
     learned::mlp_build_blob<<<1, 256, 0, s>>>(reinterpret_cast<const learned::Weights*>(weights), blob);
     return cudaGetLastError();
@@ -608,7 +667,7 @@ cudaError_t launch_mlp_build_blob(const float* weights, char* blob, cudaStream_t
 cudaError_t launch_mlp_forward(const char* blob, const float* feat, float* out, int n, unsigned int* status,
                                cudaStream_t s) {
     const int grid = (n + learned::kRows - 1) / learned::kRows;
-    const int smem = (int)sizeof(learned::NetSmem);
+    const int smem = (int)sizeof(learned::InferSmem);
     cudaError_t e = cudaFuncSetAttribute(learned::mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     learned::mlp_forward<<<grid < 1 ? 1 : grid, 128, smem, s>>>(blob, feat, out, n, status);
@@ -644,7 +703,7 @@ cudaError_t launch_resolve_learned(int history_fmt, int motion_ch, bool collect,
     learned::CollectArgs col{reinterpret_cast<Record*>(records), count, capacity, seed,
                              (uint32_t)fminf(fmaxf(sample_fraction, 0.f) * 4294967040.f, 4294967040.f), truth};
     if (history_fmt != 0) return cudaErrorInvalidValue;
-    const int smem = collect ? 0 : (int)sizeof(learned::NetSmem);
+    const int smem = collect ? 0 : (int)sizeof(learned::InferSmem);
     auto go = [&](auto kernel) {
         cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;

@@ -26,30 +26,30 @@ constexpr int kIn = 32, kHid = 32, kOut = 2, kOutPad = 16;
 constexpr int kRows = 128;  // pixels per tensor-core block (the MMA's M)
 
 // The weights as FP32 masters (row-major [out][in]), the layout of
-// taa_mlp_weights_t (include/taa_gb300.h).
+// taa_mlp_weights_t (include/taa_gb300.h).  Unit 31 of each hidden layer is
+// the constant 1 that carries the next layer's bias (input 31 is the constant
+// feature): rows 31 of w1 and w2 and columns 31 of w1, w2 and w3 are not used.
 struct Weights {
     float w1[kHid * kIn], b1[kHid];
     float w2[kHid * kHid], b2[kHid];
     float w3[kOut * kHid], b3[kOut];
 };
+constexpr int kConst = 31;
 
-// The device blob the kernels copy into shared memory: FP16 weights in the
-// canonical K-major layout as MMA B operands ([N rows][K columns]), and the
-// transposes the backward pass multiplies by, then FP32 biases.
+// The device blob the kernels copy into shared memory: the FP16 effective
+// matrices (biases in column 31, the constant units' rows) in the canonical
+// K-major layout as MMA B operands ([N rows][K columns]) for inference, then
+// the transposes the backward pass multiplies by.
 struct Blob {
-    static constexpr int W1 = 0;                       // [32 hid][32 in]
-    static constexpr int W2 = W1 + kHid * kIn * 2;     // [32 hid][32 hid]
-    static constexpr int W3 = W2 + kHid * kHid * 2;    // [16 out (2 used)][32 hid]
-    static constexpr int W3T = W3 + kOutPad * kHid * 2;  // [32 hid][16 out (2 used)]
+    static constexpr int W1 = 0;                          // [32 hid][32 in]
+    static constexpr int W2 = W1 + kHid * kIn * 2;        // [32 hid][32 hid]
+    static constexpr int W3 = W2 + kHid * kHid * 2;       // [16 out (2 used)][32 hid]
+    static constexpr int INFER_BYTES = W3 + kOutPad * kHid * 2;
+    static constexpr int W3T = INFER_BYTES;               // [32 hid][16 out (2 used)]
     static constexpr int W2T = W3T + kHid * kOutPad * 2;  // [32 in of layer 2][32 out of layer 2]
-    static constexpr int W1T = W2T + kHid * kHid * 2;     // unused by the kernels; keeps the pattern
-    static constexpr int B1 = W2T + kHid * kHid * 2;      // float[32]
-    static constexpr int B2 = B1 + kHid * 4;
-    static constexpr int B3 = B2 + kHid * 4;              // float[2] (+2 pad)
-    static constexpr int INFER_BYTES = W3T;                // W1, W2, W3 are all inference reads ...
-    static constexpr int BYTES = B3 + 16;                  // ... plus the biases at the end
+    static constexpr int BYTES = W2T + kHid * kHid * 2;
 };
-static_assert(Blob::BYTES % 16 == 0, "blob copied as 16-byte words");
+static_assert(Blob::BYTES % 16 == 0 && Blob::INFER_BYTES % 16 == 0, "blob copied as 16-byte words");
 
 // Features of one pixel (see the file comment).  All colours YCoCg.
 struct FeatureIn {
@@ -61,8 +61,11 @@ struct FeatureIn {
 
 __device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
 
+// Fast approximate divisions and logarithm: the features only need to be the
+// same in training and inference, which run this same code.
 __device__ __forceinline__ void features(const FeatureIn& p, float (&f)[kIn]) {
-    const float inv = 1.0f / (fmaxf(p.mean[0], 0.f) + 0.05f);
+    const float lum = fmaxf(p.mean[0], 0.f) + 0.05f;
+    const float inv = __fdividef(1.0f, lum);
     float ma = 0.f;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -72,21 +75,21 @@ __device__ __forceinline__ void features(const FeatureIn& p, float (&f)[kIn]) {
         f[9 + c] = p.mx[c] * inv;
         f[12 + c] = p.hist[c] * inv;
         f[15 + c] = p.cur[c] * inv;
-        const float dev = (p.hist[c] - p.mean[c]) / (p.sigma[c] + 1e-3f / inv);
+        const float dev = __fdividef(p.hist[c] - p.mean[c], p.sigma[c] + 1e-3f * lum);
         f[18 + c] = clampf(dev, -8.f, 8.f) * 0.25f;
-        ma = fmaxf(ma, fabsf(p.hist[c] - p.mean[c]) / (p.sigma[c] + 1e-7f));
+        ma = fmaxf(ma, __fdividef(fabsf(p.hist[c] - p.mean[c]), p.sigma[c] + 1e-7f));
         f[27 + c] = (p.cur[c] - p.mean[c]) * inv;
     }
     f[21] = fminf(p.vel_px, 64.f) * (1.f / 16.f);
     f[22] = clampf(p.depth_rel, -8.f, 8.f) * 0.125f;
     f[23] = p.rejected ? 1.f : 0.f;
     f[24] = fminf(ma, 8.f) * 0.125f;
-    f[25] = log2f(fmaxf(p.mean[0], 0.f) + 1e-3f) * 0.125f;
+    f[25] = __log2f(fmaxf(p.mean[0], 0.f) + 1e-3f) * 0.125f;
     f[26] = (p.mx[0] - p.mn[0]) * inv;
     f[30] = (p.hist[0] - p.cur[0]) * inv;
     f[31] = 1.f;
-#pragma unroll
-    for (int i = 0; i < kIn; ++i) f[i] = clampf(f[i], -60000.f, 60000.f);  // finite in FP16
+    // every feature stays far inside the FP16 range: colours over a luma of
+    // at least 0.05, clamped deviations and ratios, velocity capped at 64 px
 }
 
 // The network's outputs turned into the blend weight and the box scale.
@@ -101,9 +104,9 @@ __device__ __forceinline__ void rectify_blend(const float (&mean)[3], const floa
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         d[c] = hist[c] - mean[c];
-        ma = fmaxf(ma, fabsf(d[c] / e[c]));
+        ma = fmaxf(ma, fabsf(__fdividef(d[c], e[c])));
     }
-    const float k = ma > 1.f ? 1.f / ma : 1.f;
+    const float k = ma > 1.f ? __fdividef(1.f, ma) : 1.f;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const float hc = mean[c] + d[c] * k;
@@ -125,6 +128,23 @@ __device__ __forceinline__ void store_row(char* tile, int r, const float (&v)[32
         *reinterpret_cast<uint4*>(tile + tc::canon(r, 8 * j, 32)) = w;
     }
 }
+// Row r of a canonical [128][32] A tile from 32 FP32 accumulators, through the
+// ReLU (applied to the FP16 values: rounding keeps the sign).
+__device__ __forceinline__ void store_row_relu(char* tile, int r, const float (&v)[32]) {
+    const __half2 zero = __float2half2_rn(0.f);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        __half2 h[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) h[q] = __hmax2(__floats2half2_rn(v[8 * j + 2 * q], v[8 * j + 2 * q + 1]), zero);
+        uint4 w;
+        w.x = *reinterpret_cast<uint32_t*>(&h[0]);
+        w.y = *reinterpret_cast<uint32_t*>(&h[1]);
+        w.z = *reinterpret_cast<uint32_t*>(&h[2]);
+        w.w = *reinterpret_cast<uint32_t*>(&h[3]);
+        *reinterpret_cast<uint4*>(tile + tc::canon(r, 8 * j, 32)) = w;
+    }
+}
 // Reads row r of a canonical [128][32] FP16 tile as floats.
 __device__ __forceinline__ void load_row(const char* tile, int r, float (&v)[32]) {
 #pragma unroll
@@ -140,15 +160,18 @@ __device__ __forceinline__ void load_row(const char* tile, int r, float (&v)[32]
     }
 }
 
-// Polls of an MMA-completion barrier before a wait gives up.
-constexpr uint32_t kMmaPolls = 1u << 22;
+// Polls of an MMA-completion barrier before a wait gives up; each poll
+// suspends the thread in hardware until the phase completes or kPollNs pass,
+// so a waiting warp issues a handful of instructions, not a spin loop.
+constexpr uint32_t kMmaPolls = 1u << 16;
+constexpr uint32_t kPollNs = 20000;
 __device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity) {
     for (uint32_t i = 0; i < kMmaPolls; ++i) {
         uint32_t done;
         asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
             : "=r"(done)
-            : "r"(tc::saddr(bar)), "r"(parity)
+            : "r"(tc::saddr(bar)), "r"(parity), "r"(kPollNs)
             : "memory");
         if (done) return true;
     }
@@ -162,6 +185,32 @@ __device__ __forceinline__ void sync_for_mma() {
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
+}
+// The same for the 128 threads of one warpgroup (named barrier 1 + wg).
+__device__ __forceinline__ void sync_group_for_mma(int wg) {
+    tc::fence_smem_to_async();
+    tc::fence_before_sync();
+    if (wg == 0) asm volatile("bar.sync 1, 128;" ::: "memory");
+    else asm volatile("bar.sync 2, 128;" ::: "memory");
+    tc::fence_after_sync();
+}
+
+// One dense layer for one 128-row block issued by one thread of its
+// warpgroup: D = A . W^T with K = 32 (two MMAs) and N = n.  Returns false if
+// the wait gave up.
+__device__ __forceinline__ bool layer_block(const char* a_tile, const char* w, int n, uint32_t d_tmem, bool issuer,
+                                            uint64_t* bar, uint32_t& phase) {
+    if (issuer) {
+        const uint32_t idesc = tc::idesc_f16(128, n);
+        for (int ks = 0; ks < 2; ++ks)
+            tc::mma_f16(d_tmem, tc::smem_desc(a_tile + ks * 256, 128, 512), tc::smem_desc(w + ks * 256, 128, 512),
+                        idesc, ks > 0);
+        tc::commit(bar);
+    }
+    const bool ok = wait_bar(bar, phase);
+    phase ^= 1u;
+    tc::fence_after_sync();
+    return ok;
 }
 
 // One dense layer for `nblocks` blocks of 128 rows: D[b] = A[b] . W^T with

@@ -63,6 +63,12 @@ int taa_mlp_init_weights(taa_mlp_weights_t* w, uint64_t seed, float alpha0) {
     for (float& x : w->w1) x = a1 * u(rng);
     for (float& x : w->w2) x = a1 * u(rng);
     for (float& x : w->w3) x = 0.01f * u(rng);
+    // the constant unit's row and column are not weights
+    for (int i = 0; i < 32; ++i) {
+        w->w1[31 * 32 + i] = w->w1[i * 32 + 31] = 0.f;
+        w->w2[31 * 32 + i] = w->w2[i * 32 + 31] = 0.f;
+    }
+    w->w3[31] = w->w3[32 + 31] = 0.f;
     w->b3[0] = std::log(alpha0 / (1.f - alpha0));
     w->b3[1] = 0.f;
     return TAA_OK;
@@ -178,6 +184,7 @@ int taa_mlp_gradients(taa_mlp_trainer* tr, const taa_mlp_weights_t* w, int32_t f
     const int grid = std::max(1, std::min((count + 127) / 128, 2 * tr->sms));
     if (e == cudaSuccess)
         e = taa_dev::launch_mlp_train(tr->blob, tr->records, nullptr, first, count, tr->grads, tr->status, grid, nullptr);
+    if (e == cudaSuccess) e = taa_dev::launch_mlp_map_grads(tr->grads, nullptr);
     std::vector<float> g(np + kGradExtra);
     if (e == cudaSuccess) e = cudaMemcpy(g.data(), tr->grads, sizeof(float) * g.size(), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(e, "taa_mlp_gradients");
@@ -220,7 +227,10 @@ int taa_mlp_train(taa_mlp_trainer* tr, taa_mlp_weights_t* w, int32_t steps, int3
             if (step == 1 && loss_first) *loss_first = mean;
             if (step == steps && loss_last) *loss_last = mean;
         }
-        if (e == cudaSuccess) e = taa_dev::launch_mlp_adam(tr->weights, tr->m, tr->v, tr->grads, step, lr, tr->blob, nullptr);
+        // cosine decay of the learning rate to a tenth over the run
+        const float lr_t = lr * (0.1f + 0.45f * (1.f + std::cos(3.14159265f * (float)(step - 1) / (float)steps)));
+        if (e == cudaSuccess)
+            e = taa_dev::launch_mlp_adam(tr->weights, tr->m, tr->v, tr->grads, step, lr_t, tr->blob, nullptr);
     }
     if (e == cudaSuccess) e = cudaMemcpy(w, tr->weights, sizeof *w, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(e, "taa_mlp_train");

@@ -1,0 +1,101 @@
+"""The learned rectifier's kernels against its CPU restatement (run with -m gpu).
+
+* the network alone (tensor cores, FP16 weights and activations, FP32
+  accumulation) against oracle/mlp_oracle.py's forward, which rounds to FP16
+  where the kernels do;
+* the training records a resolve collects: their features against the
+  restatement of the feature definition;
+* the summed loss and weight gradients of the training kernels against the
+  restatement's, whose own analytic gradients tests/test_oracle_mlp.py checks
+  by central differences;
+* training on records of other seeds of the renderer, then the learned form
+  against the plain variance clip on a held-out sequence, both against the
+  renderer's 64-spp ground truth.
+"""
+import numpy as np
+import pytest
+import torch
+
+import learned_pipeline as LP
+import mlp_oracle as M
+import taa_abi as T
+import workloads as WL
+
+pytestmark = pytest.mark.gpu
+
+
+def random_weights(seed):
+    w = T.mlp_init_weights(seed, 0.1)
+    rng = np.random.default_rng(seed)
+    for name, lo in (("w3", 0.3), ("b1", 0.1), ("b2", 0.1)):
+        arr = getattr(w, name)
+        for i in range(len(arr)):
+            arr[i] = float(rng.uniform(-lo, lo))
+    return w
+
+
+def test_network_matches_oracle(cuda):
+    w = random_weights(3)
+    ctx = T.Taa(64, 32, form=T.TAA_FORM_LEARNED)
+    ctx.set_mlp(w)
+    rng = np.random.default_rng(0)
+    for n in (1, 127, 128, 1000):
+        feat = rng.normal(0, 1, (n, 32)).astype(np.float32)
+        out = torch.zeros(n, 2, device=cuda)
+        ctx.mlp_forward(torch.from_numpy(feat).to(cuda), out)
+        torch.cuda.synchronize()
+        ref, _ = M.forward(T.mlp_to_numpy(w), feat)
+        assert np.max(np.abs(out.cpu().numpy() - ref)) <= 2e-3, n
+    ctx.close()
+
+
+@pytest.fixture(scope="module")
+def collected(cuda):
+    wl = WL.small(96, 64, frames=4, seed=7)
+    tr = T.MlpTrainer(50000)
+    n = LP.collect(tr, wl, 4, cuda, 0.5, skip=1, seed=3)
+    return tr, n, wl
+
+
+def test_records_and_features(collected):
+    tr, n, wl = collected
+    # half of the 96x64 pixels of frames 1..3, by hash
+    assert abs(n - 0.5 * 96 * 64 * 3) < 0.05 * 96 * 64 * 3
+    rec = tr.records(0, min(n, 3000))
+    assert np.all(np.isfinite(rec["features"])) and np.all(np.isfinite(rec["truth"]))
+    # the features that depend only on the record's own quantities
+    f = M.features(rec["mean"], rec["sigma"], rec["mean"], rec["mean"], rec["history"], rec["current"], 0.0, 0.0, 0.0)
+    idx = [0, 1, 2, 3, 4, 5, 12, 13, 14, 15, 16, 17, 18, 19, 20, 24, 25, 27, 28, 29, 30, 31]
+    got, ref = rec["features"][:, idx], M.half(f[:, idx])
+    assert np.max(np.abs(got - ref) / np.maximum(1e-3, np.abs(ref))) <= 3e-3
+
+
+def test_gradients_match_oracle(collected):
+    tr, n, _ = collected
+    count = min(n, 4000)
+    rec = tr.records(0, count)
+    for seed in (3, 4):
+        w = random_weights(seed)
+        g, loss = tr.gradients(w, 0, count)
+        loss_ref, g_ref = M.gradients(T.mlp_to_numpy(w), rec)
+        assert abs(loss - loss_ref) <= 1e-5 * abs(loss_ref)
+        gn = T.mlp_to_numpy(g)
+        for k in g_ref:
+            rel = np.linalg.norm(gn[k].ravel() - g_ref[k].ravel()) / max(np.linalg.norm(g_ref[k]), 1e-12)
+            assert rel <= 1e-4, (seed, k, rel)
+    assert T.device_status(clear=True) == 0
+
+
+def test_learned_form_beats_variance_clip_on_held_out_sequence(cuda):
+    tr = T.MlpTrainer(1_200_000)
+    for s in (601, 602, 603):
+        LP.collect(tr, WL.Workload(f"train {s}", 480, 270, 24, seed=s, num_spheres=32), 24, cuda, 0.12, skip=4, seed=s)
+    w, first, last = LP.train(tr, seed=1, steps=1500, batch=8192, lr=3e-3)
+    assert last < first
+    wl = WL.Workload("held out", 480, 270, 40, seed=5, num_spheres=32)
+    fr = LP.render(wl, 40, cuda)
+    plain, _ = LP.evaluate(wl, 40, cuda, T.TAA_FORM_TILED, fr=fr)
+    learned, _ = LP.evaluate(wl, 40, cuda, T.TAA_FORM_LEARNED, weights=w, fr=fr)
+    gain = float(np.mean(learned) - np.mean(plain))
+    assert gain >= 1.0, (np.mean(plain), np.mean(learned))
+    assert T.device_status(clear=True) == 0
