@@ -63,6 +63,10 @@ typedef enum taa_status {
 #define TAA_FORM_TILED  2u  /* FP32, CTA tile staged in shared memory */
 #define TAA_FORM_FP16   3u  /* packed half2 neighbourhood, clip and sharpen; FP32 history and blend */
 #define TAA_FORM_LEARNED 4u /* blend weight and clip-box scale from a per-pixel MLP (taa_set_mlp) */
+/* taa_desc_t.flags: run the learned form's network per 128-pixel warpgroup
+ * on tcgen05 through tensor memory instead of per warp with warp-wide MMAs
+ * (the default: no block barriers, faster inside the resolve). */
+#define TAA_FLAG_LEARNED_TCGEN05 0x1u
 /* Sharpener (taa<CF>::mSharpener, source/taa.hpp:1418). */
 #define TAA_SHARPEN_OFF     0u
 #define TAA_SHARPEN_SIMPLE  1u  /* shaders/sharpen.comp */
@@ -84,7 +88,7 @@ typedef struct taa_desc_t {
     uint32_t form;            /* TAA_FORM_* */
     uint32_t sharpener;       /* TAA_SHARPEN_* */
     float    sharpen_factor;  /* mSharpenFactor, default 0.5 (source/taa.hpp:1419) */
-    uint32_t flags;           /* reserved, 0 */
+    uint32_t flags;           /* 0, or TAA_FLAG_LEARNED_TCGEN05 with TAA_FORM_LEARNED */
 } taa_desc_t;
 
 /* Per-frame bindings; one field pair per descriptor binding of set 0 in

@@ -88,7 +88,9 @@ int check_desc(const taa_desc_t& d, const char* who) {
     if (d.form > TAA_FORM_LEARNED) return fail(TAA_E_INVAL, "%s: form %u", who, d.form);
     if (d.sharpener > TAA_SHARPEN_CAS) return fail(TAA_E_INVAL, "%s: sharpener %u", who, d.sharpener);
     if (!finite(d.sharpen_factor)) return fail(TAA_E_INVAL, "%s: sharpen_factor not finite", who);
-    if (d.flags != 0) return fail(TAA_E_INVAL, "%s: flags must be 0", who);
+    if (d.flags & ~TAA_FLAG_LEARNED_TCGEN05) return fail(TAA_E_INVAL, "%s: unknown flags 0x%x", who, d.flags);
+    if (d.flags && d.form != TAA_FORM_LEARNED)
+        return fail(TAA_E_INVAL, "%s: TAA_FLAG_LEARNED_TCGEN05 needs TAA_FORM_LEARNED", who);
     return ok();
 }
 
@@ -488,7 +490,7 @@ int taa_resolve(taa_ctx* c, void* stream, const taa_frame_io_t* io) {
         if (!c->have_mlp) return fail(TAA_E_INVAL, "taa_resolve: the learned form has no weights (taa_set_mlp)");
         if ((rc = learned_supported(d, U, io, "taa_resolve"))) return rc;
         e = taa_dev::launch_resolve_learned((int)d.history_format, d.motion_format == TAA_MOTION_RGBA16F ? 4 : 2,
-                                            false, U, a, c->mlp_blob, nullptr, nullptr, 0, 0, 0.f, Img{}, s);
+                                            false, (d.flags & TAA_FLAG_LEARNED_TCGEN05) != 0, U, a, c->mlp_blob, nullptr, nullptr, 0, 0, 0.f, Img{}, s);
     } else if (form == TAA_FORM_PLAIN) {
         if (sharpen && !a.result.p) a.result = ImgW{(char*)c->scratch_screen, c->scratch_pitch};
         e = taa_dev::launch_resolve_plain(U, a, (int)d.history_format, d.motion_format == TAA_MOTION_RGBA16F ? 4 : 2, s);

@@ -82,7 +82,7 @@ cudaError_t launch_mlp_train(const char* blob, const void* records, const uint32
                              float* grads, unsigned int* status, int grid, cudaStream_t s);
 cudaError_t launch_mlp_adam(float* weights, float* m, float* v, float* grads, int step, float lr, char* blob,
                             cudaStream_t s);
-cudaError_t launch_resolve_learned(int history_fmt, int motion_ch, bool collect, const taa_uniforms_t& U,
+cudaError_t launch_resolve_learned(int history_fmt, int motion_ch, bool collect, bool tcgen05, const taa_uniforms_t& U,
                                    const FrameArgs& a, const char* blob, void* records, uint32_t* count,
                                    uint32_t capacity, uint32_t seed, float sample_fraction, const Img& truth,
                                    cudaStream_t s);

@@ -142,7 +142,7 @@ int taa_mlp_collect(taa_mlp_trainer* tr, taa_ctx* c, void* stream, const taa_fra
     if ((rc = frame_args(d, c->uniforms, c->cas_const1[0], io, "taa_mlp_collect", &a))) return rc;
     const taa_dev::Img t{(const char*)truth, truth_pitch, d.out_width, d.out_height};
     cudaError_t e = taa_dev::launch_resolve_learned((int)d.history_format, d.motion_format == TAA_MOTION_RGBA16F ? 4 : 2,
-                                                    true, c->uniforms, a, nullptr, tr->records, tr->count,
+                                                    true, false, c->uniforms, a, nullptr, tr->records, tr->count,
                                                     (uint32_t)tr->capacity, seed, fraction, t, (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(e, "taa_mlp_collect");
     return TAA_OK;

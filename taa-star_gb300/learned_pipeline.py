@@ -84,13 +84,13 @@ def psnr(a, ref) -> float:
 
 
 def evaluate(wl: WL.Workload, frames: int, dev, form: int, weights: T.MlpWeights | None = None,
-             fr: Frames | None = None, skip: int = 8):
+             fr: Frames | None = None, skip: int = 8, flags: int = 0):
     """Per-frame PSNR (frames >= skip) of the resolved history against the
     ground truth, and the largest absolute error."""
     import torch
     fr = fr or render(wl, frames, dev)
     H, W = wl.height, wl.width
-    ctx = T.Taa(W, H, form=form)
+    ctx = T.Taa(W, H, form=form, flags=flags)
     if weights is not None:
         ctx.set_mlp(weights)
     hist = [torch.zeros(H, W, 4, device=dev), torch.zeros(H, W, 4, device=dev)]

@@ -27,6 +27,7 @@ TAA_HISTORY_RGBA16F = 1
 TAA_MOTION_RGBA16F = 0
 TAA_MOTION_RG16F = 1
 TAA_FORM_AUTO, TAA_FORM_PLAIN, TAA_FORM_TILED, TAA_FORM_FP16, TAA_FORM_LEARNED = 0, 1, 2, 3, 4
+TAA_FLAG_LEARNED_TCGEN05 = 0x1
 TAA_SHARPEN_OFF, TAA_SHARPEN_SIMPLE, TAA_SHARPEN_CAS = 0, 1, 2
 
 RTFLAG = dict(OUT=0x1, DIS=0x2, NRM=0x4, DPT=0x8, MID=0x10, LUM=0x20, CNT=0x40, ALL=0x80, FXD=0x100, FXA=0x200)
@@ -260,10 +261,11 @@ class Taa:
     """One resolve context (taa_create ... taa_destroy)."""
 
     def __init__(self, in_w, in_h, out_w=None, out_h=None, history_format=TAA_HISTORY_RGBA32F,
-                 motion_format=TAA_MOTION_RG16F, form=TAA_FORM_AUTO, sharpener=TAA_SHARPEN_OFF, sharpen_factor=0.5):
+                 motion_format=TAA_MOTION_RG16F, form=TAA_FORM_AUTO, sharpener=TAA_SHARPEN_OFF, sharpen_factor=0.5,
+                 flags=0):
         self.lib = load()
         d = Desc(C.sizeof(Desc), in_w, in_h, out_w or in_w, out_h or in_h, history_format, motion_format, form,
-                 sharpener, sharpen_factor, 0)
+                 sharpener, sharpen_factor, flags)
         h = C.c_void_p()
         check(self.lib.taa_create(C.byref(d), C.byref(h)))
         self.handle = h

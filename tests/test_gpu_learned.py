@@ -98,4 +98,29 @@ def test_learned_form_beats_variance_clip_on_held_out_sequence(cuda):
     learned, _ = LP.evaluate(wl, 40, cuda, T.TAA_FORM_LEARNED, weights=w, fr=fr)
     gain = float(np.mean(learned) - np.mean(plain))
     assert gain >= 1.0, (np.mean(plain), np.mean(learned))
+    # the same network per warpgroup on tcgen05 through tensor memory: the same
+    # FP16 operands, FP32 sums in another order
+    learned_tc, _ = LP.evaluate(wl, 40, cuda, T.TAA_FORM_LEARNED, weights=w, fr=fr, flags=T.TAA_FLAG_LEARNED_TCGEN05)
+    assert abs(float(np.mean(learned_tc)) - float(np.mean(learned))) <= 0.05
     assert T.device_status(clear=True) == 0
+
+
+def test_learned_paths_agree_on_one_frame(cuda):
+    wl = WL.small(96, 64, frames=2, seed=9)
+    fr = LP.render(wl, 2, cuda)
+    w = random_weights(5)
+    outs = []
+    for flags in (0, T.TAA_FLAG_LEARNED_TCGEN05):
+        ctx = T.Taa(96, 64, form=T.TAA_FORM_LEARNED, flags=flags)
+        ctx.set_mlp(w)
+        ctx.set_uniforms(T.make_uniforms(wl.parameters(), jitter_ndc=fr.jitter[1]))
+        h = torch.full((64, 96, 4), float("nan"), device=cuda)
+        ctx.resolve(color=fr.color[1], depth=fr.depth[1], velocity=fr.motion[1], history=fr.color[0].float(),
+                    history_depth=fr.depth[0], history_out=h)
+        torch.cuda.synchronize()
+        outs.append(h[..., :3].cpu().numpy())
+        ctx.close()
+    assert np.all(np.isfinite(outs[0])) and np.all(np.isfinite(outs[1]))
+    diff = np.abs(outs[0] - outs[1]) / np.maximum(1e-2, np.abs(outs[1]))
+    # FP32 accumulation order only: equal but for pixels near a rounding of the FP16 activations
+    assert np.mean(diff <= 1e-3) >= 0.99 and np.max(diff) <= 0.05
