@@ -44,6 +44,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--profile", choices=["tiled", "fp16", "plain", "batch48"],
                     help="a small case for ncu: a few launches of one form on 4K frames (no JSON line)")
@@ -192,6 +193,61 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------ our arm
+def time_learned(T, WL, dev, stream, sid, args):
+    """The C5 configuration of the learned rectifier: records from four other
+    seeds of the renderer (about 2M pixels, resolved with the plain variance
+    clip), Adam on the library's tensor-core training kernels, then the 64-frame
+    seed-5 sequence resolved by the plain variance clip and by the learned form,
+    each against the renderer's 64-spp ground truth; and the cost of one 1080p
+    resolve of each (CUDA events, 20 launches after 3)."""
+    import numpy as np
+    import torch
+    import learned_pipeline as LP
+
+    tr = T.MlpTrainer(2_200_000)
+    for s in (501, 502, 503, 504):
+        LP.collect(tr, WL.Workload(f"C5 training seed {s}", 1920, 1080, 24, seed=s, num_spheres=32), 24, dev, 0.0125,
+                   skip=4, seed=s)
+    records = tr.count()
+    steps, batch = 2000, 8192
+    w, loss_first, loss_last = LP.train(tr, seed=1, steps=steps, batch=batch, lr=3e-3)
+    tr.close()
+    wl = WL.c5()
+    fr = LP.render(wl, wl.frames, dev)
+    plain, plain_max = LP.evaluate(wl, wl.frames, dev, T.TAA_FORM_TILED, fr=fr)
+    learned, learned_max = LP.evaluate(wl, wl.frames, dev, T.TAA_FORM_LEARNED, weights=w, fr=fr)
+    H, W = wl.height, wl.width
+    cost = {}
+    for name, form in (("tiled", T.TAA_FORM_TILED), ("learned", T.TAA_FORM_LEARNED)):
+        ctx = T.Taa(W, H, form=form)
+        if form == T.TAA_FORM_LEARNED:
+            ctx.set_mlp(w)
+        ctx.set_uniforms(T.make_uniforms(wl.parameters(), jitter_ndc=fr.jitter[5]))
+        h = [torch.zeros(H, W, 4, device=dev) for _ in range(2)]
+        b = dict(color=fr.color[5], depth=fr.depth[5], velocity=fr.motion[5], history=h[0],
+                 history_depth=fr.depth[4], history_out=h[1])
+        for _ in range(3):
+            ctx.resolve(stream=sid, **b)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(20):
+            ctx.resolve(stream=sid, **b)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        cost[name] = e0.elapsed_time(e1) * 1000 / 20
+        ctx.close()
+    return {"mpx_s": W * H / cost["learned"], "us_per_frame_1080p": cost["learned"],
+            "plain_variance_clip_us_per_frame_1080p": cost["tiled"], "cost_vs_plain": cost["learned"] / cost["tiled"],
+            "psnr_db_vs_64spp": float(np.mean(learned)), "plain_psnr_db_vs_64spp": float(np.mean(plain)),
+            "gain_db": float(np.mean(learned) - np.mean(plain)), "max_abs_err": learned_max,
+            "plain_max_abs_err": plain_max,
+            "training": {"records": records, "steps": steps, "batch": batch, "loss_first": loss_first,
+                         "loss_last": loss_last, "seeds": [501, 502, 503, 504]},
+            "evaluation": f"{wl.name}, seed {wl.seed}, frames 8..{wl.frames - 1}, PSNR of the RGB history "
+                          "against the 64-spp truth, peak = the frame's largest truth value"}
+
+
 def time_batch(T, WL, dev, stream, sid, world, args, peak, single_mpx):
     """48 views of the C4 sizes resolved by one batched launch per step; the
     batch is autotuned first (tile shape, job order, grid).  Returns its Mpx/s,
@@ -355,6 +411,10 @@ def run_ours(args):
     # the 48-view batch (C4 sizes, log-uniform 320x180 .. 3840x2160): one launch per step
     if not args.no_batch:
         forms["batch48"] = time_batch(T, WL, dev, stream, sid, world, args, peak, mpx / world)
+
+    # the learned rectifier (C5: 1920x1080): trained here, judged against the 64-spp truth
+    if not args.no_learned and rank == 0:
+        forms["learned"] = time_learned(T, WL, dev, stream, sid, args)
 
     # end to end through the C ABI with host buffers (pinned), copies inside the timed region
     e2e = None

@@ -65,12 +65,14 @@ struct LearnedPol : tiled::ExactF32 {
             mn = {fminf(mn.x, f2lo(pa)), fminf(mn.y, f2hi(pa)), fminf(mn.z, f2lo(pb))};
             mx = {fmaxf(mx.x, f2lo(pa)), fmaxf(mx.y, f2hi(pa)), fmaxf(mx.z, f2lo(pb))};
         }
-        const f2 nN = dup(-9.0f), rN = dup(1.0f / 9.0f);
-        const f2 mean_a = div_const_rn2(m1a, nN, rN, z), mean_b = div_const_rn2(m1b, nN, rN, z);
-        const f2 var_a = fma2(neg2(mean_a), mean_a, div_const_rn2(m2a, nN, rN, z));
-        const f2 var_b = fma2(neg2(mean_b), mean_b, div_const_rn2(m2b, nN, rN, z));
+        // the learned form needs no rounding parity: products by 1/9 and a hardware square root
+        const f2 rN = dup(1.0f / 9.0f);
+        const f2 mean_a = mul2(m1a, rN, z), mean_b = mul2(m1b, rN, z);
+        const f2 var_a = fma2(neg2(mean_a), mean_a, mul2(m2a, rN, z));
+        const f2 var_b = fma2(neg2(mean_b), mean_b, mul2(m2b, rN, z));
         b.mean = {f2lo(mean_a), f2hi(mean_a), f2lo(mean_b)};
-        b.sigma = {sqrtf(gmax(0.f, f2lo(var_a))), sqrtf(gmax(0.f, f2hi(var_a))), sqrtf(gmax(0.f, f2lo(var_b)))};
+        b.sigma = {sqrt_approx(fmaxf(0.f, f2lo(var_a))), sqrt_approx(fmaxf(0.f, f2hi(var_a))),
+                   sqrt_approx(fmaxf(0.f, f2lo(var_b)))};
         b.mn = mn;
         b.mx = mx;
     }
@@ -326,8 +328,8 @@ template <bool COLLECT, bool TC> struct LearnedFinish {
         fi.mn[0] = box.mn.x; fi.mn[1] = box.mn.y; fi.mn[2] = box.mn.z;
         fi.mx[0] = box.mx.x; fi.mx[1] = box.mx.y; fi.mx[2] = box.mx.z;
         const float du = (u - hu) * (float)a.out_w, dv = (v - hv) * (float)a.out_h;
-        fi.vel_px = sqrtf(du * du + dv * dv);
-        fi.depth_rel = P.mDepthCulling ? (prev_depth - ehd) / (0.1f * (1.0f - prev_depth) + 1e-6f) : 0.f;
+        fi.vel_px = sqrt_approx(du * du + dv * dv);
+        fi.depth_rel = P.mDepthCulling ? __fdividef(prev_depth - ehd, 0.1f * (1.0f - prev_depth) + 1e-6f) : 0.f;
         fi.rejected = rejected;
         float f[kIn];
         if (valid) {
@@ -395,8 +397,13 @@ template <bool COLLECT, bool TC> struct LearnedFinish {
 
 using S = tiled::DefaultShape;
 
+// Resident CTAs per SM the learned kernels' register budget is sized for
+// (the tensor-memory path needs 64 registers: 4).
+#ifndef TAA_LEARNED_MIN_BLOCKS
+#define TAA_LEARNED_MIN_BLOCKS 4
+#endif
 template <int HF, int MC, bool COLLECT, bool TC>
-__global__ void __launch_bounds__(S::NT, 4)
+__global__ void __launch_bounds__(S::NT, TC ? 4 : TAA_LEARNED_MIN_BLOCKS)
     resolve_learned(const taa_uniforms_t U, const FrameArgs a, const __grid_constant__ CUtensorMap hmap,
                     const int tma_ok, const char* __restrict__ blob, const CollectArgs col) {
     __shared__ tiled::TileSmem<LearnedPol, S, HF> sm;
