@@ -92,9 +92,21 @@ __device__ __forceinline__ void features(const FeatureIn& p, float (&f)[kIn]) {
     // at least 0.05, clamped deviations and ratios, velocity capped at 64 px
 }
 
+// Hardware approximations (MUFU): the learned form only needs training and
+// inference to agree, and both run these same functions.
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float exp2_approx(float x) {
+    float r;
+    asm("ex2.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 // The network's outputs turned into the blend weight and the box scale.
-__device__ __forceinline__ float out_alpha(float o0) { return 1.0f / (1.0f + __expf(-o0)); }
-__device__ __forceinline__ float out_scale(float o1) { return exp2f(o1); }
+__device__ __forceinline__ float out_alpha(float o0) { return __fdividef(1.0f, 1.0f + __expf(-o0)); }
+__device__ __forceinline__ float out_scale(float o1) { return exp2_approx(o1); }
 
 // Variance clip towards the mean with the box mean +- e (e = s*gamma*sigma +
 // 1e-7, taa.comp:323-345), then the blend (taa.comp:900).  YCoCg in and out.
