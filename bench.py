@@ -45,8 +45,9 @@ def parse():
     ap.add_argument("--no-forms", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-fxaa", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--profile", choices=["tiled", "fp16", "plain", "batch48"],
+    ap.add_argument("--profile", choices=["tiled", "fp16", "plain", "batch48", "fxaa"],
                     help="a small case for ncu: a few launches of one form on 4K frames (no JSON line)")
     return ap.parse_args()
 
@@ -248,6 +249,80 @@ def time_learned(T, WL, dev, stream, sid, args):
                           "against the 64-spp truth, peak = the frame's largest truth value"}
 
 
+def time_fxaa(T, WL, dev, stream, sid, args, peak, col, dep, mot, uniforms):
+    """The FXAA pass of the ray-trace-assist path at 4K: a plain-form resolve of
+    C2 frame 2 with the segmentation mask (RT-augment tests OUT, DIS, NRM, DPT,
+    MID, LUM and the FXAA flag) gives the result image and the mask; taa_fxaa
+    then runs on them, on the mask and with every pixel marked (NULL mask).
+    Four buffer sets rotate (660 MB), so no launch finds its inputs in the
+    129 MB L2.  Algorithmic bytes: 8 (result) + 4 (mask) + 8 (output) per pixel,
+    16 without a mask; the reference's prepare + FXAA dispatches move 36."""
+    import numpy as np
+    import torch
+    import oracle as O
+
+    H, W = col.shape[1], col.shape[2]
+    u = T.Uniforms()
+    ctypes_copy(u, uniforms[2])
+    for i in range(2):
+        u.param[i].mRayTraceAugment = 1
+        u.param[i].mRayTraceAugmentFlags = 0x3F | 0x200
+    ctx = T.Taa(W, H, form=T.TAA_FORM_PLAIN)
+    ctx.set_uniforms(u)
+    sets = 4
+    res = [torch.empty(H, W, 4, dtype=torch.float16, device=dev) for _ in range(sets)]
+    seg = [torch.empty(H, W, dtype=torch.int32, device=dev) for _ in range(sets)]
+    out = [torch.empty(H, W, 4, dtype=torch.float16, device=dev) for _ in range(sets)]
+    h0 = col[1].float()
+    ctx.resolve(stream=sid, color=col[2], depth=dep[2], velocity=mot[2], history=h0, history_depth=dep[1],
+                history_out=torch.empty(H, W, 4, device=dev), result=res[0], segmask=seg[0])
+    for i in range(1, sets):
+        res[i].copy_(res[0])
+        seg[i].copy_(seg[0])
+    torch.cuda.synchronize()
+    ctx.close()
+    marked = float(((seg[0] & 3) == 1).float().mean().item())
+    result = {}
+    k = max(8, args.steps * 4)
+    for name, use_mask in (("segmask", True), ("all_pixels", False)):
+        for i in range(3 * sets):
+            T.fxaa(res[i % sets], out[i % sets], seg[i % sets] if use_mask else None, stream=sid)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(k):
+            T.fxaa(res[i % sets], out[i % sets], seg[i % sets] if use_mask else None, stream=sid)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        us = e0.elapsed_time(e1) * 1000 / k
+        bpp = 20 if use_mask else 16
+        gbs = bpp * W * H / (us / 1e6) / 1e9
+        result[name] = {"us_per_frame": us, "mpx_s": W * H / us, "bytes_per_px": bpp, "gb_s": gbs,
+                        "frac_of_hbm": gbs / peak}
+    result["marked_fraction"] = marked
+    # the oracle on the same frame and mask (the checker, timed as the CPU reference)
+    img = res[0].float().cpu().numpy()
+    m = seg[0].cpu().numpy().view(np.uint32)
+    nthr = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ref = O.fxaa(img, m, nthreads=nthr)
+    t = time.perf_counter() - t0
+    T.fxaa(res[0], out[0], seg[0], stream=sid)
+    torch.cuda.synchronize()
+    got = out[0].float().cpu().numpy()
+    q = ref.astype(np.float32).astype(np.float16).astype(np.float32)
+    result["cpu_oracle"] = {"mpx_s": W * H / t / 1e6, "threads": nthr}
+    result["pixels_equal_to_oracle"] = float(np.mean(np.all(got == q, axis=-1)))
+    result["note"] = ("fused prepare + FXAA 3.11 quality preset 12 (one kernel); rotation over 4 buffer sets "
+                      "instead of an L2 flush")
+    return result
+
+
+def ctypes_copy(dst, src):
+    import ctypes as C
+    C.memmove(C.addressof(dst), C.addressof(src), C.sizeof(dst))
+
+
 def time_batch(T, WL, dev, stream, sid, world, args, peak, single_mpx):
     """48 views of the C4 sizes resolved by one batched launch per step; the
     batch is autotuned first (tile shape, job order, grid).  Returns its Mpx/s,
@@ -412,6 +487,10 @@ def run_ours(args):
     if not args.no_batch:
         forms["batch48"] = time_batch(T, WL, dev, stream, sid, world, args, peak, mpx / world)
 
+    # the FXAA pass on the segmentation mask (ray-trace-assist path) at 4K
+    if not args.no_fxaa and rank == 0:
+        forms["fxaa"] = time_fxaa(T, WL, dev, stream, sid, args, peak, col, dep, mot, uniforms)
+
     # the learned rectifier (C5: 1920x1080): trained here, judged against the 64-spp truth
     if not args.no_learned and rank == 0:
         forms["learned"] = time_learned(T, WL, dev, stream, sid, args)
@@ -553,6 +632,23 @@ def run_profile_case(args):
         T.synth_render(sc, f, stream=sid, color=col[f], depth=dep[f], motion=mot[f])
     hist = [torch.zeros(H, W, 4, dtype=torch.float32, device=dev) for _ in range(2)]
     res = torch.empty(H, W, 4, dtype=torch.float16, device=dev)
+    if args.profile == "fxaa":
+        # one resolve with the segmentation mask, then the FXAA pass: 3 launches on the mask, 1 on every pixel
+        u = T.make_uniforms(wl.parameters(), jitter_ndc=T.synth_jitter(sc, 2)[1])
+        for i in range(2):
+            u.param[i].mRayTraceAugment = 1
+            u.param[i].mRayTraceAugmentFlags = 0x3F | 0x200
+        ctx = T.Taa(W, H, form=T.TAA_FORM_PLAIN)
+        ctx.set_uniforms(u)
+        seg = torch.empty(H, W, dtype=torch.int32, device=dev)
+        ctx.resolve(stream=sid, color=col[2], depth=dep[2], velocity=mot[2], history=col[1].float(),
+                    history_depth=dep[1], history_out=hist[0], result=res, segmask=seg)
+        out = torch.empty_like(res)
+        for i in range(4):
+            T.fxaa(res, out, seg if i < 3 else None, stream=sid)
+        torch.cuda.synchronize()
+        ctx.close()
+        return 0
     form = {"tiled": T.TAA_FORM_TILED, "fp16": T.TAA_FORM_FP16, "plain": T.TAA_FORM_PLAIN}[args.profile]
     ctx = T.Taa(W, H, form=form)
     for f in range(1, F):

@@ -111,6 +111,9 @@ typedef struct taa_frame_io_t {
     void*       sharpened;     size_t sharpened_pitch;      /* the sharpen pass's output   (RGBA16F, with a sharpener) */
 } taa_frame_io_t;
 
+/* Longest list of debug sample offsets (sample distribution 5, taa_settings_t). */
+#define TAA_SETTINGS_MAX_SAMPLE_OFFSETS 64
+
 /* Jitter options: the debugging knobs of taa<CF>::get_jitter_offset_for_frame
  * (source/taa.hpp:219-232, members 1404-1407).  Pass NULL for the defaults. */
 typedef struct taa_jitter_opts_t {
@@ -142,6 +145,14 @@ int taa_get_jitter_offset(int32_t sample_distribution, uint64_t frame_id,
                           int32_t in_width, int32_t in_height,
                           const taa_jitter_opts_t* opts,
                           float out_ndc[2], int32_t* out_num_samples);
+
+/* Sample distribution 5 of the same function (source/taa.hpp:207-211): the
+ * frame's entry of `count` (1..TAA_SETTINGS_MAX_SAMPLE_OFFSETS) debug sample
+ * offsets given in pixels (taa_settings_t.mDebugSampleOffsets), scaled to NDC,
+ * then the same debugging knobs. */
+int taa_get_jitter_offset_custom(const float (*offsets_px)[2], int32_t count, uint64_t frame_id,
+                                 int32_t in_width, int32_t in_height, const taa_jitter_opts_t* opts,
+                                 float out_ndc[2]);
 
 /* translate(jitter.x, jitter.y, 0) * proj, taa<CF>::get_jittered_projection_matrix
  * (source/taa.hpp:243-253).  Column-major 4x4. */
@@ -183,6 +194,90 @@ int taa_selected_form(const taa_ctx* ctx);
  * source/taa.hpp:1125/1134).  `io->history` and `io->history_out` must not
  * overlap. */
 int taa_resolve(taa_ctx* ctx, void* stream, const taa_frame_io_t* io);
+
+/* ---- passes after the resolve ------------------------------------------- */
+
+/* FXAA settings: the push constants of the FXAA pass (source/taa.hpp:93-98). */
+typedef struct taa_fxaa_params_t {
+    float subpix;              /* fxaaQualitySubpix, 0.75: amount of sub-pixel aliasing removal */
+    float edge_threshold;      /* fxaaQualityEdgeThreshold, 0.116: local contrast needed */
+    float edge_threshold_min;  /* fxaaQualityEdgeThresholdMin, 0.0833: trims darks */
+} taa_fxaa_params_t;
+
+/* Fill `out` with the reference's FXAA settings (source/taa.hpp:95-97). */
+int taa_fxaa_default_params(taa_fxaa_params_t* out);
+
+/* FXAA on the pixels the segmentation mask marks for it: the prepare and the
+ * FXAA dispatches of the ray-trace-assist path (source/taa.hpp:1063-1104,
+ * shaders/antialias_fxaa_prepare.comp + shaders/antialias_fxaa.comp with
+ * FXAA 3.11 quality preset 12) as one pass.  `input`: the RGBA16F result image
+ * of a resolve; `segmask`: the R32UI mask the resolve wrote (pixels with
+ * (mask & 3) == 1 are antialiased), or NULL to antialias every pixel;
+ * `output`: RGBA16F, rgb and the FP16 luma in alpha as the reference's temp
+ * image holds them.  All images width x height; `output` must not overlap
+ * `input`.  `params` NULL means the defaults.  Enqueued on `stream`. */
+int taa_fxaa(void* stream, const void* input, size_t input_pitch, const void* segmask, size_t segmask_pitch,
+             void* output, size_t output_pitch, int32_t width, int32_t height, const taa_fxaa_params_t* params);
+
+/* The sharpen pass on its own (source/taa.hpp:1111-1139): sharpener
+ * TAA_SHARPEN_SIMPLE (shaders/sharpen.comp) or TAA_SHARPEN_CAS
+ * (shaders/sharpen_cas.comp, CasSetup of `factor` at this size) from an RGBA16F
+ * image into another of the same size.  For chains where the sharpener reads
+ * another pass's output (after taa_fxaa); taa_resolve fuses it otherwise. */
+int taa_sharpen(void* stream, uint32_t sharpener, float factor, const void* input, size_t input_pitch, void* output,
+                size_t output_pitch, int32_t width, int32_t height);
+
+/* ---- settings files ------------------------------------------------------ */
+
+/* The settings taa<CF> writes to and reads from its .ini file
+ * (writeSettingsToIni / readSettingsFromIni, source/taa.hpp:1198-1339): both
+ * parameter sets and the members of the sections TAA_Primary and
+ * TAA_Postprocess.  Booleans are 0/1. */
+typedef struct taa_settings_t {
+    taa_parameters_t param[2];          /* [TAA_Param_0], [TAA_Param_1] */
+    /* [TAA_Primary] */
+    uint32_t mTaaEnabled;
+    int32_t  mSampleDistribution;
+    int32_t  mSharpener;
+    float    mSharpenFactor;
+    uint32_t mSplitScreen;
+    int32_t  mSplitX;
+    int32_t  mFixedJitterIndex;
+    float    mJitterExtraScale;
+    int32_t  mJitterSlowMotion;
+    float    mJitterRotateDegrees;
+    uint32_t mResetHistoryOnChange;
+    int32_t  mDebugSampleOffsetsCount;  /* 1..TAA_SETTINGS_MAX_SAMPLE_OFFSETS */
+    float    mDebugSampleOffsets[TAA_SETTINGS_MAX_SAMPLE_OFFSETS][2];
+    /* [TAA_Postprocess] */
+    uint32_t mPostProcessEnabled;
+    uint32_t zoom;
+    uint32_t showZoomBox;
+    int32_t  zoomSrcLTWH[4];
+    int32_t  zoomDstLTWH[4];
+} taa_settings_t;
+
+/* The reference's initial values of every member above (source/taa.hpp:31-76,
+ * 101-111 for the post-processing push constants, 1350-1420 for the others). */
+int taa_settings_default(taa_settings_t* out);
+
+/* Write the settings as the reference's .ini text: the sections and keys of
+ * writeSettingsToIni, keys lower-cased and `key=value` lines as its INI
+ * library writes them, numbers formatted like std::to_string (floats with six
+ * decimals, as the reference stores them).  The length of the text (without
+ * the terminating NUL) goes to *length; with `text` NULL nothing else happens,
+ * otherwise the text and a NUL are written if they fit in `capacity` bytes and
+ * TAA_E_INVAL is returned (nothing written) if they do not. */
+int taa_settings_write_ini(const taa_settings_t* settings, char* text, size_t capacity, size_t* length);
+
+/* Read .ini text (a whole settings file of the reference, or what
+ * taa_settings_write_ini wrote) into *settings: every key readSettingsFromIni
+ * reads that is present and non-empty overwrites its member; absent keys
+ * leave the member as it was; other sections and keys are ignored.  Section
+ * and key names match case-insensitively; ';' starts a comment line.  A value
+ * that does not start with a number returns TAA_E_INVAL (the reference's
+ * std::stoi/stof throw there) and leaves *settings unchanged. */
+int taa_settings_read_ini(taa_settings_t* settings, const char* text, size_t length);
 
 /* ---- batches: many views in one persistent launch --------------------------
  * No counterpart in the reference, which resolves one view per dispatch

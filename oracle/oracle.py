@@ -35,6 +35,7 @@ def load():
                                       [dp] * 3 + [up, C.c_int]
         lib.oracle_cas.argtypes = [C.c_int, fp, C.c_int, C.c_int, C.c_uint32, dp, C.c_int]
         lib.oracle_sharpen.argtypes = [C.c_int, fp, C.c_int, C.c_int, C.c_float, dp, C.c_int]
+        lib.oracle_fxaa.argtypes = [C.c_int, fp, up, C.c_int, C.c_int] + [C.c_float] * 5 + [dp, C.c_int]
         lib.oracle_cas_setup.argtypes = [C.c_float] * 5 + [up, up]
         lib.oracle_cas_setup.restype = None
         lib.oracle_halton.argtypes = [C.c_int, C.c_int]
@@ -123,6 +124,28 @@ def sharpen(img, factor, precision=32, nthreads=None):
     h, w = a.shape[:2]
     out = np.zeros((h, w, 4))
     lib.oracle_sharpen(precision, _fp(a), w, h, factor, _dp(out), nthreads or nthreads_default())
+    return out
+
+
+FXAA_DEFAULTS = (0.75, 0.116, 0.0833)  # fxaaQualitySubpix, EdgeThreshold, EdgeThresholdMin (taa.hpp:95-97)
+
+
+def fxaa(img, segmask=None, subpix=0.75, edge_threshold=0.116, edge_threshold_min=0.0833, precision=32,
+         nthreads=None):
+    """FXAA prepare + FXAA 3.11 quality preset 12 on the pixels with (segmask & 3) == 1
+    (every pixel when segmask is None); returns rgb and the FP16-stored luma."""
+    lib = load()
+    a = _f32(img, 4)
+    h, w = a.shape[:2]
+    seg = None if segmask is None else _u32(segmask)
+    if seg is not None and seg.shape != (h, w):
+        raise ValueError("segmask must be (H, W)")
+    rcp = np.float32(1.0) / np.array([w, h], np.float32)
+    out = np.zeros((h, w, 4))
+    rc = lib.oracle_fxaa(precision, _fp(a), _up(seg), w, h, float(rcp[0]), float(rcp[1]), subpix, edge_threshold,
+                         edge_threshold_min, _dp(out), nthreads or nthreads_default())
+    if rc != 0:
+        raise ValueError("oracle_fxaa rejected its arguments")
     return out
 
 

@@ -45,6 +45,12 @@ int oracle_sharpen(int precision, const float* in, int w, int h, float factor, d
     return sharpen(precision, in, w, h, factor, out, nthreads);
 }
 
+int oracle_fxaa(int precision, const float* in, const uint32_t* segmask, int w, int h, float rcp_x, float rcp_y,
+                float subpix, float thr, float thr_min, double* out, int nthreads) {
+    const float rcp[2] = {rcp_x, rcp_y};
+    return fxaa(precision, in, segmask, w, h, rcp, subpix, thr, thr_min, out, nthreads);
+}
+
 void oracle_cas_setup(float s, float iw, float ih, float ow, float oh, uint32_t* c0, uint32_t* c1) {
     cas_setup(s, iw, ih, ow, oh, c0, c1);
 }

@@ -12,6 +12,10 @@ present (they are not built on the GPU machine).
     parameters become `T &name` (C++ spells out-parameters as references).
   * libcas_ref.so - CasSetup from shaders/ffx_cas.h with ffx_a.h's CPU path
     (A_CPU), exactly as source/taa.hpp:15-19 compiles it.
+  * libfxaa_ref32.so / libfxaa_ref64.so - shaders/antialias_fxaa_prepare.comp
+    and shaders/antialias_fxaa.comp (which includes shaders/Fxaa3_11_mod.h
+    from the reference tree as it lies) through the same shim, with the
+    sampler snapping within 1/512 texel of a texel centre.
 """
 from __future__ import annotations
 
@@ -64,6 +68,19 @@ def build(force: bool = False):
         lib = OUT / name
         if force or not lib.exists() or lib.stat().st_mtime < max(p.stat().st_mtime for p in SHIM.iterdir()):
             _run([*common, *flags, "-o", str(lib)])
+        libs[name] = lib
+    prep = OUT / "fxaa_prepare_comp.glsl.inc"
+    fx = OUT / "fxaa_comp.glsl.inc"
+    rewrite(SHADERS / "antialias_fxaa_prepare.comp", prep)
+    rewrite(SHADERS / "antialias_fxaa.comp", fx)
+    fxaa_common = [cxx, "-O1", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+                   "-Wno-pedantic", "-I", str(SHIM), "-I", str(SHADERS), "-DGLSL_SNAP=(1.0/512.0)",
+                   f'-DFXAA_PREPARE_SOURCE="{prep}"', f'-DFXAA_SOURCE="{fx}"', str(SHIM / "fxaa_ref_main.cpp")]
+    for name, flags in (("libfxaa_ref32.so", ["-DREAL=float", "-fsingle-precision-constant"]),
+                        ("libfxaa_ref64.so", ["-DREAL=double"])):
+        lib = OUT / name
+        if force or not lib.exists() or lib.stat().st_mtime < max(p.stat().st_mtime for p in SHIM.iterdir()):
+            _run([*fxaa_common, *flags, "-o", str(lib)])
         libs[name] = lib
     cas = OUT / "libcas_ref.so"
     if force or not cas.exists():

@@ -1,6 +1,8 @@
 // glsl_shim.hpp - just enough GLSL, as C++, to compile the reference's
-// compute shaders (shaders/taa.comp, shaders/sharpen.comp) unmodified except
-// for the mechanical rewrites oracle/ref_build.py applies.
+// compute shaders (shaders/taa.comp, shaders/sharpen.comp,
+// shaders/antialias_fxaa_prepare.comp, shaders/antialias_fxaa.comp with
+// shaders/Fxaa3_11_mod.h) unmodified except for the mechanical rewrites
+// oracle/ref_build.py applies.
 //
 // TEST INFRASTRUCTURE: it pins the oracle's restatement against the
 // reference's own shader source; nothing in the product uses it.
@@ -52,6 +54,7 @@ struct vec2 {
         struct { GReal x, y; };
         struct { GReal r, g; };
         GReal d[2];
+        swz<2, vec2, 0, 1> xy;
     };
     vec2() : x(0), y(0) {}
     template <class A, if_arith<A> = 0> explicit vec2(A a) : x(GReal(a)), y(GReal(a)) {}
@@ -218,6 +221,8 @@ struct texture2D {
 struct sampler {};
 struct sampler2D {
     const texture2D* t;
+    sampler2D() : t(nullptr) {}  // a combined image sampler binding (bound by the driver code)
+    explicit sampler2D(const texture2D* tex) : t(tex) {}
     sampler2D(const texture2D& tex, const sampler&) : t(&tex) {}
 };
 struct image2D {
@@ -248,9 +253,8 @@ inline ivec2 textureSize(const texture2D& t, int) { return ivec2(t.w, t.h); }
 inline vec4 texelFetch(const texture2D& t, const ivec2& c, int) { return texel(t, c.x, c.y); }
 
 // bilinear, clamp to edge, exact weights; snaps to a centre within GLSL_SNAP texels
-inline vec4 texture(const sampler2D& s, const vec2& uv) {
-    const texture2D& t = *s.t;
-    double px = double(uv.x) * t.w - 0.5, py = double(uv.y) * t.h - 0.5;
+// (px, py): the footprint position in texel units (uv * size - 0.5)
+inline vec4 texture_texels(const texture2D& t, double px, double py) {
     // a NaN coordinate reads the edge texel with weight 1 (taa.comp:535 divides
     // 0/0 at zero motion and then weights that tap by 0)
     if (px != px) px = -1e9;
@@ -267,6 +271,20 @@ inline vec4 texture(const sampler2D& s, const vec2& uv) {
     vec4 top = a * gx + b * fx, bot = c * gx + d * fx;
     return top * gy + bot * fy;
 }
+inline vec4 texture(const sampler2D& s, const vec2& uv) {
+    const texture2D& t = *s.t;
+    return texture_texels(t, double(uv.x) * t.w - 0.5, double(uv.y) * t.h - 0.5);
+}
+
+// textureLod at level 0 of a single-level image is texture(); the offset
+// variant moves the footprint by whole texels (GLSL 4.60 8.9.2).
+inline vec4 textureLod(const sampler2D& s, const vec2& uv, GReal) { return texture(s, uv); }
+inline vec4 textureLodOffset(const sampler2D& s, const vec2& uv, GReal, const ivec2& o) {
+    const texture2D& t = *s.t;
+    return texture_texels(t, double(uv.x) * t.w - 0.5 + o.x, double(uv.y) * t.h - 0.5 + o.y);
+}
+inline ivec2 textureSize(const sampler2D& s, int l) { return textureSize(*s.t, l); }
+inline vec4 texelFetch(const sampler2D& s, const ivec2& c, int l) { return texelFetch(*s.t, c, l); }
 
 inline void imageStore(image2D& im, const ivec2& c, const vec4& v) {
     if (!im.p || c.x < 0 || c.y < 0 || c.x >= im.w || c.y >= im.h) return;

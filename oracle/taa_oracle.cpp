@@ -761,6 +761,184 @@ template <class R> void sharpen_t(const float* in, int w, int h, float factor, d
     });
 }
 
+// ---------------------------------------------------------------- FXAA
+// The FXAA pair of passes source/taa.hpp:1063-1104 dispatches, as one:
+//   prepare  shaders/antialias_fxaa_prepare.comp:19-26 - rgb kept, alpha =
+//            dot(rgb, (0.299, 0.587, 0.114)), stored in an RGBA16F image;
+//   FXAA     shaders/antialias_fxaa.comp:34-64 - FXAA 3.11 quality, preset 12
+//            (shaders/Fxaa3_11_mod.h:433-440, PC quality shader 726-1249) on
+//            the pixels whose segmentation mask has (mask & 3) == 1, the
+//            prepared texel elsewhere.
+// Sampler: bilinear, clamp to edge, exact weights, except that a coordinate
+// within 1/512 texel of a texel centre reads that texel (an 8-bit sub-texel
+// filter rounds such offsets away; without it, rounding of the UV arithmetic
+// at 4K would blend neighbours in at weights near 1e-4).
+constexpr double kFxaaSnap = 1.0 / 512.0;
+
+template <class R> struct FxaaImage {
+    const float* rgba;  // source RGBA (alpha unused), w*h texels
+    int w, h;
+    // the prepared texel: rgb and the FP16-stored luma
+    V4<R> texel(int x, int y) const {
+        x = clampi(x, 0, w - 1);
+        y = clampi(y, 0, h - 1);
+        const float* q = rgba + ((size_t)y * w + x) * 4;
+        R r = R(q[0]), g = R(q[1]), b = R(q[2]);
+        R l = r * R(0.299) + g * R(0.587) + b * R(0.114);
+        return {r, g, b, R(quantize_half(float(l)))};
+    }
+    // one coordinate of the filter footprint: the lower texel and its weight
+    static void axis(R uvc, int size, int& i0, R& f) {
+        R p = uvc * R(size) - R(0.5);
+        R c = std::floor(p + R(0.5));
+        if (std::fabs(p - c) < R(kFxaaSnap)) p = c;
+        R p0 = std::floor(p);
+        f = p - p0;
+        i0 = trunc_index(p0);
+        if (!(f == f)) f = R(0);
+    }
+    V4<R> sample(V2<R> uv) const {
+        int x0, y0;
+        R fx, fy;
+        axis(uv.x, w, x0, fx);
+        axis(uv.y, h, y0, fy);
+        int x1 = x0 + 1 < x0 ? x0 : x0 + 1, y1 = y0 + 1 < y0 ? y0 : y0 + 1;
+        V4<R> a = texel(x0, y0), b = texel(x1, y0), c = texel(x0, y1), d = texel(x1, y1);
+        R gx = R(1) - fx, gy = R(1) - fy;
+        V4<R> top{a.x * gx + b.x * fx, a.y * gx + b.y * fx, a.z * gx + b.z * fx, a.w * gx + b.w * fx};
+        V4<R> bot{c.x * gx + d.x * fx, c.y * gx + d.y * fx, c.z * gx + d.z * fx, c.w * gx + d.w * fx};
+        return {top.x * gy + bot.x * fy, top.y * gy + bot.y * fy, top.z * gy + bot.z * fy, top.w * gy + bot.w * fy};
+    }
+    R luma(V2<R> uv) const { return sample(uv).w; }
+};
+
+// FxaaPixelShader, quality PC path without gather (Fxaa3_11_mod.h:841-1249;
+// the gather variant reads the same texels at a pixel centre).
+template <class R> V4<R> fxaa_pixel(const FxaaImage<R>& t, int x, int y, V2<R> rcp, R subpix, R thr, R thr_min) {
+    // preset 12: five search steps (Fxaa3_11_mod.h:433-440)
+    static const R kStep[5] = {R(1.0), R(1.5), R(2.0), R(4.0), R(12.0)};
+    V2<R> posM{(R(x) + R(0.5)) * rcp.x, (R(y) + R(0.5)) * rcp.y};  // antialias_fxaa.comp:43
+    // the taps at the pixel centre and at whole-texel offsets from it read texels
+    V4<R> rgbyM = t.texel(x, y);
+    const R lumaM = rgbyM.w;
+    auto off = [&](int dx, int dy) { return t.texel(x + dx, y + dy).w; };
+    R lumaS = off(0, 1), lumaE = off(1, 0), lumaN = off(0, -1), lumaW = off(-1, 0);
+    // local contrast and the early exit (Fxaa3_11_mod.h:890-910)
+    R maxSM = gmax(lumaS, lumaM), minSM = gmin(lumaS, lumaM);
+    R maxESM = gmax(lumaE, maxSM), minESM = gmin(lumaE, minSM);
+    R maxWN = gmax(lumaN, lumaW), minWN = gmin(lumaN, lumaW);
+    R rangeMax = gmax(maxWN, maxESM), rangeMin = gmin(minWN, minESM);
+    R rangeMaxScaled = rangeMax * thr;
+    R range = rangeMax - rangeMin;
+    R rangeMaxClamped = gmax(thr_min, rangeMaxScaled);
+    if (range < rangeMaxClamped) return rgbyM;
+    R lumaNW = off(-1, -1), lumaSE = off(1, 1), lumaNE = off(1, -1), lumaSW = off(-1, 1);
+    // edge orientation (Fxaa3_11_mod.h:923-960)
+    R lumaNS = lumaN + lumaS, lumaWE = lumaW + lumaE;
+    R subpixRcpRange = R(1.0) / range;
+    R subpixNSWE = lumaNS + lumaWE;
+    R edgeHorz1 = (R(-2.0) * lumaM) + lumaNS;
+    R edgeVert1 = (R(-2.0) * lumaM) + lumaWE;
+    R lumaNESE = lumaNE + lumaSE, lumaNWNE = lumaNW + lumaNE;
+    R edgeHorz2 = (R(-2.0) * lumaE) + lumaNESE;
+    R edgeVert2 = (R(-2.0) * lumaN) + lumaNWNE;
+    R lumaNWSW = lumaNW + lumaSW, lumaSWSE = lumaSW + lumaSE;
+    R edgeHorz4 = (std::fabs(edgeHorz1) * R(2.0)) + std::fabs(edgeHorz2);
+    R edgeVert4 = (std::fabs(edgeVert1) * R(2.0)) + std::fabs(edgeVert2);
+    R edgeHorz3 = (R(-2.0) * lumaW) + lumaNWSW;
+    R edgeVert3 = (R(-2.0) * lumaS) + lumaSWSE;
+    R edgeHorz = std::fabs(edgeHorz3) + edgeHorz4;
+    R edgeVert = std::fabs(edgeVert3) + edgeVert4;
+    R subpixNWSWNESE = lumaNWSW + lumaNESE;
+    R lengthSign = rcp.x;
+    const bool horzSpan = edgeHorz >= edgeVert;
+    R subpixA = subpixNSWE * R(2.0) + subpixNWSWNESE;
+    if (!horzSpan) {
+        lumaN = lumaW;
+        lumaS = lumaE;
+    } else {
+        lengthSign = rcp.y;
+    }
+    R subpixB = (subpixA * R(1.0 / 12.0)) - lumaM;
+    // the steeper side and the half-texel step onto the edge (963-990)
+    R gradientN = lumaN - lumaM, gradientS = lumaS - lumaM;
+    R lumaNN = lumaN + lumaM, lumaSS = lumaS + lumaM;
+    const bool pairN = std::fabs(gradientN) >= std::fabs(gradientS);
+    R gradient = gmax(std::fabs(gradientN), std::fabs(gradientS));
+    if (pairN) lengthSign = -lengthSign;
+    R subpixC = gclamp(std::fabs(subpixB) * subpixRcpRange, R(0.0), R(1.0));
+    V2<R> posB = posM;
+    V2<R> offNP{horzSpan ? rcp.x : R(0.0), horzSpan ? R(0.0) : rcp.y};
+    if (!horzSpan) posB.x += lengthSign * R(0.5);
+    else posB.y += lengthSign * R(0.5);
+    V2<R> posN{posB.x - offNP.x * kStep[0], posB.y - offNP.y * kStep[0]};
+    V2<R> posP{posB.x + offNP.x * kStep[0], posB.y + offNP.y * kStep[0]};
+    R subpixD = (R(-2.0) * subpixC) + R(3.0);
+    R lumaEndN = t.luma(posN);
+    R subpixE = subpixC * subpixC;
+    R lumaEndP = t.luma(posP);
+    if (!pairN) lumaNN = lumaSS;
+    R gradientScaled = gradient * R(1.0) / R(4.0);
+    R lumaMM = lumaM - lumaNN * R(0.5);
+    R subpixF = subpixD * subpixE;
+    const bool lumaMLTZero = lumaMM < R(0.0);
+    // walk both ends along the edge until the luma leaves the pair's average (993-1190)
+    lumaEndN -= lumaNN * R(0.5);
+    lumaEndP -= lumaNN * R(0.5);
+    bool doneN = std::fabs(lumaEndN) >= gradientScaled;
+    bool doneP = std::fabs(lumaEndP) >= gradientScaled;
+    if (!doneN) posN = {posN.x - offNP.x * kStep[1], posN.y - offNP.y * kStep[1]};
+    bool doneNP = (!doneN) || (!doneP);
+    if (!doneP) posP = {posP.x + offNP.x * kStep[1], posP.y + offNP.y * kStep[1]};
+    for (int i = 2; i < 5 && doneNP; ++i) {
+        if (!doneN) lumaEndN = t.luma(posN);
+        if (!doneP) lumaEndP = t.luma(posP);
+        if (!doneN) lumaEndN = lumaEndN - lumaNN * R(0.5);
+        if (!doneP) lumaEndP = lumaEndP - lumaNN * R(0.5);
+        doneN = std::fabs(lumaEndN) >= gradientScaled;
+        doneP = std::fabs(lumaEndP) >= gradientScaled;
+        if (!doneN) posN = {posN.x - offNP.x * kStep[i], posN.y - offNP.y * kStep[i]};
+        doneNP = (!doneN) || (!doneP);
+        if (!doneP) posP = {posP.x + offNP.x * kStep[i], posP.y + offNP.y * kStep[i]};
+    }
+    // the offset across the edge: span position or sub-pixel blend, the larger (1192-1248)
+    R dstN = horzSpan ? posM.x - posN.x : posM.y - posN.y;
+    R dstP = horzSpan ? posP.x - posM.x : posP.y - posM.y;
+    const bool goodSpanN = (lumaEndN < R(0.0)) != lumaMLTZero;
+    R spanLength = dstP + dstN;
+    const bool goodSpanP = (lumaEndP < R(0.0)) != lumaMLTZero;
+    R spanLengthRcp = R(1.0) / spanLength;
+    const bool directionN = dstN < dstP;
+    R dst = gmin(dstN, dstP);
+    const bool goodSpan = directionN ? goodSpanN : goodSpanP;
+    R subpixG = subpixF * subpixF;
+    R pixelOffset = (dst * (-spanLengthRcp)) + R(0.5);
+    R subpixH = subpixG * subpix;
+    R pixelOffsetGood = goodSpan ? pixelOffset : R(0.0);
+    R pixelOffsetSubpix = gmax(pixelOffsetGood, subpixH);
+    if (!horzSpan) posM.x += pixelOffsetSubpix * lengthSign;
+    else posM.y += pixelOffsetSubpix * lengthSign;
+    V4<R> c = t.sample(posM);
+    return {c.x, c.y, c.z, lumaM};
+}
+
+template <class R> void fxaa_t(const float* in, const uint32_t* segmask, int w, int h, const float rcp[2],
+                               float subpix, float thr, float thr_min, double* out, int nthreads) {
+    const FxaaImage<R> t{in, w, h};
+    parallel_rows(h, nthreads, [&](int y) {
+        for (int x = 0; x < w; ++x) {
+            bool marked = !segmask || (segmask[(size_t)y * w + x] & 3u) == 1u;  // antialias_fxaa.comp:39-40
+            V4<R> c = marked ? fxaa_pixel<R>(t, x, y, V2<R>{R(rcp[0]), R(rcp[1])}, R(subpix), R(thr), R(thr_min))
+                             : t.texel(x, y);
+            double* o = out + ((size_t)y * w + x) * 4;
+            o[0] = double(c.x);
+            o[1] = double(c.y);
+            o[2] = double(c.z);
+            o[3] = double(c.w);
+        }
+    });
+}
+
 }  // namespace
 
 int resolve(int precision, const taa_uniforms_t& u, const ResolveInputs& in, const ResolveOutputs& out,
@@ -790,6 +968,16 @@ int sharpen(int precision, const float* in, int w, int h, float factor, double* 
         sharpen_t<double>(in, w, h, factor, out, nthreads);
     else
         sharpen_t<float>(in, w, h, factor, out, nthreads);
+    return 0;
+}
+
+int fxaa(int precision, const float* in, const uint32_t* segmask, int w, int h, const float rcp_frame[2],
+         float subpix, float edge_threshold, float edge_threshold_min, double* out, int nthreads) {
+    if (!in || !out || w <= 0 || h <= 0) return -1;
+    if (precision == 64)
+        fxaa_t<double>(in, segmask, w, h, rcp_frame, subpix, edge_threshold, edge_threshold_min, out, nthreads);
+    else
+        fxaa_t<float>(in, segmask, w, h, rcp_frame, subpix, edge_threshold, edge_threshold_min, out, nthreads);
     return 0;
 }
 

@@ -80,6 +80,14 @@ int cas(int precision, const float* in, int w, int h, uint32_t peak_bits, double
 // shaders/sharpen.comp.
 int sharpen(int precision, const float* in, int w, int h, float factor, double* out, int nthreads);
 
+// The FXAA pass of the ray-trace-assist path (source/taa.hpp:1063-1104):
+// shaders/antialias_fxaa_prepare.comp and antialias_fxaa.comp (FXAA 3.11
+// quality preset 12) as one, on an RGBA image (alpha unused) and a segmentation
+// mask (NULL: every pixel is marked).  Output: rgb and the FP16-stored luma.
+// rcp_frame = 1 / image size in FP32 (source/taa.hpp:953).  precision 32 or 64.
+int fxaa(int precision, const float* in, const uint32_t* segmask, int w, int h, const float rcp_frame[2],
+         float subpix, float edge_threshold, float edge_threshold_min, double* out, int nthreads);
+
 // CasSetup, restated (ffx_cas.h:375-394).
 void cas_setup(float sharpness, float in_w, float in_h, float out_w, float out_h,
                uint32_t const0[4], uint32_t const1[4]);

@@ -35,12 +35,15 @@ UNITS = {
     "resolve_half.cu": [],
     "batch_tiled.cu": ["-fmad=false"],
     "learned.cu": ["-fmad=false"],
+    "fxaa.cu": ["-fmad=false"],
     "synth.cu": [],
     "static_scratch.cu": [],
     "device_state.cu": [],
     "capi.cpp": [],
     "batch_api.cpp": [],
     "learned_api.cpp": [],
+    "post_api.cpp": [],
+    "settings.cpp": [],
 }
 
 

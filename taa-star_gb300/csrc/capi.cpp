@@ -59,7 +59,7 @@ size_t motion_texel(uint32_t fmt) { return fmt == TAA_MOTION_RGBA16F ? 8 : 4; }
 
 // Validates one binding: alignment, pitch and the byte range it spans.
 int check_image(const char* name, const void* p, size_t pitch, int w, int h, size_t texel, bool required,
-                const char** lo = nullptr, const char** hi = nullptr) {
+                const char** lo, const char** hi) {
     if (!p) {
         if (required) return fail(TAA_E_INVAL, "%s: required binding is NULL", name);
         return ok();
@@ -229,6 +229,27 @@ static float halton_host(int i, int b) {
     return r;
 }
 
+namespace {
+// The frame's entry of a jitter table and the debugging knobs (source/taa.hpp:219-232).
+void pick_jitter(const float* tx, const float* ty, int n, uint64_t frame_id, const taa_jitter_opts_t* opts,
+                 float out[2]) {
+    taa_jitter_opts_t o = {-1, 1, 0.f, 1.f};
+    if (opts) o = *opts;
+    if (o.slow_motion > 1) frame_id /= (uint64_t)o.slow_motion;
+    if (o.fixed_index >= 0) frame_id = (uint64_t)o.fixed_index;
+    float x = tx[frame_id % (uint64_t)n], y = ty[frame_id % (uint64_t)n];
+    if (o.rotate_degrees != 0.f) {
+        float r = o.rotate_degrees * (float)(3.14159265358979323846 / 180.0);
+        float s = std::sin(r), c = std::cos(r);
+        float nx = x * c - y * s, ny = x * s + y * c;
+        x = nx;
+        y = ny;
+    }
+    out[0] = x * o.extra_scale;
+    out[1] = y * o.extra_scale;
+}
+}  // namespace
+
 // source/taa.hpp:150-233.  The reference fills its tables once from the
 // first resolution it sees (function-local statics); here every call uses
 // the resolution it is given.
@@ -262,21 +283,29 @@ int taa_get_jitter_offset(int32_t dist, uint64_t frame_id, int32_t w, int32_t h,
                 ty[n] = sy * ((float)(2 * j - 3) * e);
             }
     }
-    taa_jitter_opts_t o = {-1, 1, 0.f, 1.f};
-    if (opts) o = *opts;
-    if (o.slow_motion > 1) frame_id /= (uint64_t)o.slow_motion;
-    if (o.fixed_index >= 0) frame_id = (uint64_t)o.fixed_index;
-    float x = tx[frame_id % (uint64_t)n], y = ty[frame_id % (uint64_t)n];
-    if (o.rotate_degrees != 0.f) {
-        float r = o.rotate_degrees * (float)(3.14159265358979323846 / 180.0);
-        float s = std::sin(r), c = std::cos(r);
-        float nx = x * c - y * s, ny = x * s + y * c;
-        x = nx;
-        y = ny;
-    }
-    out[0] = x * o.extra_scale;
-    out[1] = y * o.extra_scale;
+    pick_jitter(tx, ty, n, frame_id, opts, out);
     if (out_n) *out_n = n;
+    return ok();
+}
+
+// Sample distribution 5 of source/taa.hpp:207-211: the debug sample offsets,
+// in pixels, scaled to NDC.
+int taa_get_jitter_offset_custom(const float (*offsets_px)[2], int32_t count, uint64_t frame_id, int32_t w, int32_t h,
+                                 const taa_jitter_opts_t* opts, float out[2]) {
+    if (!out || !offsets_px) return fail(TAA_E_INVAL, "taa_get_jitter_offset_custom: NULL argument");
+    if (w <= 0 || h <= 0) return fail(TAA_E_INVAL, "taa_get_jitter_offset_custom: bad resolution %dx%d", w, h);
+    if (count < 1 || count > TAA_SETTINGS_MAX_SAMPLE_OFFSETS)
+        return fail(TAA_E_INVAL, "taa_get_jitter_offset_custom: count %d not in 1..%d", count,
+                    TAA_SETTINGS_MAX_SAMPLE_OFFSETS);
+    const float sx = 2.0f / (float)w, sy = 2.0f / (float)h;
+    float tx[TAA_SETTINGS_MAX_SAMPLE_OFFSETS], ty[TAA_SETTINGS_MAX_SAMPLE_OFFSETS];
+    for (int i = 0; i < count; ++i) {
+        if (!finite(offsets_px[i][0]) || !finite(offsets_px[i][1]))
+            return fail(TAA_E_INVAL, "taa_get_jitter_offset_custom: offset %d not finite", i);
+        tx[i] = offsets_px[i][0] * sx;
+        ty[i] = offsets_px[i][1] * sy;
+    }
+    pick_jitter(tx, ty, count, frame_id, opts, out);
     return ok();
 }
 

@@ -30,6 +30,11 @@ namespace taa_host {
 int fail(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
 int cuda_fail(cudaError_t e, const char* what);
 bool finite(float v);
+int ok();
+// Validates one image binding: alignment to the texel, pitch, and (when lo/hi
+// are given) the byte range [lo, hi) it spans.  NULL is an error if required.
+int check_image(const char* name, const void* p, size_t pitch, int w, int h, size_t texel, bool required,
+                const char** lo = nullptr, const char** hi = nullptr);
 // Validation of a context description and of a uniform block.
 int check_desc(const taa_desc_t& d, const char* who);
 int check_uniforms(const taa_uniforms_t& u, const char* who);

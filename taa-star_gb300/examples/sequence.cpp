@@ -2,13 +2,17 @@
 // over a short synthetic sequence, the way the reference's renderer drives
 // its taa component each frame (source/main.cpp:4122-4123, taa.hpp:894, 974).
 //
-//   sequence <width> <height> <frames>
+//   sequence <width> <height> <frames> [fxaa]
 // prints one line per frame with the resolve time and the result's mean.
+// With "fxaa" the ray-trace-assist path runs: the resolve writes the
+// segmentation mask, FXAA antialiases the pixels it marks, then the sharpener
+// (source/taa.hpp:1031-1139); the line also counts the marked pixels.
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
 
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 #include <vector>
 
 #include "../../include/taa_synth.h"
@@ -17,6 +21,7 @@
 int main(int argc, char** argv) {
     const int W = argc > 1 ? atoi(argv[1]) : 320, H = argc > 2 ? atoi(argv[2]) : 180;
     const int N = argc > 3 ? atoi(argv[3]) : 8;
+    const bool fxaa = argc > 4 && std::string(argv[4]) == "fxaa";
     constexpr size_t CF = 3;
     taa_synth_scene_t scene;
     if (taa_synth_default_scene(&scene, W, H, 7) != TAA_OK) return 1;
@@ -36,12 +41,17 @@ int main(int argc, char** argv) {
     p.mColorClampingOrClipping = 2;
     p.mAlpha = 0.1f;
     p.mUseVelocityVectors = 2;
+    if (fxaa) {
+        p.mRayTraceAugment = 1;
+        p.mRayTraceAugmentFlags = TAA_RTFLAG_OUT | TAA_RTFLAG_DIS | TAA_RTFLAG_DPT | TAA_RTFLAG_LUM | TAA_RTFLAG_FXA;
+    }
     taa.mSampleDistribution = 2;
     taa.mSharpener = TAA_SHARPEN_CAS;
     taa.set_source_image_views(W, H, W, H, col, dep, mot, TAA_MOTION_RGBA16F);
     cudaStream_t s;
     cudaStreamCreate(&s);
     std::vector<__half> host((size_t)W * H * 4);
+    std::vector<uint32_t> mask((size_t)W * H);
     for (int f = 0; f < N; ++f) {
         const size_t i = f % CF;
         taa_synth_frame_t out{col[i].ptr, col[i].pitch, dep[i].ptr, dep[i].pitch, mot[i].ptr, mot[i].pitch, 4,
@@ -64,7 +74,13 @@ int main(int argc, char** argv) {
         cudaStreamSynchronize(s);
         double sum = 0;
         for (size_t k = 0; k < host.size(); k += 4) sum += __half2float(host[k]);
-        printf("frame %d resolve %.3f ms mean_r %.5f\n", f, taa.duration(), sum / (W * H));
+        long marked = 0;
+        if (fxaa && f > 0) {
+            const taa_gb300::Image& m = taa.segmentation_mask(f);
+            cudaMemcpy2D(mask.data(), (size_t)W * 4, m.ptr, m.pitch, (size_t)W * 4, H, cudaMemcpyDeviceToHost);
+            for (uint32_t v : mask) marked += (v & 3u) == 1u;
+        }
+        printf("frame %d resolve %.3f ms marked %ld mean_r %.5f\n", f, taa.duration(), marked, sum / (W * H));
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {

@@ -6,8 +6,11 @@
 // chain in render().  This header keeps that interface - the same method
 // names, parameter block and per-frame bookkeeping - for a C++ application
 // that renders with CUDA: images are device buffers, "recording" is enqueuing
-// on a CUDA stream, and the dispatch is taa_resolve().  GUI, .ini and
-// RenderDoc parts of the reference class are not carried over.
+// on a CUDA stream, and the dispatches are taa_resolve(), taa_fxaa() and
+// taa_sharpen().  The settings file (writeSettingsToIni/readSettingsFromIni)
+// is text in and out; the GUI, the post-process overlay and RenderDoc parts
+// of the reference class are not carried over (their settings are kept so a
+// settings file survives a read and a write).
 //
 // Usage, once per frame (as wookiee drives the reference, source/main.cpp:4122-4123):
 //   P_jit = taa.get_jittered_projection_matrix(P, frame);   // render the G-buffer with P_jit
@@ -22,6 +25,7 @@
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "../include/taa_gb300.h"
 
@@ -62,8 +66,18 @@ template <size_t CF> class taa {
     int mSplitX = 0;
     uint32_t mSharpener = TAA_SHARPEN_OFF;  // 0 off, 1 simple, 2 CAS
     float mSharpenFactor = 0.5f;
-    taa_jitter_opts_t mJitterDebug{-1, 1, 0.f, 1.f};
+    taa_jitter_opts_t mJitterDebug{-1, 1, 0.f, 1.f};  // mFixedJitterIndex, mJitterSlowMotion, ...
+    std::vector<std::array<float, 2>> mDebugSampleOffsets{{0.f, 0.f}};  // sample distribution 5, in pixels
     uint32_t mForm = TAA_FORM_AUTO;
+    // push_constants_for_fxaa (source/taa.hpp:93-98; the reciprocal frame size is derived per call)
+    taa_fxaa_params_t mFxaaPushConstants{0.75f, 0.116f, 0.0833f};
+    // post-processing settings (source/taa.hpp:101-111, 1359): stored and written, the overlay is not built
+    bool mPostProcessEnabled = true;
+    struct PostProcessSettings {
+        uint32_t zoom = 0, showZoomBox = 1;
+        int32_t zoomSrcLTWH[4] = {960 - 10, 540 - 10, 20, 20};
+        int32_t zoomDstLTWH[4] = {1920 - 200 - 10, 10, 200, 200};
+    } mPostProcessPushConstants;
 
     taa() {
         check(taa_default_parameters(&mParameters[0]));
@@ -91,10 +105,14 @@ template <size_t CF> class taa {
             alloc(mResult[i], 8);
             alloc(mHistory[i], 16);
             alloc(mSharpened[i], 8);
+            alloc(mTemp[i], 8);
+            alloc(mSegMask[i], 4);
         }
         taa_desc_t d{sizeof(taa_desc_t), sourceWidth, sourceHeight, targetWidth, targetHeight, TAA_HISTORY_RGBA32F,
                      motionFormat, mForm, mSharpener, mSharpenFactor, 0};
         check(taa_create(&d, &mCtx));
+        mCtxSharpener = mSharpener;
+        mCtxSharpenFactor = mSharpenFactor;
         mSplitX = targetWidth / 2;  // source/taa.hpp:354
         if (cudaEventCreate(&mT0) != cudaSuccess || cudaEventCreate(&mT1) != cudaSuccess)
             throw std::runtime_error("taa: cudaEventCreate failed");
@@ -103,9 +121,59 @@ template <size_t CF> class taa {
     // source/taa.hpp:150-233 (jitter in NDC; sample distributions 0..4)
     std::array<float, 2> get_jitter_offset_for_frame(uint64_t frameId, int32_t* numSamples = nullptr) const {
         std::array<float, 2> j{0.f, 0.f};
+        if (mSampleDistribution == 5) {  // the debug sample offsets (source/taa.hpp:207-211)
+            check(taa_get_jitter_offset_custom(reinterpret_cast<const float(*)[2]>(mDebugSampleOffsets.data()),
+                                               (int32_t)mDebugSampleOffsets.size(), frameId, mIn[0], mIn[1],
+                                               &mJitterDebug, j.data()));
+            if (numSamples) *numSamples = (int32_t)mDebugSampleOffsets.size();
+            return j;
+        }
         check(taa_get_jitter_offset(mSampleDistribution, frameId, mIn[0], mIn[1], &mJitterDebug, j.data(),
                                     numSamples));
         return j;
+    }
+
+    // source/taa.hpp:1344: the ray-trace-assist path runs for either active parameter set
+    bool needRayTraceAssist() const {
+        return mParameters[0].mRayTraceAugment || (mSplitScreen && mParameters[1].mRayTraceAugment);
+    }
+
+    // source/taa.hpp:1198-1265: the settings as .ini text (sections TAA_Param_0/1,
+    // TAA_Primary, TAA_Postprocess), written as the reference writes them.
+    std::string writeSettingsToIni() const {
+        taa_settings_t st = settings();
+        size_t n = 0;
+        check(taa_settings_write_ini(&st, nullptr, 0, &n));
+        std::string text(n + 1, '\0');
+        check(taa_settings_write_ini(&st, &text[0], text.size(), &n));
+        text.resize(n);
+        return text;
+    }
+
+    // source/taa.hpp:1267-1339: read the keys present in .ini text (a whole
+    // settings file of the reference, or writeSettingsToIni's output).
+    void readSettingsFromIni(const std::string& text) {
+        taa_settings_t st = settings();
+        check(taa_settings_read_ini(&st, text.data(), text.size()));
+        mParameters[0] = st.param[0];
+        mParameters[1] = st.param[1];
+        mTaaEnabled = st.mTaaEnabled != 0;
+        mSampleDistribution = st.mSampleDistribution;
+        mSharpener = (uint32_t)st.mSharpener;
+        mSharpenFactor = st.mSharpenFactor;
+        mSplitScreen = st.mSplitScreen != 0;
+        mSplitX = st.mSplitX;
+        mJitterDebug = taa_jitter_opts_t{st.mFixedJitterIndex, st.mJitterSlowMotion, st.mJitterRotateDegrees,
+                                         st.mJitterExtraScale};
+        mResetHistoryOnChange = st.mResetHistoryOnChange != 0;
+        mDebugSampleOffsets.assign((size_t)st.mDebugSampleOffsetsCount, {0.f, 0.f});
+        for (int32_t i = 0; i < st.mDebugSampleOffsetsCount; ++i)
+            mDebugSampleOffsets[i] = {st.mDebugSampleOffsets[i][0], st.mDebugSampleOffsets[i][1]};
+        mPostProcessEnabled = st.mPostProcessEnabled != 0;
+        mPostProcessPushConstants.zoom = st.zoom;
+        mPostProcessPushConstants.showZoomBox = st.showZoomBox;
+        std::memcpy(mPostProcessPushConstants.zoomSrcLTWH, st.zoomSrcLTWH, sizeof st.zoomSrcLTWH);
+        std::memcpy(mPostProcessPushConstants.zoomDstLTWH, st.zoomDstLTWH, sizeof st.zoomDstLTWH);
     }
 
     // source/taa.hpp:243-253
@@ -159,9 +227,15 @@ template <size_t CF> class taa {
         mUniforms.mResetHistory = mResetHistory;
         mUniforms.mCamNearPlane = nearPlane;
         mUniforms.mCamFarPlane = farPlane;
-        if (mSharpener != mCtxSharpener || mSharpenFactor != mCtxSharpenFactor) {
-            check(taa_set_sharpener(mCtx, mSharpener, mSharpenFactor));
-            mCtxSharpener = mSharpener;
+        // with FXAA on the segmentation mask the sharpener reads the FXAA output
+        // (source/taa.hpp:1111-1139 after 1063-1104): it runs as its own pass then
+        const uint32_t FXA = TAA_RTFLAG_FXA;
+        mFxaa = needRayTraceAssist() &&
+                ((mParameters[0].mRayTraceAugmentFlags & FXA) || (mSplitScreen && (mParameters[1].mRayTraceAugmentFlags & FXA)));
+        const uint32_t fused = mFxaa ? TAA_SHARPEN_OFF : mSharpener;
+        if (fused != mCtxSharpener || mSharpenFactor != mCtxSharpenFactor) {
+            check(taa_set_sharpener(mCtx, fused, mSharpenFactor));
+            mCtxSharpener = fused;
             mCtxSharpenFactor = mSharpenFactor;
         }
         mResetHistory = false;
@@ -171,7 +245,9 @@ template <size_t CF> class taa {
     }
 
     // source/taa.hpp:974-1192: the matrices of this and the previous frame in
-    // FP64, then the resolve (and the fused sharpen) of frame `frameId`.
+    // FP64, then the resolve (and the fused sharpen) of frame `frameId`; on the
+    // ray-trace-assist path the resolve also writes the segmentation mask, and
+    // with its FXAA flag the FXAA pass and then the sharpener follow.
     // The very first frame has no history: the result is the source colour.
     void render(uint64_t frameId, cudaStream_t stream) {
         const size_t cur = frameId % CF, prev = (frameId + CF - 1) % CF;
@@ -201,13 +277,32 @@ template <size_t CF> class taa {
         io.history_out_pitch = mHistory[cur].pitch;
         io.result = mResult[cur].ptr;
         io.result_pitch = mResult[cur].pitch;
-        if (mSharpener != TAA_SHARPEN_OFF) {
+        if (needRayTraceAssist()) {
+            io.segmask = mSegMask[cur].ptr;
+            io.segmask_pitch = mSegMask[cur].pitch;
+            if (mHaveSegMask) {  // binding 12: the previous frame's mask
+                io.prev_segmask = mSegMask[prev].ptr;
+                io.prev_segmask_pitch = mSegMask[prev].pitch;
+            }
+        }
+        if (mCtxSharpener != TAA_SHARPEN_OFF) {
             io.sharpened = mSharpened[cur].ptr;
             io.sharpened_pitch = mSharpened[cur].pitch;
         }
-        mShowSharpened[cur] = mSharpener != TAA_SHARPEN_OFF;
+        mShown[cur] = mSharpener != TAA_SHARPEN_OFF ? Shown::Sharpened : Shown::Result;
         cudaEventRecord(mT0, stream);
         check(taa_resolve(mCtx, stream, &io));
+        if (mFxaa) {
+            check(taa_fxaa(stream, mResult[cur].ptr, mResult[cur].pitch, mSegMask[cur].ptr, mSegMask[cur].pitch,
+                           mTemp[cur].ptr, mTemp[cur].pitch, mOut[0], mOut[1], &mFxaaPushConstants));
+            mShown[cur] = Shown::Temp;
+            if (mSharpener != TAA_SHARPEN_OFF) {
+                check(taa_sharpen(stream, mSharpener, mSharpenFactor, mTemp[cur].ptr, mTemp[cur].pitch,
+                                  mSharpened[cur].ptr, mSharpened[cur].pitch, mOut[0], mOut[1]));
+                mShown[cur] = Shown::Sharpened;
+            }
+        }
+        mHaveSegMask = needRayTraceAssist();
         cudaEventRecord(mT1, stream);
         mTimed = true;
     }
@@ -221,11 +316,16 @@ template <size_t CF> class taa {
         return ms;
     }
 
-    // the image to show for a frame: the sharpened one with a sharpener (taa.hpp:1137)
+    // the image to show for a frame: the last pass's output (pLastProducedImageView_t, taa.hpp:1029-1137)
     const Image& result(uint64_t frameId) const {
-        return mShowSharpened[frameId % CF] ? mSharpened[frameId % CF] : mResult[frameId % CF];
+        switch (mShown[frameId % CF]) {
+            case Shown::Sharpened: return mSharpened[frameId % CF];
+            case Shown::Temp: return mTemp[frameId % CF];
+            default: return mResult[frameId % CF];
+        }
     }
     const Image& history(uint64_t frameId) const { return mHistory[frameId % CF]; }
+    const Image& segmentation_mask(uint64_t frameId) const { return mSegMask[frameId % CF]; }  // taa.hpp:1341
     taa_ctx* context() const { return mCtx; }
 
    private:
@@ -233,8 +333,42 @@ template <size_t CF> class taa {
         if (cudaMallocPitch(&im.ptr, &im.pitch, (size_t)mOut[0] * texel, (size_t)mOut[1]) != cudaSuccess)
             throw std::runtime_error("taa: cudaMallocPitch failed");
     }
+    enum class Shown { Result, Sharpened, Temp };
+
+    // the members the settings file holds
+    taa_settings_t settings() const {
+        taa_settings_t st;
+        check(taa_settings_default(&st));
+        st.param[0] = mParameters[0];
+        st.param[1] = mParameters[1];
+        st.mTaaEnabled = mTaaEnabled;
+        st.mSampleDistribution = mSampleDistribution;
+        st.mSharpener = (int32_t)mSharpener;
+        st.mSharpenFactor = mSharpenFactor;
+        st.mSplitScreen = mSplitScreen;
+        st.mSplitX = mSplitX;
+        st.mFixedJitterIndex = mJitterDebug.fixed_index;
+        st.mJitterExtraScale = mJitterDebug.extra_scale;
+        st.mJitterSlowMotion = mJitterDebug.slow_motion;
+        st.mJitterRotateDegrees = mJitterDebug.rotate_degrees;
+        st.mResetHistoryOnChange = mResetHistoryOnChange;
+        if (mDebugSampleOffsets.empty() || mDebugSampleOffsets.size() > TAA_SETTINGS_MAX_SAMPLE_OFFSETS)
+            throw std::runtime_error("taa: 1..TAA_SETTINGS_MAX_SAMPLE_OFFSETS debug sample offsets");
+        st.mDebugSampleOffsetsCount = (int32_t)mDebugSampleOffsets.size();
+        for (size_t i = 0; i < mDebugSampleOffsets.size(); ++i) {
+            st.mDebugSampleOffsets[i][0] = mDebugSampleOffsets[i][0];
+            st.mDebugSampleOffsets[i][1] = mDebugSampleOffsets[i][1];
+        }
+        st.mPostProcessEnabled = mPostProcessEnabled;
+        st.zoom = mPostProcessPushConstants.zoom;
+        st.showZoomBox = mPostProcessPushConstants.showZoomBox;
+        std::memcpy(st.zoomSrcLTWH, mPostProcessPushConstants.zoomSrcLTWH, sizeof st.zoomSrcLTWH);
+        std::memcpy(st.zoomDstLTWH, mPostProcessPushConstants.zoomDstLTWH, sizeof st.zoomDstLTWH);
+        return st;
+    }
+
     void copy_source(size_t cur, cudaStream_t s) {
-        mShowSharpened[cur] = false;  // nothing was sharpened for this frame
+        mShown[cur] = Shown::Result;  // nothing was sharpened for this frame
         if (mUpsampling) return;  // the reference blits with scaling; a headless caller reads the source itself
         cudaMemcpy2DAsync(mResult[cur].ptr, mResult[cur].pitch, mSrcColor[cur].ptr, mSrcColor[cur].pitch,
                           (size_t)mOut[0] * 8, (size_t)mOut[1], cudaMemcpyDeviceToDevice, s);
@@ -246,7 +380,7 @@ template <size_t CF> class taa {
         if (mCtx) taa_destroy(mCtx);
         mCtx = nullptr;
         for (size_t i = 0; i < CF; ++i)
-            for (Image* im : {&mResult[i], &mHistory[i], &mSharpened[i]}) {
+            for (Image* im : {&mResult[i], &mHistory[i], &mSharpened[i], &mTemp[i], &mSegMask[i]}) {
                 if (im->ptr) cudaFree(im->ptr);
                 im->ptr = nullptr;
             }
@@ -259,14 +393,16 @@ template <size_t CF> class taa {
     int mIn[2] = {0, 0}, mOut[2] = {0, 0};
     bool mUpsampling = false;
     std::array<Image, CF> mSrcColor{}, mSrcDepth{}, mSrcVelocity{};
-    std::array<Image, CF> mResult{}, mHistory{}, mSharpened{};
+    std::array<Image, CF> mResult{}, mHistory{}, mSharpened{}, mTemp{}, mSegMask{};
     std::array<Mat4, CF> mProj{}, mView{};
     taa_uniforms_t mUniforms{};
     Parameters mOldParams[2]{};
     bool mOldParamsValid = false;
     bool mHaveHistory = false;
     bool mFirstResolve = true;
-    std::array<bool, CF> mShowSharpened{};
+    std::array<Shown, CF> mShown{};
+    bool mFxaa = false;
+    bool mHaveSegMask = false;
     uint32_t mCtxSharpener = TAA_SHARPEN_OFF;
     float mCtxSharpenFactor = 0.5f;
     cudaEvent_t mT0 = nullptr, mT1 = nullptr;

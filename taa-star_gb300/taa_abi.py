@@ -103,6 +103,24 @@ class MlpRecord(C.Structure):
                 ("gamma", C.c_float), ("alpha_fixed", C.c_float), ("flags", C.c_uint32), ("pad", C.c_float * 2)]
 
 
+class FxaaParams(C.Structure):
+    _fields_ = [("subpix", C.c_float), ("edge_threshold", C.c_float), ("edge_threshold_min", C.c_float)]
+
+
+SETTINGS_MAX_SAMPLE_OFFSETS = 64
+
+
+class Settings(C.Structure):
+    _fields_ = [("param", Parameters * 2), ("mTaaEnabled", C.c_uint32), ("mSampleDistribution", C.c_int32),
+                ("mSharpener", C.c_int32), ("mSharpenFactor", C.c_float), ("mSplitScreen", C.c_uint32),
+                ("mSplitX", C.c_int32), ("mFixedJitterIndex", C.c_int32), ("mJitterExtraScale", C.c_float),
+                ("mJitterSlowMotion", C.c_int32), ("mJitterRotateDegrees", C.c_float),
+                ("mResetHistoryOnChange", C.c_uint32), ("mDebugSampleOffsetsCount", C.c_int32),
+                ("mDebugSampleOffsets", (C.c_float * 2) * SETTINGS_MAX_SAMPLE_OFFSETS),
+                ("mPostProcessEnabled", C.c_uint32), ("zoom", C.c_uint32), ("showZoomBox", C.c_uint32),
+                ("zoomSrcLTWH", C.c_int32 * 4), ("zoomDstLTWH", C.c_int32 * 4)]
+
+
 TAA_SCHEDULE_VIEW_ORDER, TAA_SCHEDULE_LARGEST_FIRST, TAA_SCHEDULE_INTERLEAVED = 0, 1, 2
 BATCH_SLOTS = 4
 TAA_BATCH_CTA_PER_TILE = -1
@@ -131,6 +149,8 @@ assert C.sizeof(Parameters) == 176 and C.sizeof(Uniforms) == 544
 
 # Every symbol include/taa_gb300.h and include/taa_synth.h declare.
 EXPORTS = ["taa_version", "taa_last_error", "taa_default_parameters", "taa_get_jitter_offset",
+           "taa_get_jitter_offset_custom", "taa_fxaa_default_params", "taa_fxaa", "taa_sharpen",
+           "taa_settings_default", "taa_settings_write_ini", "taa_settings_read_ini",
            "taa_jittered_projection", "taa_compose_matrices", "taa_cas_setup", "taa_create", "taa_destroy",
            "taa_set_uniforms", "taa_set_sharpener", "taa_selected_form", "taa_resolve",
            "taa_resolve_static_scratch", "taa_device_status", "taa_batch_create", "taa_batch_destroy",
@@ -160,6 +180,16 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
         "taa_default_parameters": (C.c_int, [P(Parameters)]),
         "taa_get_jitter_offset": (C.c_int, [C.c_int32, C.c_uint64, C.c_int32, C.c_int32, P(JitterOpts),
                                             P(C.c_float), P(C.c_int32)]),
+        "taa_get_jitter_offset_custom": (C.c_int, [C.c_void_p, C.c_int32, C.c_uint64, C.c_int32, C.c_int32,
+                                                   P(JitterOpts), P(C.c_float)]),
+        "taa_fxaa_default_params": (C.c_int, [P(FxaaParams)]),
+        "taa_fxaa": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t,
+                               C.c_int32, C.c_int32, P(FxaaParams)]),
+        "taa_sharpen": (C.c_int, [C.c_void_p, C.c_uint32, C.c_float, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t,
+                                  C.c_int32, C.c_int32]),
+        "taa_settings_default": (C.c_int, [P(Settings)]),
+        "taa_settings_write_ini": (C.c_int, [P(Settings), C.c_char_p, C.c_size_t, P(C.c_size_t)]),
+        "taa_settings_read_ini": (C.c_int, [P(Settings), C.c_char_p, C.c_size_t]),
         "taa_jittered_projection": (C.c_int, [P(C.c_float), P(C.c_float), P(C.c_float)]),
         "taa_compose_matrices": (C.c_int, [P(C.c_double)] * 4 + [P(C.c_float)] * 2),
         "taa_cas_setup": (C.c_int, [C.c_float] * 5 + [P(C.c_uint32)] * 2),
@@ -229,6 +259,66 @@ def default_parameters() -> Parameters:
     p = Parameters()
     check(load().taa_default_parameters(C.byref(p)))
     return p
+
+
+def fxaa_default_params() -> FxaaParams:
+    p = FxaaParams()
+    check(load().taa_fxaa_default_params(C.byref(p)))
+    return p
+
+
+def fxaa(input, output, segmask=None, params: FxaaParams | None = None, stream: int = 0):
+    """taa_fxaa on (H, W, 4) FP16 tensors; segmask an (H, W) int32/uint32 tensor or None."""
+    h, w = int(input.shape[0]), int(input.shape[1])
+    ip, ipitch = tensor_ptr_pitch(input)
+    op, opitch = tensor_ptr_pitch(output)
+    sp, spitch = tensor_ptr_pitch(segmask) if segmask is not None else (None, 0)
+    check(load().taa_fxaa(C.c_void_p(stream), C.c_void_p(ip), ipitch, C.c_void_p(sp), spitch, C.c_void_p(op),
+                          opitch, w, h, C.byref(params) if params is not None else None))
+
+
+def sharpen(input, output, sharpener: int, factor: float, stream: int = 0):
+    """taa_sharpen on (H, W, 4) FP16 tensors."""
+    h, w = int(input.shape[0]), int(input.shape[1])
+    ip, ipitch = tensor_ptr_pitch(input)
+    op, opitch = tensor_ptr_pitch(output)
+    check(load().taa_sharpen(C.c_void_p(stream), sharpener, factor, C.c_void_p(ip), ipitch, C.c_void_p(op), opitch,
+                             w, h))
+
+
+def jitter_offset_custom(offsets_px, frame: int, w: int, h: int, opts: JitterOpts | None = None):
+    """taa_get_jitter_offset_custom: sample distribution 5 over the given pixel offsets."""
+    n = len(offsets_px)
+    arr = ((C.c_float * 2) * max(n, 1))(*[(C.c_float * 2)(float(x), float(y)) for x, y in offsets_px])
+    out = (C.c_float * 2)()
+    check(load().taa_get_jitter_offset_custom(C.cast(arr, C.c_void_p), n, frame, w, h,
+                                               C.byref(opts) if opts is not None else None, out))
+    return out[0], out[1]
+
+
+def settings_default() -> Settings:
+    s = Settings()
+    check(load().taa_settings_default(C.byref(s)))
+    return s
+
+
+def settings_to_ini(s: Settings) -> str:
+    """The .ini text of the settings, as the reference writes it."""
+    lib = load()
+    n = C.c_size_t()
+    check(lib.taa_settings_write_ini(C.byref(s), None, 0, C.byref(n)))
+    buf = C.create_string_buffer(n.value + 1)
+    check(lib.taa_settings_write_ini(C.byref(s), buf, n.value + 1, C.byref(n)))
+    return buf.value.decode()
+
+
+def settings_from_ini(text: str, base: Settings | None = None) -> Settings:
+    """Settings read from .ini text over `base` (the defaults when None)."""
+    s = Settings()
+    C.memmove(C.addressof(s), C.addressof(base if base is not None else settings_default()), C.sizeof(s))
+    raw = text.encode()
+    check(load().taa_settings_read_ini(C.byref(s), raw, len(raw)))
+    return s
 
 
 def identity16():

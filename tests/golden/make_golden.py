@@ -13,8 +13,13 @@ reference code computes:
                         and FP32 history/screen
   cas_setup_golden.json CasSetup const0/const1 for a set of sharpness values
   sharpen_golden.npz    shaders/sharpen.comp on one image (FP64 and FP32)
+  fxaa_golden.npz       shaders/antialias_fxaa_prepare.comp, then (through an
+                        RGBA16F image, as source/taa.hpp:1063-1104 chains them)
+                        shaders/antialias_fxaa.comp with Fxaa3_11_mod.h, on a
+                        rendered frame with three segmentation masks (FP64 and
+                        FP32)
 
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [taa] [cas] [sharpen] [fxaa]   (default: all)
 """
 from __future__ import annotations
 
@@ -114,6 +119,18 @@ def main():
     def u32(a):
         return np.ascontiguousarray(a, np.uint32).ctypes.data_as(up)
 
+    which = set(sys.argv[1:]) or {"taa", "cas", "sharpen", "fxaa"}
+    if "taa" in which:
+        make_taa(ref, f, u32, dp, up)
+    if "cas" in which:
+        make_cas(libs)
+    if "sharpen" in which:
+        make_sharpen(ref, f, dp)
+    if "fxaa" in which:
+        make_fxaa(libs, fp, dp, up)
+
+
+def make_taa(ref, f, u32, dp, up):
     out = {}
     cases = []
     for scene_name, (w, h, ow, oh, seed) in {"s": (24, 16, 24, 16, 21), "up": (16, 10, 32, 20, 22)}.items():
@@ -163,7 +180,10 @@ def main():
             cases.append(key)
     out["cases"] = np.array(cases)
     np.savez_compressed(HERE / "taa_comp_golden.npz", **out)
+    print(f"{len(cases)} resolve cases written to {HERE}")
 
+
+def make_cas(libs):
     cas = C.CDLL(str(libs["libcas_ref.so"]))
     rows = []
     for s in (0.0, 0.1, 0.25, 0.5, 0.75, 1.0, 1.5, -0.5):
@@ -173,7 +193,10 @@ def main():
             cas.ref_cas_setup(C.c_float(s), *map(C.c_float, dims), c0, c1)
             rows.append(dict(sharpness=s, dims=dims, const0=list(c0), const1=list(c1)))
     (HERE / "cas_setup_golden.json").write_text(json.dumps(rows, indent=1) + "\n")
+    print(f"{len(rows)} CasSetup rows written to {HERE}")
 
+
+def make_sharpen(ref, f, dp):
     rng = np.random.default_rng(5)
     img = rng.uniform(0, 1.2, (13, 19, 4)).astype(np.float16).astype(np.float32)
     sh = {}
@@ -182,7 +205,46 @@ def main():
         ref[prec].ref_sharpen(f(img), 19, 13, C.c_float(0.6), o.ctypes.data_as(dp))
         sh[f"ref{prec}"] = o
     np.savez_compressed(HERE / "sharpen_golden.npz", image=img, factor=np.float32(0.6), **sh)
-    print(f"{len(cases)} resolve cases, {len(rows)} CasSetup rows, sharpen fixture written to {HERE}")
+    print(f"sharpen fixture written to {HERE}")
+
+
+def make_fxaa(libs, fp, dp, up):
+    P = C.POINTER
+    ref = {}
+    for prec in (32, 64):
+        lib = C.CDLL(str(libs[f"libfxaa_ref{prec}.so"]))
+        lib.ref_fxaa_prepare.argtypes = [fp, C.c_int, C.c_int, dp]
+        lib.ref_fxaa.argtypes = [fp, up, C.c_int, C.c_int] + [C.c_float] * 5 + [dp]
+        ref[prec] = lib
+    # a rendered frame of the synthetic scene (sphere silhouettes, checkerboard),
+    # stored as the RGBA16F result image the FXAA passes read
+    w, h = 72, 48
+    wl = WL.small(w, h, frames=1, seed=31)
+    sc = wl.scene()
+    img = O.synth_frame(sc, T.synth_spheres(sc), 0)["color"].astype(np.float16).astype(np.float32)
+    img = np.ascontiguousarray(img)
+    rng = np.random.default_rng(7)
+    masks = {
+        "random": rng.integers(0, 1 << 20, (h, w)).astype(np.uint32),  # (mask & 3) == 1 on about a quarter
+        "all": np.ones((h, w), np.uint32),
+        "none": np.zeros((h, w), np.uint32),
+    }
+    params = (0.75, 0.116, 0.0833)  # source/taa.hpp:95-97
+    rcp = np.float32(1.0) / np.array([w, h], np.float32)
+    out = dict(image=img, params=np.array(params, np.float32), rcp=rcp)
+    for name, m in masks.items():
+        out[f"{name}/segmask"] = m
+        for prec in (64, 32):
+            prep = np.zeros((h, w, 4))
+            ref[prec].ref_fxaa_prepare(img.ctypes.data_as(fp), w, h, prep.ctypes.data_as(dp))
+            prep16 = np.ascontiguousarray(prep.astype(np.float16).astype(np.float32))  # the RGBA16F temp image
+            res = np.zeros((h, w, 4))
+            mm = np.ascontiguousarray(m)
+            ref[prec].ref_fxaa(prep16.ctypes.data_as(fp), mm.ctypes.data_as(up), w, h, float(rcp[0]), float(rcp[1]),
+                               *params, res.ctypes.data_as(dp))
+            out[f"{name}/ref{prec}"] = res if prec == 64 else res.astype(np.float32)
+    np.savez_compressed(HERE / "fxaa_golden.npz", **out)
+    print(f"fxaa fixture written to {HERE}")
 
 
 if __name__ == "__main__":

@@ -33,3 +33,16 @@ def test_mirror_runs_a_sequence(cuda, tmp_path):
     assert len(lines) == 6
     means = [float(l.split()[-1]) for l in lines]
     assert all(0.0 < m < 64.0 for m in means), r.stdout
+
+
+@pytest.mark.gpu
+def test_mirror_runs_the_fxaa_chain(cuda, tmp_path):
+    # resolve with the segmentation mask -> FXAA on the marked pixels -> CAS
+    exe = compile_example(tmp_path)
+    r = subprocess.run([str(exe), "160", "96", "6", "fxaa"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = [l.split() for l in r.stdout.splitlines() if l.startswith("frame")]
+    assert len(lines) == 6
+    marked = [int(l[l.index("marked") + 1]) for l in lines]
+    assert all(m > 0 for m in marked[1:]), r.stdout
+    assert all(0.0 < float(l[-1]) < 64.0 for l in lines), r.stdout

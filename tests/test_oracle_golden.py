@@ -12,7 +12,11 @@ no reference tree: they hold the oracle's restatement to
     frame relative L2 of 1e-5 (the oracle fuses the moment and Catmull-Rom
     sums where the shader's text does not, and evaluates the 9-tap
     Catmull-Rom as its 16-tap form);
-  * CasSetup: equal bits.
+  * CasSetup: equal bits;
+  * FXAA (shaders/antialias_fxaa_prepare.comp then shaders/antialias_fxaa.comp
+    with Fxaa3_11_mod.h, through an RGBA16F image): the FP64 oracle equals the
+    shader in double exactly; the FP32 oracle (sampler positions in float, the
+    shader's in double) agrees on all but a handful of pixels.
 """
 import ctypes as C
 import json
@@ -98,3 +102,35 @@ def test_sharpen_matches_the_reference_shader():
             assert rel_err(got, ref) <= 1e-12
         else:
             np.testing.assert_array_equal(got.astype(np.float32), ref.astype(np.float32))
+
+
+FXAA = np.load(G / "fxaa_golden.npz")
+
+
+@pytest.mark.parametrize("mask", ["random", "all", "none"])
+def test_fxaa_oracle_matches_the_reference_shaders(mask):
+    img, seg = FXAA["image"], FXAA[f"{mask}/segmask"]
+    sub, thr, tmin = FXAA["params"].tolist()
+    assert np.array_equal(FXAA["rcp"], np.float32(1.0) / np.array([img.shape[1], img.shape[0]], np.float32))
+    r64 = O.fxaa(img, seg, sub, thr, tmin, precision=64)
+    np.testing.assert_array_equal(r64, FXAA[f"{mask}/ref64"])
+    r32 = O.fxaa(img, seg, sub, thr, tmin, precision=32)
+    ref32 = FXAA[f"{mask}/ref32"].astype(np.float64)
+    rel = np.abs(r32 - ref32) / np.maximum(1.0, np.abs(ref32))
+    per_px = np.max(rel, axis=-1)
+    assert np.mean(per_px <= 1e-5) >= 0.99
+    assert np.sum(per_px > 1e-3) <= 2  # another branch of the edge search
+    assert rel_err(r32, ref32) <= 0.05
+
+
+def test_fxaa_fixture_exercises_the_edge_paths():
+    img = FXAA["image"].astype(np.float64)
+    prepared = img.copy()  # the FP64 reading: luma in double, stored as FP16
+    prepared[..., 3] = (img[..., 0] * 0.299 + img[..., 1] * 0.587 + img[..., 2] * 0.114).astype(np.float16)
+    # unmarked pixels are the prepared texels; marked ones change on edges
+    np.testing.assert_array_equal(FXAA["none/ref64"], prepared)
+    for mask, lo in (("random", 0.1), ("all", 0.5)):
+        changed = np.any(np.abs(FXAA[f"{mask}/ref64"] - prepared) > 1e-3, axis=-1)
+        assert changed.mean() >= lo
+        marked = (FXAA[f"{mask}/segmask"] & 3) == 1
+        assert not np.any(changed & ~marked)
