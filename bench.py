@@ -284,14 +284,16 @@ def time_fxaa(T, WL, dev, stream, sid, args, peak, col, dep, mot, uniforms):
     marked = float(((seg[0] & 3) == 1).float().mean().item())
     result = {}
     k = max(8, args.steps * 4)
-    for name, use_mask in (("segmask", True), ("all_pixels", False)):
+    fctx = T.Taa(W, H, form=T.TAA_FORM_PLAIN, flags=T.TAA_FLAG_FXAA)  # lends the pass its work list
+    for name, use_mask, c in (("segmask", True, fctx), ("segmask_without_list", True, None),
+                              ("all_pixels", False, None)):
         for i in range(3 * sets):
-            T.fxaa(res[i % sets], out[i % sets], seg[i % sets] if use_mask else None, stream=sid)
+            T.fxaa(res[i % sets], out[i % sets], seg[i % sets] if use_mask else None, stream=sid, ctx=c)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for i in range(k):
-            T.fxaa(res[i % sets], out[i % sets], seg[i % sets] if use_mask else None, stream=sid)
+            T.fxaa(res[i % sets], out[i % sets], seg[i % sets] if use_mask else None, stream=sid, ctx=c)
         e1.record(stream)
         torch.cuda.synchronize()
         us = e0.elapsed_time(e1) * 1000 / k
@@ -307,14 +309,16 @@ def time_fxaa(T, WL, dev, stream, sid, args, peak, col, dep, mot, uniforms):
     t0 = time.perf_counter()
     ref = O.fxaa(img, m, nthreads=nthr)
     t = time.perf_counter() - t0
-    T.fxaa(res[0], out[0], seg[0], stream=sid)
+    T.fxaa(res[0], out[0], seg[0], stream=sid, ctx=fctx)
     torch.cuda.synchronize()
     got = out[0].float().cpu().numpy()
+    fctx.close()
     q = ref.astype(np.float32).astype(np.float16).astype(np.float32)
     result["cpu_oracle"] = {"mpx_s": W * H / t / 1e6, "threads": nthr}
     result["pixels_equal_to_oracle"] = float(np.mean(np.all(got == q, axis=-1)))
-    result["note"] = ("fused prepare + FXAA 3.11 quality preset 12 (one kernel); rotation over 4 buffer sets "
-                      "instead of an L2 flush")
+    result["note"] = ("prepare + FXAA 3.11 quality preset 12: one streaming kernel (listing the marked pixels in "
+                      "the context's work list) and one over the list; without a list a second read of the mask; "
+                      "rotation over 4 buffer sets instead of an L2 flush")
     return result
 
 
@@ -644,8 +648,10 @@ def run_profile_case(args):
         ctx.resolve(stream=sid, color=col[2], depth=dep[2], velocity=mot[2], history=col[1].float(),
                     history_depth=dep[1], history_out=hist[0], result=res, segmask=seg)
         out = torch.empty_like(res)
+        fctx = T.Taa(W, H, form=T.TAA_FORM_PLAIN, flags=T.TAA_FLAG_FXAA)
         for i in range(4):
-            T.fxaa(res, out, seg if i < 3 else None, stream=sid)
+            T.fxaa(res, out, seg if i < 3 else None, stream=sid, ctx=fctx)
+        fctx.close()
         torch.cuda.synchronize()
         ctx.close()
         return 0

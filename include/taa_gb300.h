@@ -67,6 +67,10 @@ typedef enum taa_status {
  * on tcgen05 through tensor memory instead of per warp with warp-wide MMAs
  * (the default: no block barriers, faster inside the resolve). */
 #define TAA_FLAG_LEARNED_TCGEN05 0x1u
+/* taa_desc_t.flags: taa_create also sets aside the work list of the FXAA pass
+ * (taa_fxaa), 4 bytes per output pixel, so that the pass needs one read of
+ * the segmentation mask. */
+#define TAA_FLAG_FXAA 0x2u
 /* Sharpener (taa<CF>::mSharpener, source/taa.hpp:1418). */
 #define TAA_SHARPEN_OFF     0u
 #define TAA_SHARPEN_SIMPLE  1u  /* shaders/sharpen.comp */
@@ -88,7 +92,7 @@ typedef struct taa_desc_t {
     uint32_t form;            /* TAA_FORM_* */
     uint32_t sharpener;       /* TAA_SHARPEN_* */
     float    sharpen_factor;  /* mSharpenFactor, default 0.5 (source/taa.hpp:1419) */
-    uint32_t flags;           /* 0, or TAA_FLAG_LEARNED_TCGEN05 with TAA_FORM_LEARNED */
+    uint32_t flags;           /* TAA_FLAG_FXAA; TAA_FLAG_LEARNED_TCGEN05 with TAA_FORM_LEARNED */
 } taa_desc_t;
 
 /* Per-frame bindings; one field pair per descriptor binding of set 0 in
@@ -215,9 +219,15 @@ int taa_fxaa_default_params(taa_fxaa_params_t* out);
  * (mask & 3) == 1 are antialiased), or NULL to antialias every pixel;
  * `output`: RGBA16F, rgb and the FP16 luma in alpha as the reference's temp
  * image holds them.  All images width x height; `output` must not overlap
- * `input`.  `params` NULL means the defaults.  Enqueued on `stream`. */
-int taa_fxaa(void* stream, const void* input, size_t input_pitch, const void* segmask, size_t segmask_pitch,
-             void* output, size_t output_pitch, int32_t width, int32_t height, const taa_fxaa_params_t* params);
+ * `input`.  `params` NULL means the defaults.  Enqueued on `stream`.
+ * `ctx`: a context created with TAA_FLAG_FXAA whose output size holds at
+ * least width x height pixels lends the pass its work list (the pass streams
+ * the images once and antialiases the listed pixels after); NULL, or any
+ * other context, runs the pass without it (a second read of the mask).  The
+ * results are the same.  Calls sharing a context run on one stream. */
+int taa_fxaa(taa_ctx* ctx, void* stream, const void* input, size_t input_pitch, const void* segmask,
+             size_t segmask_pitch, void* output, size_t output_pitch, int32_t width, int32_t height,
+             const taa_fxaa_params_t* params);
 
 /* The sharpen pass on its own (source/taa.hpp:1111-1139): sharpener
  * TAA_SHARPEN_SIMPLE (shaders/sharpen.comp) or TAA_SHARPEN_CAS

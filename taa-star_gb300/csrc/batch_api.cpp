@@ -182,6 +182,7 @@ int taa_batch_create(const taa_desc_t* descs, int32_t n, taa_batch** out) {
             return fail(TAA_E_UNSUPPORTED, "taa_batch_create: view %d: sharpening runs with taa_resolve", v);
         if (d.form != TAA_FORM_AUTO && d.form != TAA_FORM_TILED)
             return fail(TAA_E_UNSUPPORTED, "taa_batch_create: view %d: batches run the tiled FP32 form", v);
+        if (d.flags) return fail(TAA_E_UNSUPPORTED, "taa_batch_create: view %d: flags 0x%x", v, d.flags);
         if ((d.out_width + 7) / 8 > 4096 || (d.out_height + 7) / 8 > 4096)
             return fail(TAA_E_INVAL, "taa_batch_create: view %d too large for the job encoding", v);
     }

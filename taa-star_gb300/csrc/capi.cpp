@@ -88,8 +88,9 @@ int check_desc(const taa_desc_t& d, const char* who) {
     if (d.form > TAA_FORM_LEARNED) return fail(TAA_E_INVAL, "%s: form %u", who, d.form);
     if (d.sharpener > TAA_SHARPEN_CAS) return fail(TAA_E_INVAL, "%s: sharpener %u", who, d.sharpener);
     if (!finite(d.sharpen_factor)) return fail(TAA_E_INVAL, "%s: sharpen_factor not finite", who);
-    if (d.flags & ~TAA_FLAG_LEARNED_TCGEN05) return fail(TAA_E_INVAL, "%s: unknown flags 0x%x", who, d.flags);
-    if (d.flags && d.form != TAA_FORM_LEARNED)
+    if (d.flags & ~(TAA_FLAG_LEARNED_TCGEN05 | TAA_FLAG_FXAA))
+        return fail(TAA_E_INVAL, "%s: unknown flags 0x%x", who, d.flags);
+    if ((d.flags & TAA_FLAG_LEARNED_TCGEN05) && d.form != TAA_FORM_LEARNED)
         return fail(TAA_E_INVAL, "%s: TAA_FLAG_LEARNED_TCGEN05 needs TAA_FORM_LEARNED", who);
     return ok();
 }
@@ -444,6 +445,13 @@ int taa_create(const taa_desc_t* d, taa_ctx** out) {
         if (e != cudaSuccess) rc = e == cudaErrorMemoryAllocation ? fail(TAA_E_NOMEM, "taa_create: out of device memory")
                                                                   : cuda_fail(e, "taa_create: network buffers");
     }
+    if (rc == TAA_OK && (d->flags & TAA_FLAG_FXAA)) {
+        c->fxaa_cap = (size_t)d->out_width * (size_t)d->out_height;
+        e = cudaMalloc(&c->fxaa_list, (c->fxaa_cap + 4) * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMemset(c->fxaa_list, 0, 4 * sizeof(uint32_t));  // the list head
+        if (e != cudaSuccess) rc = e == cudaErrorMemoryAllocation ? fail(TAA_E_NOMEM, "taa_create: out of device memory")
+                                                                  : cuda_fail(e, "taa_create: FXAA work list");
+    }
     if (rc != TAA_OK) {
         taa_destroy(c);
         return rc;
@@ -457,6 +465,7 @@ int taa_destroy(taa_ctx* c) {
     if (c->scratch_screen) cudaFree(c->scratch_screen);
     if (c->mlp_weights) cudaFree(c->mlp_weights);
     if (c->mlp_blob) cudaFree(c->mlp_blob);
+    if (c->fxaa_list) cudaFree(c->fxaa_list);
     delete c;
     return ok();
 }

@@ -22,6 +22,9 @@ struct taa_ctx {
     float* mlp_weights = nullptr;
     char* mlp_blob = nullptr;
     bool have_mlp = false;
+    // TAA_FLAG_FXAA: the FXAA pass's work list, a counter then fxaa_cap entries
+    uint32_t* fxaa_list = nullptr;
+    size_t fxaa_cap = 0;
 };
 
 namespace taa_host {

@@ -39,9 +39,10 @@ cudaError_t launch_resolve_half(int history_fmt, int motion_ch, int interp, cons
 // Standalone sharpen passes on an RGBA16F image (used after the plain form).
 cudaError_t launch_sharpen(int sharpener, const FrameArgs& a, cudaStream_t stream);
 // The FXAA pass (prepare + FXAA 3.11 quality preset 12) on an RGBA16F image;
-// segmask.p == nullptr marks every pixel.
+// segmask.p == nullptr marks every pixel.  `list`: a work list of a counter
+// (padded to 16 bytes) and in.w * in.h entries, or nullptr.
 cudaError_t launch_fxaa(const Img& in, const Img& segmask, const ImgW& out, const float rcp[2], float subpix,
-                        float edge_threshold, float edge_threshold_min, cudaStream_t stream);
+                        float edge_threshold, float edge_threshold_min, uint32_t* list, cudaStream_t stream);
 
 // Device address and size of the fixed screen buffer of static_scratch.cu on
 // the current device (looked up once per device).

@@ -37,8 +37,9 @@ int taa_fxaa_default_params(taa_fxaa_params_t* out) {
 }
 
 // source/taa.hpp:1063-1104 (prepare + FXAA dispatches), one kernel.
-int taa_fxaa(void* stream, const void* input, size_t input_pitch, const void* segmask, size_t segmask_pitch,
-             void* output, size_t output_pitch, int32_t width, int32_t height, const taa_fxaa_params_t* params) {
+int taa_fxaa(taa_ctx* ctx, void* stream, const void* input, size_t input_pitch, const void* segmask,
+             size_t segmask_pitch, void* output, size_t output_pitch, int32_t width, int32_t height,
+             const taa_fxaa_params_t* params) {
     static const char* who = "taa_fxaa";
     int rc;
     if ((rc = check_size(width, height, who))) return rc;
@@ -57,7 +58,10 @@ int taa_fxaa(void* stream, const void* input, size_t input_pitch, const void* se
     Img in{(const char*)input, input_pitch, width, height};
     Img seg{(const char*)segmask, segmask_pitch, width, height};
     ImgW out{(char*)output, output_pitch};
-    cudaError_t e = taa_dev::launch_fxaa(in, seg, out, rcp, p.subpix, p.edge_threshold, p.edge_threshold_min,
+    // the context's work list when it holds every pixel of this image
+    uint32_t* list = nullptr;
+    if (ctx && ctx->fxaa_list && (size_t)width * (size_t)height <= ctx->fxaa_cap) list = ctx->fxaa_list;
+    cudaError_t e = taa_dev::launch_fxaa(in, seg, out, rcp, p.subpix, p.edge_threshold, p.edge_threshold_min, list,
                                          (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(e, who);
     return ok();

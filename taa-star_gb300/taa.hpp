@@ -109,7 +109,7 @@ template <size_t CF> class taa {
             alloc(mSegMask[i], 4);
         }
         taa_desc_t d{sizeof(taa_desc_t), sourceWidth, sourceHeight, targetWidth, targetHeight, TAA_HISTORY_RGBA32F,
-                     motionFormat, mForm, mSharpener, mSharpenFactor, 0};
+                     motionFormat, mForm, mSharpener, mSharpenFactor, TAA_FLAG_FXAA};
         check(taa_create(&d, &mCtx));
         mCtxSharpener = mSharpener;
         mCtxSharpenFactor = mSharpenFactor;
@@ -293,7 +293,7 @@ template <size_t CF> class taa {
         cudaEventRecord(mT0, stream);
         check(taa_resolve(mCtx, stream, &io));
         if (mFxaa) {
-            check(taa_fxaa(stream, mResult[cur].ptr, mResult[cur].pitch, mSegMask[cur].ptr, mSegMask[cur].pitch,
+            check(taa_fxaa(mCtx, stream, mResult[cur].ptr, mResult[cur].pitch, mSegMask[cur].ptr, mSegMask[cur].pitch,
                            mTemp[cur].ptr, mTemp[cur].pitch, mOut[0], mOut[1], &mFxaaPushConstants));
             mShown[cur] = Shown::Temp;
             if (mSharpener != TAA_SHARPEN_OFF) {

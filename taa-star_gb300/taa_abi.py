@@ -28,6 +28,7 @@ TAA_MOTION_RGBA16F = 0
 TAA_MOTION_RG16F = 1
 TAA_FORM_AUTO, TAA_FORM_PLAIN, TAA_FORM_TILED, TAA_FORM_FP16, TAA_FORM_LEARNED = 0, 1, 2, 3, 4
 TAA_FLAG_LEARNED_TCGEN05 = 0x1
+TAA_FLAG_FXAA = 0x2
 TAA_SHARPEN_OFF, TAA_SHARPEN_SIMPLE, TAA_SHARPEN_CAS = 0, 1, 2
 
 RTFLAG = dict(OUT=0x1, DIS=0x2, NRM=0x4, DPT=0x8, MID=0x10, LUM=0x20, CNT=0x40, ALL=0x80, FXD=0x100, FXA=0x200)
@@ -183,8 +184,8 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
         "taa_get_jitter_offset_custom": (C.c_int, [C.c_void_p, C.c_int32, C.c_uint64, C.c_int32, C.c_int32,
                                                    P(JitterOpts), P(C.c_float)]),
         "taa_fxaa_default_params": (C.c_int, [P(FxaaParams)]),
-        "taa_fxaa": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t,
-                               C.c_int32, C.c_int32, P(FxaaParams)]),
+        "taa_fxaa": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_void_p,
+                               C.c_size_t, C.c_int32, C.c_int32, P(FxaaParams)]),
         "taa_sharpen": (C.c_int, [C.c_void_p, C.c_uint32, C.c_float, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t,
                                   C.c_int32, C.c_int32]),
         "taa_settings_default": (C.c_int, [P(Settings)]),
@@ -267,14 +268,16 @@ def fxaa_default_params() -> FxaaParams:
     return p
 
 
-def fxaa(input, output, segmask=None, params: FxaaParams | None = None, stream: int = 0):
-    """taa_fxaa on (H, W, 4) FP16 tensors; segmask an (H, W) int32/uint32 tensor or None."""
+def fxaa(input, output, segmask=None, params: FxaaParams | None = None, stream: int = 0, ctx: "Taa | None" = None):
+    """taa_fxaa on (H, W, 4) FP16 tensors; segmask an (H, W) int32/uint32 tensor or None;
+    ctx a context created with TAA_FLAG_FXAA lends its work list."""
     h, w = int(input.shape[0]), int(input.shape[1])
     ip, ipitch = tensor_ptr_pitch(input)
     op, opitch = tensor_ptr_pitch(output)
     sp, spitch = tensor_ptr_pitch(segmask) if segmask is not None else (None, 0)
-    check(load().taa_fxaa(C.c_void_p(stream), C.c_void_p(ip), ipitch, C.c_void_p(sp), spitch, C.c_void_p(op),
-                          opitch, w, h, C.byref(params) if params is not None else None))
+    check(load().taa_fxaa(ctx.handle if ctx is not None else None, C.c_void_p(stream), C.c_void_p(ip), ipitch,
+                          C.c_void_p(sp), spitch, C.c_void_p(op), opitch, w, h,
+                          C.byref(params) if params is not None else None))
 
 
 def sharpen(input, output, sharpener: int, factor: float, stream: int = 0):

@@ -1,13 +1,15 @@
 """The FXAA pass (taa_fxaa) and the standalone sharpen pass (taa_sharpen) on the
 GPU against the oracle (run with -m gpu).
 
-* FXAA: the kernel computes the prepare pass's FP16 luma and FXAA 3.11 quality
-  preset 12 with the oracle's operations in the same order, so its RGBA16F
+* FXAA: the kernels compute the prepare pass's FP16 luma and FXAA 3.11 quality
+  preset 12 with the oracle's operations in the same order, so their RGBA16F
   output equals the FP32 oracle's value rounded to FP16, bit for bit: on the
   golden fixture's frame and masks, on rendered frames at sizes that are not
-  multiples of the block, on degenerate sizes, with other settings and with
-  padded pitches; on the segmentation mask a resolve writes (the reference's
-  ray-trace-assist chain, source/taa.hpp:1063-1104).
+  multiples of the block (odd widths, whose rows are not 16-byte aligned, take
+  the scalar path), on degenerate sizes, with other settings and with padded
+  pitches; on the segmentation mask a resolve writes
+  (the reference's ray-trace-assist chain, source/taa.hpp:1063-1104).  With
+  and without a context's work list (TAA_FLAG_FXAA).
 * sharpen: taa_sharpen equals the oracle's sharpen.comp / CAS to one FP16 ulp,
   like the sharpener fused into the resolve.
 """
@@ -27,7 +29,17 @@ pytestmark = pytest.mark.gpu
 G = Path(__file__).resolve().parent / "golden"
 
 
-def run_fxaa(dev, img, seg, params=None, pad=0):
+_CTX = {}
+
+
+def list_ctx(w, h):
+    """A context with the FXAA work list for images up to w x h."""
+    if (w, h) not in _CTX:
+        _CTX[(w, h)] = T.Taa(w, h, form=T.TAA_FORM_PLAIN, flags=T.TAA_FLAG_FXAA)
+    return _CTX[(w, h)]
+
+
+def run_fxaa(dev, img, seg, params=None, pad=0, ctx=None):
     """taa_fxaa on a numpy RGBA image (FP16 values) and mask; returns the output as float32."""
     h, w = img.shape[:2]
     src = torch.zeros(h, w + pad, 4, dtype=torch.float16, device=dev)
@@ -37,7 +49,7 @@ def run_fxaa(dev, img, seg, params=None, pad=0):
     if seg is not None:
         m = torch.zeros(h, w + pad, dtype=torch.int32, device=dev)
         m[:, :w] = torch.from_numpy(np.ascontiguousarray(seg).view(np.int32)).to(dev)
-    T.fxaa(src[:, :w], out[:, :w], None if m is None else m[:, :w], params)
+    T.fxaa(src[:, :w], out[:, :w], None if m is None else m[:, :w], params, ctx=ctx)
     torch.cuda.synchronize()
     res = out.float().cpu().numpy()
     if pad:
@@ -65,10 +77,12 @@ def rendered(w, h, seed=3):
 def test_golden_frame_and_masks(cuda):
     g = np.load(G / "fxaa_golden.npz")
     img = g["image"]
+    h, w = img.shape[:2]
     for name in ("random", "all", "none"):
         seg = g[f"{name}/segmask"]
         got = run_fxaa(cuda, img, seg)
         assert_equal(got, expected(img, seg))
+        assert_equal(run_fxaa(cuda, img, seg, ctx=list_ctx(w, h)), got)
         # and close to the reference shader's own FP32 evaluation (its sampler
         # positions in double: a handful of pixels may take another branch)
         ref32 = g[f"{name}/ref32"].astype(np.float64)
@@ -84,9 +98,11 @@ def test_rendered_frames(cuda, size):
     rng = np.random.default_rng(w * 1000 + h)
     seg = rng.integers(0, 1 << 16, (h, w)).astype(np.uint32)
     for m in (seg, None):
-        got = run_fxaa(cuda, img, m)
         ref = expected(img, m)
-        assert_equal(got, ref)
+        # without a work list, with one, and with a context too small to lend it
+        for c in (None, list_ctx(w, h), list_ctx(max(1, w // 2), h)):
+            got = run_fxaa(cuda, img, m, ctx=c)
+            assert_equal(got, ref)
     if (w, h) == (256, 160):
         # the pass changes the marked edge pixels only
         changed = np.any(got != expected(img, np.zeros((h, w), np.uint32)), axis=-1)
@@ -96,9 +112,14 @@ def test_rendered_frames(cuda, size):
 def test_settings_and_padded_pitch(cuda):
     img = rendered(120, 72, seed=5)
     seg = np.ones((72, 120), np.uint32)
+    rng = np.random.default_rng(2)
+    half = rng.integers(0, 4, (72, 120)).astype(np.uint32)
     for sub, thr, tmin in ((0.0, 0.166, 0.0625), (1.0, 0.063, 0.0312), (0.75, 0.333, 0.0833)):
         p = T.FxaaParams(sub, thr, tmin)
-        assert_equal(run_fxaa(cuda, img, seg, p, pad=24), expected(img, seg, p))
+        for m in (seg, half):
+            ref = expected(img, m, p)
+            assert_equal(run_fxaa(cuda, img, m, p, pad=24), ref)
+            assert_equal(run_fxaa(cuda, img, m, p, pad=24, ctx=list_ctx(120, 72)), ref)
 
 
 def test_on_the_mask_a_resolve_writes(cuda):
@@ -117,8 +138,10 @@ def test_on_the_mask_a_resolve_writes(cuda):
              segmask=torch.zeros(h, w, dtype=torch.int32, device=cuda))
     ctx.resolve(**b)
     out = torch.empty(h, w, 4, dtype=torch.float16, device=cuda)
-    T.fxaa(b["result"], out, b["segmask"])
+    fctx = T.Taa(w, h, form=T.TAA_FORM_PLAIN, flags=T.TAA_FLAG_FXAA)
+    T.fxaa(b["result"], out, b["segmask"], ctx=fctx)
     torch.cuda.synchronize()
+    fctx.close()
     seg = b["segmask"].cpu().numpy().view(np.uint32)
     marked = (seg & 3) == 1
     assert 0.0 < marked.mean() < 1.0
@@ -132,7 +155,7 @@ def test_errors(cuda):
     a = torch.zeros(8, 8, 4, dtype=torch.float16, device=cuda)
     o = torch.zeros(8, 8, 4, dtype=torch.float16, device=cuda)
     pa, po = a.data_ptr(), o.data_ptr()
-    f = lambda *args: lib.taa_fxaa(None, *args)
+    f = lambda *args: lib.taa_fxaa(None, None, *args)
     assert f(pa, 64, None, 0, pa, 64, 8, 8, None) == T.TAA_E_INVAL           # output is the input
     assert f(pa, 64, None, 0, pa + 32, 64, 8, 8, None) == T.TAA_E_INVAL      # overlapping rows
     assert f(pa + 2, 64, None, 0, po, 64, 8, 8, None) == T.TAA_E_ALIGN       # misaligned
