@@ -59,6 +59,24 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(value: float, world: int, device=None) -> float:
+    """The largest of the ranks' values: the slowest replica's time, which sets
+    the whole job's throughput.  One rank returns its own value."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank: float, world: int, seconds_max: float) -> float:
+    """Whole-job throughput of `world` replicas that each processed
+    `units_per_rank` units, timed by the slowest of them."""
+    return world * units_per_rank / seconds_max
+
+
 def load_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -366,13 +384,9 @@ def time_batch(T, WL, dev, stream, sid, world, args, peak, single_mpx):
         batch.launch(0, stream=sid)
     e1.record(stream)
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1), world, dev)
     batch.close()
-    mpx = world * npx * k / (ms / 1e3) / 1e6
+    mpx = job_throughput(npx * k, world, ms / 1e3) / 1e6
     gbs = views[0].bytes_per_pixel(history_bytes=16, motion_bytes=4) * npx / (ms / 1e3 / k) / 1e9
     return {"mpx_s": mpx, "gb_s": gbs, "frac_of_hbm": gbs / peak, "views": len(views), "pixels": npx,
             "per_pixel_vs_single_4k": (mpx / world) / single_mpx,
@@ -453,11 +467,8 @@ def run_ours(args):
         torch.cuda.synchronize()
         if sampler:
             sampler.__exit__(None, None, None)
-        ms = e0.elapsed_time(e1)
+        ms = max_over_ranks(e0.elapsed_time(e1), world, dev)
         if world > 1:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
             dist.barrier()
         return ms
 
@@ -471,7 +482,7 @@ def run_ours(args):
     sampler = ClockSampler(local)
     ms = timed(ctx, args.steps, args.warmup, sampler)
     launches = args.steps * F
-    mpx = world * W * H * F * args.steps / (ms / 1e3) / 1e6
+    mpx = job_throughput(W * H * F * args.steps, world, ms / 1e3) / 1e6
     avg_launch_s = ms / 1e3 / launches
     achieved = launch_bytes / avg_launch_s / 1e9
     traffic, traffic_src = load_traffic(form_name)
@@ -482,7 +493,7 @@ def run_ours(args):
             c2 = make_ctx(fid)
             k = max(2, args.steps // 4)
             m2 = timed(c2, k, 1)
-            v = world * W * H * F * k / (m2 / 1e3) / 1e6
+            v = job_throughput(W * H * F * k, world, m2 / 1e3) / 1e6
             g = launch_bytes / (m2 / 1e3 / (k * F)) / 1e9
             forms[name] = {"mpx_s": v, "gb_s": g, "frac_of_hbm": g / peak}
             c2.close()
@@ -558,12 +569,8 @@ def run_ours(args):
         stream.wait_stream(s_out)
         t1.record(stream)
         torch.cuda.synchronize()
-        ms_e = t0.elapsed_time(t1)
-        if world > 1:
-            t = torch.tensor([ms_e], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms_e = float(t.item())
-        e2e = {"value": world * W * H * F * k / (ms_e / 1e3) / 1e6, "unit": UNIT,
+        ms_e = max_over_ranks(t0.elapsed_time(t1), world, dev)
+        e2e = {"value": job_throughput(W * H * F * k, world, ms_e / 1e3) / 1e6, "unit": UNIT,
                "h2d_bytes_per_step": F * H * W * (8 + 4 + 4), "d2h_bytes_per_step": F * H * W * 8,
                "note": "pinned host buffers, 3-slot copy/compute/copy pipeline on three streams"}
         ectx.close()
