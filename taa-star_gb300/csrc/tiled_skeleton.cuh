@@ -31,6 +31,7 @@
 #include <cuda.h>
 
 #include <cstring>
+#include <type_traits>
 
 #include "common.cuh"
 #include "f32x2.cuh"
@@ -67,9 +68,12 @@ template <class S, int HF> struct Win {
     static constexpr int W = HF == 0 ? S::WW : S::WW + (S::WW & 1);
     static constexpr int ALIGN = HF == 0 ? 1 : 2;
 };
-// Polls of the window's mbarrier before the wait gives up (each poll may
-// suspend the thread for a while in hardware): far above any real copy time.
-constexpr uint32_t kWaitPolls = 1u << 22;
+// Polls of the window's mbarrier before the wait gives up, each suspending the
+// thread in hardware until the phase completes or kWaitPollNs pass (so a
+// waiting warp issues a few instructions, not a spin loop): about 80 ms in
+// all, far above any real copy time.
+constexpr uint32_t kWaitPolls = 1u << 12;
+constexpr uint32_t kWaitPollNs = 20000;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -99,9 +103,9 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     uint32_t done;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done)
-        : "r"(smem_addr(bar)), "r"(parity)
+        : "r"(smem_addr(bar)), "r"(parity), "r"(kWaitPollNs)
         : "memory");
     return done != 0;
 }
@@ -225,6 +229,213 @@ template <class Pol, class S, int HF> struct TileSmem {
     int abort;     // a persistent CTA stops after this tile (a window wait gave up)
 };
 
+// One thread's inputs of a tile, as loaded (converted where they are used, so
+// that a load issued ahead of time does not stall the thread until then):
+// its pixel's depth and velocity and one or two staged colour texels.
+template <int MC> struct TileIn {
+    float depth;
+    typename std::conditional<MC == 4, uint2, uint32_t>::type vel;
+    uint2 st0, st1;
+};
+template <int MC> __device__ __forceinline__ float4 velocity_of(uint32_t v) {
+    const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&v));
+    return make_float4(f.x, f.y, 0.f, 0.f);
+}
+template <int MC> __device__ __forceinline__ float4 velocity_of(uint2 v) { return half4_to_float4(v); }
+
+template <class S, int MC>
+__device__ __forceinline__ TileIn<MC> load_tile_inputs(const FrameArgs& a, int tile_x, int tile_y) {
+    constexpr int TX = S::TX, NT = S::NT, SX = S::SX, NS = S::NS;
+    const int tid = threadIdx.x;
+    const int W = a.out_w, H = a.out_h;
+    const int x0 = tile_x * TX, y0 = tile_y * S::TY;
+    const int cx = min(x0 + tid % TX, W - 1), cy = min(y0 + tid / TX, H - 1);
+    TileIn<MC> in;
+    in.depth = __ldg(texel_ptr<float>(a.depth, cx, cy));
+    in.vel = __ldg(texel_ptr<decltype(in.vel)>(a.velocity, cx, cy));
+    const int sy = tid / SX, sx = tid - sy * SX;
+    in.st0 = __ldg(texel_ptr<uint2>(a.color, clampi(x0 - 1 + sx, 0, W - 1), clampi(y0 - 1 + sy, 0, H - 1)));
+    in.st1 = make_uint2(0u, 0u);
+    if (tid + NT < NS) {
+        const int i = tid + NT, sy1 = i / SX, sx1 = i - sy1 * SX;
+        in.st1 = __ldg(texel_ptr<uint2>(a.color, clampi(x0 - 1 + sx1, 0, W - 1), clampi(y0 - 1 + sy1, 0, H - 1)));
+    }
+    return in;
+}
+
+// The tile's reference pixel: its centre, clamped into the image.
+template <class S> __device__ __forceinline__ void reference_pixel(const FrameArgs& a, int tile_x, int tile_y, int& rx,
+                                                                   int& ry) {
+    rx = min(tile_x * S::TX + S::TX / 2, a.out_w - 1);
+    ry = min(tile_y * S::TY + S::TY / 2, a.out_h - 1);
+}
+
+// The history window of a tile, placed at its reference pixel (depth rdepth,
+// velocity rvs): the pixel's Catmull-Rom taps widened by the tile and
+// WIN_MARGIN.  The calling thread writes the origin and copy mode to org[0..2]
+// and, for a window inside the image with TMA usable, starts its copy into
+// `win` on `bar`.  Run by one thread, or by a warp whose lane 0 writes.
+template <class Pol, class S, int HF, int MC, int INTERP, bool HOT>
+__device__ __forceinline__ void place_window(const taa_uniforms_t& U, const FrameArgs& a, const Mode<HOT>& M,
+                                             const CUtensorMap* hmap, bool tma_ok, int tile_x, int tile_y,
+                                             float rdepth, float4 rvs, typename HistTexel<HF>::T* win, uint64_t* bar,
+                                             int* org, bool writer) {
+    constexpr int WWS = Win<S, HF>::W, WH = S::WH;
+    const Img& hi = a.history;
+    int rx, ry;
+    reference_pixel<S>(a, tile_x, tile_y, rx, ry);
+    const int x0 = tile_x * S::TX, y0 = tile_y * S::TY;
+    float ru = div_const_rn((float)rx + 0.5f, (float)a.out_w, a.inv_out_w);
+    float rv = div_const_rn((float)ry + 0.5f, (float)a.out_h, a.inv_out_h);
+    float rhu, rhv, rehd;
+    history_position<Pol, MC, HOT>(U, a, M, rx, ry, rvs, rdepth, ru, rv, rhu, rhv, rehd);
+    const int k0 = INTERP == 2 ? 1 : 0;  // Catmull-Rom starts one texel before floor(p - 0.5)
+    const int rux = trunc_index(floorf(rhu * (float)hi.w - 0.5f)) - k0;
+    const int ruy = trunc_index(floorf(rhv * (float)hi.h - 0.5f)) - k0;
+    // the reference pixel sits at (rx - x0, ry - y0) in the tile; floor to the stored alignment
+    const int wx0 = (rux - (rx - x0) - WIN_MARGIN) & ~(Win<S, HF>::ALIGN - 1);
+    const int wy0 = ruy - (ry - y0) - WIN_MARGIN;
+    const bool interior = wx0 >= 0 && wy0 >= 0 && wx0 <= hi.w - WWS && wy0 <= hi.h - WH;
+    const int mode = tma_ok && interior ? 1 : 2;
+    if (writer) {
+        org[0] = wx0;
+        org[1] = wy0;
+        org[2] = mode;
+        if (mode == 1) {
+            mbar_expect_tx(bar, (uint32_t)(sizeof(typename HistTexel<HF>::T) * WWS * WH));
+            if (HF == 0) tma_load_3d(win, hmap, 0, wx0, wy0, bar);
+            else tma_load_2d(win, hmap, 4 * wx0, wy0, bar);
+        }
+    }
+}
+
+// The tile after its inputs are loaded and its window placed: history
+// position, staging of the colour, the 3x3 box while the window is in flight,
+// the history sample (from the window when all taps fall inside it, from
+// global memory otherwise), then the finisher.  Every thread of the CTA
+// calls it.  `col`, `win`, `bar`, `org` are the tile's shared buffers; `phase`
+// is the barrier phase the window copy completes; prev_depth_in, when not
+// null, is this thread's previous-frame depth at its history position,
+// fetched ahead (depth culling); `abort` (persistent CTAs) is set when a
+// window wait gave up.
+// The barrier among the threads that compute a tile (the whole CTA).
+struct CtaSync {
+    static __device__ __forceinline__ void sync() { __syncthreads(); }
+};
+
+template <class Pol, class S, int HF, int MC, int INTERP, bool HOT, class Sync = CtaSync, class Fin>
+__device__ __forceinline__ void tile_compute(const taa_uniforms_t& U, const FrameArgs& a, int tile_x, int tile_y,
+                                             const TileIn<MC>& in, const float* prev_depth_in,
+                                             typename Pol::Staged* col, typename HistTexel<HF>::T* win,
+                                             uint64_t* bar, const int* org, uint32_t phase, int* abort, Fin& fin) {
+    using HT = typename HistTexel<HF>::T;
+    constexpr int TX = S::TX, NT = S::NT, SX = S::SX, NS = S::NS, WH = S::WH;
+    constexpr int WWS = Win<S, HF>::W;
+
+    const taa_parameters_t& P = U.param[0];
+    const Mode<HOT> M{P};
+    const int tid = threadIdx.x;
+    const int lx = tid % TX, ly = tid / TX;
+    const int W = a.out_w, H = a.out_h;
+    const int x = tile_x * TX + lx, y = tile_y * S::TY + ly;
+    const bool inside = x < W && y < H;
+    const int cx = min(x, W - 1), cy = min(y, H - 1);
+    const Img& hi = a.history;
+    const bool have_hist = hi.p != nullptr;
+    const bool windowed = have_hist && INTERP != 1;
+
+    // own history position; (u, v) = (texel + 0.5) / size, correctly rounded, as a pair
+    const f2 z{a.neg_zero2};
+    const f2 uv = div_const_rn2(add2(pk((float)cx, (float)cy), dup(0.5f)), pk(-(float)W, -(float)H),
+                                pk(a.inv_out_w, a.inv_out_h), z);
+    float u = f2lo(uv), v = f2hi(uv);
+    float hu, hv, ehd;
+    history_position<Pol, MC, HOT>(U, a, M, cx, cy, velocity_of<MC>(in.vel), in.depth, u, v, hu, hv, ehd);
+    float prev_depth = 0.f;
+    const bool depth_cull = P.mDepthCulling != 0;
+    if (depth_cull && a.history_depth.p) {
+        if (prev_depth_in) {
+            prev_depth = *prev_depth_in;
+        } else {
+            int tx_ = clampi(trunc_index(hu * (float)a.color.w), 0, a.color.w - 1);
+            int ty_ = clampi(trunc_index(hv * (float)a.color.h), 0, a.color.h - 1);
+            prev_depth = __ldg(texel_ptr<float>(a.history_depth, tx_, ty_));
+        }
+    }
+
+    // staged colour in the policy's working format
+    const bool tm = M.tonemap(), yc = M.ycocg();
+    col[tid] = Pol::stage(in.st0, tm, yc);
+    if (tid + NT < NS) col[tid + NT] = Pol::stage(in.st1, tm, yc);
+    Sync::sync();
+    int wx0 = 0, wy0 = 0, mode = 0;
+    if (windowed) {
+        wx0 = org[0];
+        wy0 = org[1];
+        mode = org[2];
+    }
+    if (mode == 2) {
+        // a window across the image border: every texel edge-clamped
+        const int lane = tid & 31, warp = tid >> 5;
+        for (int r = warp; r < WH; r += NT / 32) {
+            const int gy = clampi(wy0 + r, 0, hi.h - 1);
+            const char* row = hi.p + (size_t)gy * hi.pitch;
+            for (int c = lane; c < WWS; c += 32)
+                cp_async<HistTexel<HF>::B>(&win[r * WWS + c],
+                                           row + (size_t)clampi(wx0 + c, 0, hi.w - 1) * HistTexel<HF>::B);
+        }
+        cp_async_commit();
+    }
+    // the 3x3 box while the window is in flight
+    typename Pol::Box box;
+    Pol::template box<HOT>(&col[(ly + 1) * SX + lx + 1], SX, M, P.mVarClipGamma, box, z);
+    if (Pol::kExactCentre) Pol::centre_colour(box, a.color, cx, cy, tm, yc);
+
+    bool landed = true;
+    if (mode == 1) {
+        landed = mbar_wait_bounded(bar, phase & 1u);
+        if (!landed) {
+            atomicOr(a.status, kStatusWindowTimeout);
+            mbar_wait_bounded(bar, phase & 1u);  // the copy may still land in this CTA's memory
+            if (abort) *abort = 1;
+        }
+    } else if (mode == 2) {
+        cp_async_wait_all();
+        Sync::sync();
+    }
+    const bool valid = inside && landed;
+    // rejection (taa.comp:787-823) first, so its inputs die before the filter
+    bool rejected = false;
+    if (P.mRejectOutside && (hu < 0.f || hv < 0.f || hu >= 1.f || hv >= 1.f)) rejected = true;
+    if (depth_cull) {
+        float hd = prev_depth;
+        if (fabsf(hd - ehd) > 0.1f * (1.0f - hd)) rejected = true;
+    }
+    // the history sample: from the window when all taps fall inside it
+    float4 hraw = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (valid) {
+        if (have_hist) {
+            HistoryTaps<Pol, INTERP> taps;
+            taps.setup(hu, hv, hi.w, hi.h, z);
+            const int span = INTERP == 2 ? 4 : 2;
+            const int bx = taps.t[0].ux - wx0, by = taps.t[0].uy - wy0;
+            const bool in_win = windowed && bx >= 0 && by >= 0 && bx + span <= WWS && by + span <= WH;
+            if (in_win) {
+                const HT* base = &win[by * WWS + bx];
+                hraw = Pol::template filter_window<INTERP, HF>(taps, base, WWS);
+            } else {
+                hraw = Pol::template filter<INTERP>(
+                    taps, hi.w, hi.h, [&](int tx_, int ty_) { return fetch_history<HF>(hi, tx_, ty_); });
+            }
+        }
+    }
+    // rectification, blend and stores: every thread of the CTA calls the
+    // finisher (valid says whether its pixel is in the image and resolved)
+    const C3 c0 = Pol::centre(box, &col[(ly + 1) * SX + lx + 1]);
+    Fin::template run<Pol, HF, HOT>(U, a, P, M, box, c0, hraw, u, v, hu, hv, ehd, prev_depth, rejected, valid, x, y,
+                                    tm, fin);
+}
+
 // One tile of the resolve: pixels (tile_x * TX + i, tile_y * TY + j).  Pol
 // provides the working colour format and the box, tap, filter and finishing
 // arithmetic (policy_f32.cuh, resolve_half.cu).  `hmap` is the history image's
@@ -238,153 +449,20 @@ template <class Pol, class S, int HF, int MC, int INTERP, bool HOT, bool PERSIST
 __device__ __forceinline__ void tile_body(const taa_uniforms_t& U, const FrameArgs& a, const CUtensorMap* hmap,
                                           bool tma_ok, int tile_x, int tile_y, TileSmem<Pol, S, HF>& sm,
                                           uint32_t& phase, Fin& fin) {
-    using HT = typename HistTexel<HF>::T;
-    constexpr int TX = S::TX, TY = S::TY, NT = S::NT, SX = S::SX, NS = S::NS, WH = S::WH;
-    constexpr int WWS = Win<S, HF>::W;
-
-    const taa_parameters_t& P = U.param[0];
-    const Mode<HOT> M{P};
-    const int tid = threadIdx.x;
-    const int lx = tid % TX, ly = tid / TX;
-    const int W = a.out_w, H = a.out_h;
-    const int x0 = tile_x * TX, y0 = tile_y * TY;
-    const int x = x0 + lx, y = y0 + ly;
-    const bool inside = x < W && y < H;
-    const int cx = min(x, W - 1), cy = min(y, H - 1);
-
-    // 1. own depth and velocity, staged colour texels
-    float depth = __ldg(texel_ptr<float>(a.depth, cx, cy));
-    float4 vs = fetch_velocity<MC>(a.velocity, cx, cy);
-    uint2 st0, st1 = make_uint2(0u, 0u);
-    {
-        int sy = tid / SX, sx = tid - sy * SX;
-        st0 = __ldg(texel_ptr<uint2>(a.color, clampi(x0 - 1 + sx, 0, W - 1), clampi(y0 - 1 + sy, 0, H - 1)));
-        if (tid + NT < NS) {
-            int i = tid + NT, sy1 = i / SX, sx1 = i - sy1 * SX;
-            st1 = __ldg(texel_ptr<uint2>(a.color, clampi(x0 - 1 + sx1, 0, W - 1), clampi(y0 - 1 + sy1, 0, H - 1)));
-        }
-    }
-
-    // 2. warp 0 places the history window at the tile's reference pixel (its
-    //    centre, clamped into the image) and thread 0 starts the TMA copy
-    const Img& hi = a.history;
-    const bool have_hist = hi.p != nullptr;
-    const bool windowed = have_hist && INTERP != 1;
-    if (windowed && tid < 32) {
-        const int rx = min(x0 + TX / 2, W - 1), ry = min(y0 + TY / 2, H - 1);
+    const TileIn<MC> in = load_tile_inputs<S, MC>(a, tile_x, tile_y);
+    const bool windowed = a.history.p != nullptr && INTERP != 1;
+    if (windowed && threadIdx.x < 32) {
+        // warp 0 places the window at the tile's reference pixel; thread 0 starts the copy
+        int rx, ry;
+        reference_pixel<S>(a, tile_x, tile_y, rx, ry);
         const float rdepth = __ldg(texel_ptr<float>(a.depth, rx, ry));
         const float4 rvs = fetch_velocity<MC>(a.velocity, rx, ry);
-        float ru = div_const_rn((float)rx + 0.5f, (float)W, a.inv_out_w);
-        float rv = div_const_rn((float)ry + 0.5f, (float)H, a.inv_out_h);
-        float rhu, rhv, rehd;
-        history_position<Pol, MC, HOT>(U, a, M, rx, ry, rvs, rdepth, ru, rv, rhu, rhv, rehd);
-        const int k0 = INTERP == 2 ? 1 : 0;  // Catmull-Rom starts one texel before floor(p - 0.5)
-        const int rux = trunc_index(floorf(rhu * (float)hi.w - 0.5f)) - k0;
-        const int ruy = trunc_index(floorf(rhv * (float)hi.h - 0.5f)) - k0;
-        // the reference pixel sits at (rx - x0, ry - y0) in the tile; floor to the stored alignment
-        const int wx0 = (rux - (rx - x0) - WIN_MARGIN) & ~(Win<S, HF>::ALIGN - 1);
-        const int wy0 = ruy - (ry - y0) - WIN_MARGIN;
-        const bool interior = wx0 >= 0 && wy0 >= 0 && wx0 <= hi.w - WWS && wy0 <= hi.h - WH;
-        const int mode = tma_ok && interior ? 1 : 2;
-        if (tid == 0) {
-            sm.org[0] = wx0;
-            sm.org[1] = wy0;
-            sm.org[2] = mode;
-            if (mode == 1) {
-                mbar_expect_tx(&sm.bar, (uint32_t)sizeof(sm.win));
-                if (HF == 0) tma_load_3d(sm.win, hmap, 0, wx0, wy0, &sm.bar);
-                else tma_load_2d(sm.win, hmap, 4 * wx0, wy0, &sm.bar);
-            }
-        }
+        place_window<Pol, S, HF, MC, INTERP, HOT>(U, a, Mode<HOT>{U.param[0]}, hmap, tma_ok, tile_x, tile_y, rdepth,
+                                                  rvs, sm.win, &sm.bar, sm.org, threadIdx.x == 0);
     }
-
-    // own history position; (u, v) = (texel + 0.5) / size, correctly rounded, as a pair
-    const f2 z{a.neg_zero2};
-    const f2 uv = div_const_rn2(add2(pk((float)cx, (float)cy), dup(0.5f)), pk(-(float)W, -(float)H),
-                                pk(a.inv_out_w, a.inv_out_h), z);
-    float u = f2lo(uv), v = f2hi(uv);
-    float hu, hv, ehd;
-    history_position<Pol, MC, HOT>(U, a, M, cx, cy, vs, depth, u, v, hu, hv, ehd);
-    float prev_depth = 0.f;
-    const bool depth_cull = P.mDepthCulling != 0;
-    if (depth_cull && a.history_depth.p) {
-        int tx_ = clampi(trunc_index(hu * (float)a.color.w), 0, a.color.w - 1);
-        int ty_ = clampi(trunc_index(hv * (float)a.color.h), 0, a.color.h - 1);
-        prev_depth = __ldg(texel_ptr<float>(a.history_depth, tx_, ty_));
-    }
-
-    // 3. staged colour in the policy's working format
-    const bool tm = M.tonemap(), yc = M.ycocg();
-    sm.col[tid] = Pol::stage(st0, tm, yc);
-    if (tid + NT < NS) sm.col[tid + NT] = Pol::stage(st1, tm, yc);
-    __syncthreads();
-    int wx0 = 0, wy0 = 0, mode = 0;
-    if (windowed) {
-        wx0 = sm.org[0];
-        wy0 = sm.org[1];
-        mode = sm.org[2];
-    }
-    if (mode == 2) {
-        // a window across the image border: every texel edge-clamped
-        const int lane = tid & 31, warp = tid >> 5;
-        for (int r = warp; r < WH; r += NT / 32) {
-            const int gy = clampi(wy0 + r, 0, hi.h - 1);
-            const char* row = hi.p + (size_t)gy * hi.pitch;
-            for (int c = lane; c < WWS; c += 32)
-                cp_async<HistTexel<HF>::B>(&sm.win[r * WWS + c],
-                                           row + (size_t)clampi(wx0 + c, 0, hi.w - 1) * HistTexel<HF>::B);
-        }
-        cp_async_commit();
-    }
-    // the 3x3 box while the window is in flight
-    typename Pol::Box box;
-    Pol::template box<HOT>(&sm.col[(ly + 1) * SX + lx + 1], SX, M, P.mVarClipGamma, box, z);
-    if (Pol::kExactCentre) Pol::centre_colour(box, a.color, cx, cy, tm, yc);
-
-    bool landed = true;
-    if (mode == 1) {
-        landed = mbar_wait_bounded(&sm.bar, phase & 1u);
-        if (!landed) {
-            atomicOr(a.status, kStatusWindowTimeout);
-            mbar_wait_bounded(&sm.bar, phase & 1u);  // the copy may still land in this CTA's memory
-            if (PERSIST) sm.abort = 1;
-        }
-        phase ^= 1u;
-    } else if (mode == 2) {
-        cp_async_wait_all();
-        __syncthreads();
-    }
-    const bool valid = inside && landed;
-    // rejection (taa.comp:787-823) first, so its inputs die before the filter
-    bool rejected = false;
-    if (P.mRejectOutside && (hu < 0.f || hv < 0.f || hu >= 1.f || hv >= 1.f)) rejected = true;
-    if (depth_cull) {
-        float hd = prev_depth;
-        if (fabsf(hd - ehd) > 0.1f * (1.0f - hd)) rejected = true;
-    }
-    // 4. history sample: from the window when all taps fall inside it
-    float4 hraw = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (valid) {
-        if (have_hist) {
-            HistoryTaps<Pol, INTERP> taps;
-            taps.setup(hu, hv, hi.w, hi.h, z);
-            const int span = INTERP == 2 ? 4 : 2;
-            const int bx = taps.t[0].ux - wx0, by = taps.t[0].uy - wy0;
-            const bool in_win = windowed && bx >= 0 && by >= 0 && bx + span <= WWS && by + span <= WH;
-            if (in_win) {
-                const HT* base = &sm.win[by * WWS + bx];
-                hraw = Pol::template filter_window<INTERP, HF>(taps, base, WWS);
-            } else {
-                hraw = Pol::template filter<INTERP>(
-                    taps, hi.w, hi.h, [&](int tx_, int ty_) { return fetch_history<HF>(hi, tx_, ty_); });
-            }
-        }
-    }
-    // 5. rectification, blend and stores: every thread of the CTA calls the
-    //    finisher (valid says whether its pixel is in the image and resolved)
-    const C3 c0 = Pol::centre(box, &sm.col[(ly + 1) * SX + lx + 1]);
-    Fin::template run<Pol, HF, HOT>(U, a, P, M, box, c0, hraw, u, v, hu, hv, ehd, prev_depth, rejected, valid, x, y,
-                                    tm, fin);
+    tile_compute<Pol, S, HF, MC, INTERP, HOT>(U, a, tile_x, tile_y, in, nullptr, sm.col, sm.win, &sm.bar, sm.org,
+                                              phase, PERSIST ? &sm.abort : nullptr, fin);
+    if (windowed && sm.org[2] == 1) phase ^= 1u;
 }
 
 // The finisher of the plain tiled forms: the policy's rectification and
@@ -477,6 +555,7 @@ cudaError_t launch_tile(const taa_uniforms_t& U, const FrameArgs& a, cudaStream_
     resolve_tile<Pol, S, HF, MC, INTERP, HOT><<<grid, S::NT, 0, s>>>(U, a, map, tma_ok);
     return cudaGetLastError();
 }
+
 template <class Pol, int HF, int MC>
 cudaError_t launch_interp(int interp, const taa_uniforms_t& U, const FrameArgs& a, cudaStream_t s) {
     const bool hot = is_hot(U.param[0]);
