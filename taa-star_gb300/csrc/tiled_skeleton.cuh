@@ -483,6 +483,171 @@ struct StoreFinish {
     }
 };
 
+// A tile of TX x (TYT * NPX) pixels resolved by TX x TYT threads, each taking
+// NPX vertically adjacent pixels (rows NPX * ly ... NPX * ly + NPX - 1); staged
+// with a 1-pixel halo, its history window spans the reference pixel's
+// Catmull-Rom taps widened by the tile and WIN_MARGIN on each side.
+#ifndef TAA_MULTI_MIN_BLOCKS
+#define TAA_MULTI_MIN_BLOCKS 4  // resident 256-thread CTAs per SM (64 registers)
+#endif
+template <int TX_, int TYT_, int NPX_> struct MultiShape {
+    static constexpr int TX = TX_, TYT = TYT_, NPX = NPX_, TY = TYT * NPX, NT = TX * TYT;
+    static constexpr int SX = TX + 2, SY = TY + 2, NS = SX * SY;
+    static constexpr int NSPT = (NS + NT - 1) / NT;  // staged texels per thread
+    static constexpr int WW = TX + 3 + 2 * WIN_MARGIN;
+    static constexpr int WH = TY + 3 + 2 * WIN_MARGIN;
+    static_assert(NT % 32 == 0 && NT <= 1024, "whole warps");
+};
+
+// One view, one CTA per multi-pixel tile: the steps of tile_compute with each
+// thread's NPX pixels interleaved.  Shared per thread: its index arithmetic,
+// the parameter reads, the staging share, the window origin and the wait;
+// per pixel: depth, velocity and history position, the previous-frame depth,
+// the 3x3 box, the history sample and the finisher (the same arithmetic as the
+// one-pixel kernels, so the same bits).
+template <class Pol, class S, int HF, int MC, int INTERP, bool HOT>
+__global__ void __launch_bounds__(S::NT, TAA_MULTI_MIN_BLOCKS * 256 / S::NT)
+    resolve_tile_multi(const taa_uniforms_t U, const FrameArgs a, const __grid_constant__ CUtensorMap hmap,
+                       const int tma_ok) {
+    using HT = typename HistTexel<HF>::T;
+    using RawVel = typename std::conditional<MC == 4, uint2, uint32_t>::type;
+    constexpr int TX = S::TX, NT = S::NT, NPX = S::NPX, SX = S::SX, NS = S::NS, WH = S::WH;
+    constexpr int WWS = Win<S, HF>::W;
+    __shared__ TileSmem<Pol, S, HF> sm;
+    const int tid = threadIdx.x;
+    if (tid == 0) mbar_init(&sm.bar, 1);
+    const taa_parameters_t& P = U.param[0];
+    const Mode<HOT> M{P};
+    const int tile_x = blockIdx.x, tile_y = blockIdx.y;
+    const int lx = tid % TX, ly = tid / TX;
+    const int W = a.out_w, H = a.out_h;
+    const int x0 = tile_x * TX, y0 = tile_y * S::TY;
+    const int x = x0 + lx, cx = min(x, W - 1);
+    // 1. loads: the pixels' depth and velocity, this thread's staged colour texels
+    float depth[NPX];
+    RawVel vel[NPX];
+#pragma unroll
+    for (int k = 0; k < NPX; ++k) {
+        const int cy = min(y0 + NPX * ly + k, H - 1);
+        depth[k] = __ldg(texel_ptr<float>(a.depth, cx, cy));
+        vel[k] = __ldg(texel_ptr<RawVel>(a.velocity, cx, cy));
+    }
+    uint2 st[S::NSPT];
+#pragma unroll
+    for (int j = 0; j < S::NSPT; ++j) {
+        const int i = tid + j * NT;
+        st[j] = make_uint2(0u, 0u);
+        if (i < NS) {
+            const int sy = i / SX, sx = i - sy * SX;
+            st[j] = __ldg(texel_ptr<uint2>(a.color, clampi(x0 - 1 + sx, 0, W - 1), clampi(y0 - 1 + sy, 0, H - 1)));
+        }
+    }
+    // 2. warp 0 places the history window; thread 0 starts the copy
+    const Img& hi = a.history;
+    const bool have_hist = hi.p != nullptr;
+    const bool windowed = have_hist && INTERP != 1;
+    if (windowed && tid < 32) {
+        int rx, ry;
+        reference_pixel<S>(a, tile_x, tile_y, rx, ry);
+        const float rdepth = __ldg(texel_ptr<float>(a.depth, rx, ry));
+        const float4 rvs = fetch_velocity<MC>(a.velocity, rx, ry);
+        place_window<Pol, S, HF, MC, INTERP, HOT>(U, a, M, &hmap, tma_ok != 0, tile_x, tile_y, rdepth, rvs, sm.win,
+                                                  &sm.bar, sm.org, tid == 0);
+    }
+    // 3. the pixels' history positions and previous-frame depths
+    const f2 z{a.neg_zero2};
+    const bool depth_cull = P.mDepthCulling != 0;
+    float u[NPX], v[NPX], hu[NPX], hv[NPX], ehd[NPX], prev_depth[NPX];
+#pragma unroll
+    for (int k = 0; k < NPX; ++k) {
+        const int cy = min(y0 + NPX * ly + k, H - 1);
+        const f2 uv = div_const_rn2(add2(pk((float)cx, (float)cy), dup(0.5f)), pk(-(float)W, -(float)H),
+                                    pk(a.inv_out_w, a.inv_out_h), z);
+        u[k] = f2lo(uv);
+        v[k] = f2hi(uv);
+        history_position<Pol, MC, HOT>(U, a, M, cx, cy, velocity_of<MC>(vel[k]), depth[k], u[k], v[k], hu[k], hv[k],
+                                       ehd[k]);
+        prev_depth[k] = 0.f;
+        if (depth_cull && a.history_depth.p) {
+            int tx_ = clampi(trunc_index(hu[k] * (float)a.color.w), 0, a.color.w - 1);
+            int ty_ = clampi(trunc_index(hv[k] * (float)a.color.h), 0, a.color.h - 1);
+            prev_depth[k] = __ldg(texel_ptr<float>(a.history_depth, tx_, ty_));
+        }
+    }
+    // 4. staged colour in the policy's working format
+    const bool tm = M.tonemap(), yc = M.ycocg();
+#pragma unroll
+    for (int j = 0; j < S::NSPT; ++j)
+        if (tid + j * NT < NS) sm.col[tid + j * NT] = Pol::stage(st[j], tm, yc);
+    __syncthreads();
+    int wx0 = 0, wy0 = 0, mode = 0;
+    if (windowed) {
+        wx0 = sm.org[0];
+        wy0 = sm.org[1];
+        mode = sm.org[2];
+    }
+    if (mode == 2) {
+        const int lane = tid & 31, warp = tid >> 5;
+        for (int r = warp; r < WH; r += NT / 32) {
+            const int gy = clampi(wy0 + r, 0, hi.h - 1);
+            const char* row = hi.p + (size_t)gy * hi.pitch;
+            for (int c = lane; c < WWS; c += 32)
+                cp_async<HistTexel<HF>::B>(&sm.win[r * WWS + c],
+                                           row + (size_t)clampi(wx0 + c, 0, hi.w - 1) * HistTexel<HF>::B);
+        }
+        cp_async_commit();
+    }
+    // 5. the boxes while the window is in flight
+    typename Pol::Box box[NPX];
+#pragma unroll
+    for (int k = 0; k < NPX; ++k) {
+        Pol::template box<HOT>(&sm.col[(NPX * ly + k + 1) * SX + lx + 1], SX, M, P.mVarClipGamma, box[k], z);
+        if (Pol::kExactCentre)
+            Pol::centre_colour(box[k], a.color, cx, min(y0 + NPX * ly + k, H - 1), tm, yc);
+    }
+    bool landed = true;
+    if (mode == 1) {
+        landed = mbar_wait_bounded(&sm.bar, 0u);
+        if (!landed) {
+            atomicOr(a.status, kStatusWindowTimeout);
+            mbar_wait_bounded(&sm.bar, 0u);  // the copy may still land in this CTA's memory
+        }
+    } else if (mode == 2) {
+        cp_async_wait_all();
+        __syncthreads();
+    }
+    // 6. per pixel: rejection, history sample, rectification, blend, stores
+    StoreFinish fin;
+#pragma unroll
+    for (int k = 0; k < NPX; ++k) {
+        const int y = y0 + NPX * ly + k;
+        const bool valid = x < W && y < H && landed;
+        bool rejected = false;
+        if (P.mRejectOutside && (hu[k] < 0.f || hv[k] < 0.f || hu[k] >= 1.f || hv[k] >= 1.f)) rejected = true;
+        if (depth_cull) {
+            const float hd = prev_depth[k];
+            if (fabsf(hd - ehd[k]) > 0.1f * (1.0f - hd)) rejected = true;
+        }
+        float4 hraw = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (valid && have_hist) {
+            HistoryTaps<Pol, INTERP> taps;
+            taps.setup(hu[k], hv[k], hi.w, hi.h, z);
+            const int span = INTERP == 2 ? 4 : 2;
+            const int bx = taps.t[0].ux - wx0, by = taps.t[0].uy - wy0;
+            const bool in_win = windowed && bx >= 0 && by >= 0 && bx + span <= WWS && by + span <= WH;
+            if (in_win) {
+                hraw = Pol::template filter_window<INTERP, HF>(taps, &sm.win[by * WWS + bx], WWS);
+            } else {
+                hraw = Pol::template filter<INTERP>(
+                    taps, hi.w, hi.h, [&](int tx_, int ty_) { return fetch_history<HF>(hi, tx_, ty_); });
+            }
+        }
+        const C3 c0 = Pol::centre(box[k], &sm.col[(NPX * ly + k + 1) * SX + lx + 1]);
+        StoreFinish::run<Pol, HF, HOT>(U, a, P, M, box[k], c0, hraw, u[k], v[k], hu[k], hv[k], ehd[k], prev_depth[k],
+                                       rejected, valid, x, y, tm, fin);
+    }
+}
+
 // One view, one CTA per tile.
 template <class Pol, class S, int HF, int MC, int INTERP, bool HOT>
 __global__ void __launch_bounds__(S::NT, S::MIN_BLOCKS)
@@ -544,15 +709,23 @@ __global__ void __launch_bounds__(S::NT, batch_min_blocks<S>())
     }
 }
 
+#ifndef TAA_TILE_NPX
+#define TAA_TILE_NPX 2  // pixels per thread of the single-view tiled forms
+#endif
+
 template <class Pol, int HF, int MC, int INTERP, bool HOT>
 cudaError_t launch_tile(const taa_uniforms_t& U, const FrameArgs& a, cudaStream_t s) {
-    using S = DefaultShape;
+    using S = typename std::conditional<TAA_TILE_NPX == 1, DefaultShape, MultiShape<32, 8, TAA_TILE_NPX>>::type;
     dim3 grid((a.out_w + S::TX - 1) / S::TX, (a.out_h + S::TY - 1) / S::TY);
     CUtensorMap map;
     std::memset(&map, 0, sizeof map);
     const int tma_ok = INTERP != 1 && a.history.p && a.history.w >= Win<S, HF>::W && a.history.h >= S::WH &&
                        encode_history_map(a.history, HF, Win<S, HF>::W, S::WH, &map);
-    resolve_tile<Pol, S, HF, MC, INTERP, HOT><<<grid, S::NT, 0, s>>>(U, a, map, tma_ok);
+    if (TAA_TILE_NPX == 1)
+        resolve_tile<Pol, DefaultShape, HF, MC, INTERP, HOT><<<grid, S::NT, 0, s>>>(U, a, map, tma_ok);
+    else
+        resolve_tile_multi<Pol, MultiShape<32, 8, TAA_TILE_NPX>, HF, MC, INTERP, HOT><<<grid, S::NT, 0, s>>>(U, a, map,
+                                                                                                        tma_ok);
     return cudaGetLastError();
 }
 
