@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-fxaa", action="store_true")
+    ap.add_argument("--no-modes", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--profile", choices=["tiled", "fp16", "plain", "batch48", "fxaa"],
                     help="a small case for ncu: a few launches of one form on 4K frames (no JSON line)")
@@ -340,6 +341,108 @@ def time_fxaa(T, WL, dev, stream, sid, args, peak, col, dep, mot, uniforms):
     return result
 
 
+def time_modes(T, WL, dev, stream, sid, args, peak):
+    """The resolve modes outside the benchmark mode: the ray-trace-assist
+    classification writing the segmentation mask (every test, history count 8)
+    in the tiled form (the form selected by default) and in the plain form, and
+    in the plain form (one thread per pixel) TAAU upsampling (1920x1080 source,
+    3840x2160 target) and a debug output.  Each on four rotating frames of the
+    C2 scene (every frame's bindings exceed the L2), CUDA events over 12
+    launches after 3.  Material ids and uv/normals are seeded synthetic blocks
+    (48 px materials, 8 px normals)."""
+    import math
+    import torch
+
+    out = {}
+
+    def frames(wl, n):
+        sc = wl.scene()
+        H, W = wl.height, wl.width
+        col = [torch.empty(H, W, 4, dtype=torch.float16, device=dev) for _ in range(n)]
+        dep = [torch.empty(H, W, dtype=torch.float32, device=dev) for _ in range(n)]
+        mot = [torch.empty(H, W, 2, dtype=torch.float16, device=dev) for _ in range(n)]
+        for f in range(n):
+            T.synth_render(sc, f, stream=sid, color=col[f], depth=dep[f], motion=mot[f])
+        return sc, col, dep, mot
+
+    def run(name, ctx, ulist, binds, bpp, px):
+        ctx.set_uniforms(ulist[0])
+        form = {T.TAA_FORM_PLAIN: "plain", T.TAA_FORM_TILED: "tiled", T.TAA_FORM_FP16: "fp16"}[ctx.selected_form()]
+        for i in range(3):
+            ctx.set_uniforms(ulist[i % len(ulist)])
+            ctx.resolve(stream=sid, **binds(i))
+        torch.cuda.synchronize()
+        k = 12
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(k):
+            ctx.set_uniforms(ulist[i % len(ulist)])
+            ctx.resolve(stream=sid, **binds(i))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        us = e0.elapsed_time(e1) * 1000 / k
+        gbs = bpp * px / (us / 1e6) / 1e9
+        out[name] = {"us_per_frame": us, "mpx_s": px / us, "bytes_per_px": bpp, "gb_s": gbs, "frac_of_hbm": gbs / peak,
+                     "form": form}
+
+    n = 4
+    wl = WL.c2()
+    H, W = wl.height, wl.width
+    sc, col, dep, mot = frames(wl, n + 1)
+    hist = [torch.zeros(H, W, 4, device=dev) for _ in range(2)]
+    res = torch.empty(H, W, 4, dtype=torch.float16, device=dev)
+    yy = torch.arange(H, device=dev, dtype=torch.int32).view(H, 1)
+    xx = torch.arange(W, device=dev, dtype=torch.int32).view(1, W)
+    mat = ((yy // 48) * 977 + (xx // 48) * 131) % 61 + 1
+    pmat = torch.roll(mat, 1, dims=1).contiguous()
+    g = torch.Generator(device=dev).manual_seed(7)
+    blk = torch.rand(H // 8 + 1, W // 8 + 1, 4, device=dev, generator=g)
+    uvn = blk.repeat_interleave(8, 0).repeat_interleave(8, 1)[:H, :W].contiguous()
+    uvn[..., 2] *= 2 * math.pi
+    uvn[..., 3] = uvn[..., 3] * 3.0 - 1.5
+    seg = [torch.zeros(H, W, dtype=torch.int32, device=dev) for _ in range(2)]
+
+    def base(i):
+        f = 1 + i % n
+        return dict(color=col[f], depth=dep[f], velocity=mot[f], history=hist[i & 1], history_depth=dep[f - 1],
+                    history_out=hist[(i + 1) & 1], result=res)
+
+    def u_for(f, **over):
+        p = wl.parameters()
+        for k_, v_ in over.items():
+            setattr(p, k_, v_)
+        return T.make_uniforms(p, jitter_ndc=T.synth_jitter(sc, f)[1])
+
+    rt = [u_for(1 + i, mRayTraceAugment=1, mRayTraceAugmentFlags=0x7F, mRayTraceHistoryCount=8) for i in range(n)]
+    rt_binds = lambda i: dict(base(i), material=mat, prev_material=pmat, uvnrm=uvn, prev_segmask=seg[i & 1],
+                              segmask=seg[(i + 1) & 1])
+    rt_bpp = wl.bytes_per_pixel(16, 4) + 4 + 4 + 16 + 4 + 4
+    ctx = T.Taa(W, H)
+    run("rt_augment_segmask", ctx, rt, rt_binds, rt_bpp, W * H)
+    ctx.close()
+    ctx = T.Taa(W, H, form=T.TAA_FORM_PLAIN)
+    run("rt_augment_segmask_plain", ctx, rt, rt_binds, rt_bpp, W * H)
+    dbg = torch.empty(H, W, 4, dtype=torch.float16, device=dev)
+    dm = [u_for(1 + i, mDebugMode=2, mDebugScale=1.0) for i in range(n)]
+    run("debug_output", ctx, dm, lambda i: dict(base(i), debug=dbg), wl.bytes_per_pixel(16, 4) + 8, W * H)
+    ctx.close()
+    del col, dep, mot, seg, mat, pmat, uvn, dbg
+
+    # TAAU: a 1920x1080 rendering of the same scene resolved into 3840x2160
+    lo = WL.Workload("C2 scene at 1920x1080", 1920, 1080, n + 1, seed=wl.seed, num_spheres=wl.num_spheres,
+                     cam_v0=(1.0, 0.0), cam_accel=(19.0 / 63.0, 0.0), radius=(10.0, 60.0), params=dict(wl.params))
+    sc, col, dep, mot = frames(lo, n + 1)
+    ctx = T.Taa(lo.width, lo.height, W, H, form=T.TAA_FORM_PLAIN)
+    up = [T.make_uniforms(lo.parameters(), jitter_ndc=T.synth_jitter(sc, 1 + i)[1], mUpsampling=1) for i in range(n)]
+    # per target pixel history in/out 16 + 16 and screen 8; per source pixel colour 8, depth 4, motion 4, previous depth 4
+    run("upsample_2x", ctx, up, base, 40 + 20 * (lo.width * lo.height) / (W * H), W * H)
+    out["upsample_2x"]["source"] = [lo.width, lo.height]
+    ctx.close()
+    out["note"] = ("TAAU and debug outputs run in the plain form only; "
+                   "bytes per target pixel count every binding once")
+    return out
+
+
 def ctypes_copy(dst, src):
     import ctypes as C
     C.memmove(C.addressof(dst), C.addressof(src), C.sizeof(dst))
@@ -501,6 +604,10 @@ def run_ours(args):
     # the 48-view batch (C4 sizes, log-uniform 320x180 .. 3840x2160): one launch per step
     if not args.no_batch:
         forms["batch48"] = time_batch(T, WL, dev, stream, sid, world, args, peak, mpx / world)
+
+    # the ray-trace-assist classification (tiled and plain), TAAU and debug output (plain form)
+    if not args.no_modes and rank == 0:
+        forms["modes"] = time_modes(T, WL, dev, stream, sid, args, peak)
 
     # the FXAA pass on the segmentation mask (ray-trace-assist path) at 4K
     if not args.no_fxaa and rank == 0:

@@ -12,6 +12,7 @@
 // form the tiled and FP16 forms are measured against.
 #include "common.cuh"
 #include "kernels.h"
+#include "segmentation.cuh"
 
 namespace taa_dev {
 namespace {
@@ -346,72 +347,26 @@ struct PlainResolver {
                            (fractf(s * 50849.4141f) * 2.0f - 1.0f) * f, (fractf(s * 12996.89f) * 2.0f - 1.0f) * f);
     }
 
-    // taa.comp:559-702
-    __device__ float lin_depth(int x, int y) const {
-        float n = U.mCamNearPlane, f = U.mCamFarPlane, d = fetch_r32f(a.depth, x, y);
-        return n * f / (f + d * (n - f));
-    }
-    __device__ float lum_at(int x, int y) const { return rgb_to_ycocg(rgb3(col(x, y))).x; }
-    __device__ V3 normal_at(int x, int y) const {
-        float4 u = fetch_rgba32f(a.uvnrm, x, y);
-        return {cosf(u.z) * cosf(u.w), sinf(u.z) * cosf(u.w), sinf(u.w)};
-    }
-    __device__ static V2 sobel(float c00, float c01, float c02, float c10, float c12, float c20, float c21, float c22) {
-        return {c00 - c20 + 2.0f * c01 - 2.0f * c21 + c02 - c22, c00 - c02 + 2.0f * c10 - 2.0f * c12 + c20 - c22};
-    }
+    // taa.comp:559-702 through segmentation.cuh, reading global memory
+    struct SegAccess {
+        const PlainResolver& r;
+        __device__ uint32_t material(int x, int y) const { return fetch_r32u(r.a.material, x, y); }
+        __device__ uint32_t prev_material(int x, int y) const { return fetch_r32u(r.a.prev_material, x, y); }
+        __device__ uint32_t prev_segmask(int x, int y) const { return fetch_r32u(r.a.prev_segmask, x, y); }
+        __device__ seg::N3 normal(int x, int y) const {
+            const float4 u = fetch_rgba32f(r.a.uvnrm, x, y);
+            return seg::normal_from(u.z, u.w);
+        }
+        __device__ float lin_depth(int x, int y) const {
+            return seg::lin_depth(fetch_r32f(r.a.depth, x, y), r.U.mCamNearPlane, r.U.mCamFarPlane);
+        }
+        __device__ float luma(int x, int y) const {
+            const float4 c = r.col(x, y);
+            return seg::luma(c.x, c.y, c.z);
+        }
+    };
     __device__ uint32_t segmentation(int ix, int iy, V2 hu) const {
-        const uint32_t fl = P->mRayTraceAugmentFlags;
-        auto cx = [&](int v) { return clampi(v, 0, loW - 1); };
-        auto cy = [&](int v) { return clampi(v, 0, loH - 1); };
-        if (fl & TAA_RTFLAG_FXD) {
-            const int b = 100;
-            if (ix < b || iy < b || ix >= loW - b || iy >= loH - b) return 1u;
-        }
-        if (fl & TAA_RTFLAG_ALL) return 2u;
-        bool cnt = (fl & TAA_RTFLAG_CNT) != 0;
-        uint32_t newc = cnt ? ((uint32_t)P->mRayTraceHistoryCount << 16) : 0u;
-        if (fl & TAA_RTFLAG_OUT) {
-            if (hu.x < 0.f || hu.y < 0.f || hu.x >= 1.f || hu.y >= 1.f) return 1u;
-        }
-        uint32_t mat = fetch_r32u(a.material, ix, iy);
-        if (fl & TAA_RTFLAG_DIS) {
-            int tx = trunc_index(hu.x * (float)loW), ty = trunc_index(hu.y * (float)loH);
-            if (tx >= 0 && ty >= 0 && tx < loW && ty < loH) {
-                uint32_t pm = fetch_r32u(a.prev_material, tx, ty);
-                if (pm != mat && (pm & 0x80000000u) != 0) return 2u | newc;
-            }
-        }
-        float nv = 0.f, dv = 0.f, mv = 0.f, lv = 0.f;
-        if (fl & TAA_RTFLAG_NRM) {
-            V3 nC = normal_at(ix, iy), nL = normal_at(cx(ix - 1), cy(iy)), nR = normal_at(cx(ix + 1), cy(iy));
-            V3 nT = normal_at(cx(ix), cy(iy - 1)), nB = normal_at(cx(ix), cy(iy + 1));
-            auto d3 = [](V3 p, V3 q) { return p.x * q.x + p.y * q.y + p.z * q.z; };
-            float m = gmax(0.f, gmin(gmin(gmin(d3(nC, nL), d3(nC, nR)), d3(nC, nT)), d3(nC, nB)));
-            nv = 1.0f - m;
-        }
-        if (fl & TAA_RTFLAG_DPT) {
-            auto L = [&](int dx, int dy) { return lin_depth(cx(ix + dx), cy(iy + dy)); };
-            V2 g = sobel(L(-1, -1), L(0, -1), L(1, -1), L(-1, 0), L(1, 0), L(-1, 1), L(0, 1), L(1, 1));
-            dv = sqrtf(g.x * g.x + g.y * g.y);
-        }
-        if (fl & TAA_RTFLAG_MID) {
-            if (mat != fetch_r32u(a.material, cx(ix - 1), cy(iy)) || mat != fetch_r32u(a.material, cx(ix + 1), cy(iy)) ||
-                mat != fetch_r32u(a.material, cx(ix), cy(iy - 1)) || mat != fetch_r32u(a.material, cx(ix), cy(iy + 1)))
-                mv = 1.0f;
-        }
-        if (fl & TAA_RTFLAG_LUM) {
-            auto L = [&](int dx, int dy) { return lum_at(cx(ix + dx), cy(iy + dy)); };
-            V2 g = sobel(L(-1, -1), L(0, -1), L(1, -1), L(-1, 0), L(1, 0), L(-1, 1), L(0, 1), L(1, 1));
-            lv = sqrtf(g.x * g.x + g.y * g.y);
-        }
-        float total = nv * P->mRayTraceAugment_WNrm + dv * P->mRayTraceAugment_WDpt + mv * P->mRayTraceAugment_WMId +
-                      lv * P->mRayTraceAugment_WLum;
-        if (total >= P->mRayTraceAugment_Thresh) return 2u | newc;
-        if (cnt) {
-            uint32_t old = (fetch_r32u(a.prev_segmask, ix, iy) & 0xffff0000u) >> 16;
-            if (old > 0) return 2u | ((old - 1) << 16);
-        }
-        return 0u;
+        return seg::classify(*P, ix, iy, hu.x, hu.y, loW, loH, SegAccess{*this});
     }
 
     // taa.comp:708-960

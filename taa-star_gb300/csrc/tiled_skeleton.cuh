@@ -36,6 +36,7 @@
 #include "common.cuh"
 #include "f32x2.cuh"
 #include "kernels.h"
+#include "segmentation.cuh"
 
 namespace taa_dev {
 namespace tiled {
@@ -149,7 +150,7 @@ template <bool Hot> struct Mode {
 };
 
 inline bool is_hot(const taa_parameters_t& P) {
-    return P.mUseYCoCg && !P.mToneMapLumaKaris && P.mVarianceClipping && !P.mShrinkChromaAxis &&
+    return P.mUseYCoCg && !P.mToneMapLumaKaris && P.mVarianceClipping && !P.mShrinkChromaAxis && !P.mRayTraceAugment &&
            P.mColorClampingOrClipping == 2 && P.mUseVelocityVectors == 2 && P.mVelocitySampleMode == 0 &&
            !P.mVelBasedAlpha && !P.mLumaWeightingLottes && !P.mReduceBlendNearClamp;
 }
@@ -499,13 +500,41 @@ template <int TX_, int TYT_, int NPX_> struct MultiShape {
     static_assert(NT % 32 == 0 && NT <= 1024, "whole warps");
 };
 
+// The neighbourhood the ray-trace-assist classification reads, staged for a
+// tile and its 1-pixel halo: material ids, view-space depth, normals and luma
+// (each computed once per texel instead of once per tap).
+template <class S, bool RT> struct SegStage {
+    uint32_t mat[S::NS];
+    float ldep[S::NS];
+    seg::N3 nrm[S::NS];
+    float lum[S::NS];
+};
+template <class S> struct SegStage<S, false> {};
+
+// segmentation.cuh's accessor over a staged tile whose first staged texel is
+// the image texel (x0 - 1, y0 - 1); coordinates come edge-clamped.
+template <class S> struct StagedSeg {
+    const SegStage<S, true>& st;
+    const FrameArgs& a;
+    int x0, y0;
+    __device__ int at(int x, int y) const { return (y - y0 + 1) * S::SX + (x - x0 + 1); }
+    __device__ uint32_t material(int x, int y) const { return st.mat[at(x, y)]; }
+    __device__ seg::N3 normal(int x, int y) const { return st.nrm[at(x, y)]; }
+    __device__ float lin_depth(int x, int y) const { return st.ldep[at(x, y)]; }
+    __device__ float luma(int x, int y) const { return st.lum[at(x, y)]; }
+    __device__ uint32_t prev_material(int x, int y) const { return fetch_r32u(a.prev_material, x, y); }
+    __device__ uint32_t prev_segmask(int x, int y) const { return fetch_r32u(a.prev_segmask, x, y); }
+};
+
 // One view, one CTA per multi-pixel tile: the steps of tile_compute with each
 // thread's NPX pixels interleaved.  Shared per thread: its index arithmetic,
 // the parameter reads, the staging share, the window origin and the wait;
 // per pixel: depth, velocity and history position, the previous-frame depth,
 // the 3x3 box, the history sample and the finisher (the same arithmetic as the
-// one-pixel kernels, so the same bits).
-template <class Pol, class S, int HF, int MC, int INTERP, bool HOT>
+// one-pixel kernels, so the same bits).  RT adds the ray-trace-assist
+// classification (segmentation.cuh) on a staged neighbourhood: a pixel it
+// marks is rejected, and the mask is stored when bound.
+template <class Pol, class S, int HF, int MC, int INTERP, bool HOT, bool RT>
 __global__ void __launch_bounds__(S::NT, TAA_MULTI_MIN_BLOCKS * 256 / S::NT)
     resolve_tile_multi(const taa_uniforms_t U, const FrameArgs a, const __grid_constant__ CUtensorMap hmap,
                        const int tma_ok) {
@@ -514,6 +543,7 @@ __global__ void __launch_bounds__(S::NT, TAA_MULTI_MIN_BLOCKS * 256 / S::NT)
     constexpr int TX = S::TX, NT = S::NT, NPX = S::NPX, SX = S::SX, NS = S::NS, WH = S::WH;
     constexpr int WWS = Win<S, HF>::W;
     __shared__ TileSmem<Pol, S, HF> sm;
+    __shared__ SegStage<S, RT> ss;
     const int tid = threadIdx.x;
     if (tid == 0) mbar_init(&sm.bar, 1);
     const taa_parameters_t& P = U.param[0];
@@ -574,11 +604,32 @@ __global__ void __launch_bounds__(S::NT, TAA_MULTI_MIN_BLOCKS * 256 / S::NT)
             prev_depth[k] = __ldg(texel_ptr<float>(a.history_depth, tx_, ty_));
         }
     }
-    // 4. staged colour in the policy's working format
+    // 4. staged colour in the policy's working format (and the classification's neighbourhood)
     const bool tm = M.tonemap(), yc = M.ycocg();
 #pragma unroll
     for (int j = 0; j < S::NSPT; ++j)
         if (tid + j * NT < NS) sm.col[tid + j * NT] = Pol::stage(st[j], tm, yc);
+    if constexpr (RT) {
+        const uint32_t fl = P.mRayTraceAugmentFlags;
+#pragma unroll
+        for (int j = 0; j < S::NSPT; ++j) {
+            const int i = tid + j * NT;
+            if (i >= NS) continue;
+            const int sy = i / SX, sx = i - sy * SX;
+            const int gx = clampi(x0 - 1 + sx, 0, W - 1), gy = clampi(y0 - 1 + sy, 0, H - 1);
+            if (fl & (TAA_RTFLAG_MID | TAA_RTFLAG_DIS)) ss.mat[i] = fetch_r32u(a.material, gx, gy);
+            if (fl & TAA_RTFLAG_DPT)
+                ss.ldep[i] = seg::lin_depth(fetch_r32f(a.depth, gx, gy), U.mCamNearPlane, U.mCamFarPlane);
+            if (fl & TAA_RTFLAG_NRM) {
+                const float4 un = fetch_rgba32f(a.uvnrm, gx, gy);
+                ss.nrm[i] = seg::normal_from(un.z, un.w);
+            }
+            if (fl & TAA_RTFLAG_LUM) {
+                const float4 c = half4_to_float4(st[j]);
+                ss.lum[i] = seg::luma(c.x, c.y, c.z);
+            }
+        }
+    }
     __syncthreads();
     int wx0 = 0, wy0 = 0, mode = 0;
     if (windowed) {
@@ -627,6 +678,13 @@ __global__ void __launch_bounds__(S::NT, TAA_MULTI_MIN_BLOCKS * 256 / S::NT)
         if (depth_cull) {
             const float hd = prev_depth[k];
             if (fabsf(hd - ehd[k]) > 0.1f * (1.0f - hd)) rejected = true;
+        }
+        if constexpr (RT) {
+            if (x < W && y < H) {
+                const uint32_t sg = seg::classify(P, x, y, hu[k], hv[k], W, H, StagedSeg<S>{ss, a, x0, y0});
+                if ((sg & 3u) != 0) rejected = true;
+                if (valid && a.segmask.p) *texel_ptr_w<uint32_t>(a.segmask, x, y) = sg;
+            }
         }
         float4 hraw = make_float4(0.f, 0.f, 0.f, 0.f);
         if (valid && have_hist) {
@@ -713,7 +771,7 @@ __global__ void __launch_bounds__(S::NT, batch_min_blocks<S>())
 #define TAA_TILE_NPX 2  // pixels per thread of the single-view tiled forms
 #endif
 
-template <class Pol, int HF, int MC, int INTERP, bool HOT>
+template <class Pol, int HF, int MC, int INTERP, bool HOT, bool RT = false>
 cudaError_t launch_tile(const taa_uniforms_t& U, const FrameArgs& a, cudaStream_t s) {
     using S = typename std::conditional<TAA_TILE_NPX == 1, DefaultShape, MultiShape<32, 8, TAA_TILE_NPX>>::type;
     dim3 grid((a.out_w + S::TX - 1) / S::TX, (a.out_h + S::TY - 1) / S::TY);
@@ -721,21 +779,30 @@ cudaError_t launch_tile(const taa_uniforms_t& U, const FrameArgs& a, cudaStream_
     std::memset(&map, 0, sizeof map);
     const int tma_ok = INTERP != 1 && a.history.p && a.history.w >= Win<S, HF>::W && a.history.h >= S::WH &&
                        encode_history_map(a.history, HF, Win<S, HF>::W, S::WH, &map);
-    if (TAA_TILE_NPX == 1)
+    if (TAA_TILE_NPX == 1 && !RT)
         resolve_tile<Pol, DefaultShape, HF, MC, INTERP, HOT><<<grid, S::NT, 0, s>>>(U, a, map, tma_ok);
     else
-        resolve_tile_multi<Pol, MultiShape<32, 8, TAA_TILE_NPX>, HF, MC, INTERP, HOT><<<grid, S::NT, 0, s>>>(U, a, map,
-                                                                                                        tma_ok);
+        resolve_tile_multi<Pol, MultiShape<32, 8, TAA_TILE_NPX>, HF, MC, INTERP, HOT, RT><<<grid, S::NT, 0, s>>>(
+            U, a, map, tma_ok);
     return cudaGetLastError();
 }
 
 template <class Pol, int HF, int MC>
 cudaError_t launch_interp(int interp, const taa_uniforms_t& U, const FrameArgs& a, cudaStream_t s) {
-    const bool hot = is_hot(U.param[0]);
+    const bool hot = is_hot(U.param[0]), rt = U.param[0].mRayTraceAugment != 0;
     switch (interp) {
-        case 0: return hot ? launch_tile<Pol, HF, MC, 0, true>(U, a, s) : launch_tile<Pol, HF, MC, 0, false>(U, a, s);
-        case 1: return hot ? launch_tile<Pol, HF, MC, 1, true>(U, a, s) : launch_tile<Pol, HF, MC, 1, false>(U, a, s);
-        default: return hot ? launch_tile<Pol, HF, MC, 2, true>(U, a, s) : launch_tile<Pol, HF, MC, 2, false>(U, a, s);
+        case 0:
+            return hot  ? launch_tile<Pol, HF, MC, 0, true>(U, a, s)
+                   : rt ? launch_tile<Pol, HF, MC, 0, false, true>(U, a, s)
+                        : launch_tile<Pol, HF, MC, 0, false>(U, a, s);
+        case 1:
+            return hot  ? launch_tile<Pol, HF, MC, 1, true>(U, a, s)
+                   : rt ? launch_tile<Pol, HF, MC, 1, false, true>(U, a, s)
+                        : launch_tile<Pol, HF, MC, 1, false>(U, a, s);
+        default:
+            return hot  ? launch_tile<Pol, HF, MC, 2, true>(U, a, s)
+                   : rt ? launch_tile<Pol, HF, MC, 2, false, true>(U, a, s)
+                        : launch_tile<Pol, HF, MC, 2, false>(U, a, s);
     }
 }
 

@@ -57,10 +57,10 @@ def gpu(key, form, dev):
              prev_segmask=t(g("prev_segmask").view(np.int32), torch.int32), uvnrm=t(g("uvnrm"), torch.float32),
              history_out=torch.full((oh, ow, 4), float("nan"), device=dev),
              result=torch.full((oh, ow, 4), float("nan"), dtype=torch.float16, device=dev),
-             # debug and segmask bindings route a call to the plain form, so only that form gets them
+             # a debug binding routes a call to the plain form, so only that form gets it
              debug=torch.full((oh, ow, 4), float("nan"), dtype=torch.float16, device=dev)
              if form == T.TAA_FORM_PLAIN else None,
-             segmask=torch.zeros((oh, ow), dtype=torch.int32, device=dev) if form == T.TAA_FORM_PLAIN else None)
+             segmask=torch.zeros((oh, ow), dtype=torch.int32, device=dev))
     used = ctx.selected_form()
     ctx.resolve(**b)
     torch.cuda.synchronize()
@@ -94,9 +94,19 @@ def test_plain_form_on_reference_fixtures(cuda, key):
 
 @pytest.mark.parametrize("key", CASES)
 def test_tiled_form_on_reference_fixtures(cuda, key):
-    used, hist, _ = gpu(key, T.TAA_FORM_TILED, cuda)
+    used, hist, seg = gpu(key, T.TAA_FORM_TILED, cuda)
     ref32 = FIX[f"{key}/ref32_history"].astype(np.float64)
     rel = np.linalg.norm(hist - ref32) / max(np.linalg.norm(ref32), 1e-30)
     assert rel <= rel_bound(key), (used, rel)
-    if used == T.TAA_FORM_TILED:
+    name = key.split(":")[1]
+    if name.startswith("segmask"):
+        # the ray-trace-assist classification runs in the tiled form on a staged
+        # neighbourhood: the plain form's bits (both call CUDA's sinf/cosf for the
+        # normals) and the reference's mask
+        assert used == T.TAA_FORM_TILED
+        _, phist, pseg = gpu(key, T.TAA_FORM_PLAIN, cuda)
+        np.testing.assert_array_equal(hist, phist)
+        np.testing.assert_array_equal(seg, pseg)
+        assert np.mean(seg == FIX[f"{key}/ref64_segmask"]) >= 0.99
+    elif used == T.TAA_FORM_TILED:
         np.testing.assert_array_equal(hist, oracle32(key)["history"].astype(np.float32))
