@@ -13,8 +13,8 @@ using tiled::Shape;
 
 // tile shapes by id (include/taa_gb300.h lists them for the tuning record)
 using S0 = Shape<32, 8>;
-using S1 = Shape<16, 16>;
-using S2 = Shape<32, 16>;
+using S1 = tiled::MultiShape<16, 8, 2>;  // 16x16, two pixels per thread
+using S2 = tiled::MultiShape<32, 8, 2>;  // 32x16, two pixels per thread
 using S3 = Shape<16, 8>;
 using S4 = Shape<8, 8>;
 

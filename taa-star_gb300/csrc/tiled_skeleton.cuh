@@ -52,7 +52,8 @@ constexpr int WIN_MARGIN = 3;  // motion difference (px) the history window abso
 // its history window spans the reference pixel's Catmull-Rom taps widened by
 // the tile and WIN_MARGIN on each side.
 template <int TX_, int TY_> struct Shape {
-    static constexpr int TX = TX_, TY = TY_, NT = TX * TY;
+    static constexpr int TX = TX_, TY = TY_, NT = TX * TY, NPX = 1;
+    static constexpr bool kMulti = false;  // one pixel per thread (tile_body)
     static constexpr int SX = TX + 2, SY = TY + 2, NS = SX * SY;
     static constexpr int WW = TX + 3 + 2 * WIN_MARGIN;
     static constexpr int WH = TY + 3 + 2 * WIN_MARGIN;
@@ -493,6 +494,7 @@ struct StoreFinish {
 #endif
 template <int TX_, int TYT_, int NPX_> struct MultiShape {
     static constexpr int TX = TX_, TYT = TYT_, NPX = NPX_, TY = TYT * NPX, NT = TX * TYT;
+    static constexpr bool kMulti = true;  // NPX pixels per thread (multi_body)
     static constexpr int SX = TX + 2, SY = TY + 2, NS = SX * SY;
     static constexpr int NSPT = (NS + NT - 1) / NT;  // staged texels per thread
     static constexpr int WW = TX + 3 + 2 * WIN_MARGIN;
@@ -526,29 +528,28 @@ template <class S> struct StagedSeg {
     __device__ uint32_t prev_segmask(int x, int y) const { return fetch_r32u(a.prev_segmask, x, y); }
 };
 
-// One view, one CTA per multi-pixel tile: the steps of tile_compute with each
-// thread's NPX pixels interleaved.  Shared per thread: its index arithmetic,
-// the parameter reads, the staging share, the window origin and the wait;
-// per pixel: depth, velocity and history position, the previous-frame depth,
-// the 3x3 box, the history sample and the finisher (the same arithmetic as the
-// one-pixel kernels, so the same bits).  RT adds the ray-trace-assist
-// classification (segmentation.cuh) on a staged neighbourhood: a pixel it
-// marks is rejected, and the mask is stored when bound.
-template <class Pol, class S, int HF, int MC, int INTERP, bool HOT, bool RT>
-__global__ void __launch_bounds__(S::NT, TAA_MULTI_MIN_BLOCKS * 256 / S::NT)
-    resolve_tile_multi(const taa_uniforms_t U, const FrameArgs a, const __grid_constant__ CUtensorMap hmap,
-                       const int tma_ok) {
-    using HT = typename HistTexel<HF>::T;
+// One multi-pixel tile: the steps of tile_compute with each thread's NPX
+// pixels interleaved.  Shared per thread: its index arithmetic, the parameter
+// reads, the staging share, the window origin and the wait; per pixel: depth,
+// velocity and history position, the previous-frame depth, the 3x3 box, the
+// history sample and the finisher (the same arithmetic as the one-pixel
+// kernels, so the same bits).  RT adds the ray-trace-assist classification
+// (segmentation.cuh) on a staged neighbourhood: a pixel it marks is rejected,
+// and the mask is stored when bound.  `sm.bar` is initialised by the caller;
+// `phase` is the barrier phase the next TMA copy completes.  A wait that gives
+// up sets the status bit and leaves the tile's pixels unwritten; in a
+// persistent loop (PERSIST) it also sets sm.abort, which the caller reads
+// after the barrier that separates tiles.
+template <class Pol, class S, int HF, int MC, int INTERP, bool HOT, bool RT, bool PERSIST>
+__device__ __forceinline__ void multi_body(const taa_uniforms_t& U, const FrameArgs& a, const CUtensorMap* hmap,
+                                           bool tma_ok, int tile_x, int tile_y, TileSmem<Pol, S, HF>& sm,
+                                           SegStage<S, RT>& ss, uint32_t& phase) {
     using RawVel = typename std::conditional<MC == 4, uint2, uint32_t>::type;
     constexpr int TX = S::TX, NT = S::NT, NPX = S::NPX, SX = S::SX, NS = S::NS, WH = S::WH;
     constexpr int WWS = Win<S, HF>::W;
-    __shared__ TileSmem<Pol, S, HF> sm;
-    __shared__ SegStage<S, RT> ss;
     const int tid = threadIdx.x;
-    if (tid == 0) mbar_init(&sm.bar, 1);
     const taa_parameters_t& P = U.param[0];
     const Mode<HOT> M{P};
-    const int tile_x = blockIdx.x, tile_y = blockIdx.y;
     const int lx = tid % TX, ly = tid / TX;
     const int W = a.out_w, H = a.out_h;
     const int x0 = tile_x * TX, y0 = tile_y * S::TY;
@@ -581,7 +582,7 @@ __global__ void __launch_bounds__(S::NT, TAA_MULTI_MIN_BLOCKS * 256 / S::NT)
         reference_pixel<S>(a, tile_x, tile_y, rx, ry);
         const float rdepth = __ldg(texel_ptr<float>(a.depth, rx, ry));
         const float4 rvs = fetch_velocity<MC>(a.velocity, rx, ry);
-        place_window<Pol, S, HF, MC, INTERP, HOT>(U, a, M, &hmap, tma_ok != 0, tile_x, tile_y, rdepth, rvs, sm.win,
+        place_window<Pol, S, HF, MC, INTERP, HOT>(U, a, M, hmap, tma_ok, tile_x, tile_y, rdepth, rvs, sm.win,
                                                   &sm.bar, sm.org, tid == 0);
     }
     // 3. the pixels' history positions and previous-frame depths
@@ -658,11 +659,13 @@ __global__ void __launch_bounds__(S::NT, TAA_MULTI_MIN_BLOCKS * 256 / S::NT)
     }
     bool landed = true;
     if (mode == 1) {
-        landed = mbar_wait_bounded(&sm.bar, 0u);
+        landed = mbar_wait_bounded(&sm.bar, phase & 1u);
         if (!landed) {
             atomicOr(a.status, kStatusWindowTimeout);
-            mbar_wait_bounded(&sm.bar, 0u);  // the copy may still land in this CTA's memory
+            mbar_wait_bounded(&sm.bar, phase & 1u);  // the copy may still land in this CTA's memory
+            if (PERSIST) sm.abort = 1;
         }
+        phase ^= 1u;
     } else if (mode == 2) {
         cp_async_wait_all();
         __syncthreads();
@@ -706,6 +709,20 @@ __global__ void __launch_bounds__(S::NT, TAA_MULTI_MIN_BLOCKS * 256 / S::NT)
     }
 }
 
+
+// One view, one CTA per multi-pixel tile.
+template <class Pol, class S, int HF, int MC, int INTERP, bool HOT, bool RT>
+__global__ void __launch_bounds__(S::NT, TAA_MULTI_MIN_BLOCKS * 256 / S::NT)
+    resolve_tile_multi(const taa_uniforms_t U, const FrameArgs a, const __grid_constant__ CUtensorMap hmap,
+                       const int tma_ok) {
+    __shared__ TileSmem<Pol, S, HF> sm;
+    __shared__ SegStage<S, RT> ss;
+    if (threadIdx.x == 0) mbar_init(&sm.bar, 1);
+    uint32_t phase = 0;
+    multi_body<Pol, S, HF, MC, INTERP, HOT, RT, false>(U, a, &hmap, tma_ok != 0, blockIdx.x, blockIdx.y, sm, ss,
+                                                        phase);
+}
+
 // One view, one CTA per tile.
 template <class Pol, class S, int HF, int MC, int INTERP, bool HOT>
 __global__ void __launch_bounds__(S::NT, S::MIN_BLOCKS)
@@ -722,10 +739,14 @@ __global__ void __launch_bounds__(S::NT, S::MIN_BLOCKS)
 #ifndef TAA_BATCH_MIN_BLOCKS
 #define TAA_BATCH_MIN_BLOCKS 4
 #endif
+// The same for the multi-pixel shapes, which hold more live state per thread
+// (3: up to 85 registers, measured fastest on the 48-view batch).
+#ifndef TAA_BATCH_MULTI_MIN_BLOCKS
+#define TAA_BATCH_MULTI_MIN_BLOCKS 3
+#endif
 template <class S> constexpr int batch_min_blocks() {
-    return TAA_BATCH_MIN_BLOCKS * 256 / S::NT < 1 ? 1
-                                                  : (TAA_BATCH_MIN_BLOCKS * 256 / S::NT > 32 ? 32
-                                                                                             : TAA_BATCH_MIN_BLOCKS * 256 / S::NT);
+    constexpr int b = (S::kMulti ? TAA_BATCH_MULTI_MIN_BLOCKS : TAA_BATCH_MIN_BLOCKS) * 256 / S::NT;
+    return b < 1 ? 1 : (b > 32 ? 32 : b);
 }
 
 // Many views in one launch: each CTA takes jobs blockIdx.x, blockIdx.x +
@@ -759,9 +780,16 @@ __global__ void __launch_bounds__(S::NT, batch_min_blocks<S>())
             cur_view = vi;
             __syncthreads();
         }
-        StoreFinish fin;
-        tile_body<Pol, S, HF, MC, INTERP, HOT, true>(s_view.U, s_view.a, maps + vi, __ldg(tma_ok + vi) != 0,
-                                                     job_tile_x(job), job_tile_y(job), sm, phase, fin);
+        if constexpr (S::kMulti) {
+            SegStage<S, false> none;
+            multi_body<Pol, S, HF, MC, INTERP, HOT, false, true>(s_view.U, s_view.a, maps + vi,
+                                                                  __ldg(tma_ok + vi) != 0, job_tile_x(job),
+                                                                  job_tile_y(job), sm, none, phase);
+        } else {
+            StoreFinish fin;
+            tile_body<Pol, S, HF, MC, INTERP, HOT, true>(s_view.U, s_view.a, maps + vi, __ldg(tma_ok + vi) != 0,
+                                                         job_tile_x(job), job_tile_y(job), sm, phase, fin);
+        }
         __syncthreads();  // the next tile reuses the shared memory
         if (sm.abort) return;
     }
