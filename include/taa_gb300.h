@@ -237,6 +237,36 @@ int taa_fxaa(taa_ctx* ctx, void* stream, const void* input, size_t input_pitch, 
 int taa_sharpen(void* stream, uint32_t sharpener, float factor, const void* input, size_t input_pitch, void* output,
                 size_t output_pitch, int32_t width, int32_t height);
 
+/* The post-process pass's push constants (push_constants_for_postprocess,
+ * source/taa.hpp:101-111; the same 84-byte layout). */
+typedef struct taa_post_process_params_t {
+    int32_t zoom_src_ltwh[4];  /* zoomSrcLTWH: left, top, width, height of the magnified box */
+    int32_t zoom_dst_ltwh[4];  /* zoomDstLTWH: the inset it is drawn into */
+    float debug_l_mask[4];     /* debugL_mask (param[0].mDebugMask): .w > 0 shows alpha in red and blue */
+    float debug_r_mask[4];     /* debugR_mask (param[1].mDebugMask) */
+    uint32_t zoom;             /* draw the inset */
+    uint32_t show_zoom_box;    /* outline the magnified box in red */
+    int32_t split_x;           /* column of the split line; -1: no split (the left side is the whole image) */
+    uint32_t debug_l_show;     /* left of the split: the debug image instead of the input (param[0].mDebugToScreenOutput) */
+    uint32_t debug_r_show;     /* right of the split (param[1].mDebugToScreenOutput) */
+} taa_post_process_params_t;
+
+/* Fill `out` with the reference's post-process settings for a width x height
+ * output: the struct's defaults (source/taa.hpp:101-111) with the zoom boxes
+ * that set_source_image_views derives from the size (source/taa.hpp:352-359). */
+int taa_post_process_default_params(int32_t width, int32_t height, taa_post_process_params_t* out);
+
+/* The post-process pass (shaders/post_process.comp, source/taa.hpp:1141-1158)
+ * from the last image of the chain (`input`, RGBA16F) and the resolve's debug
+ * image (`debug`, RGBA16F; may be NULL when neither debug_*_show is set) into
+ * `output` (RGBA16F), all width x height.  `output` must not overlap `input`
+ * or `debug`.  Box coordinates beyond +-2^24 are rejected (TAA_E_INVAL); the
+ * magnified box reads the input clamped to the image where it leaves it (the
+ * reference's texelFetch is undefined there).  Enqueued on `stream`. */
+int taa_post_process(void* stream, const taa_post_process_params_t* params, const void* input, size_t input_pitch,
+                     const void* debug, size_t debug_pitch, void* output, size_t output_pitch, int32_t width,
+                     int32_t height);
+
 /* ---- settings files ------------------------------------------------------ */
 
 /* The settings taa<CF> writes to and reads from its .ini file

@@ -37,6 +37,9 @@ def load():
         lib.oracle_sharpen.argtypes = [C.c_int, fp, C.c_int, C.c_int, C.c_float, dp, C.c_int]
         lib.oracle_fxaa.argtypes = [C.c_int, fp, up, C.c_int, C.c_int] + [C.c_float] * 5 + [dp, C.c_int]
         lib.oracle_cas_setup.argtypes = [C.c_float] * 5 + [up, up]
+        ip = C.POINTER(C.c_int)
+        lib.oracle_post_process.argtypes = [C.c_int, fp, fp, C.c_int, C.c_int, ip, ip, fp, fp] + [C.c_int] * 5 + \
+            [dp, C.c_int]
         lib.oracle_cas_setup.restype = None
         lib.oracle_halton.argtypes = [C.c_int, C.c_int]
         lib.oracle_halton.restype = C.c_float
@@ -146,6 +149,40 @@ def fxaa(img, segmask=None, subpix=0.75, edge_threshold=0.116, edge_threshold_mi
                          edge_threshold_min, _dp(out), nthreads or nthreads_default())
     if rc != 0:
         raise ValueError("oracle_fxaa rejected its arguments")
+    return out
+
+
+POST_DEFAULTS = dict(zoom_src=(950, 530, 20, 20), zoom_dst=(1710, 10, 200, 200), mask_l=(1.0, 1.0, 1.0, 0.0),
+                     mask_r=(1.0, 1.0, 1.0, 0.0), zoom=False, show_zoom_box=True, split_x=-1, show_l=False,
+                     show_r=False)
+
+
+def post_process(img, debug=None, precision=32, nthreads=None, **params):
+    """The post-process pass (shaders/post_process.comp) on an RGBA image and an
+    RGBA debug image: split line, zoom box and inset, debug image per side.
+    Parameters as POST_DEFAULTS (the push constants of source/taa.hpp:101-111);
+    returns the RGBA output unrounded."""
+    lib = load()
+    pp = dict(POST_DEFAULTS)
+    unknown = set(params) - set(pp)
+    if unknown:
+        raise TypeError(f"unknown post-process parameters {sorted(unknown)}")
+    pp.update(params)
+    a = _f32(img, 4)
+    h, w = a.shape[:2]
+    d = None if debug is None else _f32(debug, 4)
+    if d is not None and d.shape != a.shape:
+        raise ValueError("debug must match the image")
+    iv = lambda v: (C.c_int * 4)(*[int(x) for x in v])
+    fv = lambda v: np.ascontiguousarray(v, dtype=np.float32)
+    ml, mr = fv(pp["mask_l"]), fv(pp["mask_r"])
+    out = np.zeros((h, w, 4))
+    rc = lib.oracle_post_process(precision, _fp(a), _fp(d), w, h, iv(pp["zoom_src"]), iv(pp["zoom_dst"]), _fp(ml),
+                                 _fp(mr), int(bool(pp["zoom"])), int(bool(pp["show_zoom_box"])), int(pp["split_x"]),
+                                 int(bool(pp["show_l"])), int(bool(pp["show_r"])), _dp(out),
+                                 nthreads or nthreads_default())
+    if rc != 0:
+        raise ValueError("oracle_post_process rejected its arguments")
     return out
 
 

@@ -51,6 +51,24 @@ int oracle_fxaa(int precision, const float* in, const uint32_t* segmask, int w, 
     return fxaa(precision, in, segmask, w, h, rcp, subpix, thr, thr_min, out, nthreads);
 }
 
+int oracle_post_process(int precision, const float* in, const float* debug, int w, int h, const int* zoom_src,
+                        const int* zoom_dst, const float* mask_l, const float* mask_r, int zoom, int show_zoom_box,
+                        int split_x, int show_l, int show_r, double* out, int nthreads) {
+    PostParams pp{};
+    for (int i = 0; i < 4; ++i) {
+        pp.zoom_src[i] = zoom_src[i];
+        pp.zoom_dst[i] = zoom_dst[i];
+        pp.mask_l[i] = mask_l[i];
+        pp.mask_r[i] = mask_r[i];
+    }
+    pp.zoom = zoom;
+    pp.show_zoom_box = show_zoom_box;
+    pp.split_x = split_x;
+    pp.show_l = show_l;
+    pp.show_r = show_r;
+    return post_process(precision, in, debug, w, h, pp, out, nthreads);
+}
+
 void oracle_cas_setup(float s, float iw, float ih, float ow, float oh, uint32_t* c0, uint32_t* c1) {
     cas_setup(s, iw, ih, ow, oh, c0, c1);
 }

@@ -16,6 +16,8 @@ present (they are not built on the GPU machine).
     and shaders/antialias_fxaa.comp (which includes shaders/Fxaa3_11_mod.h
     from the reference tree as it lies) through the same shim, with the
     sampler snapping within 1/512 texel of a texel centre.
+  * libpost_ref32.so / libpost_ref64.so - shaders/post_process.comp (which
+    includes shaders/shader_cpu_common.h) through the same shim.
 """
 from __future__ import annotations
 
@@ -81,6 +83,17 @@ def build(force: bool = False):
         lib = OUT / name
         if force or not lib.exists() or lib.stat().st_mtime < max(p.stat().st_mtime for p in SHIM.iterdir()):
             _run([*fxaa_common, *flags, "-o", str(lib)])
+        libs[name] = lib
+    post = OUT / "post_process_comp.glsl.inc"
+    rewrite(SHADERS / "post_process.comp", post)
+    post_common = [cxx, "-O1", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+                   "-Wno-pedantic", "-I", str(SHIM), "-I", str(SHADERS), f'-DPOST_SOURCE="{post}"',
+                   str(SHIM / "post_ref_main.cpp")]
+    for name, flags in (("libpost_ref32.so", ["-DREAL=float", "-fsingle-precision-constant"]),
+                        ("libpost_ref64.so", ["-DREAL=double"])):
+        lib = OUT / name
+        if force or not lib.exists() or lib.stat().st_mtime < max(p.stat().st_mtime for p in SHIM.iterdir()):
+            _run([*post_common, *flags, "-o", str(lib)])
         libs[name] = lib
     cas = OUT / "libcas_ref.so"
     if force or not cas.exists():

@@ -1,8 +1,8 @@
 // glsl_shim.hpp - just enough GLSL, as C++, to compile the reference's
 // compute shaders (shaders/taa.comp, shaders/sharpen.comp,
 // shaders/antialias_fxaa_prepare.comp, shaders/antialias_fxaa.comp with
-// shaders/Fxaa3_11_mod.h) unmodified except for the mechanical rewrites
-// oracle/ref_build.py applies.
+// shaders/Fxaa3_11_mod.h, shaders/post_process.comp) unmodified except for
+// the mechanical rewrites oracle/ref_build.py applies.
 //
 // TEST INFRASTRUCTURE: it pins the oracle's restatement against the
 // reference's own shader source; nothing in the product uses it.
@@ -45,6 +45,10 @@ template <int N, class V, int... I> struct swz {
         const GReal src[] = {v[0], v[1], v[2], v[3]};
         int k = 0;
         ((d[I] = src[k++]), ...);
+        return *this;
+    }
+    swz& operator+=(GReal s) {
+        ((d[I] = d[I] + s), ...);
         return *this;
     }
 };
@@ -91,6 +95,7 @@ struct vec4 {
         swz<4, vec2, 0, 1> rg;
         swz<4, vec3, 0, 1, 2> xyz;
         swz<4, vec3, 0, 1, 2> rgb;
+        swz<4, vec2, 0, 2> rb;
     };
     vec4() : x(0), y(0), z(0), w(0) {}
     template <class A, if_arith<A> = 0> explicit vec4(A a) : x(GReal(a)), y(GReal(a)), z(GReal(a)), w(GReal(a)) {}
@@ -129,6 +134,21 @@ struct uvec4 {
     };
     uvec4() : x(0), y(0), z(0), w(0) {}
     template <class A, class B, class C, class D> uvec4(A a_, B b_, C c_, D d_) : x(uint(a_)), y(uint(b_)), z(uint(c_)), w(uint(d_)) {}
+};
+// an integer 4-vector with the two swizzles the shaders read (.xy, .zw)
+template <int A, int B> struct iswz {
+    int d[4];
+    operator ivec2() const { return ivec2(d[A], d[B]); }
+};
+struct ivec4 {
+    union {
+        struct { int x, y, z, w; };
+        int d[4];
+        iswz<0, 1> xy;
+        iswz<2, 3> zw;
+    };
+    ivec4() : x(0), y(0), z(0), w(0) {}
+    ivec4(int a_, int b_, int c_, int d_) : x(a_), y(b_), z(c_), w(d_) {}
 };
 inline ivec2::ivec2(const uvec2& v) : x(int(v.x)), y(int(v.y)) {}
 inline vec2::vec2(const ivec2& v) : x(GReal(v.x)), y(GReal(v.y)) {}
@@ -193,6 +213,15 @@ inline bool operator==(const ivec2& a, const ivec2& b) { return a.x == b.x && a.
 inline ivec2 min(const ivec2& a, const ivec2& b) { return ivec2(b.x < a.x ? b.x : a.x, b.y < a.y ? b.y : a.y); }
 inline ivec2 max(const ivec2& a, const ivec2& b) { return ivec2(a.x < b.x ? b.x : a.x, a.y < b.y ? b.y : a.y); }
 inline ivec2 clamp(const ivec2& x, const ivec2& lo, const ivec2& hi) { return min(max(x, lo), hi); }
+// mixed integer / float vectors: the integer operand converts to float (GLSL 4.60 4.1.10)
+inline vec2 operator+(const vec2& a, const ivec2& b) { return a + vec2(b); }
+inline vec2 operator+(const ivec2& a, const vec2& b) { return vec2(a) + b; }
+inline vec2 operator-(const vec2& a, const ivec2& b) { return a - vec2(b); }
+inline vec2 operator-(const ivec2& a, const vec2& b) { return vec2(a) - b; }
+inline vec2 operator*(const vec2& a, const ivec2& b) { return a * vec2(b); }
+inline vec2 operator*(const ivec2& a, const vec2& b) { return vec2(a) * b; }
+inline vec2 operator/(const vec2& a, const ivec2& b) { return a / vec2(b); }
+inline vec2 operator/(const ivec2& a, const vec2& b) { return vec2(a) / b; }
 
 // comparisons
 inline bvec2 lessThan(const vec2& a, const vec2& b) { return {a.x < b.x, a.y < b.y}; }

@@ -981,6 +981,71 @@ int fxaa(int precision, const float* in, const uint32_t* segmask, int w, int h, 
     return 0;
 }
 
+// shaders/post_process.comp:32-91, one output texel (x, y) inside the image.
+// texelFetch clamps to the image (the shader's zoom fetch stays inside for
+// source boxes inside the image; outside, Vulkan leaves it undefined).
+template <class R>
+void post_pixel(const float* in, const float* dbg, int w, int h, const PostParams& pp, int x, int y, double* o) {
+    auto put = [&](R r, R g, R b, R a) {
+        o[0] = double(r);
+        o[1] = double(g);
+        o[2] = double(b);
+        o[3] = double(a);
+    };
+    // the split-screen line (43-46)
+    if (x == pp.split_x) return put(R(0), R(0), R(0), R(0));
+    const int* zs = pp.zoom_src;
+    const int* zd = pp.zoom_dst;
+    // the border one texel outside the zoomed source box (49-54)
+    if (pp.zoom && pp.show_zoom_box) {
+        const bool col = (x == zs[0] - 1 || x == zs[0] + zs[2]) && y >= zs[1] - 1 && y <= zs[1] + zs[3];
+        const bool row = (y == zs[1] - 1 || y == zs[1] + zs[3]) && x >= zs[0] - 1 && x <= zs[0] + zs[2];
+        if (col || row) return put(R(1), R(0), R(0), R(0));
+    }
+    // the magnified inset: its border, else the texel it maps to in the source box (57-70)
+    int fx = x, fy = y;
+    if (pp.zoom && x >= zd[0] && y >= zd[1] && x < zd[0] + zd[2] && y < zd[1] + zd[3]) {
+        const bool col = (x == zd[0] || x == zd[0] + zd[2] - 1) && y >= zd[1] && y <= zd[1] + zd[3] - 1;
+        const bool row = (y == zd[1] || y == zd[1] + zd[3] - 1) && x >= zd[0] && x <= zd[0] + zd[2] - 1;
+        if (col || row) return put(R(1), R(1), R(1), R(0));
+        const R ux = (R(x - zd[0]) + R(0.5)) / R(zd[2]);
+        const R uy = (R(y - zd[1]) + R(0.5)) / R(zd[3]);
+        fx = int(R(zs[0]) + ux * R(zs[2]));  // int() truncates toward zero, as GLSL's ivec2(vec2)
+        fy = int(R(zs[1]) + uy * R(zs[3]));
+    }
+    fx = std::min(std::max(fx, 0), w - 1);
+    fy = std::min(std::max(fy, 0), h - 1);
+    const size_t i = ((size_t)fy * w + fx) * 4;
+    // the debug image or the input, by the side of the split (73-89)
+    const bool left = pp.split_x < 0 || x < pp.split_x;
+    const bool show = left ? pp.show_l != 0 : pp.show_r != 0;
+    const float* mask = left ? pp.mask_l : pp.mask_r;
+    if (show) {
+        R r = R(dbg[i]), g = R(dbg[i + 1]), b = R(dbg[i + 2]);
+        const R a = R(dbg[i + 3]);
+        if (R(mask[3]) > R(0)) {  // the alpha channel made visible in red and blue
+            r = r + a;
+            b = b + a;
+        }
+        return put(r, g, b, R(1));
+    }
+    put(R(in[i]), R(in[i + 1]), R(in[i + 2]), R(in[i + 3]));
+}
+
+int post_process(int precision, const float* in, const float* debug, int w, int h, const PostParams& pp, double* out,
+                 int nthreads) {
+    if (!in || !out || w <= 0 || h <= 0) return -1;
+    if (!debug && (pp.show_l || pp.show_r)) return -1;
+    parallel_rows(h, nthreads, [&](int y) {
+        for (int x = 0; x < w; ++x) {
+            double* o = out + ((size_t)y * w + x) * 4;
+            if (precision == 64) post_pixel<double>(in, debug, w, h, pp, x, y, o);
+            else post_pixel<float>(in, debug, w, h, pp, x, y, o);
+        }
+    });
+    return 0;
+}
+
 // ffx_cas.h:375-394 with ffx_a.h's CPU helpers: ARcpF1(a) = 1/a,
 // ALerpF1(a,b,c) = b*c + (-a*c + a), ASatF1 = clamp to [0,1].
 void cas_setup(float sharpness, float in_w, float in_h, float out_w, float out_h, uint32_t const0[4],

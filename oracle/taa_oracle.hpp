@@ -88,6 +88,19 @@ int sharpen(int precision, const float* in, int w, int h, float factor, double* 
 int fxaa(int precision, const float* in, const uint32_t* segmask, int w, int h, const float rcp_frame[2],
          float subpix, float edge_threshold, float edge_threshold_min, double* out, int nthreads);
 
+// The post-process pass (shaders/post_process.comp; push constants of
+// source/taa.hpp:101-111): split line, zoom box and inset, debug image per side
+// of the split (its alpha made visible in red and blue when the side's mask .w
+// is positive).  `debug` may be NULL when neither side shows it.  precision 32
+// or 64.
+struct PostParams {
+    int zoom_src[4], zoom_dst[4];  // left, top, width, height
+    float mask_l[4], mask_r[4];
+    int zoom, show_zoom_box, split_x, show_l, show_r;
+};
+int post_process(int precision, const float* in, const float* debug, int w, int h, const PostParams& pp, double* out,
+                 int nthreads);
+
 // CasSetup, restated (ffx_cas.h:375-394).
 void cas_setup(float sharpness, float in_w, float in_h, float out_w, float out_h,
                uint32_t const0[4], uint32_t const1[4]);

@@ -36,6 +36,7 @@ UNITS = {
     "batch_tiled.cu": ["-fmad=false"],
     "learned.cu": ["-fmad=false"],
     "fxaa.cu": ["-fmad=false"],
+    "post_process.cu": ["-fmad=false"],
     "synth.cu": [],
     "static_scratch.cu": [],
     "device_state.cu": [],

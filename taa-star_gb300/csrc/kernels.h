@@ -47,6 +47,17 @@ cudaError_t launch_sharpen(int sharpener, const FrameArgs& a, cudaStream_t strea
 cudaError_t launch_fxaa(const Img& in, const Img& segmask, const ImgW& out, const float rcp[2], float subpix,
                         float edge_threshold, float edge_threshold_min, uint32_t* list, cudaStream_t stream);
 
+// The post-process pass (post_process.cu) on RGBA16F images of w x h texels.
+struct PostArgs {
+    Img in, debug;  // debug.p may be null when neither side shows it
+    ImgW out;
+    int w, h;
+    int zoom_src[4], zoom_dst[4];  // left, top, width, height
+    float mask_l_w, mask_r_w;      // .w of each side's debug mask
+    int zoom, show_zoom_box, split_x, show_l, show_r;
+};
+cudaError_t launch_post_process(const PostArgs& a, cudaStream_t stream);
+
 // Device address and size of the fixed screen buffer of static_scratch.cu on
 // the current device (looked up once per device).
 cudaError_t static_screen_scratch(void** address, size_t* bytes);

@@ -1,7 +1,8 @@
 // post_api.cpp - the passes that follow the resolve in the reference's frame
-// (source/taa.hpp:1028-1139): FXAA on the segmentation mask and the sharpen
-// pass on its own.  Validation and launch only; the kernels are in fxaa.cu
-// and resolve_fast.cu.
+// (source/taa.hpp:1028-1158): FXAA on the segmentation mask, the sharpen pass
+// on its own and the post-process visualisation.  Validation and launch only;
+// the kernels are in fxaa.cu, resolve_fast.cu and post_process.cu.
+#include <cmath>
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -91,6 +92,79 @@ int taa_sharpen(void* stream, uint32_t sharpener, float factor, const void* inpu
     a.cas_peak_bits = c1[0];
     a.sharpen_factor = factor;
     cudaError_t e = taa_dev::launch_sharpen((int)sharpener, a, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, who);
+    return ok();
+}
+
+static_assert(sizeof(taa_post_process_params_t) == 84, "push_constants_for_postprocess is 84 bytes");
+
+// push_constants_for_postprocess (source/taa.hpp:101-111) and the zoom boxes of
+// set_source_image_views (source/taa.hpp:352-359; w is unsigned there)
+int taa_post_process_default_params(int32_t width, int32_t height, taa_post_process_params_t* out) {
+    if (!out) return fail(TAA_E_INVAL, "taa_post_process_default_params: NULL argument");
+    int rc;
+    if ((rc = check_size(width, height, "taa_post_process_default_params"))) return rc;
+    const uint32_t w = (uint32_t)width, h = (uint32_t)height;
+    const int src = (int)std::round((float)w / 96.f);
+    const int dst = (int)std::round((float)w / 9.6f);
+    const int brd = (int)std::round((float)w / (96.f * 2.f));
+    const int32_t zs[4] = {(int32_t)((w - (uint32_t)src) / 2u), (int32_t)((h - (uint32_t)src) / 2u), src, src};
+    const int32_t zd[4] = {(int32_t)(w - (uint32_t)dst - (uint32_t)brd), brd, dst, dst};
+    for (int i = 0; i < 4; ++i) {
+        out->zoom_src_ltwh[i] = zs[i];
+        out->zoom_dst_ltwh[i] = zd[i];
+        out->debug_l_mask[i] = out->debug_r_mask[i] = i < 3 ? 1.f : 0.f;
+    }
+    out->zoom = 0;
+    out->show_zoom_box = 1;
+    out->split_x = -1;
+    out->debug_l_show = 0;
+    out->debug_r_show = 0;
+    return ok();
+}
+
+// source/taa.hpp:1141-1158: the post-process dispatch.
+int taa_post_process(void* stream, const taa_post_process_params_t* params, const void* input, size_t input_pitch,
+                     const void* debug, size_t debug_pitch, void* output, size_t output_pitch, int32_t width,
+                     int32_t height) {
+    static const char* who = "taa_post_process";
+    int rc;
+    if ((rc = check_size(width, height, who))) return rc;
+    if (!params) return fail(TAA_E_INVAL, "%s: NULL params", who);
+    const taa_post_process_params_t& p = *params;
+    const int32_t lim = 1 << 24;
+    for (int i = 0; i < 4; ++i)
+        if (p.zoom_src_ltwh[i] < -lim || p.zoom_src_ltwh[i] > lim || p.zoom_dst_ltwh[i] < -lim ||
+            p.zoom_dst_ltwh[i] > lim)
+            return fail(TAA_E_INVAL, "%s: zoom box coordinates beyond +-2^24", who);
+    if (std::isnan(p.debug_l_mask[3]) || std::isnan(p.debug_r_mask[3]))
+        return fail(TAA_E_INVAL, "%s: debug mask .w is NaN", who);
+    const bool need_debug = p.debug_l_show || p.debug_r_show;
+    const char *ilo = nullptr, *ihi = nullptr, *dlo = nullptr, *dhi = nullptr, *olo = nullptr, *ohi = nullptr;
+    if ((rc = check_image("input", input, input_pitch, width, height, 8, true, &ilo, &ihi))) return rc;
+    if ((rc = check_image("debug", debug, debug_pitch, width, height, 8, need_debug, &dlo, &dhi))) return rc;
+    if ((rc = check_image("output", output, output_pitch, width, height, 8, true, &olo, &ohi))) return rc;
+    if (overlaps(ilo, ihi, olo, ohi)) return fail(TAA_E_INVAL, "%s: output overlaps input", who);
+    if (debug && overlaps(dlo, dhi, olo, ohi)) return fail(TAA_E_INVAL, "%s: output overlaps debug", who);
+    taa_dev::PostArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.in = Img{(const char*)input, input_pitch, width, height};
+    a.debug = Img{(const char*)debug, debug_pitch, width, height};
+    a.out = ImgW{(char*)output, output_pitch};
+    a.w = width;
+    a.h = height;
+    for (int i = 0; i < 4; ++i) {
+        a.zoom_src[i] = p.zoom_src_ltwh[i];
+        a.zoom_dst[i] = p.zoom_dst_ltwh[i];
+    }
+    a.mask_l_w = p.debug_l_mask[3];
+    a.mask_r_w = p.debug_r_mask[3];
+    a.zoom = p.zoom != 0;
+    a.show_zoom_box = p.show_zoom_box != 0;
+    a.split_x = p.split_x;
+    a.show_l = p.debug_l_show != 0;
+    a.show_r = p.debug_r_show != 0;
+    cudaError_t e = taa_dev::launch_post_process(a, (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(e, who);
     return ok();
 }

@@ -108,6 +108,13 @@ class FxaaParams(C.Structure):
     _fields_ = [("subpix", C.c_float), ("edge_threshold", C.c_float), ("edge_threshold_min", C.c_float)]
 
 
+class PostProcessParams(C.Structure):
+    """taa_post_process_params_t: the post-process pass's push constants."""
+    _fields_ = [("zoom_src_ltwh", C.c_int32 * 4), ("zoom_dst_ltwh", C.c_int32 * 4), ("debug_l_mask", C.c_float * 4),
+                ("debug_r_mask", C.c_float * 4), ("zoom", C.c_uint32), ("show_zoom_box", C.c_uint32),
+                ("split_x", C.c_int32), ("debug_l_show", C.c_uint32), ("debug_r_show", C.c_uint32)]
+
+
 SETTINGS_MAX_SAMPLE_OFFSETS = 64
 
 
@@ -151,6 +158,7 @@ assert C.sizeof(Parameters) == 176 and C.sizeof(Uniforms) == 544
 # Every symbol include/taa_gb300.h and include/taa_synth.h declare.
 EXPORTS = ["taa_version", "taa_last_error", "taa_default_parameters", "taa_get_jitter_offset",
            "taa_get_jitter_offset_custom", "taa_fxaa_default_params", "taa_fxaa", "taa_sharpen",
+           "taa_post_process_default_params", "taa_post_process",
            "taa_settings_default", "taa_settings_write_ini", "taa_settings_read_ini",
            "taa_jittered_projection", "taa_compose_matrices", "taa_cas_setup", "taa_create", "taa_destroy",
            "taa_set_uniforms", "taa_set_sharpener", "taa_selected_form", "taa_resolve",
@@ -188,6 +196,9 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
                                C.c_size_t, C.c_int32, C.c_int32, P(FxaaParams)]),
         "taa_sharpen": (C.c_int, [C.c_void_p, C.c_uint32, C.c_float, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t,
                                   C.c_int32, C.c_int32]),
+        "taa_post_process_default_params": (C.c_int, [C.c_int32, C.c_int32, P(PostProcessParams)]),
+        "taa_post_process": (C.c_int, [C.c_void_p, P(PostProcessParams), C.c_void_p, C.c_size_t, C.c_void_p,
+                                       C.c_size_t, C.c_void_p, C.c_size_t, C.c_int32, C.c_int32]),
         "taa_settings_default": (C.c_int, [P(Settings)]),
         "taa_settings_write_ini": (C.c_int, [P(Settings), C.c_char_p, C.c_size_t, P(C.c_size_t)]),
         "taa_settings_read_ini": (C.c_int, [P(Settings), C.c_char_p, C.c_size_t]),
@@ -287,6 +298,22 @@ def sharpen(input, output, sharpener: int, factor: float, stream: int = 0):
     op, opitch = tensor_ptr_pitch(output)
     check(load().taa_sharpen(C.c_void_p(stream), sharpener, factor, C.c_void_p(ip), ipitch, C.c_void_p(op), opitch,
                              w, h))
+
+
+def post_process_default_params(w: int, h: int) -> PostProcessParams:
+    p = PostProcessParams()
+    check(load().taa_post_process_default_params(w, h, C.byref(p)))
+    return p
+
+
+def post_process(input, output, params: PostProcessParams, debug=None, stream: int = 0):
+    """taa_post_process on (H, W, 4) FP16 tensors (debug may be None when no side shows it)."""
+    h, w = int(input.shape[0]), int(input.shape[1])
+    ip, ipitch = tensor_ptr_pitch(input)
+    op, opitch = tensor_ptr_pitch(output)
+    dp, dpitch = tensor_ptr_pitch(debug) if debug is not None else (None, 0)
+    check(load().taa_post_process(C.c_void_p(stream), C.byref(params), C.c_void_p(ip), ipitch, C.c_void_p(dp), dpitch,
+                                  C.c_void_p(op), opitch, w, h))
 
 
 def jitter_offset_custom(offsets_px, frame: int, w: int, h: int, opts: JitterOpts | None = None):

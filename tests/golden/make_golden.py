@@ -18,8 +18,13 @@ reference code computes:
                         shaders/antialias_fxaa.comp with Fxaa3_11_mod.h, on a
                         rendered frame with three segmentation masks (FP64 and
                         FP32)
+  post_golden.npz       shaders/post_process.comp on a seeded RGBA16F image and
+                        debug image for seven push-constant sets (split line,
+                        debug on either side with and without its alpha shown,
+                        zoom box and inset, the size-derived defaults of
+                        source/taa.hpp:352-359) (FP64 and FP32)
 
-Usage: python tests/golden/make_golden.py [taa] [cas] [sharpen] [fxaa]   (default: all)
+Usage: python tests/golden/make_golden.py [taa] [cas] [sharpen] [fxaa] [post]   (default: all)
 """
 from __future__ import annotations
 
@@ -119,7 +124,7 @@ def main():
     def u32(a):
         return np.ascontiguousarray(a, np.uint32).ctypes.data_as(up)
 
-    which = set(sys.argv[1:]) or {"taa", "cas", "sharpen", "fxaa"}
+    which = set(sys.argv[1:]) or {"taa", "cas", "sharpen", "fxaa", "post"}
     if "taa" in which:
         make_taa(ref, f, u32, dp, up)
     if "cas" in which:
@@ -128,6 +133,8 @@ def main():
         make_sharpen(ref, f, dp)
     if "fxaa" in which:
         make_fxaa(libs, fp, dp, up)
+    if "post" in which:
+        make_post(libs, fp, dp)
 
 
 def make_taa(ref, f, u32, dp, up):
@@ -245,6 +252,52 @@ def make_fxaa(libs, fp, dp, up):
             out[f"{name}/ref{prec}"] = res if prec == 64 else res.astype(np.float32)
     np.savez_compressed(HERE / "fxaa_golden.npz", **out)
     print(f"fxaa fixture written to {HERE}")
+
+
+POST_CASES = {
+    "defaults": dict(),
+    "split_debug_left_alpha": dict(split_x=36, show_l=True, mask_l=(1.0, 1.0, 1.0, 1.0)),
+    "split_debug_right": dict(split_x=20, show_r=True, mask_r=(0.0, 1.0, 0.0, 0.0)),
+    "zoom_box": dict(zoom=True, zoom_src=(10, 8, 7, 5), zoom_dst=(40, 20, 25, 18)),
+    "zoom_no_box_split": dict(zoom=True, show_zoom_box=False, zoom_src=(3, 4, 9, 9), zoom_dst=(50, 25, 16, 16),
+                              split_x=30, show_l=True, mask_l=(1.0, 1.0, 1.0, 0.5)),
+    "zoom_debug_both_sides": dict(zoom=True, zoom_src=(60, 30, 6, 6), zoom_dst=(2, 2, 30, 30), split_x=50,
+                                  show_l=True, show_r=True, mask_r=(1.0, 1.0, 1.0, 1.0)),
+    # source/taa.hpp:352-359 at 72 x 48: zoom source (35, 23, 1, 1), inset (65, 0, 7, 7) (72 / 9.6f < 7.5)
+    "size_defaults_zoom": dict(zoom=True, zoom_src=(35, 23, 1, 1), zoom_dst=(65, 0, 7, 7)),
+}
+
+
+def make_post(libs, fp, dp):
+    ip = C.POINTER(C.c_int)
+    ref = {}
+    for prec in (32, 64):
+        lib = C.CDLL(str(libs[f"libpost_ref{prec}.so"]))
+        lib.ref_post_process.argtypes = [fp, fp, C.c_int, C.c_int, ip, ip, fp, fp] + [C.c_int] * 5 + [dp]
+        ref[prec] = lib
+    w, h = 72, 48
+    rng = np.random.default_rng(17)
+    img = np.ascontiguousarray(rng.uniform(0.0, 4.0, (h, w, 4)).astype(np.float16).astype(np.float32))
+    dbg = np.ascontiguousarray(rng.uniform(-1.0, 2.0, (h, w, 4)).astype(np.float16).astype(np.float32))
+    out = dict(image=img, debug=dbg)
+    for name, over in POST_CASES.items():
+        pp = dict(O.POST_DEFAULTS)
+        pp.update(over)
+        out[f"{name}/params"] = np.array(json.dumps({k: list(v) if isinstance(v, tuple) else v for k, v in pp.items()}))
+        iv = lambda v: (C.c_int * 4)(*v)
+        fv = lambda v: np.ascontiguousarray(v, np.float32)
+        ml, mr = fv(pp["mask_l"]), fv(pp["mask_r"])
+        for prec in (64, 32):
+            res = np.zeros((h, w, 4))
+            ref[prec].ref_post_process(img.ctypes.data_as(fp), dbg.ctypes.data_as(fp), w, h, iv(pp["zoom_src"]),
+                                       iv(pp["zoom_dst"]), ml.ctypes.data_as(fp), mr.ctypes.data_as(fp),
+                                       int(pp["zoom"]), int(pp["show_zoom_box"]), int(pp["split_x"]),
+                                       int(pp["show_l"]), int(pp["show_r"]), res.ctypes.data_as(dp))
+            # every FP64 output here is a float32 value (copied half texels, 0/1, half + half)
+            r32 = res.astype(np.float32)
+            out[f"{name}/ref{prec}"] = r32 if np.array_equal(r32.astype(np.float64), res) else res
+    np.savez_compressed(HERE / "post_golden.npz", **out)
+    print(f"post-process fixture written to {HERE}")
 
 
 if __name__ == "__main__":

@@ -16,7 +16,9 @@ no reference tree: they hold the oracle's restatement to
   * FXAA (shaders/antialias_fxaa_prepare.comp then shaders/antialias_fxaa.comp
     with Fxaa3_11_mod.h, through an RGBA16F image): the FP64 oracle equals the
     shader in double exactly; the FP32 oracle (sampler positions in float, the
-    shader's in double) agrees on all but a handful of pixels.
+    shader's in double) agrees on all but a handful of pixels;
+  * the post-process pass (shaders/post_process.comp): the FP32 and FP64
+    oracle equal the shader exactly for every push-constant case.
 """
 import ctypes as C
 import json
@@ -134,3 +136,36 @@ def test_fxaa_fixture_exercises_the_edge_paths():
         assert changed.mean() >= lo
         marked = (FXAA[f"{mask}/segmask"] & 3) == 1
         assert not np.any(changed & ~marked)
+
+
+POST = np.load(G / "post_golden.npz")
+POST_CASES = sorted({k.split("/")[0] for k in POST.files if "/" in k})
+
+
+def post_params(name):
+    pp = json.loads(str(POST[f"{name}/params"]))
+    return {k: tuple(v) if isinstance(v, list) else v for k, v in pp.items()}
+
+
+@pytest.mark.parametrize("name", POST_CASES)
+def test_post_process_oracle_matches_the_reference_shader(name):
+    pp = post_params(name)
+    for prec in (64, 32):
+        got = O.post_process(POST["image"], POST["debug"], precision=prec, **pp)
+        np.testing.assert_array_equal(got, POST[f"{name}/ref{prec}"].astype(np.float64))
+
+
+def test_post_process_fixture_covers_each_branch():
+    img, dbg = POST["image"].astype(np.float64), POST["debug"].astype(np.float64)
+    assert len(POST_CASES) == 7
+    np.testing.assert_array_equal(POST["defaults/ref64"], img)  # no split, zoom or debug: a copy
+    r = POST["split_debug_left_alpha/ref64"]
+    assert np.all(r[:, 36] == 0)  # the split line
+    np.testing.assert_array_equal(r[:, :36, 0], dbg[:, :36, 0] + dbg[:, :36, 3])  # alpha shown in red and blue
+    np.testing.assert_array_equal(r[:, :36, 3], 1.0)
+    np.testing.assert_array_equal(r[:, 37:], img[:, 37:])
+    z = POST["zoom_box/ref64"]
+    assert np.all(z[7, 9:18] == (1, 0, 0, 0))  # the red box one texel outside (10, 8, 7, 5)
+    assert np.all(z[20, 40:65] == (1, 1, 1, 0))  # the inset's white border
+    inner = z[21:37, 41:64]
+    assert len({tuple(v) for v in inner.reshape(-1, 4)}) <= 35  # magnified: the 7 x 5 source texels
