@@ -349,7 +349,8 @@ def time_modes(T, WL, dev, stream, sid, args, peak):
     3840x2160 target) and a debug output.  Each on four rotating frames of the
     C2 scene (every frame's bindings exceed the L2), CUDA events over 12
     launches after 3.  Material ids and uv/normals are seeded synthetic blocks
-    (48 px materials, 8 px normals)."""
+    (48 px materials, 8 px normals).  Last the post-process pass at 4K (split,
+    debug image on the left, zoom inset), 24 launches after 3."""
     import math
     import torch
 
@@ -438,6 +439,31 @@ def time_modes(T, WL, dev, stream, sid, args, peak):
     run("upsample_2x", ctx, up, base, 40 + 20 * (lo.width * lo.height) / (W * H), W * H)
     out["upsample_2x"]["source"] = [lo.width, lo.height]
     ctx.close()
+    # the post-process pass at 4K: split at W / 2, the left side shows the debug
+    # image with its alpha, the zoom inset drawn; 16 B/px (8 read from the input
+    # or the debug image, 8 written); four rotating buffer sets (800 MB)
+    pp = T.post_process_default_params(W, H)
+    pp.zoom, pp.split_x, pp.debug_l_show = 1, W // 2, 1
+    pp.debug_l_mask[3] = 1.0
+    g2 = torch.Generator(device=dev).manual_seed(11)
+    srcs = [torch.rand(H, W, 4, device=dev, generator=g2).half() for _ in range(n)]
+    dbgs = [torch.rand(H, W, 4, device=dev, generator=g2).half() for _ in range(n)]
+    outs = [torch.empty(H, W, 4, dtype=torch.float16, device=dev) for _ in range(n)]
+    for i in range(3):
+        T.post_process(srcs[i % n], outs[i % n], pp, debug=dbgs[i % n], stream=sid)
+    torch.cuda.synchronize()
+    k = 24
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(k):
+        T.post_process(srcs[i % n], outs[i % n], pp, debug=dbgs[i % n], stream=sid)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    us = e0.elapsed_time(e1) * 1000 / k
+    gbs = 16 * W * H / (us / 1e6) / 1e9
+    out["post_process"] = {"us_per_frame": us, "mpx_s": W * H / us, "bytes_per_px": 16, "gb_s": gbs,
+                           "frac_of_hbm": gbs / peak, "form": "post_process_kernel"}
+    del srcs, dbgs, outs
     out["note"] = ("TAAU and debug outputs run in the plain form only; "
                    "bytes per target pixel count every binding once")
     return out
@@ -605,7 +631,7 @@ def run_ours(args):
     if not args.no_batch:
         forms["batch48"] = time_batch(T, WL, dev, stream, sid, world, args, peak, mpx / world)
 
-    # the ray-trace-assist classification (tiled and plain), TAAU and debug output (plain form)
+    # the ray-trace-assist classification (tiled and plain), TAAU and debug output (plain form), post-process
     if not args.no_modes and rank == 0:
         forms["modes"] = time_modes(T, WL, dev, stream, sid, args, peak)
 

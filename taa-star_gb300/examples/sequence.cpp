@@ -2,11 +2,14 @@
 // over a short synthetic sequence, the way the reference's renderer drives
 // its taa component each frame (source/main.cpp:4122-4123, taa.hpp:894, 974).
 //
-//   sequence <width> <height> <frames> [fxaa]
+//   sequence <width> <height> <frames> [fxaa | post]
 // prints one line per frame with the resolve time and the result's mean.
 // With "fxaa" the ray-trace-assist path runs: the resolve writes the
 // segmentation mask, FXAA antialiases the pixels it marks, then the sharpener
-// (source/taa.hpp:1031-1139); the line also counts the marked pixels.
+// (source/taa.hpp:1031-1139); the line also counts the marked pixels.  With
+// "post" the screen is split, the left side shows the debug image (mode 2)
+// and the zoom inset is drawn (source/taa.hpp:1141-1158); the line also
+// counts the texels of the split column that are black.
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
 
@@ -22,6 +25,7 @@ int main(int argc, char** argv) {
     const int W = argc > 1 ? atoi(argv[1]) : 320, H = argc > 2 ? atoi(argv[2]) : 180;
     const int N = argc > 3 ? atoi(argv[3]) : 8;
     const bool fxaa = argc > 4 && std::string(argv[4]) == "fxaa";
+    const bool post = argc > 4 && std::string(argv[4]) == "post";
     constexpr size_t CF = 3;
     taa_synth_scene_t scene;
     if (taa_synth_default_scene(&scene, W, H, 7) != TAA_OK) return 1;
@@ -48,6 +52,14 @@ int main(int argc, char** argv) {
     taa.mSampleDistribution = 2;
     taa.mSharpener = TAA_SHARPEN_CAS;
     taa.set_source_image_views(W, H, W, H, col, dep, mot, TAA_MOTION_RGBA16F);
+    if (post) {
+        taa.mParameters[1] = p;
+        taa.mSplitScreen = true;  // split at W / 2 (set_source_image_views)
+        p.mDebugMode = 2;
+        p.mDebugScale = 1.f;
+        p.mDebugToScreenOutput = 1;
+        taa.mPostProcessPushConstants.zoom = 1;
+    }
     cudaStream_t s;
     cudaStreamCreate(&s);
     std::vector<__half> host((size_t)W * H * 4);
@@ -74,13 +86,20 @@ int main(int argc, char** argv) {
         cudaStreamSynchronize(s);
         double sum = 0;
         for (size_t k = 0; k < host.size(); k += 4) sum += __half2float(host[k]);
-        long marked = 0;
+        long marked = 0, split_black = 0;
+        if (post) {
+            for (int y = 0; y < H; ++y) {
+                const __half* t = &host[((size_t)y * W + W / 2) * 4];
+                split_black += __half2float(t[0]) == 0.f && __half2float(t[1]) == 0.f && __half2float(t[2]) == 0.f;
+            }
+        }
         if (fxaa && f > 0) {
             const taa_gb300::Image& m = taa.segmentation_mask(f);
             cudaMemcpy2D(mask.data(), (size_t)W * 4, m.ptr, m.pitch, (size_t)W * 4, H, cudaMemcpyDeviceToHost);
             for (uint32_t v : mask) marked += (v & 3u) == 1u;
         }
-        printf("frame %d resolve %.3f ms marked %ld mean_r %.5f\n", f, taa.duration(), marked, sum / (W * H));
+        printf("frame %d resolve %.3f ms marked %ld split_black %ld mean_r %.5f\n", f, taa.duration(), marked,
+               split_black, sum / (W * H));
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {

@@ -6,17 +6,16 @@
 // chain in render().  This header keeps that interface - the same method
 // names, parameter block and per-frame bookkeeping - for a C++ application
 // that renders with CUDA: images are device buffers, "recording" is enqueuing
-// on a CUDA stream, and the dispatches are taa_resolve(), taa_fxaa() and
-// taa_sharpen().  The settings file (writeSettingsToIni/readSettingsFromIni)
-// is text in and out; the GUI, the post-process overlay and RenderDoc parts
-// of the reference class are not carried over (their settings are kept so a
-// settings file survives a read and a write).
+// on a CUDA stream, and the dispatches are taa_resolve(), taa_fxaa(),
+// taa_sharpen() and taa_post_process().  The settings file
+// (writeSettingsToIni/readSettingsFromIni) is text in and out; the GUI and
+// RenderDoc parts of the reference class are not carried over.
 //
 // Usage, once per frame (as wookiee drives the reference, source/main.cpp:4122-4123):
 //   P_jit = taa.get_jittered_projection_matrix(P, frame);   // render the G-buffer with P_jit
 //   taa.save_history_proj_matrix(P, frame);
 //   taa.update(view, frame, seconds);
-//   taa.render(frame, stream);                             // result(frame) / sharpened(frame)
+//   taa.render(frame, stream);                             // result(frame): the last pass's image
 #pragma once
 #include <cuda_runtime.h>
 
@@ -71,7 +70,7 @@ template <size_t CF> class taa {
     uint32_t mForm = TAA_FORM_AUTO;
     // push_constants_for_fxaa (source/taa.hpp:93-98; the reciprocal frame size is derived per call)
     taa_fxaa_params_t mFxaaPushConstants{0.75f, 0.116f, 0.0833f};
-    // post-processing settings (source/taa.hpp:101-111, 1359): stored and written, the overlay is not built
+    // post-processing (source/taa.hpp:101-111, 1352): split line, zoom box and inset, debug image per side
     bool mPostProcessEnabled = true;
     struct PostProcessSettings {
         uint32_t zoom = 0, showZoomBox = 1;
@@ -107,6 +106,8 @@ template <size_t CF> class taa {
             alloc(mSharpened[i], 8);
             alloc(mTemp[i], 8);
             alloc(mSegMask[i], 4);
+            alloc(mDebug[i], 8);
+            alloc(mPost[i], 8);
         }
         taa_desc_t d{sizeof(taa_desc_t), sourceWidth, sourceHeight, targetWidth, targetHeight, TAA_HISTORY_RGBA32F,
                      motionFormat, mForm, mSharpener, mSharpenFactor, TAA_FLAG_FXAA};
@@ -114,6 +115,10 @@ template <size_t CF> class taa {
         mCtxSharpener = mSharpener;
         mCtxSharpenFactor = mSharpenFactor;
         mSplitX = targetWidth / 2;  // source/taa.hpp:354
+        taa_post_process_params_t pp;  // the zoom boxes for this size (source/taa.hpp:355-359)
+        check(taa_post_process_default_params(targetWidth, targetHeight, &pp));
+        std::memcpy(mPostProcessPushConstants.zoomSrcLTWH, pp.zoom_src_ltwh, sizeof pp.zoom_src_ltwh);
+        std::memcpy(mPostProcessPushConstants.zoomDstLTWH, pp.zoom_dst_ltwh, sizeof pp.zoom_dst_ltwh);
         if (cudaEventCreate(&mT0) != cudaSuccess || cudaEventCreate(&mT1) != cudaSuccess)
             throw std::runtime_error("taa: cudaEventCreate failed");
     }
@@ -247,7 +252,9 @@ template <size_t CF> class taa {
     // source/taa.hpp:974-1192: the matrices of this and the previous frame in
     // FP64, then the resolve (and the fused sharpen) of frame `frameId`; on the
     // ray-trace-assist path the resolve also writes the segmentation mask, and
-    // with its FXAA flag the FXAA pass and then the sharpener follow.
+    // with its FXAA flag the FXAA pass and then the sharpener follow; last the
+    // post-process pass when enabled (it reads the resolve's debug image when
+    // a side of the split shows it).
     // The very first frame has no history: the result is the source colour.
     void render(uint64_t frameId, cudaStream_t stream) {
         const size_t cur = frameId % CF, prev = (frameId + CF - 1) % CF;
@@ -289,6 +296,12 @@ template <size_t CF> class taa {
             io.sharpened = mSharpened[cur].ptr;
             io.sharpened_pitch = mSharpened[cur].pitch;
         }
+        const bool showDebug = mPostProcessEnabled && (mParameters[0].mDebugToScreenOutput ||
+                                                       (mSplitScreen && mParameters[1].mDebugToScreenOutput));
+        if (showDebug) {  // binding 6 (the reference writes it every frame)
+            io.debug = mDebug[cur].ptr;
+            io.debug_pitch = mDebug[cur].pitch;
+        }
         mShown[cur] = mSharpener != TAA_SHARPEN_OFF ? Shown::Sharpened : Shown::Result;
         cudaEventRecord(mT0, stream);
         check(taa_resolve(mCtx, stream, &io));
@@ -301,6 +314,23 @@ template <size_t CF> class taa {
                                   mSharpened[cur].ptr, mSharpened[cur].pitch, mOut[0], mOut[1]));
                 mShown[cur] = Shown::Sharpened;
             }
+        }
+        if (mPostProcessEnabled) {  // source/taa.hpp:1141-1158, from the last pass's image
+            const Image& last = result(frameId);
+            taa_post_process_params_t pp;
+            check(taa_post_process_default_params(mOut[0], mOut[1], &pp));
+            std::memcpy(pp.zoom_src_ltwh, mPostProcessPushConstants.zoomSrcLTWH, sizeof pp.zoom_src_ltwh);
+            std::memcpy(pp.zoom_dst_ltwh, mPostProcessPushConstants.zoomDstLTWH, sizeof pp.zoom_dst_ltwh);
+            pp.zoom = mPostProcessPushConstants.zoom;
+            pp.show_zoom_box = mPostProcessPushConstants.showZoomBox;
+            pp.split_x = mSplitScreen ? mSplitX : -1;  // source/taa.hpp:955-959
+            std::memcpy(pp.debug_l_mask, mParameters[0].mDebugMask, sizeof pp.debug_l_mask);
+            std::memcpy(pp.debug_r_mask, mParameters[1].mDebugMask, sizeof pp.debug_r_mask);
+            pp.debug_l_show = showDebug && mParameters[0].mDebugToScreenOutput;
+            pp.debug_r_show = showDebug && mParameters[1].mDebugToScreenOutput;
+            check(taa_post_process(stream, &pp, last.ptr, last.pitch, showDebug ? mDebug[cur].ptr : nullptr,
+                                   mDebug[cur].pitch, mPost[cur].ptr, mPost[cur].pitch, mOut[0], mOut[1]));
+            mShown[cur] = Shown::Post;
         }
         mHaveSegMask = needRayTraceAssist();
         cudaEventRecord(mT1, stream);
@@ -321,11 +351,13 @@ template <size_t CF> class taa {
         switch (mShown[frameId % CF]) {
             case Shown::Sharpened: return mSharpened[frameId % CF];
             case Shown::Temp: return mTemp[frameId % CF];
+            case Shown::Post: return mPost[frameId % CF];
             default: return mResult[frameId % CF];
         }
     }
     const Image& history(uint64_t frameId) const { return mHistory[frameId % CF]; }
     const Image& segmentation_mask(uint64_t frameId) const { return mSegMask[frameId % CF]; }  // taa.hpp:1341
+    const Image& debug_image(uint64_t frameId) const { return mDebug[frameId % CF]; }
     taa_ctx* context() const { return mCtx; }
 
    private:
@@ -333,7 +365,7 @@ template <size_t CF> class taa {
         if (cudaMallocPitch(&im.ptr, &im.pitch, (size_t)mOut[0] * texel, (size_t)mOut[1]) != cudaSuccess)
             throw std::runtime_error("taa: cudaMallocPitch failed");
     }
-    enum class Shown { Result, Sharpened, Temp };
+    enum class Shown { Result, Sharpened, Temp, Post };
 
     // the members the settings file holds
     taa_settings_t settings() const {
@@ -380,7 +412,7 @@ template <size_t CF> class taa {
         if (mCtx) taa_destroy(mCtx);
         mCtx = nullptr;
         for (size_t i = 0; i < CF; ++i)
-            for (Image* im : {&mResult[i], &mHistory[i], &mSharpened[i], &mTemp[i], &mSegMask[i]}) {
+            for (Image* im : {&mResult[i], &mHistory[i], &mSharpened[i], &mTemp[i], &mSegMask[i], &mDebug[i], &mPost[i]}) {
                 if (im->ptr) cudaFree(im->ptr);
                 im->ptr = nullptr;
             }
@@ -393,7 +425,7 @@ template <size_t CF> class taa {
     int mIn[2] = {0, 0}, mOut[2] = {0, 0};
     bool mUpsampling = false;
     std::array<Image, CF> mSrcColor{}, mSrcDepth{}, mSrcVelocity{};
-    std::array<Image, CF> mResult{}, mHistory{}, mSharpened{}, mTemp{}, mSegMask{};
+    std::array<Image, CF> mResult{}, mHistory{}, mSharpened{}, mTemp{}, mSegMask{}, mDebug{}, mPost{};
     std::array<Mat4, CF> mProj{}, mView{};
     taa_uniforms_t mUniforms{};
     Parameters mOldParams[2]{};

@@ -46,3 +46,15 @@ def test_mirror_runs_the_fxaa_chain(cuda, tmp_path):
     marked = [int(l[l.index("marked") + 1]) for l in lines]
     assert all(m > 0 for m in marked[1:]), r.stdout
     assert all(0.0 < float(l[-1]) < 64.0 for l in lines), r.stdout
+
+
+@pytest.mark.gpu
+def test_mirror_runs_the_post_process_pass(cuda, tmp_path):
+    # split screen, debug image on the left, zoom inset: the split column is black
+    exe = compile_example(tmp_path)
+    r = subprocess.run([str(exe), "160", "96", "4", "post"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = [l.split() for l in r.stdout.splitlines() if l.startswith("frame")]
+    assert len(lines) == 4
+    black = [int(l[l.index("split_black") + 1]) for l in lines]
+    assert all(b == 96 for b in black[1:]), r.stdout  # every row of column W / 2 (frame 0 is the source copy)
