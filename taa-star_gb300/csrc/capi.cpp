@@ -88,10 +88,12 @@ int check_desc(const taa_desc_t& d, const char* who) {
     if (d.form > TAA_FORM_LEARNED) return fail(TAA_E_INVAL, "%s: form %u", who, d.form);
     if (d.sharpener > TAA_SHARPEN_CAS) return fail(TAA_E_INVAL, "%s: sharpener %u", who, d.sharpener);
     if (!finite(d.sharpen_factor)) return fail(TAA_E_INVAL, "%s: sharpen_factor not finite", who);
-    if (d.flags & ~(TAA_FLAG_LEARNED_TCGEN05 | TAA_FLAG_FXAA))
+    if (d.flags & ~(TAA_FLAG_LEARNED_TCGEN05 | TAA_FLAG_FXAA | TAA_FLAG_FP16_GUARD))
         return fail(TAA_E_INVAL, "%s: unknown flags 0x%x", who, d.flags);
     if ((d.flags & TAA_FLAG_LEARNED_TCGEN05) && d.form != TAA_FORM_LEARNED)
         return fail(TAA_E_INVAL, "%s: TAA_FLAG_LEARNED_TCGEN05 needs TAA_FORM_LEARNED", who);
+    if ((d.flags & TAA_FLAG_FP16_GUARD) && d.form != TAA_FORM_FP16)
+        return fail(TAA_E_INVAL, "%s: TAA_FLAG_FP16_GUARD needs TAA_FORM_FP16", who);
     return ok();
 }
 
@@ -537,7 +539,9 @@ int taa_resolve(taa_ctx* c, void* stream, const taa_frame_io_t* io) {
     } else {
         const int mc = d.motion_format == TAA_MOTION_RGBA16F ? 4 : 2;
         if (form == TAA_FORM_FP16) {
-            e = taa_dev::launch_resolve_half((int)d.history_format, mc, U.param[0].mInterpolationMode, U, a, s);
+            e = (d.flags & TAA_FLAG_FP16_GUARD)
+                    ? taa_dev::launch_resolve_half_guarded((int)d.history_format, mc, U.param[0].mInterpolationMode, U, a, s)
+                    : taa_dev::launch_resolve_half((int)d.history_format, mc, U.param[0].mInterpolationMode, U, a, s);
         } else if (!sharpen) {
             e = taa_dev::launch_resolve_tiled((int)d.history_format, mc, U.param[0].mInterpolationMode, U, a, s);
         } else {

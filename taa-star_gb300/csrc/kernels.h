@@ -38,6 +38,9 @@ cudaError_t launch_resolve_tiled(int history_fmt, int motion_ch, int interp, con
                                  const FrameArgs& a, cudaStream_t stream);
 cudaError_t launch_resolve_half(int history_fmt, int motion_ch, int interp, const taa_uniforms_t& U,
                                 const FrameArgs& a, cudaStream_t stream);
+// The FP16 form with TAA_FLAG_FP16_GUARD (resolve_half_guard.cu).
+cudaError_t launch_resolve_half_guarded(int history_fmt, int motion_ch, int interp, const taa_uniforms_t& U,
+                                        const FrameArgs& a, cudaStream_t stream);
 
 // Standalone sharpen passes on an RGBA16F image (used after the plain form).
 cudaError_t launch_sharpen(int sharpener, const FrameArgs& a, cudaStream_t stream);

@@ -28,6 +28,8 @@ struct ExactF32 : HistoryFilter {
     }
     // the staged centre texel already is the exact current colour
     static constexpr bool kExactCentre = false;
+    // the FP32 box needs no fallback
+    static constexpr bool kExactFallback = false;
     static __device__ __forceinline__ void centre_colour(Box&, const Img&, int, int, bool, bool) {}
 
     // working-space conversion of one source texel (taa.comp:182-213)

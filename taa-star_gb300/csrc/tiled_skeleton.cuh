@@ -476,7 +476,15 @@ struct StoreFinish {
                                                float4 hraw, float u, float v, float hu, float hv, float, float,
                                                bool rejected, bool valid, int x, int y, bool tm, StoreFinish&) {
         if (!valid) return;
-        float4 o = Pol::template finish<HOT>(U, P, M, box, c0, hraw, u, v, hu, hv, rejected);
+        float4 o;
+        if constexpr (Pol::kExactFallback) {
+            // a policy whose clip can be ill-conditioned for its precision finishes
+            // such a pixel from the source texels in FP32
+            const typename Pol::At at{&a, x, y, tm};
+            o = Pol::template finish_at<HOT>(U, P, M, box, c0, hraw, u, v, hu, hv, rejected, &at);
+        } else {
+            o = Pol::template finish<HOT>(U, P, M, box, c0, hraw, u, v, hu, hv, rejected);
+        }
         store_history<HF>(a.history_out, x, y, make_float4(o.x, o.y, o.z, 0.f));
         if (a.result.p) {
             if (tm) o = Pol::un_tonemap(o);

@@ -255,8 +255,9 @@ FP16_MODES = ["base", "c2", "bilinear", "bspline", "clamp_rgb", "clip_slow_shape
               "tonemap_lottes", "reduce_blend_velalpha", "closest_velocity"]
 
 
+@pytest.mark.parametrize("guard", [0, 1], ids=["fast", "guarded"])
 @pytest.mark.parametrize("mode", FP16_MODES)
-def test_fp16_form_frame_error_vs_fp64(cuda, mode):
+def test_fp16_form_frame_error_vs_fp64(cuda, mode, guard):
     """The FP16 form's contract: per frame, PSNR >= 50 dB against the FP64
     oracle fed the same history, relative L2 <= 1e-2 (see test_gpu_sequences
     for why FP16 chroma cannot hold 1e-3 next to fireflies)."""
@@ -266,11 +267,12 @@ def test_fp16_form_frame_error_vs_fp64(cuda, mode):
     hist = np.ascontiguousarray(fr[0]["color"].astype(np.float32))
     u = T.make_uniforms(wl.parameters(), jitter_ndc=fr[1]["jitter"])
     ref = oracle_for(u, fr[1], fr[0], hist, precision=64)
-    ctx = T.Taa(w, h, form=T.TAA_FORM_FP16)
+    ctx = T.Taa(w, h, form=T.TAA_FORM_FP16, flags=T.TAA_FLAG_FP16_GUARD if guard else 0)
     ctx.set_uniforms(u)
     assert ctx.selected_form() == T.TAA_FORM_FP16
     out = gpu_resolve(ctx, cuda, fr[1]["color"], fr[1]["depth"], fr[1]["motion"], hist, fr[0]["depth"])
     got, want = out["history_out"][..., :3], ref["history"][..., :3]
+    print(mode, "guarded" if guard else "fast", "relL2", rel_l2(got, want), "PSNR", psnr(got, want))
     assert rel_l2(got, want) <= 1e-2, rel_l2(got, want)
     assert psnr(got, want) >= 50.0
 

@@ -31,10 +31,10 @@ def render(wl, sc, f, dev, motion_ch=2):
     return col, dep, mot
 
 
-def run_sequence(dev, wl, frames, check_frames, form=T.TAA_FORM_TILED, fp64_report=None):
+def run_sequence(dev, wl, frames, check_frames, form=T.TAA_FORM_TILED, fp64_report=None, flags=0):
     sc = wl.scene()
     H, W = wl.height, wl.width
-    ctx = T.Taa(W, H, form=form)
+    ctx = T.Taa(W, H, form=form, flags=flags)
     hist = torch.zeros(H, W, 4, dtype=torch.float32, device=dev)
     hout = torch.empty_like(hist)
     res = torch.empty(H, W, 4, dtype=torch.float16, device=dev)
@@ -127,3 +127,27 @@ def test_4k_constant_image_is_a_fixed_point(cuda):
     ctx.resolve(color=col, depth=dep, velocity=mot, history=hist, history_depth=dep, history_out=out)
     torch.cuda.synchronize()
     assert torch.allclose(out[..., :3], hist[..., :3], rtol=2e-7, atol=0)
+
+
+# With TAA_FLAG_FP16_GUARD a pixel whose clip engages on a box FP16 cannot
+# resolve (its tightest channel 256 times narrower than its widest: the tight
+# chroma box next to a firefly) is finished in FP32, and the frame error falls
+# below the spec bar of 1e-3 relative L2 against FP64.
+FP16_GUARD_RELL2 = 1e-3
+
+
+def test_c1_fp16_guarded_sixteen_frames(cuda):
+    rep = []
+    run_sequence(cuda, WL.c1(), 16, set(range(1, 16)), form=T.TAA_FORM_FP16, fp64_report=rep,
+                 flags=T.TAA_FLAG_FP16_GUARD)
+    print("C1 guarded FP16 form vs FP64 (relL2, PSNR):", rep)
+    assert max(r for r, _ in rep) <= FP16_GUARD_RELL2
+    assert min(p for _, p in rep) >= FP16_PSNR
+
+
+def test_c2_4k_fp16_guarded(cuda):
+    rep = []
+    run_sequence(cuda, WL.c2(), 6, {1, 5}, form=T.TAA_FORM_FP16, fp64_report=rep, flags=T.TAA_FLAG_FP16_GUARD)
+    print("C2 guarded FP16 form vs FP64 (relL2, PSNR):", rep)
+    assert max(r for r, _ in rep) <= FP16_GUARD_RELL2
+    assert min(p for _, p in rep) >= FP16_PSNR
