@@ -426,14 +426,20 @@ __global__ void __launch_bounds__(kBX * kBY, TAA_FXAA_MIN_BLOCKS) fxaa_marked_ke
 bool aligned16(const void* p, size_t pitch) { return ((uintptr_t)p % 16 == 0) && (pitch % 16 == 0); }
 
 // CTAs of the list kernel: the SMs x its resident CTAs on the current device
+// (looked up once per device, so that later calls, e.g. under stream capture,
+// only launch)
 unsigned list_ctas() {
+    constexpr int kMaxDevices = 64;
+    static unsigned cached[kMaxDevices] = {};
     int dev = 0, sms = 0, per_sm = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        sms < 1)
-        sms = 1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) dev = 0;
+    if (dev < kMaxDevices && cached[dev]) return cached[dev];
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 1;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fxaa_list_kernel, kBX * kBY, 0) != cudaSuccess || per_sm < 1)
         per_sm = 1;
-    return (unsigned)(sms * per_sm);
+    const unsigned n = (unsigned)(sms * per_sm);
+    if (dev < kMaxDevices) cached[dev] = n;
+    return n;
 }
 
 }  // namespace
