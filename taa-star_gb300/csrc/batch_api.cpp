@@ -246,7 +246,7 @@ int taa_batch_prepare(taa_batch* b, void* stream, int32_t slot, const taa_frame_
         if (!b->have_uniforms[v]) return fail(TAA_E_INVAL, "taa_batch_prepare: view %d has no uniforms", v);
         const taa_desc_t& d = b->desc[v];
         const taa_uniforms_t& U = b->uniforms[v];
-        if (!taa_dev::fast_path_supported(U, d.in_width, d.in_height, d.out_width, d.out_height))
+        if (!taa_dev::fast_path_supported(U, d.in_width, d.in_height, d.out_width, d.out_height, false, true))
             return fail(TAA_E_UNSUPPORTED, "taa_batch_prepare: view %d: its parameters need the plain form", v);
         const int interp = U.param[0].mInterpolationMode, hot = taa_dev::hot_parameters(U.param[0]) ? 1 : 0;
         if (interp != 0 && interp != 2)

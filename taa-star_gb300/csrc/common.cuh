@@ -143,6 +143,18 @@ template <int HF> __device__ __forceinline__ void store_history(const ImgW& im, 
     else *texel_ptr_w<uint2>(im, x, y) = float4_to_half4(v);
 }
 
+__device__ __forceinline__ float fractf(float x) { return x - floorf(x); }
+
+// taa.comp:551-556: the noise added to the result when mAddNoise is set,
+// seeded by the pixel's uv and mSinTime.x.
+__device__ __forceinline__ float4 taa_noise(const taa_uniforms_t& U, const taa_parameters_t& P, float u, float v) {
+    const float sx = u + U.mSinTime[0] + 0.6959174f, sy = v + U.mSinTime[0] + 0.6959174f;
+    const float s = sinf(sx * 12.9898f + sy * 78.233f);
+    const float f = P.mNoiseFactor;
+    return make_float4((fractf(s * 43758.5453f) * 2.0f - 1.0f) * f, (fractf(s * 28001.8384f) * 2.0f - 1.0f) * f,
+                       (fractf(s * 50849.4141f) * 2.0f - 1.0f) * f, (fractf(s * 12996.89f) * 2.0f - 1.0f) * f);
+}
+
 // Correctly rounded x / d for a constant divisor d with precomputed
 // rd = RN(1/d): one product and one FMA-based residual correction
 // (P. Markstein, "Computation of elementary functions on the IBM RISC

@@ -70,54 +70,61 @@ struct HistoryFilter {
         }
     }
 
-    // one exact-weight 2x2 set read through texel(x, y) at clamped coordinates
-    template <class F>
+    // one exact-weight 2x2 set read through texel(x, y) at clamped coordinates;
+    // W4: the fourth channel too (the history's dynamic mask), else 0
+    template <bool W4 = false, class F>
     static __device__ __forceinline__ float4 bil(const Taps& t, int w, int h, F&& texel) {
         const int xa = t.xs(0, w), xb = t.xs(1, w), ya = t.ys(0, h), yb = t.ys(1, h);
         float4 A = texel(xa, ya), B = texel(xb, ya);
         float4 C = texel(xa, yb), D = texel(xb, yb);
+        return bil_weights<W4>(t, A, B, C, D);
+    }
+    template <bool W4>
+    static __device__ __forceinline__ float4 bil_weights(const Taps& t, float4 A, float4 B, float4 C, float4 D) {
         float gx = t.wx[0], fx = t.wx[1], gy = t.wy[0], fy = t.wy[1];
-        float4 tt = make_float4(A.x * gx + B.x * fx, A.y * gx + B.y * fx, A.z * gx + B.z * fx, 0.f);
-        float4 bb = make_float4(C.x * gx + D.x * fx, C.y * gx + D.y * fx, C.z * gx + D.z * fx, 0.f);
-        return make_float4(tt.x * gy + bb.x * fy, tt.y * gy + bb.y * fy, tt.z * gy + bb.z * fy, 0.f);
+        float4 tt = make_float4(A.x * gx + B.x * fx, A.y * gx + B.y * fx, A.z * gx + B.z * fx,
+                                W4 ? A.w * gx + B.w * fx : 0.f);
+        float4 bb = make_float4(C.x * gx + D.x * fx, C.y * gx + D.y * fx, C.z * gx + D.z * fx,
+                                W4 ? C.w * gx + D.w * fx : 0.f);
+        return make_float4(tt.x * gy + bb.x * fy, tt.y * gy + bb.y * fy, tt.z * gy + bb.z * fy,
+                           W4 ? tt.w * gy + bb.w * fy : 0.f);
     }
 
-    // The Catmull-Rom accumulation: rows of four taps, then the rows.
-    template <class F>
+    // The Catmull-Rom accumulation: rows of four taps, then the rows (W4: the
+    // fourth channel too).
+    template <bool W4 = false, class F>
     static __device__ __forceinline__ float4 catmullrom_sum(const Taps& t, F&& at) {
         float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            float rx = 0.f, ry = 0.f, rz = 0.f;
+            float rx = 0.f, ry = 0.f, rz = 0.f, rw = 0.f;
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 float4 s = at(i, j);
                 rx = __fmaf_rn(t.wx[i], s.x, rx);
                 ry = __fmaf_rn(t.wx[i], s.y, ry);
                 rz = __fmaf_rn(t.wx[i], s.z, rz);
+                if (W4) rw = __fmaf_rn(t.wx[i], s.w, rw);
             }
             acc.x = __fmaf_rn(t.wy[j], rx, acc.x);
             acc.y = __fmaf_rn(t.wy[j], ry, acc.y);
             acc.z = __fmaf_rn(t.wy[j], rz, acc.z);
+            if (W4) acc.w = __fmaf_rn(t.wy[j], rw, acc.w);
         }
         return acc;
     }
 
     // the filter reading 4x4 (or 2x2) consecutive window entries from `base`
-    template <int INTERP, int HF, class Taps_, class HT>
+    template <int INTERP, int HF, bool W4 = false, class Taps_, class HT>
     static __device__ __forceinline__ float4 filter_window(const Taps_& h, const HT* base, int stride) {
         const Taps& t = h.t[0];
         auto at = [&](int i, int j) { return to_f4<HF>(base[j * stride + i]); };
-        if (INTERP == 2) return catmullrom_sum(t, at);
-        float4 A = at(0, 0), B = at(1, 0), C = at(0, 1), D = at(1, 1);
-        float gx = t.wx[0], fx = t.wx[1], gy = t.wy[0], fy = t.wy[1];
-        float4 tt = make_float4(A.x * gx + B.x * fx, A.y * gx + B.y * fx, A.z * gx + B.z * fx, 0.f);
-        float4 bb = make_float4(C.x * gx + D.x * fx, C.y * gx + D.y * fx, C.z * gx + D.z * fx, 0.f);
-        return make_float4(tt.x * gy + bb.x * fy, tt.y * gy + bb.y * fy, tt.z * gy + bb.z * fy, 0.f);
+        if (INTERP == 2) return catmullrom_sum<W4>(t, at);
+        return bil_weights<W4>(t, at(0, 0), at(1, 0), at(0, 1), at(1, 1));
     }
 
     // the filter reading texel(x, y) at clamped coordinates of a w x h image
-    template <int INTERP, class Taps_, class F>
+    template <int INTERP, bool W4 = false, class Taps_, class F>
     static __device__ __forceinline__ float4 filter(const Taps_& h, int w, int hh, F&& texel) {
         if (INTERP == 2) {
             const Taps& t = h.t[0];
@@ -127,15 +134,16 @@ struct HistoryFilter {
                 xs[k] = t.xs(k, w);
                 ys[k] = t.ys(k, hh);
             }
-            return catmullrom_sum(t, [&](int i, int j) { return texel(xs[i], ys[j]); });
+            return catmullrom_sum<W4>(t, [&](int i, int j) { return texel(xs[i], ys[j]); });
         }
-        if (INTERP == 0) return bil(h.t[0], w, hh, texel);
-        float4 A = bil(h.t[0], w, hh, texel), B = bil(h.t[1], w, hh, texel), C = bil(h.t[2], w, hh, texel),
-               D = bil(h.t[3], w, hh, texel);
+        if (INTERP == 0) return bil<W4>(h.t[0], w, hh, texel);
+        float4 A = bil<W4>(h.t[0], w, hh, texel), B = bil<W4>(h.t[1], w, hh, texel),
+               C = bil<W4>(h.t[2], w, hh, texel), D = bil<W4>(h.t[3], w, hh, texel);
         const float *s0 = h.s0, *s1 = h.s1;
         return make_float4((A.x * s0[0] + B.x * s1[0]) * s0[1] + (C.x * s0[0] + D.x * s1[0]) * s1[1],
                            (A.y * s0[0] + B.y * s1[0]) * s0[1] + (C.y * s0[0] + D.y * s1[0]) * s1[1],
-                           (A.z * s0[0] + B.z * s1[0]) * s0[1] + (C.z * s0[0] + D.z * s1[0]) * s1[1], 0.f);
+                           (A.z * s0[0] + B.z * s1[0]) * s0[1] + (C.z * s0[0] + D.z * s1[0]) * s1[1],
+                           W4 ? (A.w * s0[0] + B.w * s1[0]) * s0[1] + (C.w * s0[0] + D.w * s1[0]) * s1[1] : 0.f);
     }
 };
 

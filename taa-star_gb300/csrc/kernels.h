@@ -22,11 +22,13 @@ struct FastKey {
     int sharpen;       // 0 off, 1 simple, 2 CAS (fused epilogue)
 };
 
-// True when the fast forms implement every feature the uniforms ask for.
-// Whether the tiled forms run these parameters and sizes (the ray-trace-assist
-// classification only where rt_augment_ok: the tiled forms without a fused
-// sharpener run it, the batch, the learned form and the fused sharpener do not).
-bool fast_path_supported(const taa_uniforms_t& U, int in_w, int in_h, int out_w, int out_h, bool rt_augment_ok = false);
+// Whether the tiled forms run these parameters and sizes.  The ray-trace-assist
+// classification only where rt_augment_ok (the tiled forms without a fused
+// sharpener run it; the batch, the learned form and the fused sharpener do
+// not); noise, dynamic anti-ghosting and the 3x3-longest velocity only where
+// extra_modes_ok (the tiled forms without a fused sharpener and the batch).
+bool fast_path_supported(const taa_uniforms_t& U, int in_w, int in_h, int out_w, int out_h, bool rt_augment_ok = false,
+                         bool extra_modes_ok = false);
 
 // Tiled FP32 / FP16 resolve, optionally with the fused sharpen (resolve_fast.cu).
 cudaError_t launch_resolve_fast(const FastKey& key, const taa_uniforms_t& U, const FrameArgs& a,

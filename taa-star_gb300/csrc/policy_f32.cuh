@@ -158,7 +158,7 @@ struct ExactF32 : HistoryFilter {
 
     // the window filter with each tap as two pairs (x, y), (z, w): a row sums
     // its four taps, then the rows are summed, both with one FMA per step
-    template <int INTERP, int HF, class Taps_, class HT>
+    template <int INTERP, int HF, bool W4 = false, class Taps_, class HT>
     static __device__ __forceinline__ float4 filter_window(const Taps_& h, const HT* base, int stride) {
         if constexpr (INTERP == 2 && HF == 0) {
             const Taps& t = h.t[0];
@@ -181,9 +181,9 @@ struct ExactF32 : HistoryFilter {
                 acc_xy = fma2(wyd, r_xy, acc_xy);
                 acc_zw = fma2(wyd, r_zw, acc_zw);
             }
-            return make_float4(f2lo(acc_xy), f2hi(acc_xy), f2lo(acc_zw), 0.f);
+            return make_float4(f2lo(acc_xy), f2hi(acc_xy), f2lo(acc_zw), W4 ? f2hi(acc_zw) : 0.f);
         } else {
-            return HistoryFilter::filter_window<INTERP, HF>(h, base, stride);
+            return HistoryFilter::filter_window<INTERP, HF, W4>(h, base, stride);
         }
     }
 
@@ -256,6 +256,10 @@ struct ExactF32 : HistoryFilter {
         if (yc) {
             float tmp = o.x - o.z;
             o = {tmp + o.y, o.x + o.z, tmp - o.y};
+        }
+        if (M.noise()) {  // taa.comp:903-906
+            const float4 n = taa_noise(U, P, u, v);
+            o = {o.x + n.x, o.y + n.y, o.z + n.z};
         }
         return make_float4(o.x, o.y, o.z, 0.f);
     }

@@ -299,6 +299,10 @@ template <bool GUARD> struct HalfPol : tiled::HistoryFilter {
             float tmp = o.x - o.z;
             o = {tmp + o.y, o.x + o.z, tmp - o.y};
         }
+        if (M.noise()) {  // taa.comp:903-906
+            const float4 n = taa_noise(U, P, u, v);
+            o = {o.x + n.x, o.y + n.y, o.z + n.z};
+        }
         return make_float4(o.x, o.y, o.z, 0.f);
     }
 

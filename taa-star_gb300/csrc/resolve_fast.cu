@@ -25,16 +25,17 @@
 
 namespace taa_dev {
 
-bool fast_path_supported(const taa_uniforms_t& U, int in_w, int in_h, int out_w, int out_h, bool rt_augment_ok) {
+bool fast_path_supported(const taa_uniforms_t& U, int in_w, int in_h, int out_w, int out_h, bool rt_augment_ok,
+                         bool extra_modes_ok) {
     if (in_w != out_w || in_h != out_h) return false;
     if (U.mUpsampling || U.mBypassHistoryUpdate) return false;
     if (U.splitScreen && U.splitX < out_w - 1) return false;
     const taa_parameters_t& P = U.param[0];
-    if (P.mPassThrough || (P.mRayTraceAugment && !rt_augment_ok) || P.mAddNoise || P.mDynamicAntiGhosting) return false;
+    if (P.mPassThrough || (P.mRayTraceAugment && !rt_augment_ok)) return false;
+    if (!extra_modes_ok && (P.mAddNoise || P.mDynamicAntiGhosting || P.mVelocitySampleMode == 1)) return false;
     bool jitter_zero = U.mJitterNdc[0] * 0.5f * P.mUnjitterFactor == 0.f &&
                        U.mJitterNdc[1] * 0.5f * P.mUnjitterFactor == 0.f;
     if ((P.mUnjitterNeighbourhood || P.mUnjitterCurrentSample) && !jitter_zero) return false;
-    if (P.mVelocitySampleMode == 1) return false;
     if (P.mInterpolationMode < 0 || P.mInterpolationMode > 2) return false;
     return true;
 }

@@ -39,7 +39,6 @@ __device__ __forceinline__ V3 vmix(V3 x, V3 y, float a) {
     float t = 1.0f - a;
     return {x.x * t + y.x * a, x.y * t + y.y * a, x.z * t + y.z * a};
 }
-__device__ __forceinline__ float fractf(float x) { return x - floorf(x); }
 
 // Exact-weight bilinear, clamp to edge (texel centres at k + 0.5).
 template <class F>
@@ -339,13 +338,7 @@ struct PlainResolver {
     }
 
     // taa.comp:551-556
-    __device__ float4 noise(V2 uv) const {
-        float sx = uv.x + U.mSinTime[0] + 0.6959174f, sy = uv.y + U.mSinTime[0] + 0.6959174f;
-        float s = sinf(sx * 12.9898f + sy * 78.233f);
-        float f = P->mNoiseFactor;
-        return make_float4((fractf(s * 43758.5453f) * 2.0f - 1.0f) * f, (fractf(s * 28001.8384f) * 2.0f - 1.0f) * f,
-                           (fractf(s * 50849.4141f) * 2.0f - 1.0f) * f, (fractf(s * 12996.89f) * 2.0f - 1.0f) * f);
-    }
+    __device__ float4 noise(V2 uv) const { return taa_noise(U, *P, uv.x, uv.y); }
 
     // taa.comp:559-702 through segmentation.cuh, reading global memory
     struct SegAccess {

@@ -148,12 +148,15 @@ template <bool Hot> struct Mode {
     __device__ bool vel_alpha() const { return !Hot && P.mVelBasedAlpha; }
     __device__ bool lottes() const { return !Hot && P.mLumaWeightingLottes; }
     __device__ bool near_clamp() const { return !Hot && P.mReduceBlendNearClamp; }
+    __device__ bool noise() const { return !Hot && P.mAddNoise; }
+    __device__ bool anti_ghost() const { return !Hot && P.mDynamicAntiGhosting; }
 };
 
 inline bool is_hot(const taa_parameters_t& P) {
     return P.mUseYCoCg && !P.mToneMapLumaKaris && P.mVarianceClipping && !P.mShrinkChromaAxis && !P.mRayTraceAugment &&
            P.mColorClampingOrClipping == 2 && P.mUseVelocityVectors == 2 && P.mVelocitySampleMode == 0 &&
-           !P.mVelBasedAlpha && !P.mLumaWeightingLottes && !P.mReduceBlendNearClamp;
+           !P.mVelBasedAlpha && !P.mLumaWeightingLottes && !P.mReduceBlendNearClamp && !P.mAddNoise &&
+           !P.mDynamicAntiGhosting;
 }
 
 struct C3 { float x, y, z; };
@@ -203,7 +206,13 @@ __device__ __forceinline__ void history_position(const taa_uniforms_t& U, const 
                                                  float& hv, float& ehd) {
     const bool can = !(M.use_velocity() == 0 || (M.use_velocity() == 1 && vs.w < 0.5f));
     if (can) {
-        if (M.velocity_sample() == 2) {
+        if (M.velocity_sample() == 1) {
+            // 3x3 "longest": the reference keeps the last of its eight taps,
+            // (+1, +1), whatever their lengths (taa.comp:398-412)
+            const float4 s = fetch_velocity<MC>(a.velocity, cx + 1, cy + 1);
+            vs.x = s.x;
+            vs.y = s.y;
+        } else if (M.velocity_sample() == 2) {
             int bdx = -1, bdy = -1;
             float dc = fetch_r32f(a.depth, cx - 1, cy - 1);
 #pragma unroll
@@ -220,6 +229,22 @@ __device__ __forceinline__ void history_position(const taa_uniforms_t& U, const 
     } else {
         Pol::reproject(U, u, v, depth, hu, hv, ehd);
     }
+}
+
+// taa.comp:796-811, dynamic anti-ghosting: a pixel with no moving object in
+// its cross whose history was written under one (history alpha > 0) is
+// rejected; its own "moving" bit becomes the history alpha it writes.
+template <int MC>
+__device__ __forceinline__ void anti_ghosting(const FrameArgs& a, int cx, int cy, float hist_alpha, bool& rejected,
+                                              float& dyn) {
+    const float eps = 1e-5f;
+    auto mov = [&](int dx, int dy) {
+        const float4 v = fetch_velocity<MC>(a.velocity, cx + dx, cy + dy);
+        return (fabsf(v.x) > eps || fabsf(v.y) > eps) && (fabsf(v.w) >= 0.5f);
+    };
+    const bool mL = mov(-1, 0), mR = mov(1, 0), mT = mov(0, -1), mB = mov(0, 1), mC = mov(0, 0);
+    if (!(mL || mR || mT || mB || mC) && hist_alpha > 0.0f) rejected = true;
+    dyn = mC ? 1.0f : 0.0f;
 }
 
 // Shared memory of one tile.
@@ -320,6 +345,11 @@ __device__ __forceinline__ void place_window(const taa_uniforms_t& U, const Fram
 // null, is this thread's previous-frame depth at its history position,
 // fetched ahead (depth culling); `abort` (persistent CTAs) is set when a
 // window wait gave up.
+// The anti-ghosting mask reaches the finishers that store a history alpha.
+template <class Fin> __device__ __forceinline__ void set_dynamic_mask(Fin&, float) {}
+struct StoreFinish;
+__device__ __forceinline__ void set_dynamic_mask(StoreFinish& fin, float dyn);
+
 // The barrier among the threads that compute a tile (the whole CTA).
 struct CtaSync {
     static __device__ __forceinline__ void sync() { __syncthreads(); }
@@ -424,12 +454,17 @@ __device__ __forceinline__ void tile_compute(const taa_uniforms_t& U, const Fram
             const bool in_win = windowed && bx >= 0 && by >= 0 && bx + span <= WWS && by + span <= WH;
             if (in_win) {
                 const HT* base = &win[by * WWS + bx];
-                hraw = Pol::template filter_window<INTERP, HF>(taps, base, WWS);
+                hraw = Pol::template filter_window<INTERP, HF, !HOT>(taps, base, WWS);
             } else {
-                hraw = Pol::template filter<INTERP>(
+                hraw = Pol::template filter<INTERP, !HOT>(
                     taps, hi.w, hi.h, [&](int tx_, int ty_) { return fetch_history<HF>(hi, tx_, ty_); });
             }
         }
+    }
+    if (M.anti_ghost()) {
+        float dyn = 0.f;
+        anti_ghosting<MC>(a, cx, cy, hraw.w, rejected, dyn);
+        set_dynamic_mask(fin, dyn);
     }
     // rectification, blend and stores: every thread of the CTA calls the
     // finisher (valid says whether its pixel is in the image and resolved)
@@ -468,13 +503,15 @@ __device__ __forceinline__ void tile_body(const taa_uniforms_t& U, const FrameAr
 }
 
 // The finisher of the plain tiled forms: the policy's rectification and
-// blend (taa.comp:825-900), then the history and screen stores.
+// blend (taa.comp:825-900), then the history and screen stores; `dyn` is the
+// history alpha it writes (the anti-ghosting mask, else 0).
 struct StoreFinish {
+    float dyn = 0.f;
     template <class Pol, int HF, bool HOT>
     static __device__ __forceinline__ void run(const taa_uniforms_t& U, const FrameArgs& a, const taa_parameters_t& P,
                                                const Mode<HOT>& M, const typename Pol::Box& box, const C3& c0,
                                                float4 hraw, float u, float v, float hu, float hv, float, float,
-                                               bool rejected, bool valid, int x, int y, bool tm, StoreFinish&) {
+                                               bool rejected, bool valid, int x, int y, bool tm, StoreFinish& fin) {
         if (!valid) return;
         float4 o;
         if constexpr (Pol::kExactFallback) {
@@ -485,13 +522,15 @@ struct StoreFinish {
         } else {
             o = Pol::template finish<HOT>(U, P, M, box, c0, hraw, u, v, hu, hv, rejected);
         }
-        store_history<HF>(a.history_out, x, y, make_float4(o.x, o.y, o.z, 0.f));
+        store_history<HF>(a.history_out, x, y, make_float4(o.x, o.y, o.z, fin.dyn));
         if (a.result.p) {
             if (tm) o = Pol::un_tonemap(o);
             store_rgba16f(a.result, x, y, make_float4(o.x, o.y, o.z, 1.0f));
         }
     }
 };
+
+__device__ __forceinline__ void set_dynamic_mask(StoreFinish& fin, float dyn) { fin.dyn = dyn; }
 
 // A tile of TX x (TYT * NPX) pixels resolved by TX x TYT threads, each taking
 // NPX vertically adjacent pixels (rows NPX * ly ... NPX * ly + NPX - 1); staged
@@ -705,12 +744,13 @@ __device__ __forceinline__ void multi_body(const taa_uniforms_t& U, const FrameA
             const int bx = taps.t[0].ux - wx0, by = taps.t[0].uy - wy0;
             const bool in_win = windowed && bx >= 0 && by >= 0 && bx + span <= WWS && by + span <= WH;
             if (in_win) {
-                hraw = Pol::template filter_window<INTERP, HF>(taps, &sm.win[by * WWS + bx], WWS);
+                hraw = Pol::template filter_window<INTERP, HF, !HOT>(taps, &sm.win[by * WWS + bx], WWS);
             } else {
-                hraw = Pol::template filter<INTERP>(
+                hraw = Pol::template filter<INTERP, !HOT>(
                     taps, hi.w, hi.h, [&](int tx_, int ty_) { return fetch_history<HF>(hi, tx_, ty_); });
             }
         }
+        if (M.anti_ghost()) anti_ghosting<MC>(a, cx, min(y, H - 1), hraw.w, rejected, fin.dyn);
         const C3 c0 = Pol::centre(box[k], &sm.col[(NPX * ly + k + 1) * SX + lx + 1]);
         StoreFinish::run<Pol, HF, HOT>(U, a, P, M, box[k], c0, hraw, u[k], v[k], hu[k], hv[k], ehd[k], prev_depth[k],
                                        rejected, valid, x, y, tm, fin);

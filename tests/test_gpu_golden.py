@@ -108,5 +108,27 @@ def test_tiled_form_on_reference_fixtures(cuda, key):
         np.testing.assert_array_equal(hist, phist)
         np.testing.assert_array_equal(seg, pseg)
         assert np.mean(seg == FIX[f"{key}/ref64_segmask"]) >= 0.99
+    elif used == T.TAA_FORM_TILED and name in TRANSCENDENTAL:
+        # the noise hashes CUDA's sinf like the plain form: the plain form's bits
+        _, phist, _ = gpu(key, T.TAA_FORM_PLAIN, cuda)
+        np.testing.assert_array_equal(hist, phist)
     elif used == T.TAA_FORM_TILED:
         np.testing.assert_array_equal(hist, oracle32(key)["history"].astype(np.float32))
+
+
+# parameter modes the tiled forms run since they gained noise, dynamic
+# anti-ghosting (the mask in the history alpha) and the 3x3-longest velocity
+TILED_NOW = ("noise", "anti_ghosting", "velocity_longest")
+
+
+@pytest.mark.parametrize("name", TILED_NOW)
+def test_tiled_form_runs_the_extra_modes(cuda, name):
+    key = f"s:{name}"
+    used, hist, _ = gpu(key, T.TAA_FORM_TILED, cuda)
+    assert used == T.TAA_FORM_TILED
+    _, phist, _ = gpu(key, T.TAA_FORM_PLAIN, cuda)
+    np.testing.assert_array_equal(hist, phist)  # alpha included: the dynamic mask
+    used16, hist16, _ = gpu(key, T.TAA_FORM_FP16, cuda)
+    assert used16 == T.TAA_FORM_FP16
+    np.testing.assert_array_equal(hist16[..., 3], phist[..., 3])
+    assert np.linalg.norm(hist16[..., :3] - phist[..., :3]) <= 1e-2 * np.linalg.norm(phist[..., :3])

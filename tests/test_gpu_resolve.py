@@ -13,11 +13,12 @@ import itertools
 
 import numpy as np
 import pytest
+import torch
 
 import oracle as O
 import taa_abi as T
 import workloads as WL
-from helpers import cpu_frames, gpu_resolve, half_ulp, max_rel, psnr, rel_l2
+from helpers import cpu_frames, gpu_resolve, half_ulp, max_rel, psnr, rel_l2, to_dev
 
 pytestmark = pytest.mark.gpu
 
@@ -291,3 +292,69 @@ def test_device_status_stays_clear(cuda):
         gpu_resolve(ctx, cuda, fr[1]["color"], fr[1]["depth"], fr[1]["motion"], hist, fr[0]["depth"])
         ctx.close()
     assert T.device_status(clear=True) == 0
+
+
+@pytest.mark.parametrize("mode", ["anti_ghosting", "velocity_longest", "noise", "all_three"])
+def test_tiled_and_batch_run_the_extra_modes(cuda, mode):
+    """Dynamic anti-ghosting (5-tap mover test, the mask in the history alpha),
+    the 3x3-longest velocity (the reference keeps the last tap) and noise run in
+    the tiled forms and the batch: on a frame with moving blocks (motion .w set)
+    and a history whose alpha marks earlier movers, the tiled form gives the FP32
+    oracle's bits (the plain form's for noise, which hashes CUDA's sinf) and the
+    batch gives each view the tiled form's bits."""
+    w, h = 97, 61
+    over = {"anti_ghosting": dict(mDynamicAntiGhosting=1), "velocity_longest": dict(mVelocitySampleMode=1),
+            "noise": dict(mAddNoise=1, mNoiseFactor=1.0 / 64.0),
+            "all_three": dict(mDynamicAntiGhosting=1, mVelocitySampleMode=1, mAddNoise=1)}[mode]
+    wl = WL.small(w, h, frames=2, seed=29, params=dict(mUseVelocityVectors=1, **over))
+    fr = cpu_frames(wl, range(2), motion_channels=4)
+    rng = np.random.default_rng(3)
+    mot = fr[1]["motion"].astype(np.float32)
+    yy, xx = np.mgrid[0:h, 0:w]
+    movers = ((yy // 8 + xx // 8) % 3) == 0
+    mot[..., 3] = np.where(movers, 1.0, 0.0)
+    mot[movers, 0] += np.float32(2.0 / w)  # movers move by two texels
+    fr[1]["motion"] = mot.astype(np.float16)
+    hist = fr[0]["color"].astype(np.float32)
+    hist[..., 3] = (rng.uniform(size=(h, w)) < 0.4).astype(np.float32)  # earlier movers
+    u = T.make_uniforms(wl.parameters(), jitter_ndc=fr[1]["jitter"], mSinTime=(0.37, 0.0, 0.0, 0.0))
+    outs = {}
+    for form in (T.TAA_FORM_PLAIN, T.TAA_FORM_TILED, T.TAA_FORM_FP16):
+        ctx = T.Taa(w, h, motion_format=T.TAA_MOTION_RGBA16F, form=form)
+        ctx.set_uniforms(u)
+        assert ctx.selected_form() == form
+        outs[form] = gpu_resolve(ctx, cuda, fr[1]["color"], fr[1]["depth"], fr[1]["motion"], hist,
+                                 fr[0]["depth"])["history_out"]
+        ctx.close()
+    tiled, plain = outs[T.TAA_FORM_TILED], outs[T.TAA_FORM_PLAIN]
+    if mode in ("noise", "all_three"):
+        np.testing.assert_array_equal(tiled, plain)
+    else:
+        ref = oracle_for(u, fr[1], fr[0], hist)["history"].astype(np.float32)
+        np.testing.assert_array_equal(tiled, ref)
+        np.testing.assert_array_equal(plain, ref)
+    if "anti" in mode or mode == "all_three":
+        assert 0.0 < tiled[..., 3].mean() < 1.0  # the mask marks the movers and only them
+    np.testing.assert_array_equal(outs[T.TAA_FORM_FP16][..., 3], tiled[..., 3])
+    # the batch: two views of the same frame
+    b = T.Batch([(w, h), (w, h)], motion_format=T.TAA_MOTION_RGBA16F)
+    views = []
+    for v in range(2):
+        b.set_uniforms(v, u)
+        views.append(dict(color=to_dev(fr[1]["color"], torch.float16, cuda),
+                          depth=to_dev(fr[1]["depth"], torch.float32, cuda),
+                          velocity=to_dev(fr[1]["motion"], torch.float16, cuda),
+                          history=to_dev(hist, torch.float32, cuda),
+                          history_depth=to_dev(fr[0]["depth"], torch.float32, cuda),
+                          history_out=torch.full((h, w, 4), float("nan"), device=cuda),
+                          result=torch.empty(h, w, 4, dtype=torch.float16, device=cuda)))
+    b.prepare(0, views)
+    for shape in ((16, 16), (16, 8)):  # the two-pixel and the one-pixel tile bodies
+        b.set_tuning(shape[0], shape[1], T.TAA_SCHEDULE_INTERLEAVED)
+        for v in range(2):
+            views[v]["history_out"].fill_(float("nan"))
+        b.launch(0)
+        torch.cuda.synchronize()
+        for v in range(2):
+            np.testing.assert_array_equal(views[v]["history_out"].cpu().numpy(), tiled)
+    b.close()
