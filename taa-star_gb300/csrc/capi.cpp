@@ -502,8 +502,13 @@ static int select_form(const taa_ctx* c, const taa_frame_io_t* io) {
     const taa_desc_t& d = c->desc;
     const bool sharpen = d.sharpener != TAA_SHARPEN_OFF;
     if (!taa_dev::fast_path_supported(c->uniforms, d.in_width, d.in_height, d.out_width, d.out_height, !sharpen,
-                                      !sharpen))
+                                      !sharpen)) {
+        // upsampling: the tiled FP32 form's path for it
+        if (!sharpen && !(io && io->debug) &&
+            taa_dev::up_path_supported(c->uniforms, d.in_width, d.in_height, d.out_width, d.out_height))
+            return TAA_FORM_TILED;
         return TAA_FORM_PLAIN;
+    }
     if (io && io->debug) return TAA_FORM_PLAIN;
     if (d.form == TAA_FORM_FP16 && !sharpen) return TAA_FORM_FP16;
     return TAA_FORM_TILED;

@@ -145,6 +145,54 @@ template <int HF> __device__ __forceinline__ void store_history(const ImgW& im, 
 
 __device__ __forceinline__ float fractf(float x) { return x - floorf(x); }
 
+// Exact-weight bilinear sample at (u, v) of a w x h image read through
+// tex(x, y), clamp to edge (texel centres at k + 0.5) - the sampler model of
+// the oracle; a NaN fraction weights the first tap by 1.
+template <class F>
+__device__ __forceinline__ float4 bilinear_uv(int w, int h, float u, float v, F&& tex) {
+    float px = u * (float)w - 0.5f;
+    float py = v * (float)h - 0.5f;
+    float fx0 = floorf(px), fy0 = floorf(py);
+    float fx = px - fx0, fy = py - fy0;
+    int x0 = trunc_index(fx0), y0 = trunc_index(fy0);
+    if (!(fx == fx)) fx = 0.f;
+    if (!(fy == fy)) fy = 0.f;
+    int xa = clampi(x0, 0, w - 1), xb = clampi(x0 + 1 < x0 ? x0 : x0 + 1, 0, w - 1);
+    int ya = clampi(y0, 0, h - 1), yb = clampi(y0 + 1 < y0 ? y0 : y0 + 1, 0, h - 1);
+    float4 a = tex(xa, ya), b = tex(xb, ya), c = tex(xa, yb), d = tex(xb, yb);
+    float gx = 1.0f - fx, gy = 1.0f - fy;
+    float4 top = make_float4(a.x * gx + b.x * fx, a.y * gx + b.y * fx, a.z * gx + b.z * fx, a.w * gx + b.w * fx);
+    float4 bot = make_float4(c.x * gx + d.x * fx, c.y * gx + d.y * fx, c.z * gx + d.z * fx, c.w * gx + d.w * fx);
+    return make_float4(top.x * gy + bot.x * fy, top.y * gy + bot.y * fy, top.z * gy + bot.z * fy,
+                       top.w * gy + bot.w * fy);
+}
+
+// taa.comp:222-257: which jittered source sample lands in target texel
+// (tx, ty) of a loW x loH -> hiW x hiH upsampling; true (beta = 1) with the
+// source texel (fx, fy) when one does, false (beta = 0) otherwise.
+__device__ __forceinline__ bool upsampled_source(const taa_uniforms_t& U, const taa_parameters_t& P, int tx, int ty,
+                                                 int hiW, int hiH, int loW, int loH, int& fx, int& fy) {
+    const float scx = (float)hiW / (float)loW, scy = (float)hiH / (float)loH;
+    const float jux = U.mJitterNdc[0] * 0.5f * P.mUnjitterFactor, juy = U.mJitterNdc[1] * 0.5f * P.mUnjitterFactor;
+    const float tjx = jux * (float)loW * -1.0f, tjy = juy * (float)loH * -1.0f;
+    float fdx = -1.f, fdy = -1.f;
+    const float one = 0.999999f;
+    const float ox[4] = {0.f, one, 0.f, one};
+    const float oy[4] = {0.f, 0.f, one, one};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float sx = floorf((float)loW * ((float)tx + ox[k]) / (float)hiW) + 0.5f + tjx;
+        const float sy = floorf((float)loH * ((float)ty + oy[k]) / (float)hiH) + 0.5f + tjy;
+        if (trunc_index(sx * scx) == tx && trunc_index(sy * scy) == ty) {
+            fdx = sx;
+            fdy = sy;
+        }
+    }
+    fx = trunc_index(floorf(fdx));
+    fy = trunc_index(floorf(fdy));
+    return fdx >= 0.0f;
+}
+
 // taa.comp:551-556: the noise added to the result when mAddNoise is set,
 // seeded by the pixel's uv and mSinTime.x.
 __device__ __forceinline__ float4 taa_noise(const taa_uniforms_t& U, const taa_parameters_t& P, float u, float v) {

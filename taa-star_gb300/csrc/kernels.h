@@ -29,6 +29,12 @@ struct FastKey {
 // extra_modes_ok (the tiled forms without a fused sharpener and the batch).
 bool fast_path_supported(const taa_uniforms_t& U, int in_w, int in_h, int out_w, int out_h, bool rt_augment_ok = false,
                          bool extra_modes_ok = false);
+// Whether the tiled FP32 form's upsampling path (tiled_up.cuh) runs these
+// parameters and sizes: TAAU (mUpsampling) from a source no larger than the
+// target in either axis, simple velocity sampling, no anti-ghosting, no
+// segmentation mask, no split screen, pass-through or bypass, and an
+// unjittered neighbourhood only with a zero jitter.
+bool up_path_supported(const taa_uniforms_t& U, int in_w, int in_h, int out_w, int out_h);
 
 // Tiled FP32 / FP16 resolve, optionally with the fused sharpen (resolve_fast.cu).
 cudaError_t launch_resolve_fast(const FastKey& key, const taa_uniforms_t& U, const FrameArgs& a,

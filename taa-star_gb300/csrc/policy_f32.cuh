@@ -187,11 +187,13 @@ struct ExactF32 : HistoryFilter {
         }
     }
 
-    // taa.comp:825-900: rectification and blend; returns the RGB result
-    template <bool HOT>
+    // taa.comp:825-900: rectification and blend; returns the RGB result.  UP:
+    // the upsampling form's blend, mix(history, current, alpha * beta) with
+    // beta = 1 on rejection and reset (beta 0: no source sample in the texel).
+    template <bool HOT, bool UP = false>
     static __device__ __forceinline__ float4 finish(const taa_uniforms_t& U, const taa_parameters_t& P,
                                                     const Mode<HOT>& M, const Box& b, const C3& c0, float4 hraw, float u,
-                                                    float v, float hu, float hv, bool rejected) {
+                                                    float v, float hu, float hv, bool rejected, float beta = 1.0f) {
         const bool yc = M.ycocg();
         C3 hc{hraw.x, hraw.y, hraw.z};
         if (yc)
@@ -251,6 +253,10 @@ struct ExactF32 : HistoryFilter {
             }
         }
         if (U.mResetHistory) alpha = 1.0f;
+        if constexpr (UP) {
+            if (rejected || U.mResetHistory) beta = 1.0f;
+            alpha = alpha * beta;
+        }
         float t = 1.0f - alpha;
         C3 o{hc.x * t + c0.x * alpha, hc.y * t + c0.y * alpha, hc.z * t + c0.z * alpha};
         if (yc) {

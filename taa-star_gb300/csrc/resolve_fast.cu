@@ -40,6 +40,17 @@ bool fast_path_supported(const taa_uniforms_t& U, int in_w, int in_h, int out_w,
     return true;
 }
 
+bool up_path_supported(const taa_uniforms_t& U, int in_w, int in_h, int out_w, int out_h) {
+    if (!U.mUpsampling || in_w > out_w || in_h > out_h || (in_w == out_w && in_h == out_h)) return false;
+    if (U.mBypassHistoryUpdate || (U.splitScreen && U.splitX < out_w - 1)) return false;
+    const taa_parameters_t& P = U.param[0];
+    if (P.mPassThrough || P.mRayTraceAugment || P.mDynamicAntiGhosting || P.mVelocitySampleMode != 0) return false;
+    if (P.mInterpolationMode < 0 || P.mInterpolationMode > 2) return false;
+    const bool jitter_zero = U.mJitterNdc[0] * 0.5f * P.mUnjitterFactor == 0.f &&
+                             U.mJitterNdc[1] * 0.5f * P.mUnjitterFactor == 0.f;
+    return !P.mUnjitterNeighbourhood || jitter_zero;
+}
+
 namespace {
 
 constexpr int kTileX = 32;

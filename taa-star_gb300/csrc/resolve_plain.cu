@@ -43,21 +43,7 @@ __device__ __forceinline__ V3 vmix(V3 x, V3 y, float a) {
 // Exact-weight bilinear, clamp to edge (texel centres at k + 0.5).
 template <class F>
 __device__ __forceinline__ float4 bilinear(int w, int h, V2 uv, F&& tex) {
-    float px = uv.x * (float)w - 0.5f;
-    float py = uv.y * (float)h - 0.5f;
-    float fx0 = floorf(px), fy0 = floorf(py);
-    float fx = px - fx0, fy = py - fy0;
-    int x0 = trunc_index(fx0), y0 = trunc_index(fy0);
-    if (!(fx == fx)) fx = 0.f;
-    if (!(fy == fy)) fy = 0.f;
-    int xa = clampi(x0, 0, w - 1), xb = clampi(x0 + 1 < x0 ? x0 : x0 + 1, 0, w - 1);
-    int ya = clampi(y0, 0, h - 1), yb = clampi(y0 + 1 < y0 ? y0 : y0 + 1, 0, h - 1);
-    float4 a = tex(xa, ya), b = tex(xb, ya), c = tex(xa, yb), d = tex(xb, yb);
-    float gx = 1.0f - fx, gy = 1.0f - fy;
-    float4 top = make_float4(a.x * gx + b.x * fx, a.y * gx + b.y * fx, a.z * gx + b.z * fx, a.w * gx + b.w * fx);
-    float4 bot = make_float4(c.x * gx + d.x * fx, c.y * gx + d.y * fx, c.z * gx + d.z * fx, c.w * gx + d.w * fx);
-    return make_float4(top.x * gy + bot.x * fy, top.y * gy + bot.y * fy, top.z * gy + bot.z * fy,
-                       top.w * gy + bot.w * fy);
+    return bilinear_uv(w, h, uv.x, uv.y, tex);
 }
 
 template <int HF, int MC>
@@ -112,23 +98,10 @@ struct PlainResolver {
 
     // taa.comp:222-257
     __device__ V3 upsampled_color(int tx, int ty, float& beta) const {
-        V2 scale{(float)hiW / (float)loW, (float)hiH / (float)loH};
-        V2 ju = jitter_uv();
-        V2 tj{ju.x * (float)loW * -1.0f, ju.y * (float)loH * -1.0f};
-        V2 found{-1.f, -1.f};
-        const float one = 0.999999f;
-        const float ox[4] = {0.f, one, 0.f, one};
-        const float oy[4] = {0.f, 0.f, one, one};
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            V2 s{floorf((float)loW * ((float)tx + ox[k]) / (float)hiW) + 0.5f + tj.x,
-                 floorf((float)loH * ((float)ty + oy[k]) / (float)hiH) + 0.5f + tj.y};
-            if (trunc_index(s.x * scale.x) == tx && trunc_index(s.y * scale.y) == ty) found = s;
-        }
-        if (found.x >= 0.0f) {
+        int fx, fy;
+        if (upsampled_source(U, *P, tx, ty, hiW, hiH, loW, loH, fx, fy)) {
             beta = 1.0f;
-            return maybe_rgb_to_ycocg(
-                tonemap_rgb(rgb3(col(trunc_index(floorf(found.x)), trunc_index(floorf(found.y))))));
+            return maybe_rgb_to_ycocg(tonemap_rgb(rgb3(col(fx, fy))));
         }
         beta = 0.0f;
         return {0.f, 0.f, 0.f};

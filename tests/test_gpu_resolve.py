@@ -358,3 +358,42 @@ def test_tiled_and_batch_run_the_extra_modes(cuda, mode):
         for v in range(2):
             np.testing.assert_array_equal(views[v]["history_out"].cpu().numpy(), tiled)
     b.close()
+
+
+UP_MODES = {
+    "base": {}, "c2": dict(mDepthCulling=1, mRejectOutside=1), "bilinear": dict(mInterpolationMode=0),
+    "bspline": dict(mInterpolationMode=1), "clamp_rgb": dict(mColorClampingOrClipping=1, mUseYCoCg=0,
+                                                            mVarianceClipping=0),
+    "clip_slow_shaped": dict(mColorClampingOrClipping=3, mShapedNeighbourhood=1, mVarianceClipping=0),
+    "tonemap_lottes": dict(mToneMapLumaKaris=1, mLumaWeightingLottes=1),
+    "reprojection": dict(mUseVelocityVectors=0), "noise": dict(mAddNoise=1),
+}
+
+
+@pytest.mark.parametrize("sizes", [((48, 32), (96, 64)), ((64, 40), (96, 60)), ((80, 45), (97, 61)),
+                                   ((40, 40), (40, 72))], ids=["2x", "1.5x", "odd", "one_axis"])
+@pytest.mark.parametrize("mode", list(UP_MODES))
+def test_upsampling_runs_in_the_tiled_form(cuda, mode, sizes):
+    """TAAU (taa.comp:222-257): the tiled form's upsampling path gives the FP32
+    oracle's bits (the plain form's for noise, which hashes CUDA's sinf) at
+    integer, fractional and one-axis ratios and odd sizes."""
+    (w, h), (ow, oh) = sizes
+    wl = WL.small(w, h, frames=2, seed=ow + oh, params=UP_MODES[mode])
+    fr = cpu_frames(wl, range(2), motion_channels=2)
+    rng = np.random.default_rng(ow)
+    hist = np.ascontiguousarray(rng.uniform(0.0, 2.0, (oh, ow, 4)).astype(np.float32))
+    u = T.make_uniforms(wl.parameters(), jitter_ndc=fr[1]["jitter"], mUpsampling=1)
+    outs = {}
+    for form in (T.TAA_FORM_PLAIN, T.TAA_FORM_AUTO):
+        ctx = T.Taa(w, h, ow, oh, form=form)
+        ctx.set_uniforms(u)
+        outs[ctx.selected_form()] = gpu_resolve(ctx, cuda, fr[1]["color"], fr[1]["depth"], fr[1]["motion"], hist,
+                                                fr[0]["depth"])
+        ctx.close()
+    assert set(outs) == {T.TAA_FORM_PLAIN, T.TAA_FORM_TILED}
+    tiled, plain = outs[T.TAA_FORM_TILED], outs[T.TAA_FORM_PLAIN]
+    np.testing.assert_array_equal(tiled["history_out"], plain["history_out"])
+    np.testing.assert_array_equal(tiled["result"], plain["result"])
+    if mode != "noise":
+        ref = oracle_for(u, fr[1], fr[0], hist, out_size=(ow, oh))
+        np.testing.assert_array_equal(tiled["history_out"], ref["history"].astype(np.float32))
