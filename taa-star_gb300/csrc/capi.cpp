@@ -509,7 +509,8 @@ static int select_form(const taa_ctx* c, const taa_frame_io_t* io) {
             return TAA_FORM_TILED;
         return TAA_FORM_PLAIN;
     }
-    if (io && io->debug) return TAA_FORM_PLAIN;
+    // a debug binding: the tiled FP32 form writes it (the fused sharpener does not)
+    if (io && io->debug) return sharpen ? TAA_FORM_PLAIN : TAA_FORM_TILED;
     if (d.form == TAA_FORM_FP16 && !sharpen) return TAA_FORM_FP16;
     return TAA_FORM_TILED;
 }

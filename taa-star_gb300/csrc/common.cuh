@@ -167,30 +167,52 @@ __device__ __forceinline__ float4 bilinear_uv(int w, int h, float u, float v, F&
                        top.w * gy + bot.w * fy);
 }
 
-// taa.comp:222-257: which jittered source sample lands in target texel
-// (tx, ty) of a loW x loH -> hiW x hiH upsampling; true (beta = 1) with the
-// source texel (fx, fy) when one does, false (beta = 0) otherwise.
-__device__ __forceinline__ bool upsampled_source(const taa_uniforms_t& U, const taa_parameters_t& P, int tx, int ty,
-                                                 int hiW, int hiH, int loW, int loH, int& fx, int& fy) {
-    const float scx = (float)hiW / (float)loW, scy = (float)hiH / (float)loH;
-    const float jux = U.mJitterNdc[0] * 0.5f * P.mUnjitterFactor, juy = U.mJitterNdc[1] * 0.5f * P.mUnjitterFactor;
-    const float tjx = jux * (float)loW * -1.0f, tjy = juy * (float)loH * -1.0f;
+// taa.comp:222-257: which jittered source sample lands in a target texel of
+// a loW x loH -> hiW x hiH upsampling.  The shader tries the four corner
+// offsets (0, 0), (1, 0), (0, 1), (1, 1) (1 = 0.999999) and keeps the last
+// sample that lands in the texel; each coordinate depends on one axis only,
+// so the candidates are formed per axis (upsample_axis, the shader's
+// arithmetic on that axis) and paired (upsampled_pick).
+struct UpAxis {
+    float s[2];    // the candidate sample coordinate for offsets 0 and 0.999999
+    bool hit[2];   // whether it lands in the texel on this axis
+};
+__device__ __forceinline__ UpAxis upsample_axis(int t, int hi, int lo, float tj, float scale) {
+    UpAxis r;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const float o = j ? 0.999999f : 0.f;
+        r.s[j] = floorf((float)lo * ((float)t + o) / (float)hi) + 0.5f + tj;
+        r.hit[j] = trunc_index(r.s[j] * scale) == t;
+    }
+    return r;
+}
+// The jitter of an axis in source texels (taa.comp:225-227) and the axis scale.
+__device__ __forceinline__ float upsample_jitter(float jitter_ndc, float unjitter_factor, int lo) {
+    return jitter_ndc * 0.5f * unjitter_factor * (float)lo * -1.0f;
+}
+// True (beta = 1) with the source texel (fx, fy) when a sample lands.
+__device__ __forceinline__ bool upsampled_pick(const UpAxis& X, const UpAxis& Y, int& fx, int& fy) {
     float fdx = -1.f, fdy = -1.f;
-    const float one = 0.999999f;
-    const float ox[4] = {0.f, one, 0.f, one};
-    const float oy[4] = {0.f, 0.f, one, one};
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        const float sx = floorf((float)loW * ((float)tx + ox[k]) / (float)hiW) + 0.5f + tjx;
-        const float sy = floorf((float)loH * ((float)ty + oy[k]) / (float)hiH) + 0.5f + tjy;
-        if (trunc_index(sx * scx) == tx && trunc_index(sy * scy) == ty) {
-            fdx = sx;
-            fdy = sy;
+        const int jx = k & 1, jy = k >> 1;
+        if (X.hit[jx] && Y.hit[jy]) {
+            fdx = X.s[jx];
+            fdy = Y.s[jy];
         }
     }
     fx = trunc_index(floorf(fdx));
     fy = trunc_index(floorf(fdy));
     return fdx >= 0.0f;
+}
+__device__ __forceinline__ bool upsampled_source(const taa_uniforms_t& U, const taa_parameters_t& P, int tx, int ty,
+                                                 int hiW, int hiH, int loW, int loH, int& fx, int& fy) {
+    const UpAxis X = upsample_axis(tx, hiW, loW, upsample_jitter(U.mJitterNdc[0], P.mUnjitterFactor, loW),
+                                   (float)hiW / (float)loW);
+    const UpAxis Y = upsample_axis(ty, hiH, loH, upsample_jitter(U.mJitterNdc[1], P.mUnjitterFactor, loH),
+                                   (float)hiH / (float)loH);
+    return upsampled_pick(X, Y, fx, fy);
 }
 
 // taa.comp:551-556: the noise added to the result when mAddNoise is set,
@@ -201,6 +223,55 @@ __device__ __forceinline__ float4 taa_noise(const taa_uniforms_t& U, const taa_p
     const float f = P.mNoiseFactor;
     return make_float4((fractf(s * 43758.5453f) * 2.0f - 1.0f) * f, (fractf(s * 28001.8384f) * 2.0f - 1.0f) * f,
                        (fractf(s * 50849.4141f) * 2.0f - 1.0f) * f, (fractf(s * 12996.89f) * 2.0f - 1.0f) * f);
+}
+
+// taa.comp:912-942: a pixel's debug output - mode mDebugMode of the box
+// extents (0, 1), the rejection and the rectification's move (2), the blend
+// weight (3), the velocity (4), the pixel speed (5), the screen and history
+// values (6, 7) or the ray-trace-assist class (8) - scaled by mDebugScale and
+// the mask and optionally centred.  Shared by the plain and tiled forms.
+struct DebugIn {
+    float3 mn, mx, rdiff;  // box bounds, clipped minus unclipped history (working space)
+    bool rejected;
+    float alpha, speed;     // the blend weight (after a reset), |uv - history uv|
+    float4 vel, to_screen, to_hist;
+    uint32_t seg;
+};
+__device__ __forceinline__ float4 debug_value(const taa_parameters_t& P, const DebugIn& d) {
+    float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+    switch (P.mDebugMode) {
+        case 0: g = make_float4(d.mx.x - d.mn.x, d.mx.y - d.mn.y, d.mx.z - d.mn.z, 0.f); break;
+        case 1: {
+            const float tx = d.mx.x - d.mn.x, ty = d.mx.y - d.mn.y, tz = d.mx.z - d.mn.z;
+            const float v = tx * ty * tz;
+            g = make_float4(v, v, v, 0.f);
+            break;
+        }
+        case 2: {
+            const float l = sqrtf(d.rdiff.x * d.rdiff.x + d.rdiff.y * d.rdiff.y + d.rdiff.z * d.rdiff.z);
+            g = make_float4(d.rejected ? 1.f : 0.f, l, 0.f, 0.f);
+            break;
+        }
+        case 3: g = make_float4(d.alpha, d.alpha, d.alpha, 0.f); break;
+        case 4: g = d.vel; break;
+        case 5: g = make_float4(d.speed, 0.f, 0.f, 0.f); break;
+        case 6: g = d.to_screen; break;
+        case 7: g = d.to_hist; break;
+        case 8:
+            switch (d.seg & 3u) {
+                case 0: g = make_float4(0.f, 0.f, 1.f, 0.f); break;
+                case 1: g = make_float4(1.f, 0.f, 0.f, 0.f); break;
+                case 2: g = make_float4(1.f, 1.f, 0.f, 0.f); break;
+                default: break;
+            }
+            break;
+        default: break;
+    }
+    const float s = P.mDebugScale;
+    g = make_float4(g.x * (s * P.mDebugMask[0]), g.y * (s * P.mDebugMask[1]), g.z * (s * P.mDebugMask[2]),
+                    g.w * (s * P.mDebugMask[3]));
+    if (P.mDebugCenter) g = make_float4(g.x * 0.5f + 0.5f, g.y * 0.5f + 0.5f, g.z * 0.5f + 0.5f, g.w * 0.5f + 0.5f);
+    return g;
 }
 
 // Correctly rounded x / d for a constant divisor d with precomputed

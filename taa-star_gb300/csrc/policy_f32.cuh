@@ -30,6 +30,12 @@ struct ExactF32 : HistoryFilter {
     static constexpr bool kExactCentre = false;
     // the FP32 box needs no fallback
     static constexpr bool kExactFallback = false;
+    // debug outputs (taa.comp:912-942): the box bounds and what finish records
+    static constexpr bool kDebug = true;
+    template <class B> static __device__ __forceinline__ void box_bounds(const B& b, float3& mn, float3& mx) {
+        mn = make_float3(b.mn.x, b.mn.y, b.mn.z);
+        mx = make_float3(b.mx.x, b.mx.y, b.mx.z);
+    }
     static __device__ __forceinline__ void centre_colour(Box&, const Img&, int, int, bool, bool) {}
 
     // working-space conversion of one source texel (taa.comp:182-213)
@@ -193,7 +199,8 @@ struct ExactF32 : HistoryFilter {
     template <bool HOT, bool UP = false>
     static __device__ __forceinline__ float4 finish(const taa_uniforms_t& U, const taa_parameters_t& P,
                                                     const Mode<HOT>& M, const Box& b, const C3& c0, float4 hraw, float u,
-                                                    float v, float hu, float hv, bool rejected, float beta = 1.0f) {
+                                                    float v, float hu, float hv, bool rejected, float beta = 1.0f,
+                                                    FinishOut* fo = nullptr) {
         const bool yc = M.ycocg();
         C3 hc{hraw.x, hraw.y, hraw.z};
         if (yc)
@@ -229,6 +236,7 @@ struct ExactF32 : HistoryFilter {
             }
             default: break;
         }
+        if (fo) fo->rdiff = make_float3(hc.x - orig.x, hc.y - orig.y, hc.z - orig.z);
         float alpha = P.mAlpha;
         if (rejected) {
             alpha = P.mRejectionAlpha;
@@ -253,6 +261,7 @@ struct ExactF32 : HistoryFilter {
             }
         }
         if (U.mResetHistory) alpha = 1.0f;
+        if (fo) fo->alpha = alpha;
         if constexpr (UP) {
             if (rejected || U.mResetHistory) beta = 1.0f;
             alpha = alpha * beta;

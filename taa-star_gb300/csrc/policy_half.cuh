@@ -319,6 +319,7 @@ template <bool GUARD> struct HalfPol : tiled::HistoryFilter {
     // narrower than its widest - is finished in FP32 from the source texels
     // instead (exact_finish).
     static constexpr bool kExactFallback = GUARD;
+    static constexpr bool kDebug = false;  // a debug binding runs the tiled FP32 form
     static constexpr float kExactRatio = TAA_FP16_EXACT_RATIO;
     // The pixel as the FP32 form resolves it: its 3x3 source texels staged in
     // FP32, the FP32 box and the FP32 rectification and blend.

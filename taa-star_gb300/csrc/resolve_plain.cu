@@ -433,36 +433,18 @@ struct PlainResolver {
         float4 to_screen = make_float4(sc.x, sc.y, sc.z, 1.0f);
 
         if (a.debug.p) {
-            float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
-            switch (P->mDebugMode) {
-                case 0: { V3 t = mx - mn; g = make_float4(t.x, t.y, t.z, 0.f); break; }
-                case 1: { V3 t = mx - mn; float v = t.x * t.y * t.z; g = make_float4(v, v, v, 0.f); break; }
-                case 2: {
-                    float l = sqrtf(rdiff.x * rdiff.x + rdiff.y * rdiff.y + rdiff.z * rdiff.z);
-                    g = make_float4(rejected ? 1.f : 0.f, l, 0.f, 0.f);
-                    break;
-                }
-                case 3: g = make_float4(alpha, alpha, alpha, 0.f); break;
-                case 4: g = vel(x, y); break;
-                case 5: g = make_float4(speed, 0.f, 0.f, 0.f); break;
-                case 6: g = to_screen; break;
-                case 7: g = to_hist; break;
-                case 8:
-                    switch (seg & 3u) {
-                        case 0: g = make_float4(0.f, 0.f, 1.f, 0.f); break;
-                        case 1: g = make_float4(1.f, 0.f, 0.f, 0.f); break;
-                        case 2: g = make_float4(1.f, 1.f, 0.f, 0.f); break;
-                        default: break;
-                    }
-                    break;
-                default: break;
-            }
-            float s = P->mDebugScale;
-            g = make_float4(g.x * (s * P->mDebugMask[0]), g.y * (s * P->mDebugMask[1]), g.z * (s * P->mDebugMask[2]),
-                            g.w * (s * P->mDebugMask[3]));
-            if (P->mDebugCenter)
-                g = make_float4(g.x * 0.5f + 0.5f, g.y * 0.5f + 0.5f, g.z * 0.5f + 0.5f, g.w * 0.5f + 0.5f);
-            store_rgba16f(a.debug, x, y, g);
+            DebugIn d;
+            d.mn = make_float3(mn.x, mn.y, mn.z);
+            d.mx = make_float3(mx.x, mx.y, mx.z);
+            d.rdiff = make_float3(rdiff.x, rdiff.y, rdiff.z);
+            d.rejected = rejected;
+            d.alpha = alpha;
+            d.speed = speed;
+            d.vel = P->mDebugMode == 4 ? vel(x, y) : make_float4(0.f, 0.f, 0.f, 0.f);
+            d.to_screen = to_screen;
+            d.to_hist = to_hist;
+            d.seg = seg;
+            store_rgba16f(a.debug, x, y, debug_value(*P, d));
         }
         store_history<HF>(a.history_out, x, y, to_hist);
         if (a.result.p) store_rgba16f(a.result, x, y, to_screen);

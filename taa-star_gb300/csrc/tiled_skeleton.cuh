@@ -161,6 +161,13 @@ inline bool is_hot(const taa_parameters_t& P) {
 
 struct C3 { float x, y, z; };
 
+// What a policy's finish records for the debug outputs: the rectification's
+// move (clipped minus unclipped history) and the blend weight.
+struct FinishOut {
+    float3 rdiff;
+    float alpha;
+};
+
 // History filter taps: up to 16 texels (clamped coordinates) with weights.
 // INTERP 2: 4x4 separable Catmull-Rom; 0: one bilinear 2x2; 1: four bilinear
 // 2x2 sets combined with the "b-spline" weights.
@@ -507,6 +514,8 @@ __device__ __forceinline__ void tile_body(const taa_uniforms_t& U, const FrameAr
 // history alpha it writes (the anti-ghosting mask, else 0).
 struct StoreFinish {
     float dyn = 0.f;
+    uint32_t seg = 0;                            // the ray-trace-assist class (debug mode 8)
+    float4 dvel = make_float4(0.f, 0.f, 0.f, 0.f);  // the pixel's velocity (debug mode 4)
     template <class Pol, int HF, bool HOT>
     static __device__ __forceinline__ void run(const taa_uniforms_t& U, const FrameArgs& a, const taa_parameters_t& P,
                                                const Mode<HOT>& M, const typename Pol::Box& box, const C3& c0,
@@ -514,18 +523,39 @@ struct StoreFinish {
                                                bool rejected, bool valid, int x, int y, bool tm, StoreFinish& fin) {
         if (!valid) return;
         float4 o;
+        constexpr bool kDebug = Pol::kDebug && !HOT;
+        FinishOut fo;
         if constexpr (Pol::kExactFallback) {
             // a policy whose clip can be ill-conditioned for its precision finishes
             // such a pixel from the source texels in FP32
             const typename Pol::At at{&a, x, y, tm};
             o = Pol::template finish_at<HOT>(U, P, M, box, c0, hraw, u, v, hu, hv, rejected, &at);
+        } else if constexpr (kDebug) {
+            o = Pol::template finish<HOT>(U, P, M, box, c0, hraw, u, v, hu, hv, rejected, 1.0f,
+                                          a.debug.p ? &fo : nullptr);
         } else {
             o = Pol::template finish<HOT>(U, P, M, box, c0, hraw, u, v, hu, hv, rejected);
         }
-        store_history<HF>(a.history_out, x, y, make_float4(o.x, o.y, o.z, fin.dyn));
-        if (a.result.p) {
-            if (tm) o = Pol::un_tonemap(o);
-            store_rgba16f(a.result, x, y, make_float4(o.x, o.y, o.z, 1.0f));
+        const float4 to_hist = make_float4(o.x, o.y, o.z, fin.dyn);
+        store_history<HF>(a.history_out, x, y, to_hist);
+        if (tm) o = Pol::un_tonemap(o);
+        const float4 to_screen = make_float4(o.x, o.y, o.z, 1.0f);
+        if (a.result.p) store_rgba16f(a.result, x, y, to_screen);
+        if constexpr (kDebug) {
+            if (a.debug.p) {
+                DebugIn d;
+                Pol::box_bounds(box, d.mn, d.mx);
+                d.rdiff = fo.rdiff;
+                d.rejected = rejected;
+                d.alpha = fo.alpha;
+                const float du = u - hu, dv = v - hv;
+                d.speed = sqrtf(du * du + dv * dv);
+                d.vel = fin.dvel;
+                d.to_screen = to_screen;
+                d.to_hist = to_hist;
+                d.seg = fin.seg;
+                store_rgba16f(a.debug, x, y, debug_value(P, d));
+            }
         }
     }
 };
@@ -734,6 +764,7 @@ __device__ __forceinline__ void multi_body(const taa_uniforms_t& U, const FrameA
                 const uint32_t sg = seg::classify(P, x, y, hu[k], hv[k], W, H, StagedSeg<S>{ss, a, x0, y0});
                 if ((sg & 3u) != 0) rejected = true;
                 if (valid && a.segmask.p) *texel_ptr_w<uint32_t>(a.segmask, x, y) = sg;
+                fin.seg = sg;
             }
         }
         float4 hraw = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -751,6 +782,7 @@ __device__ __forceinline__ void multi_body(const taa_uniforms_t& U, const FrameA
             }
         }
         if (M.anti_ghost()) anti_ghosting<MC>(a, cx, min(y, H - 1), hraw.w, rejected, fin.dyn);
+        if (!HOT && a.debug.p && P.mDebugMode == 4) fin.dvel = fetch_velocity<MC>(a.velocity, x, y);
         const C3 c0 = Pol::centre(box[k], &sm.col[(NPX * ly + k + 1) * SX + lx + 1]);
         StoreFinish::run<Pol, HF, HOT>(U, a, P, M, box[k], c0, hraw, u[k], v[k], hu[k], hv[k], ehd[k], prev_depth[k],
                                        rejected, valid, x, y, tm, fin);
@@ -865,7 +897,7 @@ cudaError_t launch_tile(const taa_uniforms_t& U, const FrameArgs& a, cudaStream_
 
 template <class Pol, int HF, int MC>
 cudaError_t launch_interp(int interp, const taa_uniforms_t& U, const FrameArgs& a, cudaStream_t s) {
-    const bool hot = is_hot(U.param[0]), rt = U.param[0].mRayTraceAugment != 0;
+    const bool hot = is_hot(U.param[0]) && !a.debug.p, rt = U.param[0].mRayTraceAugment != 0;
     switch (interp) {
         case 0:
             return hot  ? launch_tile<Pol, HF, MC, 0, true>(U, a, s)

@@ -10,7 +10,8 @@
 //      history window at the tile's centre (TMA, or cp.async at the border);
 //   2. per target pixel: its source texel (int(uv * lo size)), the 3x3 box on
 //      the staged neighbourhood, the jittered source sample that lands in the
-//      pixel (upsampled_source, shared with the plain form) as the current
+//      pixel (upsample_axis / upsampled_pick, shared with the plain form; the
+//      column's half once per thread) as the current
 //      colour with beta = 1, else beta = 0; velocity sampled bilinearly at the
 //      pixel's uv, the history position and sample, rejection, and the
 //      policy's rectification with the blend mix(history, current,
@@ -101,6 +102,10 @@ __global__ void __launch_bounds__(S::NT, TAA_MULTI_MIN_BLOCKS * 256 / S::NT)
     // 2. per pixel: box, current sample, history position (before the window wait)
     const bool depth_cull = P.mDepthCulling != 0;
     const int x = x0 + lx, cx = min(x, W - 1);
+    // this thread's column of the upsampled-sample search (its pixels share it)
+    const UpAxis ux = upsample_axis(cx, W, loW, upsample_jitter(U.mJitterNdc[0], P.mUnjitterFactor, loW),
+                                    (float)W / (float)loW);
+    const float jy = upsample_jitter(U.mJitterNdc[1], P.mUnjitterFactor, loH), scy = (float)H / (float)loH;
     typename Pol::Box box[NPX];
     C3 cur[NPX];
     float beta[NPX], u[NPX], v[NPX], hu[NPX], hv[NPX], ehd[NPX], prev_depth[NPX];
@@ -117,7 +122,7 @@ __global__ void __launch_bounds__(S::NT, TAA_MULTI_MIN_BLOCKS * 256 / S::NT)
         int fx, fy;
         cur[k] = C3{0.f, 0.f, 0.f};
         beta[k] = 0.f;
-        if (upsampled_source(U, P, cx, cy, W, H, loW, loH, fx, fy)) {
+        if (upsampled_pick(ux, upsample_axis(cy, H, loH, jy, scy), fx, fy)) {
             beta[k] = 1.f;
             const int ix = fx - rx0, iy = fy - ry0;
             const float4 c = ix >= 0 && iy >= 0 && ix < rw && iy < rh

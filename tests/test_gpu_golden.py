@@ -39,7 +39,7 @@ def uniforms_of(key):
     return u
 
 
-def gpu(key, form, dev):
+def gpu(key, form, dev, debug=False):
     scene = key.split(":")[0]
     g = lambda k: FIX[f"{scene}/{k}"]
     hist = g("history")
@@ -57,15 +57,21 @@ def gpu(key, form, dev):
              prev_segmask=t(g("prev_segmask").view(np.int32), torch.int32), uvnrm=t(g("uvnrm"), torch.float32),
              history_out=torch.full((oh, ow, 4), float("nan"), device=dev),
              result=torch.full((oh, ow, 4), float("nan"), dtype=torch.float16, device=dev),
-             # a debug binding routes a call to the plain form, so only that form gets it
-             debug=torch.full((oh, ow, 4), float("nan"), dtype=torch.float16, device=dev)
-             if form == T.TAA_FORM_PLAIN else None,
+             debug=torch.full((oh, ow, 4), float("nan"), dtype=torch.float16, device=dev) if debug else None,
              segmask=torch.zeros((oh, ow), dtype=torch.int32, device=dev))
     used = ctx.selected_form()
     ctx.resolve(**b)
     torch.cuda.synchronize()
+    if debug:
+        # taa_selected_form answers for calls without a debug binding; with one the
+        # tiled FP32 form writes it unless the parameters need the plain form
+        # (upsampling with a debug binding runs in the plain form)
+        up = ow != w or oh != h
+        used = T.TAA_FORM_PLAIN if used == T.TAA_FORM_PLAIN or up else T.TAA_FORM_TILED
     ctx.close()
     seg = b["segmask"].cpu().numpy().view(np.uint32) if b["segmask"] is not None else None
+    if debug:
+        return used, b["history_out"].cpu().numpy(), seg, b["debug"].cpu().numpy()
     return used, b["history_out"].cpu().numpy(), seg
 
 
@@ -132,3 +138,19 @@ def test_tiled_form_runs_the_extra_modes(cuda, name):
     assert used16 == T.TAA_FORM_FP16
     np.testing.assert_array_equal(hist16[..., 3], phist[..., 3])
     assert np.linalg.norm(hist16[..., :3] - phist[..., :3]) <= 1e-2 * np.linalg.norm(phist[..., :3])
+
+
+
+@pytest.mark.parametrize("key", [k for k in CASES if k.split(":")[1].startswith("debug") or
+                                 k.split(":")[1] in ("base", "c2_depth_reject", "segmask_all_tests")])
+def test_debug_output_of_the_tiled_form(cuda, key):
+    """With a debug binding the tiled FP32 form writes the debug image
+    (taa.comp:912-942) with the plain form's bits, and the history is unchanged."""
+    used, hist, seg, dbg = gpu(key, T.TAA_FORM_TILED, cuda, debug=True)
+    assert used == T.TAA_FORM_TILED
+    pused, phist, pseg, pdbg = gpu(key, T.TAA_FORM_PLAIN, cuda, debug=True)
+    assert pused == T.TAA_FORM_PLAIN
+    np.testing.assert_array_equal(dbg, pdbg)
+    np.testing.assert_array_equal(hist, phist)
+    _, hist_nodebug, _ = gpu(key, T.TAA_FORM_TILED, cuda)
+    np.testing.assert_array_equal(hist, hist_nodebug)
