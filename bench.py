@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-fxaa", action="store_true")
     ap.add_argument("--no-modes", action="store_true")
+    ap.add_argument("--no-c3", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--profile", choices=["tiled", "fp16", "plain", "batch48", "fxaa"],
                     help="a small case for ncu: a few launches of one form on 4K frames (no JSON line)")
@@ -476,6 +477,72 @@ def time_modes(T, WL, dev, stream, sid, args, peak):
     return out
 
 
+def time_c3(T, WL, dev, stream, sid, args, peak):
+    """The resolve with a CAS sharpener (strength 0.5) on the C3 sequence
+    (2560x1440, 32 frames, spinning spheres), bilinear and Catmull-Rom history.
+    Per history filter and form: the resolve followed by the sharpen pass on
+    its RGBA16F result (the library's default, and the reference's structure
+    of two dispatches, taa.hpp:1027 and 1111-1139) in the FP16, tiled FP32 and
+    plain forms, and the tiled FP32 form's single launch that resolves each
+    tile with a 1-pixel ring and sharpens it from shared memory
+    (TAA_FLAG_FUSED_SHARPEN).  A step is the 32-frame sequence; 1 warm-up
+    step, 3 timed.  Bytes per pixel: 56 for one launch (colour 8, depth 4,
+    motion 4, history 16 + 16, sharpened 8); two add the result image, written
+    and read back (72)."""
+    import torch
+
+    out = {}
+    for interp, iname in ((2, "catmull_rom"), (0, "bilinear")):
+        wl = WL.c3(interp)
+        H, W, F = wl.height, wl.width, wl.frames
+        sc = wl.scene()
+        col = torch.empty(F, H, W, 4, dtype=torch.float16, device=dev)
+        dep = torch.empty(F, H, W, dtype=torch.float32, device=dev)
+        mot = torch.empty(F, H, W, 2, dtype=torch.float16, device=dev)
+        for f in range(F):
+            T.synth_render(sc, f, stream=sid, color=col[f], depth=dep[f], motion=mot[f])
+        ul = [T.make_uniforms(wl.parameters(), jitter_ndc=T.synth_jitter(sc, f)[1],
+                              mResetHistory=1 if f == 0 else 0) for f in range(F)]
+        hist = [torch.zeros(H, W, 4, dtype=torch.float32, device=dev) for _ in range(2)]
+        shp = torch.empty(H, W, 4, dtype=torch.float16, device=dev)
+        torch.cuda.synchronize()
+
+        def seq(ctx):
+            for f in range(F):
+                ctx.set_uniforms(ul[f])
+                ctx.resolve(stream=sid, color=col[f], depth=dep[f], velocity=mot[f], history=hist[f & 1],
+                            history_depth=dep[f - 1] if f else dep[0], history_out=hist[(f + 1) & 1], sharpened=shp)
+
+        cas = dict(sharpener=T.TAA_SHARPEN_CAS, sharpen_factor=0.5)
+        variants = (("fp16_then_cas", dict(form=T.TAA_FORM_FP16, **cas), 72),
+                    ("tiled_then_cas", dict(form=T.TAA_FORM_AUTO, **cas), 72),
+                    ("tiled_fused_cas", dict(form=T.TAA_FORM_AUTO, flags=T.TAA_FLAG_FUSED_SHARPEN, **cas), 56),
+                    ("plain_then_cas", dict(form=T.TAA_FORM_PLAIN, **cas), 72))
+        res_i = {}
+        for name, kw, bpp in variants:
+            ctx = T.Taa(W, H, **kw)
+            ctx.set_uniforms(ul[1])
+            form = {T.TAA_FORM_PLAIN: "plain", T.TAA_FORM_TILED: "tiled", T.TAA_FORM_FP16: "fp16"}[ctx.selected_form()]
+            seq(ctx)
+            torch.cuda.synchronize()
+            k = 3
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(k):
+                seq(ctx)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            us = e0.elapsed_time(e1) * 1000 / (k * F)
+            gbs = bpp * W * H / (us / 1e6) / 1e9
+            res_i[name] = {"us_per_frame": us, "mpx_s": W * H / us, "bytes_per_px": bpp, "gb_s": gbs,
+                           "frac_of_hbm": gbs / peak, "resolve_form": form}
+            ctx.close()
+        out[iname] = res_i
+        del col, dep, mot, hist, shp
+    out["workload"] = "C3 2560x1440, 32 frames, CAS 0.5"
+    return out
+
+
 def ctypes_copy(dst, src):
     import ctypes as C
     C.memmove(C.addressof(dst), C.addressof(src), C.sizeof(dst))
@@ -644,6 +711,10 @@ def run_ours(args):
     # the ray-trace-assist classification (tiled and plain), TAAU and debug output (plain form), post-process
     if not args.no_modes and rank == 0:
         forms["modes"] = time_modes(T, WL, dev, stream, sid, args, peak)
+
+    # the resolve with the CAS sharpener (C3: 2560x1440), one pass against two dispatches
+    if not args.no_c3 and rank == 0:
+        forms["c3_cas"] = time_c3(T, WL, dev, stream, sid, args, peak)
 
     # the FXAA pass on the segmentation mask (ray-trace-assist path) at 4K
     if not args.no_fxaa and rank == 0:

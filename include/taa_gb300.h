@@ -78,6 +78,16 @@ typedef enum taa_status {
  * relative L2 on the benchmark scenes (up to 8.6e-3 without); the form runs
  * about 15 % slower. */
 #define TAA_FLAG_FP16_GUARD 0x4u
+/* taa_desc_t.flags, with a sharpener and the tiled FP32 form: one launch
+ * resolves each tile and the 1-pixel ring around it (recomputing what the
+ * neighbouring tiles resolve, bit for bit) and sharpens the tile from shared
+ * memory, so the unsharpened image never reaches device memory.  Without the
+ * flag the tiled and FP16 forms launch the resolve, which writes the RGBA16F
+ * result image, and then the sharpen pass on it, as the reference dispatches
+ * taa.comp and then the sharpener (source/taa.hpp:1027, 1111-1139): the
+ * resolve kernels are bound by instruction issue, not by memory, and the
+ * ring's recomputation costs more than the result image's round trip. */
+#define TAA_FLAG_FUSED_SHARPEN 0x8u
 /* Sharpener (taa<CF>::mSharpener, source/taa.hpp:1418). */
 #define TAA_SHARPEN_OFF     0u
 #define TAA_SHARPEN_SIMPLE  1u  /* shaders/sharpen.comp */
@@ -99,7 +109,8 @@ typedef struct taa_desc_t {
     uint32_t form;            /* TAA_FORM_* */
     uint32_t sharpener;       /* TAA_SHARPEN_* */
     float    sharpen_factor;  /* mSharpenFactor, default 0.5 (source/taa.hpp:1419) */
-    uint32_t flags;           /* TAA_FLAG_FXAA; TAA_FLAG_LEARNED_TCGEN05 with TAA_FORM_LEARNED; TAA_FLAG_FP16_GUARD with TAA_FORM_FP16 */
+    uint32_t flags;           /* TAA_FLAG_FXAA; TAA_FLAG_LEARNED_TCGEN05 with TAA_FORM_LEARNED; TAA_FLAG_FP16_GUARD with TAA_FORM_FP16;
+                                 TAA_FLAG_FUSED_SHARPEN with a sharpener */
 } taa_desc_t;
 
 /* Per-frame bindings; one field pair per descriptor binding of set 0 in
@@ -467,12 +478,13 @@ int taa_device_status(uint32_t* bits, int clear);
  * at load time and hands out only images from it (or images imported from
  * Vulkan), or a frame loop where cudaMalloc/cudaFree would stall or
  * synchronise the device.  taa_create with TAA_SHARPEN_OFF allocates no device
- * memory; with a sharpener it allocates the screen image that the plain form
- * hands from its resolve to its sharpen pass when io->result is NULL.  Create
- * the context with TAA_SHARPEN_OFF and name the sharpener here instead: when
- * the call runs the plain form with a sharpener and no result binding, that
- * screen image lives in a fixed buffer inside the library, and nothing is
- * allocated.  Otherwise the call is taa_resolve with the sharpener given.
+ * memory; with a sharpener it allocates the screen image that a resolve
+ * hands to the sharpen pass after it when io->result is NULL.  Create the
+ * context with TAA_SHARPEN_OFF and name the sharpener here instead: when the
+ * call resolves and then sharpens (every form but the tiled form with
+ * TAA_FLAG_FUSED_SHARPEN) with no result binding, that screen image lives in
+ * a fixed buffer inside the library, and nothing is allocated.  Otherwise the
+ * call is taa_resolve with the sharpener given.
  *  - The first call on each device looks the buffer up (cudaGetSymbolAddress,
  *    on the current device); make it before any stream capture.
  *  - The buffer holds TAA_STATIC_SCRATCH_MAX_TEXELS texels: a call that needs

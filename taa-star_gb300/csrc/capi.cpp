@@ -88,7 +88,7 @@ int check_desc(const taa_desc_t& d, const char* who) {
     if (d.form > TAA_FORM_LEARNED) return fail(TAA_E_INVAL, "%s: form %u", who, d.form);
     if (d.sharpener > TAA_SHARPEN_CAS) return fail(TAA_E_INVAL, "%s: sharpener %u", who, d.sharpener);
     if (!finite(d.sharpen_factor)) return fail(TAA_E_INVAL, "%s: sharpen_factor not finite", who);
-    if (d.flags & ~(TAA_FLAG_LEARNED_TCGEN05 | TAA_FLAG_FXAA | TAA_FLAG_FP16_GUARD))
+    if (d.flags & ~(TAA_FLAG_LEARNED_TCGEN05 | TAA_FLAG_FXAA | TAA_FLAG_FP16_GUARD | TAA_FLAG_FUSED_SHARPEN))
         return fail(TAA_E_INVAL, "%s: unknown flags 0x%x", who, d.flags);
     if ((d.flags & TAA_FLAG_LEARNED_TCGEN05) && d.form != TAA_FORM_LEARNED)
         return fail(TAA_E_INVAL, "%s: TAA_FLAG_LEARNED_TCGEN05 needs TAA_FORM_LEARNED", who);
@@ -492,6 +492,14 @@ int taa_set_sharpener(taa_ctx* c, uint32_t sharpener, float factor) {
     return ensure_scratch(c);
 }
 
+// True when a sharpener runs in the same launch as the tiled FP32 resolve
+// (TAA_FLAG_FUSED_SHARPEN); otherwise a sharpener is a pass of its own after
+// the resolve, in every form.
+static bool fused_sharpen(const taa_desc_t& d) {
+    return d.sharpener != TAA_SHARPEN_OFF && (d.flags & TAA_FLAG_FUSED_SHARPEN) &&
+           d.form != TAA_FORM_PLAIN && d.form != TAA_FORM_LEARNED;
+}
+
 // AUTO picks the tiled FP32 form (bit-identical to the plain form); the FP16
 // form is used only when asked for, since its error contract is looser.
 // Parameters the tiled forms do not implement fall back to the plain form;
@@ -500,18 +508,18 @@ static int select_form(const taa_ctx* c, const taa_frame_io_t* io) {
     if (c->desc.form == TAA_FORM_PLAIN) return TAA_FORM_PLAIN;
     if (c->desc.form == TAA_FORM_LEARNED) return TAA_FORM_LEARNED;
     const taa_desc_t& d = c->desc;
-    const bool sharpen = d.sharpener != TAA_SHARPEN_OFF;
-    if (!taa_dev::fast_path_supported(c->uniforms, d.in_width, d.in_height, d.out_width, d.out_height, !sharpen,
-                                      !sharpen)) {
+    const bool fused = fused_sharpen(d);
+    if (!taa_dev::fast_path_supported(c->uniforms, d.in_width, d.in_height, d.out_width, d.out_height, !fused,
+                                      !fused)) {
         // upsampling: the tiled FP32 form's path for it
-        if (!sharpen && !(io && io->debug) &&
+        if (!fused && !(io && io->debug) &&
             taa_dev::up_path_supported(c->uniforms, d.in_width, d.in_height, d.out_width, d.out_height))
             return TAA_FORM_TILED;
         return TAA_FORM_PLAIN;
     }
     // a debug binding: the tiled FP32 form writes it (the fused sharpener does not)
-    if (io && io->debug) return sharpen ? TAA_FORM_PLAIN : TAA_FORM_TILED;
-    if (d.form == TAA_FORM_FP16 && !sharpen) return TAA_FORM_FP16;
+    if (io && io->debug) return fused ? TAA_FORM_PLAIN : TAA_FORM_TILED;
+    if (d.form == TAA_FORM_FP16 && !fused) return TAA_FORM_FP16;
     return TAA_FORM_TILED;
 }
 
@@ -545,12 +553,17 @@ int taa_resolve(taa_ctx* c, void* stream, const taa_frame_io_t* io) {
         if (e == cudaSuccess && sharpen) e = taa_dev::launch_sharpen((int)d.sharpener, a, s);
     } else {
         const int mc = d.motion_format == TAA_MOTION_RGBA16F ? 4 : 2;
+        // without TAA_FLAG_FUSED_SHARPEN a sharpener reads the RGBA16F result
+        // image the resolve writes (the caller's, or the context's)
+        if (sharpen && !fused_sharpen(d) && !a.result.p) a.result = ImgW{(char*)c->scratch_screen, c->scratch_pitch};
         if (form == TAA_FORM_FP16) {
             e = (d.flags & TAA_FLAG_FP16_GUARD)
                     ? taa_dev::launch_resolve_half_guarded((int)d.history_format, mc, U.param[0].mInterpolationMode, U, a, s)
                     : taa_dev::launch_resolve_half((int)d.history_format, mc, U.param[0].mInterpolationMode, U, a, s);
-        } else if (!sharpen) {
+            if (e == cudaSuccess && sharpen) e = taa_dev::launch_sharpen((int)d.sharpener, a, s);
+        } else if (!fused_sharpen(d)) {
             e = taa_dev::launch_resolve_tiled((int)d.history_format, mc, U.param[0].mInterpolationMode, U, a, s);
+            if (e == cudaSuccess && sharpen) e = taa_dev::launch_sharpen((int)d.sharpener, a, s);
         } else {
             taa_dev::FastKey k;
             k.form = form;
@@ -566,7 +579,7 @@ int taa_resolve(taa_ctx* c, void* stream, const taa_frame_io_t* io) {
 }
 
 // taa_resolve on a copy of the context that carries the given sharpener and,
-// where the plain form needs a screen image between its two passes, the
+// where a resolve hands a screen image to the sharpen pass after it, the
 // library's fixed buffer (static_scratch.cu) instead of an allocated one.
 int taa_resolve_static_scratch(taa_ctx* c, void* stream, const taa_frame_io_t* io, uint32_t sharpener, float factor) {
     if (!c || !io) return fail(TAA_E_INVAL, "taa_resolve_static_scratch: NULL argument");
@@ -580,7 +593,9 @@ int taa_resolve_static_scratch(taa_ctx* c, void* stream, const taa_frame_io_t* i
     taa_cas_setup(factor, (float)ow, (float)oh, (float)ow, (float)oh, v.cas_const0, v.cas_const1);
     v.scratch_screen = nullptr;
     v.scratch_pitch = 0;
-    if (sharpener != TAA_SHARPEN_OFF && !io->result && select_form(&v, io) == TAA_FORM_PLAIN) {
+    const int vform = select_form(&v, io);
+    const bool two_pass = vform == TAA_FORM_PLAIN || (vform != TAA_FORM_LEARNED && !fused_sharpen(v.desc));
+    if (sharpener != TAA_SHARPEN_OFF && !io->result && two_pass) {
         const size_t texels = (size_t)ow * (size_t)oh;
         if (texels > (size_t)TAA_STATIC_SCRATCH_MAX_TEXELS)
             return fail(TAA_E_INVAL,

@@ -250,7 +250,7 @@ template <size_t CF> class taa {
     }
 
     // source/taa.hpp:974-1192: the matrices of this and the previous frame in
-    // FP64, then the resolve (and the fused sharpen) of frame `frameId`; on the
+    // FP64, then the resolve (and the sharpen pass) of frame `frameId`; on the
     // ray-trace-assist path the resolve also writes the segmentation mask, and
     // with its FXAA flag the FXAA pass and then the sharpener follow; last the
     // post-process pass when enabled (it reads the resolve's debug image when

@@ -30,6 +30,7 @@ TAA_FORM_AUTO, TAA_FORM_PLAIN, TAA_FORM_TILED, TAA_FORM_FP16, TAA_FORM_LEARNED =
 TAA_FLAG_LEARNED_TCGEN05 = 0x1
 TAA_FLAG_FXAA = 0x2
 TAA_FLAG_FP16_GUARD = 0x4
+TAA_FLAG_FUSED_SHARPEN = 0x8
 TAA_SHARPEN_OFF, TAA_SHARPEN_SIMPLE, TAA_SHARPEN_CAS = 0, 1, 2
 
 RTFLAG = dict(OUT=0x1, DIS=0x2, NRM=0x4, DPT=0x8, MID=0x10, LUM=0x20, CNT=0x40, ALL=0x80, FXD=0x100, FXA=0x200)

@@ -165,7 +165,7 @@ def test_create_rejects_bad_descriptions(built):
         T.Desc(12, 64, 64, 64, 64, 0, 1, 0, 0, 0.5, 0),
         T.Desc(C.sizeof(T.Desc), 64, 64, 64, 64, 0, 1, T.TAA_FORM_TILED, 0, 0.5, T.TAA_FLAG_FP16_GUARD),
         T.Desc(C.sizeof(T.Desc), 64, 64, 64, 64, 0, 1, T.TAA_FORM_AUTO, 0, 0.5, T.TAA_FLAG_FP16_GUARD),
-        T.Desc(C.sizeof(T.Desc), 64, 64, 64, 64, 0, 1, 0, 0, 0.5, 0x8),
+        T.Desc(C.sizeof(T.Desc), 64, 64, 64, 64, 0, 1, 0, 0, 0.5, 0x10),
     ]
     for d in bad:
         assert lib.taa_create(C.byref(d), C.byref(h)) == T.TAA_E_INVAL

@@ -118,8 +118,12 @@ def test_formats(cuda, hist_fp16, motion4):
 
 
 @pytest.mark.parametrize("sharpener,interp", [(T.TAA_SHARPEN_CAS, 2), (T.TAA_SHARPEN_CAS, 0), (T.TAA_SHARPEN_SIMPLE, 2)])
-@pytest.mark.parametrize("form", [T.TAA_FORM_TILED, T.TAA_FORM_PLAIN])
-def test_fused_sharpen_matches_two_pass_oracle(cuda, sharpener, interp, form):
+@pytest.mark.parametrize("form,flags", [(T.TAA_FORM_TILED, 0), (T.TAA_FORM_TILED, T.TAA_FLAG_FUSED_SHARPEN),
+                                        (T.TAA_FORM_PLAIN, 0)])
+def test_sharpened_resolve_matches_two_pass_oracle(cuda, sharpener, interp, form, flags):
+    """The sharpened image of a resolve with a sharpener - the resolve then the
+    sharpen pass, or the tiled form's single launch (TAA_FLAG_FUSED_SHARPEN) -
+    is the oracle's sharpener applied to its RGBA16F result image."""
     w, h = 70, 41
     wl = WL.small(w, h, frames=2, params=dict(mInterpolationMode=interp))
     fr = cpu_frames(wl, range(2))
@@ -132,7 +136,7 @@ def test_fused_sharpen_matches_two_pass_oracle(cuda, sharpener, interp, form):
         sref = O.cas(screen16, c1[0])
     else:
         sref = O.sharpen(screen16, 0.5)
-    ctx = T.Taa(w, h, form=form, sharpener=sharpener, sharpen_factor=0.5)
+    ctx = T.Taa(w, h, form=form, sharpener=sharpener, sharpen_factor=0.5, flags=flags)
     ctx.set_uniforms(u)
     out = gpu_resolve(ctx, cuda, fr[1]["color"], fr[1]["depth"], fr[1]["motion"], hist, fr[0]["depth"],
                       want_result=False, want_sharpened=True)

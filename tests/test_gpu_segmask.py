@@ -86,9 +86,13 @@ def test_tiled_classification_matches_the_plain_form(cuda, size, flags):
     assert psnr(hist_h[..., :3], hist_p[..., :3]) >= 50.0
 
 
-def test_a_sharpener_keeps_the_classification_in_the_plain_form(cuda):
-    ctx = T.Taa(32, 16, sharpener=T.TAA_SHARPEN_CAS)
+def test_a_fused_sharpener_keeps_the_classification_in_the_plain_form(cuda):
+    """The tiled form's single resolve-and-sharpen launch has no classifier;
+    a sharpener run as a pass of its own after the resolve (the default)
+    leaves the classification in the tiled form."""
     p = WL.base_parameters(mRayTraceAugment=1, mRayTraceAugmentFlags=0x3F)
-    ctx.set_uniforms(T.make_uniforms(p))
-    assert ctx.selected_form() == T.TAA_FORM_PLAIN
-    ctx.close()
+    for flags, form in ((T.TAA_FLAG_FUSED_SHARPEN, T.TAA_FORM_PLAIN), (0, T.TAA_FORM_TILED)):
+        ctx = T.Taa(32, 16, sharpener=T.TAA_SHARPEN_CAS, flags=flags)
+        ctx.set_uniforms(T.make_uniforms(p))
+        assert ctx.selected_form() == form
+        ctx.close()

@@ -151,3 +151,64 @@ def test_c2_4k_fp16_guarded(cuda):
     print("C2 guarded FP16 form vs FP64 (relL2, PSNR):", rep)
     assert max(r for r, _ in rep) <= FP16_GUARD_RELL2
     assert min(p for _, p in rep) >= FP16_PSNR
+
+
+def half_ulp_ok(gpu16, ref):
+    """FP16-stored GPU value within one FP16 ulp of the oracle's value."""
+    from helpers import half_ulp
+    ref = np.asarray(ref, np.float64)
+    q = ref.astype(np.float32).astype(np.float16).astype(np.float64)
+    return bool(np.all(np.abs(np.asarray(gpu16, np.float64) - q) <= half_ulp(ref) + 1e-12))
+
+
+@pytest.mark.parametrize("interp", [2, 0])
+def test_c3_1440p_cas_sequence(cuda, interp):
+    """C3 (2560x1440, spinning spheres, CAS 0.5) for Catmull-Rom and bilinear
+    history: the one-launch resolve + CAS gives the FP32 oracle's history bits
+    and, within one FP16 ulp, the oracle's CAS of its RGBA16F result; the
+    FP16 form followed by taa_sharpen (the reference's two dispatches) stays
+    within the FP16 form's contract against FP64, and its sharpened image is
+    the oracle's CAS of the FP16 form's own result."""
+    wl = WL.c3(interp)
+    sc = wl.scene()
+    H, W = wl.height, wl.width
+    one = T.Taa(W, H, sharpener=T.TAA_SHARPEN_CAS, sharpen_factor=0.5)
+    two = T.Taa(W, H, form=T.TAA_FORM_FP16)
+    _, c1 = O.cas_setup(0.5, W, H, W, H)
+    hist = [torch.zeros(H, W, 4, dtype=torch.float32, device=cuda) for _ in range(2)]
+    hist2 = [torch.zeros(H, W, 4, dtype=torch.float32, device=cuda) for _ in range(2)]
+    shp = torch.empty(H, W, 4, dtype=torch.float16, device=cuda)
+    res2 = torch.empty(H, W, 4, dtype=torch.float16, device=cuda)
+    shp2 = torch.empty(H, W, 4, dtype=torch.float16, device=cuda)
+    prev = None
+    rep = []
+    for f in range(6):
+        col, dep, mot = render(wl, sc, f, cuda)
+        u = T.make_uniforms(wl.parameters(), jitter_ndc=T.synth_jitter(sc, f)[1], mResetHistory=1 if f == 0 else 0)
+        pd = prev if prev is not None else dep
+        b = dict(color=col, depth=dep, velocity=mot, history_depth=pd)
+        one.set_uniforms(u)
+        one.resolve(history=hist[f & 1], history_out=hist[(f + 1) & 1], sharpened=shp, **b)
+        two.set_uniforms(u)
+        two.resolve(history=hist2[f & 1], history_out=hist2[(f + 1) & 1], result=res2, **b)
+        T.sharpen(res2, shp2, T.TAA_SHARPEN_CAS, 0.5)
+        torch.cuda.synchronize()
+        if f in (1, 5):
+            args = (u, col.float().cpu().numpy(), dep.cpu().numpy(), mot.float().cpu().numpy())
+            ref = O.resolve(*args, history=hist[f & 1].cpu().numpy(), history_depth=pd.cpu().numpy())
+            np.testing.assert_array_equal(hist[(f + 1) & 1].cpu().numpy(), ref["history"].astype(np.float32))
+            screen16 = ref["screen"].astype(np.float32).astype(np.float16).astype(np.float32)
+            got = shp.float().cpu().numpy()
+            assert half_ulp_ok(got[..., :3], O.cas(screen16, c1[0])[..., :3]), f"frame {f}"
+            assert np.all(got[..., 3] == 1.0)
+            r64 = O.resolve(*args, precision=64, history=hist2[f & 1].cpu().numpy(), history_depth=pd.cpu().numpy())
+            h2 = hist2[(f + 1) & 1].cpu().numpy()[..., :3]
+            rep.append((rel_l2(h2, r64["history"][..., :3]), psnr(h2, r64["history"][..., :3])))
+            got2 = shp2.float().cpu().numpy()
+            assert half_ulp_ok(got2[..., :3], O.cas(res2.float().cpu().numpy(), c1[0])[..., :3]), f"frame {f}"
+        prev = dep
+    one.close()
+    two.close()
+    print(f"C3 interp {interp} FP16 form vs FP64 (relL2, PSNR):", rep)
+    assert max(r for r, _ in rep) <= FP16_RELL2
+    assert min(p for _, p in rep) >= FP16_PSNR

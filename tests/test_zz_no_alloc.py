@@ -1,11 +1,11 @@
 """taa_resolve_static_scratch against taa_resolve through the C ABI (run with -m gpu).
 
-The entry point runs the plain form's resolve and sharpen passes with the
-screen image between them in the library's fixed device buffer instead of an
-image the context allocates.  Its outputs must equal those of taa_resolve on a
+The entry point runs a resolve and then the sharpen pass with the screen
+image between them in the library's fixed device buffer instead of an image
+the context allocates.  Its outputs must equal those of taa_resolve on a
 context created with the same sharpener (the same kernels; the tests'
-tolerance for plain against plain is equality), on two calls in a row with the
-history chained.  This file is collected last, so it also runs after every
+tolerance for a form against itself is equality), on two calls in a row with
+the history chained.  This file is collected last, so it also runs after every
 other GPU test has used the device.
 """
 import ctypes as C
@@ -63,7 +63,11 @@ CASES = {
     "plain_simple": (T.TAA_FORM_PLAIN, T.TAA_SHARPEN_SIMPLE, {}),
     # split screen is a plain-form feature, so AUTO runs the plain form here
     "auto_split_screen_cas": (T.TAA_FORM_AUTO, T.TAA_SHARPEN_CAS, dict(splitScreen=1, splitX=30)),
+    # the tiled FP32 and FP16 forms: the resolve, then the sharpen pass
+    "tiled_cas": (T.TAA_FORM_TILED, T.TAA_SHARPEN_CAS, {}),
+    "fp16_simple": (T.TAA_FORM_FP16, T.TAA_SHARPEN_SIMPLE, {}),
 }
+FORM_RUN = {"tiled_cas": T.TAA_FORM_TILED, "fp16_simple": T.TAA_FORM_FP16}
 
 
 @pytest.mark.parametrize("case", list(CASES))
@@ -76,7 +80,7 @@ def test_static_scratch_matches_taa_resolve(cuda, case):
     ctx_static = T.Taa(W, H, form=form)  # no sharpener: taa_create allocates no device memory
     for c in (ctx_ref, ctx_static):
         c.set_uniforms(u)
-    assert ctx_static.selected_form() == T.TAA_FORM_PLAIN
+    assert ctx_static.selected_form() == FORM_RUN.get(case, T.TAA_FORM_PLAIN)
     run_pair(ctx_ref, ctx_static, u, fr, sharpener, 0.4, cuda)
     ctx_ref.close()
     ctx_static.close()
