@@ -422,23 +422,48 @@ __global__ void __launch_bounds__(kTileX * BY) resolve_tiled_kernel(const taa_un
     }
 }
 
-// Standalone sharpen of an RGBA16F image (result -> sharpened).
+// Sharpen of an RGBA16F image (result -> sharpened), one 32 x 32 tile per
+// 256-thread CTA: the tile and its 1-texel ring are staged once in shared
+// memory as FP32 (edge-clamped coordinates, as the per-tap clamp of
+// sharpen.comp and CAS reads them; each warp loads consecutive texels of a
+// row), then each thread sharpens four pixels of its column, rows 8 apart.
+// Launched after a resolve as a programmatic dependent: griddepcontrol.wait
+// holds the loads until the resolve's result image is complete (without that
+// launch attribute the wait returns at once).
+constexpr int kSharpenTile = 32;
 template <int SHARPEN>
 __global__ void __launch_bounds__(256) sharpen_kernel(const FrameArgs a) {
-    int x = blockIdx.x * 16 + threadIdx.x, y = blockIdx.y * 16 + threadIdx.y;
-    int W = a.out_w, H = a.out_h;
-    if (x >= W || y >= H) return;
-    Img src{a.result.p, a.result.pitch, W, H};
-    auto at = [&](int dx, int dy) {
-        float4 c = fetch_rgba16f(src, x + dx, y + dy);
-        return make_float3(c.x, c.y, c.z);
-    };
-    float3 r;
-    if (SHARPEN == 2)
-        r = cas_pixel(at(0, -1), at(-1, 0), at(0, 0), at(1, 0), at(0, 1), __uint_as_float(a.cas_peak_bits));
-    else
-        r = simple_sharpen_pixel(at(-1, 0), at(1, 0), at(0, -1), at(0, 1), at(0, 0), a.sharpen_factor);
-    store_rgba16f(a.sharpened, x, y, make_float4(r.x, r.y, r.z, 1.0f));
+    constexpr int T = kSharpenTile, S = T + 2;
+    __shared__ float4 s[S * S];
+    const int W = a.out_w, H = a.out_h;
+    const int x0 = blockIdx.x * T, y0 = blockIdx.y * T;
+    const int tid = threadIdx.x;
+    const Img src{a.result.p, a.result.pitch, W, H};
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    for (int i = tid; i < S * S; i += 256) {
+        const int sy = i / S, sx = i - sy * S;
+        const int gx = clampi(x0 - 1 + sx, 0, W - 1), gy = clampi(y0 - 1 + sy, 0, H - 1);
+        s[i] = half4_to_float4(__ldg(texel_ptr<uint2>(src, gx, gy)));
+    }
+    __syncthreads();
+    const int lx = tid & 31, ly = tid >> 5;
+    const int x = x0 + lx;
+    if (x >= W) return;
+#pragma unroll
+    for (int k = 0; k < T / 8; ++k) {
+        const int ry = ly + 8 * k, y = y0 + ry;
+        if (y >= H) break;
+        auto at = [&](int dx, int dy) {
+            const float4 c = s[(ry + 1 + dy) * S + lx + 1 + dx];
+            return make_float3(c.x, c.y, c.z);
+        };
+        float3 r;
+        if (SHARPEN == 2)
+            r = cas_pixel(at(0, -1), at(-1, 0), at(0, 0), at(1, 0), at(0, 1), __uint_as_float(a.cas_peak_bits));
+        else
+            r = simple_sharpen_pixel(at(-1, 0), at(1, 0), at(0, -1), at(0, 1), at(0, 0), a.sharpen_factor);
+        store_rgba16f(a.sharpened, x, y, make_float4(r.x, r.y, r.z, 1.0f));
+    }
 }
 
 template <int HF, int MC, int INTERP, int SHARPEN>
@@ -477,10 +502,16 @@ cudaError_t launch_resolve_fast(const FastKey& k, const taa_uniforms_t& U, const
 }
 
 cudaError_t launch_sharpen(int sharpener, const FrameArgs& a, cudaStream_t s) {
-    dim3 block(16, 16), grid((a.out_w + 15) / 16, (a.out_h + 15) / 16);
-    if (sharpener == 2) sharpen_kernel<2><<<grid, block, 0, s>>>(a);
-    else sharpen_kernel<1><<<grid, block, 0, s>>>(a);
-    return cudaGetLastError();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((a.out_w + kSharpenTile - 1) / kSharpenTile, (a.out_h + kSharpenTile - 1) / kSharpenTile);
+    cfg.blockDim = dim3(256);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return sharpener == 2 ? cudaLaunchKernelEx(&cfg, sharpen_kernel<2>, a) : cudaLaunchKernelEx(&cfg, sharpen_kernel<1>, a);
 }
 
 }  // namespace taa_dev
