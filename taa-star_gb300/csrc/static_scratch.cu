@@ -1,7 +1,8 @@
 // static_scratch.cu - the fixed device buffer behind taa_resolve_static_scratch.
 //
-// When the plain form runs with a sharpener and the caller binds no result
-// image, the resolved screen image has to live somewhere between the resolve
+// When a resolve runs with a sharpener as a pass of its own after it and the
+// caller binds no result image, the resolved screen image has to live
+// somewhere between the resolve
 // kernel and the sharpen kernel.  taa_resolve keeps it in an image the context
 // allocates with cudaMallocPitch; taa_resolve_static_scratch keeps it here, in
 // a file-scope device array that the CUDA runtime sets aside when it loads this
