@@ -485,7 +485,8 @@ def time_c3(T, WL, dev, stream, sid, args, peak):
     of two dispatches, taa.hpp:1027 and 1111-1139) in the FP16, tiled FP32 and
     plain forms, and the tiled FP32 form's single launch that resolves each
     tile with a 1-pixel ring and sharpens it from shared memory
-    (TAA_FLAG_FUSED_SHARPEN).  A step is the 32-frame sequence; 1 warm-up
+    (TAA_FLAG_FUSED_SHARPEN); last the tiled resolve alone (result image, no
+    sharpener), which prices the sharpen pass.  A step is the 32-frame sequence; 1 warm-up
     step, 3 timed.  Bytes per pixel: 56 for one launch (colour 8, depth 4,
     motion 4, history 16 + 16, sharpened 8); two add the result image, written
     and read back (72)."""
@@ -508,16 +509,19 @@ def time_c3(T, WL, dev, stream, sid, args, peak):
         torch.cuda.synchronize()
 
         def seq(ctx):
+            sharp = ctx.desc.sharpener != T.TAA_SHARPEN_OFF
             for f in range(F):
                 ctx.set_uniforms(ul[f])
+                out_img = dict(sharpened=shp) if sharp else dict(result=shp)
                 ctx.resolve(stream=sid, color=col[f], depth=dep[f], velocity=mot[f], history=hist[f & 1],
-                            history_depth=dep[f - 1] if f else dep[0], history_out=hist[(f + 1) & 1], sharpened=shp)
+                            history_depth=dep[f - 1] if f else dep[0], history_out=hist[(f + 1) & 1], **out_img)
 
         cas = dict(sharpener=T.TAA_SHARPEN_CAS, sharpen_factor=0.5)
         variants = (("fp16_then_cas", dict(form=T.TAA_FORM_FP16, **cas), 72),
                     ("tiled_then_cas", dict(form=T.TAA_FORM_AUTO, **cas), 72),
                     ("tiled_fused_cas", dict(form=T.TAA_FORM_AUTO, flags=T.TAA_FLAG_FUSED_SHARPEN, **cas), 56),
-                    ("plain_then_cas", dict(form=T.TAA_FORM_PLAIN, **cas), 72))
+                    ("plain_then_cas", dict(form=T.TAA_FORM_PLAIN, **cas), 72),
+                    ("tiled_no_sharpener", dict(form=T.TAA_FORM_AUTO), 56))
         res_i = {}
         for name, kw, bpp in variants:
             ctx = T.Taa(W, H, **kw)

@@ -422,47 +422,58 @@ __global__ void __launch_bounds__(kTileX * BY) resolve_tiled_kernel(const taa_un
     }
 }
 
-// Sharpen of an RGBA16F image (result -> sharpened), one 32 x 32 tile per
-// 256-thread CTA: the tile and its 1-texel ring are staged once in shared
-// memory as FP32 (edge-clamped coordinates, as the per-tap clamp of
-// sharpen.comp and CAS reads them; each warp loads consecutive texels of a
-// row), then each thread sharpens four pixels of its column, rows 8 apart.
+// Sharpen of an RGBA16F image (result -> sharpened), streaming: each warp
+// takes a strip of 30 output columns and kSharpenRows rows.  Lane l loads
+// column x0 - 1 + l of the strip's rows and of the rows above and below it
+// (edge-clamped coordinates, as the per-tap clamp of sharpen.comp and CAS
+// reads them), every load issued before the first use; the left and right
+// neighbours come from the adjacent lanes by shuffles, and lanes 1..30 store.
 // Launched after a resolve as a programmatic dependent: griddepcontrol.wait
 // holds the loads until the resolve's result image is complete (without that
 // launch attribute the wait returns at once).
-constexpr int kSharpenTile = 32;
+#ifndef TAA_SHARPEN_ROWS
+#define TAA_SHARPEN_ROWS 8  // rows per warp strip (a tuning constant)
+#endif
+constexpr int kSharpenRows = TAA_SHARPEN_ROWS, kSharpenCols = 30;
 template <int SHARPEN>
 __global__ void __launch_bounds__(256) sharpen_kernel(const FrameArgs a) {
-    constexpr int T = kSharpenTile, S = T + 2;
-    __shared__ float4 s[S * S];
+    constexpr int R = kSharpenRows;
     const int W = a.out_w, H = a.out_h;
-    const int x0 = blockIdx.x * T, y0 = blockIdx.y * T;
-    const int tid = threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int strips_x = (W + kSharpenCols - 1) / kSharpenCols;
+    const int warp = blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int sy = warp / strips_x, sx = warp - sy * strips_x;
+    const int y0 = sy * R;
+    if (y0 >= H) return;  // the same for every lane of the warp
+    const int x = sx * kSharpenCols - 1 + lane;
+    const int cx = clampi(x, 0, W - 1);
     const Img src{a.result.p, a.result.pitch, W, H};
     asm volatile("griddepcontrol.wait;" ::: "memory");
-    for (int i = tid; i < S * S; i += 256) {
-        const int sy = i / S, sx = i - sy * S;
-        const int gx = clampi(x0 - 1 + sx, 0, W - 1), gy = clampi(y0 - 1 + sy, 0, H - 1);
-        s[i] = half4_to_float4(__ldg(texel_ptr<uint2>(src, gx, gy)));
-    }
-    __syncthreads();
-    const int lx = tid & 31, ly = tid >> 5;
-    const int x = x0 + lx;
-    if (x >= W) return;
+    uint2 t[R + 2];
 #pragma unroll
-    for (int k = 0; k < T / 8; ++k) {
-        const int ry = ly + 8 * k, y = y0 + ry;
-        if (y >= H) break;
-        auto at = [&](int dx, int dy) {
-            const float4 c = s[(ry + 1 + dy) * S + lx + 1 + dx];
-            return make_float3(c.x, c.y, c.z);
-        };
-        float3 r;
-        if (SHARPEN == 2)
-            r = cas_pixel(at(0, -1), at(-1, 0), at(0, 0), at(1, 0), at(0, 1), __uint_as_float(a.cas_peak_bits));
-        else
-            r = simple_sharpen_pixel(at(-1, 0), at(1, 0), at(0, -1), at(0, 1), at(0, 0), a.sharpen_factor);
-        store_rgba16f(a.sharpened, x, y, make_float4(r.x, r.y, r.z, 1.0f));
+    for (int r = 0; r < R + 2; ++r) t[r] = __ldg(texel_ptr<uint2>(src, cx, clampi(y0 - 1 + r, 0, H - 1)));
+    const bool col_out = lane >= 1 && lane <= kSharpenCols && x < W;
+    auto rgb = [](uint2 v) {
+        const float4 c = half4_to_float4(v);
+        return make_float3(c.x, c.y, c.z);
+    };
+#pragma unroll
+    for (int r = 1; r <= R; ++r) {
+        const uint2 c = t[r];
+        uint2 lf, rt;
+        lf.x = __shfl_up_sync(0xffffffffu, c.x, 1);
+        lf.y = __shfl_up_sync(0xffffffffu, c.y, 1);
+        rt.x = __shfl_down_sync(0xffffffffu, c.x, 1);
+        rt.y = __shfl_down_sync(0xffffffffu, c.y, 1);
+        const int y = y0 + r - 1;
+        if (col_out && y < H) {
+            float3 o;
+            if (SHARPEN == 2)
+                o = cas_pixel(rgb(t[r - 1]), rgb(lf), rgb(c), rgb(rt), rgb(t[r + 1]), __uint_as_float(a.cas_peak_bits));
+            else
+                o = simple_sharpen_pixel(rgb(lf), rgb(rt), rgb(t[r - 1]), rgb(t[r + 1]), rgb(c), a.sharpen_factor);
+            store_rgba16f(a.sharpened, x, y, make_float4(o.x, o.y, o.z, 1.0f));
+        }
     }
 }
 
@@ -503,7 +514,9 @@ cudaError_t launch_resolve_fast(const FastKey& k, const taa_uniforms_t& U, const
 
 cudaError_t launch_sharpen(int sharpener, const FrameArgs& a, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((a.out_w + kSharpenTile - 1) / kSharpenTile, (a.out_h + kSharpenTile - 1) / kSharpenTile);
+    const long long warps = (long long)((a.out_w + kSharpenCols - 1) / kSharpenCols) *
+                            ((a.out_h + kSharpenRows - 1) / kSharpenRows);
+    cfg.gridDim = dim3((unsigned)((warps + 7) / 8));
     cfg.blockDim = dim3(256);
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
