@@ -31,6 +31,21 @@ def test_library_exports_every_declared_symbol(built):
     assert set(T.EXPORTS) == names
 
 
+def test_binding_constants_match_the_header():
+    """Every TAA_FORM_*, TAA_FLAG_*, TAA_SHARPEN_*, TAA_HISTORY_* and
+    TAA_MOTION_* value the ctypes binding names equals the header's."""
+    text = (ROOT / "include" / "taa_gb300.h").read_text()
+    defs = {m.group(1): int(m.group(2), 0)
+            for m in re.finditer(r"^#define\s+(TAA_(?:FORM|FLAG|SHARPEN|HISTORY|MOTION)_\w+)\s+(0x[0-9a-fA-F]+|\d+)u?\b",
+                                 text, flags=re.M)}
+    assert "TAA_FLAG_FUSED_SHARPEN" in defs and "TAA_FORM_FP16" in defs
+    for name, value in defs.items():
+        if hasattr(T, name):
+            assert getattr(T, name) == value, name
+    flags = [v for k, v in defs.items() if k.startswith("TAA_FLAG_")]
+    assert len(set(flags)) == len(flags) and all(f & (f - 1) == 0 for f in flags)
+
+
 def test_struct_layout_matches_reference_block():
     # std140 offsets of the reference blocks (source/taa.hpp:30-129)
     assert C.sizeof(T.Parameters) == 176
