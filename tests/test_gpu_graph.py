@@ -67,3 +67,36 @@ def test_graph_replay_equals_eager(cuda, form):
     assert marked > 0  # the FXAA pass had pixels to work on
     assert T.device_status(clear=True) == 0
     ctx.close()
+
+
+@pytest.mark.parametrize("form", [T.TAA_FORM_TILED, T.TAA_FORM_FP16])
+def test_graph_replay_with_a_sharpener(cuda, form):
+    """A resolve with CAS (the resolve, then the sharpen pass launched as its
+    programmatic dependent, the screen image in the context's buffer) captured
+    in a CUDA graph replays to the eager bits."""
+    w, h = 160, 96
+    u, b = frame_inputs(cuda, w, h)
+    ctx = T.Taa(w, h, form=form, sharpener=T.TAA_SHARPEN_CAS, sharpen_factor=0.5)
+    ctx.set_uniforms(u)
+    assert ctx.selected_form() == form
+
+    def outs():
+        return dict(history_out=torch.full((h, w, 4), float("nan"), device=cuda),
+                    sharpened=torch.full((h, w, 4), float("nan"), dtype=torch.float16, device=cuda))
+
+    eager, replay = outs(), outs()
+    ctx.resolve(stream=torch.cuda.current_stream().cuda_stream, **eager, **b)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        with torch.cuda.graph(g, stream=side):
+            ctx.resolve(stream=torch.cuda.current_stream().cuda_stream, **replay, **b)
+    torch.cuda.synchronize()
+    for _ in range(2):
+        g.replay()
+    torch.cuda.synchronize()
+    for k in eager:
+        np.testing.assert_array_equal(replay[k].cpu().numpy(), eager[k].cpu().numpy(), err_msg=k)
+    assert not torch.isnan(eager["sharpened"].float()).any()
+    ctx.close()
