@@ -1,7 +1,9 @@
-// resolve_fast.cu - tile-staged resolve forms (FP32 "tiled"), with the
-// sharpen pass of source/taa.hpp:1111-1139 fused into the same launch.
+// resolve_fast.cu - the sharpen pass of source/taa.hpp:1111-1139 that runs
+// after a resolve (and as taa_sharpen), and the one-launch resolve + sharpen
+// of the tiled FP32 form (TAA_FLAG_FUSED_SHARPEN).
 //
-// One CTA owns a BX x BY tile of output pixels.  It stages the source colour
+// The one-launch kernel: one CTA owns a BX x BY tile of output pixels.  It
+// stages the source colour
 // of the tile plus a 1-pixel halo (plus a further pixel when a sharpener is
 // fused) in shared memory, converted once per texel to the working colour
 // space (tonemap + YCoCg, taa.comp:182-213), and every thread then reads its
