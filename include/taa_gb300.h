@@ -488,7 +488,9 @@ int taa_device_status(uint32_t* bits, int clear);
  *  - The first call on each device looks the buffer up (cudaGetSymbolAddress,
  *    on the current device); make it before any stream capture.
  *  - The buffer holds TAA_STATIC_SCRATCH_MAX_TEXELS texels: a call that needs
- *    it for a larger output returns TAA_E_INVAL (bind io->result instead).
+ *    it for a larger output returns TAA_E_INVAL (bind io->result instead, or
+ *    create a tiled-form context with TAA_FLAG_FUSED_SHARPEN, whose single
+ *    launch needs no screen image).
  *  - One buffer per device: calls that overlap on the same device (two
  *    streams, or two host threads) race on it.  Calls queued on one stream
  *    do not.
