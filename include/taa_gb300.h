@@ -5,7 +5,8 @@
  * pass that source/taa.hpp:1008-1027 records for shaders/taa.comp, plus the
  * optional sharpen pass that follows it in the same command buffer
  * (source/taa.hpp:1111-1139, shaders/sharpen.comp and shaders/sharpen_cas.comp),
- * which this library fuses into the resolve.  Everything else in the
+ * which this library launches after the resolve (or, with
+ * TAA_FLAG_FUSED_SHARPEN, in the same launch).  Everything else in the
  * reference (scene rendering, ray tracing, post-process overlay, GUI) stays
  * outside.
  *
@@ -211,7 +212,7 @@ int taa_set_sharpener(taa_ctx* ctx, uint32_t sharpener, float factor);
 /* Kernel form actually used for the current uniforms (TAA_FORM_*). */
 int taa_selected_form(const taa_ctx* ctx);
 
-/* Enqueue the resolve (and the fused sharpen when enabled) on `stream`
+/* Enqueue the resolve (and, with a sharpener, the sharpen pass) on `stream`
  * (replaces the dispatch at source/taa.hpp:1027 and the sharpen dispatch at
  * source/taa.hpp:1125/1134).  `io->history` and `io->history_out` must not
  * overlap. */
@@ -251,7 +252,7 @@ int taa_fxaa(taa_ctx* ctx, void* stream, const void* input, size_t input_pitch, 
  * TAA_SHARPEN_SIMPLE (shaders/sharpen.comp) or TAA_SHARPEN_CAS
  * (shaders/sharpen_cas.comp, CasSetup of `factor` at this size) from an RGBA16F
  * image into another of the same size.  For chains where the sharpener reads
- * another pass's output (after taa_fxaa); taa_resolve fuses it otherwise. */
+ * another pass's output (after taa_fxaa); taa_resolve runs it otherwise. */
 int taa_sharpen(void* stream, uint32_t sharpener, float factor, const void* input, size_t input_pitch, void* output,
                 size_t output_pitch, int32_t width, int32_t height);
 
