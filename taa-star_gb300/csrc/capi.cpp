@@ -127,7 +127,8 @@ int frame_args(const taa_desc_t& d, const taa_uniforms_t& U, uint32_t cas_peak_b
     if ((rc = check_image("history_out", io->history_out, io->history_out_pitch, ow, oh, ht, true, &olo, &ohi))) return rc;
     bool depth_cull = any_param(U, ow, &taa_parameters_t::mDepthCulling);
     if ((rc = check_image("history_depth", io->history_depth, io->history_depth_pitch, iw, ih, 4, depth_cull))) return rc;
-    if ((rc = check_image("result", io->result, io->result_pitch, ow, oh, 8, false))) return rc;
+    const char *rlo = nullptr, *rhi = nullptr, *slo = nullptr, *shi = nullptr;
+    if ((rc = check_image("result", io->result, io->result_pitch, ow, oh, 8, false, &rlo, &rhi))) return rc;
     if ((rc = check_image("debug", io->debug, io->debug_pitch, ow, oh, 8, false))) return rc;
     if ((rc = check_image("segmask", io->segmask, io->segmask_pitch, ow, oh, 4, false))) return rc;
     if ((rc = check_image("material", io->material, io->material_pitch, iw, ih, 4, false))) return rc;
@@ -135,8 +136,11 @@ int frame_args(const taa_desc_t& d, const taa_uniforms_t& U, uint32_t cas_peak_b
     if ((rc = check_image("prev_segmask", io->prev_segmask, io->prev_segmask_pitch, ow, oh, 4, false))) return rc;
     if ((rc = check_image("uvnrm", io->uvnrm, io->uvnrm_pitch, iw, ih, 16, false))) return rc;
     const bool sharpen = d.sharpener != TAA_SHARPEN_OFF;
-    if ((rc = check_image("sharpened", io->sharpened, io->sharpened_pitch, ow, oh, 8, sharpen))) return rc;
+    if ((rc = check_image("sharpened", io->sharpened, io->sharpened_pitch, ow, oh, 8, sharpen, &slo, &shi))) return rc;
     if (hlo && hlo < ohi && olo < hhi) return fail(TAA_E_INVAL, "%s: history and history_out overlap", who);
+    // the sharpen pass reads the result image around each pixel it writes
+    if (sharpen && rlo && slo && rlo < shi && slo < rhi)
+        return fail(TAA_E_INVAL, "%s: result and sharpened overlap", who);
 
     FrameArgs& a = *out;
     a = FrameArgs{};

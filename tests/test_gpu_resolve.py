@@ -225,6 +225,13 @@ def test_validation_errors(cuda):
     ctx.set_uniforms(T.make_uniforms(p))
     with pytest.raises(T.TaaError):  # depth culling needs the previous depth
         ctx.resolve(color=col, depth=dep, velocity=vel, history=hist, history_out=out)
+    sctx = T.Taa(w, h, sharpener=T.TAA_SHARPEN_CAS)
+    sctx.set_uniforms(T.make_uniforms(WL.base_parameters()))
+    img = torch.zeros(h, w, 4, dtype=torch.float16, device=cuda)
+    with pytest.raises(T.TaaError) as e:  # the sharpen pass reads the result around each pixel it writes
+        sctx.resolve(color=col, depth=dep, velocity=vel, history=hist, history_out=out, result=img, sharpened=img)
+    assert e.value.code == T.TAA_E_INVAL
+    sctx.close()
 
 
 def test_gpu_renderer_matches_fp64_scene(cuda):
