@@ -806,6 +806,10 @@ def run_ours(args):
         cpu = {"value": wl.pixels * done / t / 1e6, "unit": UNIT, "cores": nthr, "kind": "port",
                "sample": f"{done} consecutive 3840x2160 frames of the C2 workload through the FP32 oracle "
                          f"restatement of taa.comp ({t:.1f} s, {nthr} threads)"}
+        # the same restatement on one core: one 3840x2160 frame at least
+        done1, t1 = time_oracle(wl, frames, 1, min(3.0, args.cpu_seconds))
+        cpu["single_core"] = {"value": wl.pixels * done1 / t1 / 1e6, "unit": UNIT, "cores": 1,
+                              "sample": f"{done1} 3840x2160 frame(s) ({t1:.1f} s, 1 thread)"}
 
     if rank == 0:
         line = {
