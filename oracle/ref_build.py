@@ -12,6 +12,14 @@ present (they are not built on the GPU machine).
     parameters become `T &name` (C++ spells out-parameters as references).
   * libcas_ref.so - CasSetup from shaders/ffx_cas.h with ffx_a.h's CPU path
     (A_CPU), exactly as source/taa.hpp:15-19 compiles it.
+  * libcas_filter_ref.so - shaders/sharpen_cas.comp (CasFilter of
+    shaders/ffx_cas.h on the GLSL half of shaders/ffx_a.h, A_GPU + A_GLSL)
+    through oracle/ref_shim/ffx_glsl.hpp, FP32; ffx_a.h and ffx_cas.h get the
+    same rewrites (plus `#define outAF2 out AF2` -> `#define outAF2 AF2 &`)
+    and are written beside the shader so that its includes find them.
+
+The reference tree is read from $TAA_REFERENCE_ROOT, by default
+/root/reference (where this build's container mounts it).
   * libfxaa_ref32.so / libfxaa_ref64.so - shaders/antialias_fxaa_prepare.comp
     and shaders/antialias_fxaa.comp (which includes shaders/Fxaa3_11_mod.h
     from the reference tree as it lies) through the same shim, with the
@@ -21,6 +29,7 @@ present (they are not built on the GPU machine).
 """
 from __future__ import annotations
 
+import os
 import re
 import shutil
 import subprocess
@@ -28,7 +37,7 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent
-REF = Path("/root/reference")
+REF = Path(os.environ.get("TAA_REFERENCE_ROOT", "/root/reference"))
 SHADERS = REF / "shaders"
 OUT = HERE / "_ref"
 SHIM = HERE / "ref_shim"
@@ -43,6 +52,8 @@ def rewrite(src: Path, dst: Path) -> None:
     lines = [ln for ln in text.splitlines() if not re.match(r"\s*#\s*(version|extension)\b", ln)]
     text = "\n".join(lines) + "\n"
     text = re.sub(r"\b(?:inout|out)\s+(\w+)\s+(\w+)\b", r"\1 &\2", text)
+    # the same qualifier inside a macro that names a parameter type (ffx_a.h:1720-1731)
+    text = re.sub(r"^(\s*#\s*define\s+\w+\s+)(?:inout|out)\s+(\w+)\s*$", r"\1\2 &", text, flags=re.M)
     dst.write_text(text)
 
 
@@ -100,6 +111,17 @@ def build(force: bool = False):
         _run([cxx, "-O1", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-I", str(SHADERS),
               str(SHIM / "cas_setup_ref.cpp"), "-o", str(cas)])
     libs["libcas_ref.so"] = cas
+    # sharpen_cas.comp includes ffx_a.h and ffx_cas.h; the rewritten copies sit
+    # beside it, so the compiler's search from the including file finds them first
+    rewrite(SHADERS / "sharpen_cas.comp", OUT / "sharpen_cas_comp.glsl.inc")
+    rewrite(SHADERS / "ffx_a.h", OUT / "ffx_a.h")
+    rewrite(SHADERS / "ffx_cas.h", OUT / "ffx_cas.h")
+    casf = OUT / "libcas_filter_ref.so"
+    if force or not casf.exists() or casf.stat().st_mtime < max(p.stat().st_mtime for p in SHIM.iterdir()):
+        _run([cxx, "-O1", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+              "-fsingle-precision-constant", "-Wno-pedantic", "-I", str(SHIM), "-I", str(SHADERS),
+              f'-DCAS_SOURCE="{OUT / "sharpen_cas_comp.glsl.inc"}"', str(SHIM / "cas_ref_main.cpp"), "-o", str(casf)])
+    libs["libcas_filter_ref.so"] = casf
     return libs
 
 

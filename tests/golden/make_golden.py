@@ -13,6 +13,10 @@ reference code computes:
                         and FP32 history/screen
   cas_setup_golden.json CasSetup const0/const1 for a set of sharpness values
   sharpen_golden.npz    shaders/sharpen.comp on one image (FP64 and FP32)
+  cas_golden.npz        shaders/sharpen_cas.comp (FidelityFX CAS, FP32) on
+                        seeded HDR images of several sizes (values up to 4,
+                        so the filter's saturation is exercised) for several
+                        sharpness values, with CasSetup's constants
   fxaa_golden.npz       shaders/antialias_fxaa_prepare.comp, then (through an
                         RGBA16F image, as source/taa.hpp:1063-1104 chains them)
                         shaders/antialias_fxaa.comp with Fxaa3_11_mod.h, on a
@@ -24,7 +28,7 @@ reference code computes:
                         zoom box and inset, the size-derived defaults of
                         source/taa.hpp:352-359) (FP64 and FP32)
 
-Usage: python tests/golden/make_golden.py [taa] [cas] [sharpen] [fxaa] [post]   (default: all)
+Usage: python tests/golden/make_golden.py [taa] [cas] [casfilter] [sharpen] [fxaa] [post]   (default: all)
 """
 from __future__ import annotations
 
@@ -124,11 +128,13 @@ def main():
     def u32(a):
         return np.ascontiguousarray(a, np.uint32).ctypes.data_as(up)
 
-    which = set(sys.argv[1:]) or {"taa", "cas", "sharpen", "fxaa", "post"}
+    which = set(sys.argv[1:]) or {"taa", "cas", "casfilter", "sharpen", "fxaa", "post"}
     if "taa" in which:
         make_taa(ref, f, u32, dp, up)
     if "cas" in which:
         make_cas(libs)
+    if "casfilter" in which:
+        make_cas_filter(libs, f, dp)
     if "sharpen" in which:
         make_sharpen(ref, f, dp)
     if "fxaa" in which:
@@ -201,6 +207,37 @@ def make_cas(libs):
             rows.append(dict(sharpness=s, dims=dims, const0=list(c0), const1=list(c1)))
     (HERE / "cas_setup_golden.json").write_text(json.dumps(rows, indent=1) + "\n")
     print(f"{len(rows)} CasSetup rows written to {HERE}")
+
+
+def make_cas_filter(libs, f, dp):
+    setup = C.CDLL(str(libs["libcas_ref.so"]))
+    filt = C.CDLL(str(libs["libcas_filter_ref.so"]))
+    filt.ref_cas.argtypes = [C.POINTER(C.c_float), C.c_int, C.c_int, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                             C.POINTER(C.c_double)]
+    rng = np.random.default_rng(11)
+    out = {}
+    cases = []
+    # sizes: a whole 16x16 work group, ragged edges, one row and one column
+    for (w, h) in ((16, 16), (37, 23), (70, 41), (1, 9), (9, 1)):
+        # RGBA16F values: mostly [0, 1.2] with 3 % of texels up to 4 (HDR, clipped by the filter)
+        img = rng.uniform(0.0, 1.2, (h, w, 4))
+        hot = rng.uniform(size=(h, w)) < 0.03
+        img[hot, :3] = rng.uniform(1.0, 4.0, (int(hot.sum()), 3))
+        img = img.astype(np.float16).astype(np.float32)
+        for s_ in (0.0, 0.25, 0.5, 1.0):
+            c0 = (C.c_uint32 * 4)()
+            c1 = (C.c_uint32 * 4)()
+            setup.ref_cas_setup(C.c_float(s_), *(C.c_float(v) for v in (w, h, w, h)), c0, c1)
+            o = np.zeros((h, w, 4))
+            filt.ref_cas(f(img), w, h, c0, c1, o.ctypes.data_as(dp))
+            key = f"{w}x{h}_s{s_}"
+            out[f"{key}/image"] = img
+            out[f"{key}/const1"] = np.array(list(c1), np.uint32)
+            out[f"{key}/ref32"] = o[..., :3].astype(np.float32)
+            cases.append(key)
+    out["cases"] = np.array(cases)
+    np.savez_compressed(HERE / "cas_golden.npz", **out)
+    print(f"{len(cases)} CAS filter cases written to {HERE}")
 
 
 def make_sharpen(ref, f, dp):

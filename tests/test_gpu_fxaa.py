@@ -187,3 +187,23 @@ def test_standalone_sharpen(cuda, sharpener):
     q = ref.astype(np.float32).astype(np.float16).astype(np.float64)
     assert np.all(np.abs(got[..., :3] - q[..., :3]) <= half_ulp(ref[..., :3]) + 1e-12)
     assert np.all(got[..., 3] == 1.0)
+
+
+CASF = np.load(Path(__file__).resolve().parent / "golden" / "cas_golden.npz")
+
+
+@pytest.mark.parametrize("key", list(CASF["cases"]))
+def test_standalone_cas_matches_the_reference_shader(cuda, key):
+    """taa_sharpen with CAS against shaders/sharpen_cas.comp compiled here
+    (tests/golden/cas_golden.npz): within one FP16 ulp of the shader's FP32
+    result after the RGBA16F store."""
+    img, ref = CASF[f"{key}/image"], CASF[f"{key}/ref32"].astype(np.float64)
+    h, w = img.shape[:2]
+    s = float(key.split("_s")[1])
+    src = to_dev(img, torch.float16, cuda)
+    out = torch.empty_like(src)
+    T.sharpen(src, out, T.TAA_SHARPEN_CAS, s)
+    torch.cuda.synchronize()
+    got = out.float().cpu().numpy()
+    assert np.all(np.abs(got[..., :3] - ref) <= half_ulp(ref) + 1e-12)
+    assert np.all(got[..., 3] == 1.0)

@@ -106,6 +106,22 @@ def test_sharpen_matches_the_reference_shader():
             np.testing.assert_array_equal(got.astype(np.float32), ref.astype(np.float32))
 
 
+CASF = np.load(G / "cas_golden.npz")
+
+
+@pytest.mark.parametrize("key", list(CASF["cases"]))
+def test_cas_filter_matches_the_reference_shader(key):
+    """The FP32 restatement of CasFilter (ffx_cas.h:424-537 with ffx_a.h's
+    approximations) gives the bits of shaders/sharpen_cas.comp compiled here,
+    HDR inputs above 1 included."""
+    img, c1, ref = CASF[f"{key}/image"], CASF[f"{key}/const1"], CASF[f"{key}/ref32"]
+    w, s = key.split("_s")
+    _, setup1 = O.cas_setup(float(s), *([float(v) for v in w.split("x")] * 2))
+    assert setup1[0] == int(c1[0])
+    got = O.cas(img, int(c1[0]), precision=32)[..., :3].astype(np.float32)
+    np.testing.assert_array_equal(got, ref)
+
+
 FXAA = np.load(G / "fxaa_golden.npz")
 
 
