@@ -487,7 +487,11 @@ int taa_device_status(uint32_t* bits, int clear);
  * a fixed buffer inside the library, and nothing is allocated.  Otherwise the
  * call is taa_resolve with the sharpener given.
  *  - The first call on each device looks the buffer up (cudaGetSymbolAddress,
- *    on the current device); make it before any stream capture.
+ *    on the current device); make it before any stream capture.  The address
+ *    is kept with the CUDA context it was looked up in: after a
+ *    cudaDeviceReset (a new context, into which the runtime loads the
+ *    library's device code at another address) the next call looks it up
+ *    again, so make that call before any capture too.
  *  - The buffer holds TAA_STATIC_SCRATCH_MAX_TEXELS texels: a call that needs
  *    it for a larger output returns TAA_E_INVAL (bind io->result instead, or
  *    create a tiled-form context with TAA_FLAG_FUSED_SHARPEN, whose single

@@ -4,6 +4,8 @@
 //  * the device status word: kernels that wait on an mbarrier give up after a
 //    bounded number of polls and set a bit here instead of hanging; the host
 //    reads it with taa_device_status (include/taa_gb300.h);
+//  * the id of the current CUDA context (cuCtxGetId), with which the host
+//    keeps addresses of __device__ variables valid across cudaDeviceReset;
 //  * tensor maps for the history window copy (cp.async.bulk.tensor), encoded
 //    through the driver's cuTensorMapEncodeTiled, reached with
 //    cudaGetDriverEntryPointByVersion so the library needs no link to libcuda.
@@ -22,22 +24,66 @@ namespace taa_dev {
 namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_lock;
+// the status word's address per device, with the id of the context it was looked up in
 unsigned int* g_status[kMaxDevices] = {};
+unsigned long long g_status_ctx[kMaxDevices] = {};
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 bool g_encode_looked_up = false;
+using PFN_ctx_get_current = CUresult (*)(CUcontext*);
+using PFN_ctx_get_id = CUresult (*)(CUcontext, unsigned long long*);
+PFN_ctx_get_current g_ctx_get_current = nullptr;
+PFN_ctx_get_id g_ctx_get_id = nullptr;
+bool g_ctx_looked_up = false;
 }  // namespace
 
+cudaError_t current_context_id(unsigned long long* id) {
+    {
+        std::lock_guard<std::mutex> hold(g_lock);
+        if (!g_ctx_looked_up) {
+            g_ctx_looked_up = true;
+            cudaDriverEntryPointQueryResult q{};
+            void* fn = nullptr;
+            if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+                q == cudaDriverEntryPointSuccess)
+                g_ctx_get_current = reinterpret_cast<PFN_ctx_get_current>(fn);
+            fn = nullptr;
+            if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+                q == cudaDriverEntryPointSuccess)
+                g_ctx_get_id = reinterpret_cast<PFN_ctx_get_id>(fn);
+        }
+    }
+    if (!g_ctx_get_current || !g_ctx_get_id) return cudaErrorNotSupported;
+    CUcontext ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS) return cudaErrorDeviceUninitialized;
+    if (!ctx) {
+        // no context yet on this thread (nothing has touched the device, or
+        // cudaDeviceReset destroyed it): the runtime makes the device's
+        // primary context current.  Queries of an existing context stay free
+        // of runtime calls that stream capture forbids.
+        const cudaError_t e = cudaFree(nullptr);
+        if (e != cudaSuccess) return e;
+        if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx) return cudaErrorDeviceUninitialized;
+    }
+    return g_ctx_get_id(ctx, id) == CUDA_SUCCESS ? cudaSuccess : cudaErrorDeviceUninitialized;
+}
+
+// The status word's device address, looked up again whenever the current
+// context is not the one of the cached address (after cudaDeviceReset the
+// module is loaded anew, at another address).
 cudaError_t device_status_word(unsigned int** out) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    unsigned long long ctx = 0;
+    if ((e = current_context_id(&ctx)) != cudaSuccess) return e;
     std::lock_guard<std::mutex> hold(g_lock);
-    if (!g_status[dev]) {
+    if (!g_status[dev] || g_status_ctx[dev] != ctx) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, status_word);
         if (e != cudaSuccess) return e;
         g_status[dev] = static_cast<unsigned int*>(p);
+        g_status_ctx[dev] = ctx;
     }
     *out = g_status[dev];
     return cudaSuccess;

@@ -75,6 +75,10 @@ cudaError_t static_screen_scratch(void** address, size_t* bytes);
 
 // Address of the device status word on the current device (device_state.cu).
 cudaError_t device_status_word(unsigned int** out);
+// Id of the current CUDA context (cuCtxGetId): unique for the process's
+// lifetime, so a cached device address can be checked against the context
+// it was looked up in.
+cudaError_t current_context_id(unsigned long long* id);
 
 // Tensor map of a history image for box_w x box_h texel window copies;
 // false when the image cannot be a TMA source (alignment, driver entry point).

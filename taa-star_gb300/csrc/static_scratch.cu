@@ -25,24 +25,30 @@ namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_lock;
 void* g_address[kMaxDevices] = {};
+unsigned long long g_context[kMaxDevices] = {};  // id of the context each address belongs to
 }  // namespace
 
 // Device address of screen_scratch on the current device.  The first call on
 // each device looks it up with cudaGetSymbolAddress (with that device current,
 // which loads the device code there if the runtime has not yet); later calls
-// return the cached address.
+// return the cached address while the device's context is the same one.  A
+// new context (after cudaDeviceReset the runtime creates one, and loads this
+// library's device code into it at another address) is looked up again.
 cudaError_t static_screen_scratch(void** address, size_t* bytes) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    unsigned long long ctx = 0;
+    if ((e = current_context_id(&ctx)) != cudaSuccess) return e;
     std::lock_guard<std::mutex> hold(g_lock);
-    if (!g_address[dev]) {
+    if (!g_address[dev] || g_context[dev] != ctx) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, screen_scratch);
         if (e != cudaSuccess) return e;
         if (!p) return cudaErrorInvalidSymbol;
         g_address[dev] = p;
+        g_context[dev] = ctx;
     }
     *address = g_address[dev];
     *bytes = sizeof screen_scratch;
