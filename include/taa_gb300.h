@@ -461,12 +461,26 @@ int taa_mlp_train(taa_mlp_trainer* tr, taa_mlp_weights_t* w, int32_t steps, int3
 /* Bits of the device status word (taa_device_status). */
 #define TAA_DEVICE_WINDOW_TIMEOUT 0x1u /* a history-window copy did not land within its bounded wait */
 
+/* Polls of the first bounded wait for a history-window copy; each poll
+ * suspends the waiting thread for at most 20 microseconds (about 80 ms in all). */
+#define TAA_WINDOW_WAIT_POLLS 4096u
+
 /* Read (and with clear != 0, reset) the device status word of the current
  * device.  Kernels never spin without bound: a wait that gives up sets a bit
  * here and leaves the affected pixels unwritten instead of hanging.  This
  * call waits for the device (a synchronous read); it has no counterpart in
  * the reference, whose shaders do not wait. */
 int taa_device_status(uint32_t* bits, int clear);
+
+/* Test hook, no counterpart in the reference: set on the current device how
+ * many polls the first wait for a history-window copy makes before it gives
+ * up (TAA_WINDOW_WAIT_POLLS by default).  With 0 every such wait gives up at
+ * once, so the failure path runs without a fault: the kernel sets
+ * TAA_DEVICE_WINDOW_TIMEOUT, waits for the copy a second time (always with the
+ * default bound, so no copy is still in flight when the tile's threads
+ * leave) and leaves the tile's pixels unwritten.  Applies to resolves
+ * enqueued after the call; waits for the device. */
+int taa_debug_set_window_wait(uint32_t first_wait_polls);
 
 /* Largest out_width * out_height that taa_resolve_static_scratch accepts when
  * it needs its buffer: one 3840x2160 RGBA16F screen image, 66,355,200 bytes

@@ -648,6 +648,16 @@ int taa_device_status(uint32_t* bits, int clear) {
     return ok();
 }
 
+int taa_debug_set_window_wait(uint32_t first_wait_polls) {
+    unsigned int* w = nullptr;
+    cudaError_t e = taa_dev::device_status_word(&w);
+    if (e != cudaSuccess) return cuda_fail(e, "taa_debug_set_window_wait: device status word");
+    const unsigned int v = first_wait_polls;
+    e = cudaMemcpy(w + 1, &v, sizeof v, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "taa_debug_set_window_wait");
+    return ok();
+}
+
 // ---------------------------------------------------------------- synthetic scene
 
 int taa_synth_default_scene(taa_synth_scene_t* o, int32_t w, int32_t h, uint64_t seed) {

@@ -3,7 +3,8 @@
 //
 //  * the device status word: kernels that wait on an mbarrier give up after a
 //    bounded number of polls and set a bit here instead of hanging; the host
-//    reads it with taa_device_status (include/taa_gb300.h);
+//    reads it with taa_device_status (include/taa_gb300.h).  The word after
+//    it holds the poll count of the first window wait (a test hook);
 //  * the id of the current CUDA context (cuCtxGetId), with which the host
 //    keeps addresses of __device__ variables valid across cudaDeviceReset;
 //  * tensor maps for the history window copy (cp.async.bulk.tensor), encoded
@@ -15,9 +16,12 @@
 
 #include <mutex>
 
+#include "../../include/taa_gb300.h"
 #include "kernels.h"
 
-static __device__ unsigned int status_word;
+// [0]: the status bits; [1]: polls of the first bounded wait for a
+// history-window copy (taa_debug_set_window_wait)
+static __device__ unsigned int status_word[2] = {0u, TAA_WINDOW_WAIT_POLLS};
 
 namespace taa_dev {
 

@@ -33,6 +33,7 @@
 #include <cstring>
 #include <type_traits>
 
+#include "../../include/taa_gb300.h"
 #include "common.cuh"
 #include "f32x2.cuh"
 #include "kernels.h"
@@ -73,8 +74,11 @@ template <class S, int HF> struct Win {
 // Polls of the window's mbarrier before the wait gives up, each suspending the
 // thread in hardware until the phase completes or kWaitPollNs pass (so a
 // waiting warp issues a few instructions, not a spin loop): about 80 ms in
-// all, far above any real copy time.
-constexpr uint32_t kWaitPolls = 1u << 12;
+// all, far above any real copy time.  The first wait of a tile reads its
+// limit from the word after the device status word (kWaitPolls unless a test
+// lowers it); the second, which drains a copy that the first gave up on,
+// always polls kWaitPolls times.
+constexpr uint32_t kWaitPolls = TAA_WINDOW_WAIT_POLLS;
 constexpr uint32_t kWaitPollNs = 20000;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
@@ -111,12 +115,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
         : "memory");
     return done != 0;
 }
-// Bounded wait for phase `parity` of the barrier: false after kWaitPolls polls.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-    for (uint32_t i = 0; i < kWaitPolls; ++i)
+// Bounded wait for phase `parity` of the barrier: false after `polls` polls.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t polls = kWaitPolls) {
+    for (uint32_t i = 0; i < polls; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
+// The first window wait's poll limit (the word after the status word).
+__device__ __forceinline__ uint32_t first_wait_polls(const unsigned int* status) { return __ldcg(status + 1); }
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, uint64_t* bar) {
     asm volatile(
         "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
@@ -432,7 +438,7 @@ __device__ __forceinline__ void tile_compute(const taa_uniforms_t& U, const Fram
 
     bool landed = true;
     if (mode == 1) {
-        landed = mbar_wait_bounded(bar, phase & 1u);
+        landed = mbar_wait_bounded(bar, phase & 1u, first_wait_polls(a.status));
         if (!landed) {
             atomicOr(a.status, kStatusWindowTimeout);
             mbar_wait_bounded(bar, phase & 1u);  // the copy may still land in this CTA's memory
@@ -736,7 +742,7 @@ __device__ __forceinline__ void multi_body(const taa_uniforms_t& U, const FrameA
     }
     bool landed = true;
     if (mode == 1) {
-        landed = mbar_wait_bounded(&sm.bar, phase & 1u);
+        landed = mbar_wait_bounded(&sm.bar, phase & 1u, first_wait_polls(a.status));
         if (!landed) {
             atomicOr(a.status, kStatusWindowTimeout);
             mbar_wait_bounded(&sm.bar, phase & 1u);  // the copy may still land in this CTA's memory

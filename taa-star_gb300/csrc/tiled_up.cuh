@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(S::NT, TAA_MULTI_MIN_BLOCKS * 256 / S::NT)
     }
     bool landed = true;
     if (mode == 1) {
-        landed = mbar_wait_bounded(&sm.bar, 0u);
+        landed = mbar_wait_bounded(&sm.bar, 0u, first_wait_polls(a.status));
         if (!landed) {
             atomicOr(a.status, kStatusWindowTimeout);
             mbar_wait_bounded(&sm.bar, 0u);  // the copy may still land in this CTA's memory

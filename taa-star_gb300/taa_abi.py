@@ -31,6 +31,8 @@ TAA_FLAG_LEARNED_TCGEN05 = 0x1
 TAA_FLAG_FXAA = 0x2
 TAA_FLAG_FP16_GUARD = 0x4
 TAA_FLAG_FUSED_SHARPEN = 0x8
+TAA_DEVICE_WINDOW_TIMEOUT = 0x1
+TAA_WINDOW_WAIT_POLLS = 4096
 TAA_SHARPEN_OFF, TAA_SHARPEN_SIMPLE, TAA_SHARPEN_CAS = 0, 1, 2
 
 RTFLAG = dict(OUT=0x1, DIS=0x2, NRM=0x4, DPT=0x8, MID=0x10, LUM=0x20, CNT=0x40, ALL=0x80, FXD=0x100, FXA=0x200)
@@ -164,7 +166,7 @@ EXPORTS = ["taa_version", "taa_last_error", "taa_default_parameters", "taa_get_j
            "taa_settings_default", "taa_settings_write_ini", "taa_settings_read_ini",
            "taa_jittered_projection", "taa_compose_matrices", "taa_cas_setup", "taa_create", "taa_destroy",
            "taa_set_uniforms", "taa_set_sharpener", "taa_selected_form", "taa_resolve",
-           "taa_resolve_static_scratch", "taa_device_status", "taa_batch_create", "taa_batch_destroy",
+           "taa_resolve_static_scratch", "taa_device_status", "taa_debug_set_window_wait", "taa_batch_create", "taa_batch_destroy",
            "taa_batch_set_uniforms", "taa_batch_prepare", "taa_batch_launch", "taa_batch_autotune",
            "taa_batch_get_tuning", "taa_batch_set_tuning", "taa_mlp_init_weights", "taa_set_mlp", "taa_mlp_forward",
            "taa_mlp_trainer_create", "taa_mlp_trainer_destroy", "taa_mlp_collect", "taa_mlp_record_count",
@@ -215,6 +217,7 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
         "taa_resolve": (C.c_int, [C.c_void_p, C.c_void_p, P(FrameIO)]),
         "taa_resolve_static_scratch": (C.c_int, [C.c_void_p, C.c_void_p, P(FrameIO), C.c_uint32, C.c_float]),
         "taa_device_status": (C.c_int, [P(C.c_uint32), C.c_int]),
+        "taa_debug_set_window_wait": (C.c_int, [C.c_uint32]),
         "taa_batch_create": (C.c_int, [P(Desc), C.c_int32, P(C.c_void_p)]),
         "taa_batch_destroy": (C.c_int, [C.c_void_p]),
         "taa_batch_set_uniforms": (C.c_int, [C.c_void_p, C.c_int32, P(Uniforms)]),
@@ -267,6 +270,12 @@ def device_status(clear: bool = True) -> int:
     bits = C.c_uint32()
     check(load().taa_device_status(C.byref(bits), int(clear)))
     return bits.value
+
+
+def set_window_wait(first_wait_polls: int = None):
+    """Test hook: the first window wait's poll limit on the current device
+    (None: the default, TAA_WINDOW_WAIT_POLLS)."""
+    check(load().taa_debug_set_window_wait(TAA_WINDOW_WAIT_POLLS if first_wait_polls is None else first_wait_polls))
 
 
 def default_parameters() -> Parameters:

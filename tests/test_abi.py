@@ -36,9 +36,9 @@ def test_binding_constants_match_the_header():
     TAA_MOTION_* value the ctypes binding names equals the header's."""
     text = (ROOT / "include" / "taa_gb300.h").read_text()
     defs = {m.group(1): int(m.group(2), 0)
-            for m in re.finditer(r"^#define\s+(TAA_(?:FORM|FLAG|SHARPEN|HISTORY|MOTION)_\w+)\s+(0x[0-9a-fA-F]+|\d+)u?\b",
+            for m in re.finditer(r"^#define\s+(TAA_(?:FORM|FLAG|SHARPEN|HISTORY|MOTION|DEVICE|WINDOW)_\w+)\s+(0x[0-9a-fA-F]+|\d+)u?\b",
                                  text, flags=re.M)}
-    assert "TAA_FLAG_FUSED_SHARPEN" in defs and "TAA_FORM_FP16" in defs
+    assert "TAA_FLAG_FUSED_SHARPEN" in defs and "TAA_FORM_FP16" in defs and "TAA_WINDOW_WAIT_POLLS" in defs
     for name, value in defs.items():
         if hasattr(T, name):
             assert getattr(T, name) == value, name

@@ -148,3 +148,59 @@ def test_batch_rejects_what_it_does_not_run(cuda):
     bad = T.BatchTuning(24, 8, 0, 0, 0.0)
     assert lib.taa_batch_set_tuning(batch.handle, C.byref(bad)) == T.TAA_E_INVAL
     batch.close()
+
+
+def test_c4_views_from_a_graph_match_the_oracle(cuda):
+    """The C4 configuration: 48 views (log-uniform 320x180 .. 3840x2160, each
+    with its own scene, jitter phase and pan), frame 1 of each resolved on the
+    history of its frame 0, all in one batch launch captured in a CUDA graph
+    and replayed.  The 6 smallest and the 2 largest views get the FP32 oracle's
+    bits; every view has the bits of its own taa_resolve."""
+    import oracle as O
+    wls = WL.c4_views()
+    views = []
+    for wl in wls:
+        sc = wl.scene()
+        w, h = wl.width, wl.height
+        fr = []
+        for f in range(2):
+            col = torch.empty(h, w, 4, dtype=torch.float16, device=cuda)
+            dep = torch.empty(h, w, device=cuda)
+            mot = torch.empty(h, w, 2, dtype=torch.float16, device=cuda)
+            T.synth_render(sc, f, color=col, depth=dep, motion=mot)
+            fr.append((col, dep, mot))
+        u = T.make_uniforms(wl.parameters(), jitter_ndc=T.synth_jitter(sc, 1)[1])
+        b = dict(color=fr[1][0], depth=fr[1][1], velocity=fr[1][2], history=fr[0][0].float().contiguous(),
+                 history_depth=fr[0][1], history_out=torch.full((h, w, 4), float("nan"), device=cuda),
+                 result=torch.full((h, w, 4), float("nan"), dtype=torch.float16, device=cuda))
+        views.append(dict(size=(w, h), u=u, b=b))
+    assert len(views) == 48
+    batch = make_batch(views, T.TAA_MOTION_RG16F)
+    batch.autotune(0, reps=1)
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        batch.launch(0, stream=torch.cuda.current_stream().cuda_stream)
+    reset_outputs(views)
+    torch.cuda.synchronize()
+    g.replay()
+    torch.cuda.synchronize()
+    assert T.device_status(clear=True) == 0
+    order = sorted(range(48), key=lambda i: views[i]["size"][0] * views[i]["size"][1])
+    for i in order[:6] + order[-2:]:
+        v = views[i]
+        b = v["b"]
+        ref = O.resolve(v["u"], b["color"].float().cpu().numpy(), b["depth"].cpu().numpy(),
+                        b["velocity"].float().cpu().numpy(), history=b["history"].cpu().numpy(),
+                        history_depth=b["history_depth"].cpu().numpy())
+        np.testing.assert_array_equal(b["history_out"].cpu().numpy(), ref["history"].astype(np.float32),
+                                      err_msg=str(v["size"]))
+        np.testing.assert_array_equal(b["result"].float().cpu().numpy(),
+                                      ref["screen"].astype(np.float32).astype(np.float16).astype(np.float32),
+                                      err_msg=str(v["size"]))
+    got = [(v["b"]["history_out"].cpu().numpy(), v["b"]["result"].float().cpu().numpy()) for v in views]
+    ref = reference(views, T.TAA_MOTION_RG16F)
+    for (h_g, r_g), (h_r, r_r), v in zip(got, ref, views):
+        np.testing.assert_array_equal(h_g, h_r, err_msg=str(v["size"]))
+        np.testing.assert_array_equal(r_g, r_r, err_msg=str(v["size"]))
+    batch.close()

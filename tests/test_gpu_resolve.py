@@ -408,3 +408,36 @@ def test_upsampling_runs_in_the_tiled_form(cuda, mode, sizes):
     if mode != "noise":
         ref = oracle_for(u, fr[1], fr[0], hist, out_size=(ow, oh))
         np.testing.assert_array_equal(tiled["history_out"], ref["history"].astype(np.float32))
+
+
+def test_overlapping_result_and_sharpened_are_rejected(cuda):
+    """With a sharpener the sharpen pass reads the result image around every
+    pixel it writes, so taa_resolve refuses a sharpened binding inside the
+    result image (TAA_E_INVAL before any launch); without a sharpener the same
+    bindings are accepted."""
+    import ctypes as C
+    w, h = 40, 24
+    lib = T.load()
+    u = T.make_uniforms(T.default_parameters())
+    big = torch.zeros((h + 4, w, 4), dtype=torch.float16, device=cuda)  # result; sharpened starts 2 rows in
+    bind = dict(color=torch.zeros((h, w, 4), dtype=torch.float16, device=cuda),
+                depth=torch.zeros((h, w), dtype=torch.float32, device=cuda),
+                velocity=torch.zeros((h, w, 2), dtype=torch.float16, device=cuda),
+                history_out=torch.zeros((h, w, 4), dtype=torch.float32, device=cuda))
+    io = T.FrameIO()
+    for name, t in bind.items():
+        p, pitch = T.tensor_ptr_pitch(t)
+        setattr(io, name, p)
+        setattr(io, name + "_pitch", pitch)
+    io.result, io.result_pitch = big.data_ptr(), w * 8
+    io.sharpened, io.sharpened_pitch = big.data_ptr() + 2 * w * 8, w * 8
+    for sharpener, want in ((T.TAA_SHARPEN_CAS, T.TAA_E_INVAL), (T.TAA_SHARPEN_SIMPLE, T.TAA_E_INVAL),
+                            (T.TAA_SHARPEN_OFF, T.TAA_OK)):
+        ctx = T.Taa(w, h, form=T.TAA_FORM_TILED, sharpener=sharpener)
+        ctx.set_uniforms(u)
+        rc = lib.taa_resolve(ctx.handle, None, C.byref(io))
+        assert rc == want, (sharpener, rc)
+        if want != T.TAA_OK:
+            assert b"result and sharpened overlap" in lib.taa_last_error()
+        ctx.close()
+    torch.cuda.synchronize()

@@ -33,8 +33,10 @@ def frame_io(**bindings):
     return io
 
 
-def run_pair(ctx_ref, ctx_static, u, frames, sharpener, factor, dev):
-    """Two calls in a row on each entry point, each chaining its own history."""
+def run_pair(ctx_ref, ctx_static, u, frames, sharpener, factor, dev, bind_result=False):
+    """Two calls in a row on each entry point, each chaining its own history;
+    bind_result: both calls also get a result image (the static buffer is then
+    not used)."""
     lib = T.load()
     hist_ref = hist_static = None
     for cur, prev in ((frames[1], frames[0]), (frames[2], frames[1])):
@@ -45,12 +47,13 @@ def run_pair(ctx_ref, ctx_static, u, frames, sharpener, factor, dev):
         for key, ctx, hist in (("ref", ctx_ref, hist_ref), ("static", ctx_static, hist_static)):
             h_out = torch.full((H, W, 4), float("nan"), device=dev)
             sharp = torch.full((H, W, 4), float("nan"), dtype=torch.float16, device=dev)
-            io = frame_io(history=hist, history_out=h_out, sharpened=sharp, **ins)
+            res = torch.full((H, W, 4), float("nan"), dtype=torch.float16, device=dev) if bind_result else None
+            io = frame_io(history=hist, history_out=h_out, sharpened=sharp, result=res, **ins)
             if key == "ref":
                 T.check(lib.taa_resolve(ctx.handle, None, C.byref(io)))
             else:
                 T.check(lib.taa_resolve_static_scratch(ctx.handle, None, C.byref(io), sharpener, factor))
-            outs[key] = (h_out, sharp)
+            outs[key] = (h_out, sharp) + ((res,) if bind_result else ())
         torch.cuda.synchronize()
         for a, b in zip(outs["ref"], outs["static"]):
             np.testing.assert_array_equal(b.float().cpu().numpy(), a.float().cpu().numpy())
@@ -82,6 +85,34 @@ def test_static_scratch_matches_taa_resolve(cuda, case):
         c.set_uniforms(u)
     assert ctx_static.selected_form() == FORM_RUN.get(case, T.TAA_FORM_PLAIN)
     run_pair(ctx_ref, ctx_static, u, fr, sharpener, 0.4, cuda)
+    ctx_ref.close()
+    ctx_static.close()
+
+
+# The branches that do not use the buffer, and a context that has a sharpener
+# of its own: (form, flags, sharpener the context is created with, sharpener
+# the call names, whether a result image is bound).
+BRANCHES = {
+    # a bound result image carries the screen image to the sharpen pass
+    "result_bound": (T.TAA_FORM_TILED, 0, T.TAA_SHARPEN_OFF, T.TAA_SHARPEN_CAS, True),
+    # the tiled form's single launch with the sharpener needs no screen image
+    "fused_tiled": (T.TAA_FORM_TILED, T.TAA_FLAG_FUSED_SHARPEN, T.TAA_SHARPEN_OFF, T.TAA_SHARPEN_CAS, False),
+    # a context created with CAS; the call names the simple sharpener and uses the buffer
+    "own_sharpener": (T.TAA_FORM_TILED, 0, T.TAA_SHARPEN_CAS, T.TAA_SHARPEN_SIMPLE, False),
+}
+
+
+@pytest.mark.parametrize("case", list(BRANCHES))
+def test_static_scratch_branches_match_taa_resolve(cuda, case):
+    form, flags, own, named, bind_result = BRANCHES[case]
+    wl = WL.small(W, H, frames=3)
+    fr = cpu_frames(wl, range(3))
+    u = T.make_uniforms(wl.parameters(), jitter_ndc=fr[1]["jitter"])
+    ctx_ref = T.Taa(W, H, form=form, sharpener=named, sharpen_factor=0.4, flags=flags)
+    ctx_static = T.Taa(W, H, form=form, sharpener=own, sharpen_factor=0.7, flags=flags)
+    for c in (ctx_ref, ctx_static):
+        c.set_uniforms(u)
+    run_pair(ctx_ref, ctx_static, u, fr, named, 0.4, cuda, bind_result=bind_result)
     ctx_ref.close()
     ctx_static.close()
 
