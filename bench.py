@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--no-modes", action="store_true")
     ap.add_argument("--no-c3", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--profile", choices=["tiled", "fp16", "plain", "batch48", "fxaa"],
+    ap.add_argument("--profile", choices=["fast", "tiled", "fp16", "plain", "batch48", "fxaa"],
                     help="a small case for ncu: a few launches of one form on 4K frames (no JSON line)")
     return ap.parse_args()
 
@@ -147,34 +147,54 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ reference arm
-def cpu_frames_for_reference(wl, n):
+# The reference's path on the host cores is the oracle's FP32 restatement of
+# taa.comp (the shader itself needs Vulkan).  This arm builds its inputs from
+# the oracle alone - scene, sphere table, jitter, parameter and uniform blocks
+# (oracle/oracle.py) - so the library is never loaded in it.
+C2_SCENE = dict(width=3840, height=2160, seed=2, num_spheres=128, cam_v0=(2.0, 0.0), cam_accel=(38.0 / 63.0, 0.0))
+C2_NAME = "C2 3840x2160x64 depth+velocity rejection"
+
+
+def reference_c2():
+    """The C2 workload (workloads.c2()) from the oracle's helpers: its scene and
+    parameter block (Catmull-Rom, YCoCg variance clip gamma 1, clip-fast,
+    alpha 0.1, velocity for every pixel, depth culling, reject outside)."""
+    import oracle as O
+    c = dict(C2_SCENE)
+    sc = O.synth_scene(c.pop("width"), c.pop("height"), c.pop("seed"), **c)
+    p = O.default_parameters()
+    for k, v in dict(mInterpolationMode=2, mUseYCoCg=1, mVarianceClipping=1, mVarClipGamma=1.0,
+                     mColorClampingOrClipping=2, mAlpha=0.1, mUseVelocityVectors=2, mVelocitySampleMode=0,
+                     mDepthCulling=1, mRejectOutside=1).items():
+        setattr(p, k, v)
+    return sc, p
+
+
+def cpu_frames_for_reference(sc, n):
     """Inputs of the first n+1 frames, rendered on the host by the FP64 scene evaluator."""
     import numpy as np
     import oracle as O
-    import taa_abi as T
-    sc = wl.scene()
-    sph = T.synth_spheres(sc)
+    sph = O.synth_spheres(sc)
     out = []
     for f in range(n + 1):
         r = O.synth_frame(sc, sph, f)
         out.append(dict(color=r["color"].astype(np.float16).astype(np.float32), depth=r["depth"].astype(np.float32),
                         motion=r["motion"][..., :2].astype(np.float16).astype(np.float32),
-                        jitter=T.synth_jitter(sc, f)[1]))
+                        jitter=O.synth_jitter(sc, f)))
     return out
 
 
-def time_oracle(wl, frames, nthreads, budget_s, min_frames=1):
+def time_oracle(params, frames, nthreads, budget_s, min_frames=1):
     """Oracle FP32 resolve over consecutive frames until the time budget is spent."""
     import numpy as np
     import oracle as O
-    import taa_abi as T
     hist = frames[0]["color"].copy()
     done, t_total = 0, 0.0
     i = 1
     while done < min_frames or t_total < budget_s:
         f = frames[1 + (i - 1) % (len(frames) - 1)]
         prev = frames[(i - 1) % (len(frames) - 1)]
-        u = T.make_uniforms(wl.parameters(), jitter_ndc=f["jitter"])
+        u = O.make_uniforms(params, jitter_ndc=f["jitter"])
         t0 = time.perf_counter()
         r = O.resolve(u, f["color"], f["depth"], f["motion"], history=hist, history_depth=prev["depth"],
                       nthreads=nthreads)
@@ -191,19 +211,18 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    import workloads as WL
-    wl = WL.c2()
+    sc, params = reference_c2()
     n = os.cpu_count() or 1
-    frames = cpu_frames_for_reference(wl, 2)
+    frames = cpu_frames_for_reference(sc, 2)
     # warm-up frames, then `steps` timed frames (one 4K frame per step)
-    time_oracle(wl, frames, n, 0.0, min_frames=max(1, args.warmup))
-    done, t = time_oracle(wl, frames, n, 0.0, min_frames=args.steps)
-    mpx = wl.pixels * done / t / 1e6
+    time_oracle(params, frames, n, 0.0, min_frames=max(1, args.warmup))
+    done, t = time_oracle(params, frames, n, 0.0, min_frames=args.steps)
+    mpx = sc.width * sc.height * done / t / 1e6
     line = {
         "impl": "reference", "metric": METRIC, "value": mpx, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t / done * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded analytic scene, rendered on the host)",
-        "config": {"workload": wl.name, "width": wl.width, "height": wl.height, "frames_per_step": 1,
+        "config": {"workload": C2_NAME, "width": sc.width, "height": sc.height, "frames_per_step": 1,
                    "mode": "Catmull-Rom, YCoCg variance clip gamma 1, clip-fast, alpha 0.1, depth culling, reject outside"},
         "cpu_baseline": {"value": mpx, "unit": UNIT, "cores": n, "kind": "port",
                          "sample": f"{done} consecutive 3840x2160 frames of the C2 scene, FP32 oracle restatement of taa.comp, {n} threads"},
@@ -369,7 +388,8 @@ def time_modes(T, WL, dev, stream, sid, args, peak):
 
     def run(name, ctx, ulist, binds, bpp, px):
         ctx.set_uniforms(ulist[0])
-        form = {T.TAA_FORM_PLAIN: "plain", T.TAA_FORM_TILED: "tiled", T.TAA_FORM_FP16: "fp16"}[ctx.selected_form()]
+        form = {T.TAA_FORM_PLAIN: "plain", T.TAA_FORM_TILED: "tiled", T.TAA_FORM_FP16: "fp16",
+                    T.TAA_FORM_FAST: "fast"}[ctx.selected_form()]
         for i in range(3):
             ctx.set_uniforms(ulist[i % len(ulist)])
             ctx.resolve(stream=sid, **binds(i))
@@ -526,7 +546,8 @@ def time_c3(T, WL, dev, stream, sid, args, peak):
         for name, kw, bpp in variants:
             ctx = T.Taa(W, H, **kw)
             ctx.set_uniforms(ul[1])
-            form = {T.TAA_FORM_PLAIN: "plain", T.TAA_FORM_TILED: "tiled", T.TAA_FORM_FP16: "fp16"}[ctx.selected_form()]
+            form = {T.TAA_FORM_PLAIN: "plain", T.TAA_FORM_TILED: "tiled", T.TAA_FORM_FP16: "fp16",
+                    T.TAA_FORM_FAST: "fast"}[ctx.selected_form()]
             seq(ctx)
             torch.cuda.synchronize()
             k = 3
@@ -685,7 +706,7 @@ def run_ours(args):
 
     ctx = make_ctx(T.TAA_FORM_AUTO)
     form_used = ctx.selected_form()
-    form_name = {1: "plain", 2: "tiled", 3: "fp16"}[form_used]
+    form_name = {1: "plain", 2: "tiled", 3: "fp16", 5: "fast"}[form_used]
     sampler = ClockSampler(local)
     ms = timed(ctx, args.steps, args.warmup, sampler)
     launches = args.steps * F
@@ -696,8 +717,10 @@ def run_ours(args):
 
     forms = {form_name: {"mpx_s": mpx, "gb_s": achieved, "frac_of_hbm": achieved / peak}}
     if not args.no_forms:
-        for fid, name, fl in ((T.TAA_FORM_PLAIN, "plain", 0), (T.TAA_FORM_FP16, "fp16", 0),
-                              (T.TAA_FORM_FP16, "fp16_guarded", T.TAA_FLAG_FP16_GUARD)):
+        for fid, name, fl in ((T.TAA_FORM_TILED, "tiled", 0), (T.TAA_FORM_PLAIN, "plain", 0),
+                              (T.TAA_FORM_FP16, "fp16", 0), (T.TAA_FORM_FP16, "fp16_guarded", T.TAA_FLAG_FP16_GUARD)):
+            if name in forms:
+                continue
             c2 = make_ctx(fid, fl)
             k = max(2, args.steps // 4)
             m2 = timed(c2, k, 1)
@@ -802,12 +825,13 @@ def run_ours(args):
         for f in range(3):
             frames.append(dict(color=col[f].float().cpu().numpy(), depth=dep[f].cpu().numpy(),
                                motion=mot[f].float().cpu().numpy(), jitter=T.synth_jitter(sc, f)[1]))
-        done, t = time_oracle(wl, frames, nthr, args.cpu_seconds)
+        params = O.Parameters.from_buffer_copy(bytes(wl.parameters()))
+        done, t = time_oracle(params, frames, nthr, args.cpu_seconds)
         cpu = {"value": wl.pixels * done / t / 1e6, "unit": UNIT, "cores": nthr, "kind": "port",
                "sample": f"{done} consecutive 3840x2160 frames of the C2 workload through the FP32 oracle "
                          f"restatement of taa.comp ({t:.1f} s, {nthr} threads)"}
         # the same restatement on one core: one 3840x2160 frame at least
-        done1, t1 = time_oracle(wl, frames, 1, min(3.0, args.cpu_seconds))
+        done1, t1 = time_oracle(params, frames, 1, min(3.0, args.cpu_seconds))
         cpu["single_core"] = {"value": wl.pixels * done1 / t1 / 1e6, "unit": UNIT, "cores": 1,
                               "sample": f"{done1} 3840x2160 frame(s) ({t1:.1f} s, 1 thread)"}
 
@@ -884,7 +908,8 @@ def run_profile_case(args):
         torch.cuda.synchronize()
         ctx.close()
         return 0
-    form = {"tiled": T.TAA_FORM_TILED, "fp16": T.TAA_FORM_FP16, "plain": T.TAA_FORM_PLAIN}[args.profile]
+    form = {"fast": T.TAA_FORM_FAST, "tiled": T.TAA_FORM_TILED, "fp16": T.TAA_FORM_FP16,
+            "plain": T.TAA_FORM_PLAIN}[args.profile]
     ctx = T.Taa(W, H, form=form)
     for f in range(1, F):
         ctx.set_uniforms(T.make_uniforms(wl.parameters(), jitter_ndc=T.synth_jitter(sc, f)[1]))

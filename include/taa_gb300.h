@@ -59,11 +59,21 @@ typedef enum taa_status {
 #define TAA_MOTION_RGBA16F  0u
 #define TAA_MOTION_RG16F    1u
 /* Kernel form. */
-#define TAA_FORM_AUTO   0u  /* fastest form whose precision contract holds for the parameters */
+#define TAA_FORM_AUTO   0u  /* fastest FP32 form for the parameters: TAA_FORM_FAST where it runs them, else TILED, else PLAIN */
 #define TAA_FORM_PLAIN  1u  /* one thread per pixel, FP32, every parameter honoured */
-#define TAA_FORM_TILED  2u  /* FP32, CTA tile staged in shared memory */
+#define TAA_FORM_TILED  2u  /* FP32, CTA tile staged in shared memory; the FP32 shader's bits */
 #define TAA_FORM_FP16   3u  /* packed half2 neighbourhood, clip and sharpen; FP32 history and blend */
 #define TAA_FORM_LEARNED 4u /* blend weight and clip-box scale from a per-pixel MLP (taa_set_mlp) */
+/* FP32 with the arithmetic reassociated: contracted FMAs, the 3x3 moments from
+ * row sums two pixels share, hardware square-root and reciprocal
+ * approximations in the variance box and the clip.  Frame error within 1e-5
+ * relative L2 of TAA_FORM_TILED.  It runs the benchmark mode of the
+ * parameter block (YCoCg variance clip toward the box centre, velocity for
+ * every pixel with simple sampling, no tonemap, luma weighting, near-clamp
+ * reduction, velocity-based alpha, noise or anti-ghosting) with Catmull-Rom
+ * or bilinear history, RGBA32F history, equal source and target sizes and no
+ * debug binding; other parameters run in TAA_FORM_TILED. */
+#define TAA_FORM_FAST   5u
 /* taa_desc_t.flags: run the learned form's network per 128-pixel warpgroup
  * on tcgen05 through tensor memory instead of per warp with warp-wide MMAs
  * (the default: no block barriers, faster inside the resolve). */

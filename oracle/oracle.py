@@ -228,3 +228,100 @@ def synth_frame(scene, spheres, frame, truth=False, nthreads=None):
     lib.oracle_synth_frame(C.addressof(scene), _fp(sph), frame, _dp(col), _dp(dep), _dp(mot), _dp(tru),
                            nthreads or nthreads_default())
     return dict(color=col, depth=dep, motion=mot, truth=tru)
+
+
+# ---------------------------------------------------------------- inputs without the library
+# The parameter block, the uniform block and the scene description as the
+# oracle's own ctypes types (the layouts of include/taa_params.h and
+# include/taa_synth.h), so that a caller that must not load the library - the
+# benchmark's reference arm - builds the same inputs from the oracle alone.
+_PF = "f i u u u f u u u u u u f f f f u i i i u u f u u u f f u u f f f f f i f4 i f u u".split()
+_PN = ("mAlpha mColorClampingOrClipping mDepthCulling mUnjitterNeighbourhood mUnjitterCurrentSample "
+       "mUnjitterFactor mPassThrough mUseYCoCg mShrinkChromaAxis mVarianceClipping mShapedNeighbourhood "
+       "mLumaWeightingLottes mVarClipGamma mMinAlpha mMaxAlpha mRejectionAlpha mRejectOutside mUseVelocityVectors "
+       "mVelocitySampleMode mInterpolationMode mToneMapLumaKaris mAddNoise mNoiseFactor mReduceBlendNearClamp "
+       "mDynamicAntiGhosting mVelBasedAlpha mVelBasedAlphaMax mVelBasedAlphaFactor mRayTraceAugment "
+       "mRayTraceAugmentFlags mRayTraceAugment_WNrm mRayTraceAugment_WDpt mRayTraceAugment_WMId "
+       "mRayTraceAugment_WLum mRayTraceAugment_Thresh mRayTraceHistoryCount mDebugMask mDebugMode mDebugScale "
+       "mDebugCenter mDebugToScreenOutput").split()
+_T = {"f": C.c_float, "i": C.c_int32, "u": C.c_uint32, "f4": C.c_float * 4}
+
+
+class Parameters(C.Structure):
+    """Parameters of source/taa.hpp:30-77 (176 bytes)."""
+    _fields_ = [(n, _T[t]) for n, t in zip(_PN, _PF)]
+
+
+class Uniforms(C.Structure):
+    """uniforms_for_taa of source/taa.hpp:113-129 (544 bytes)."""
+    _fields_ = [("mHistoryViewProjMatrix", C.c_float * 16), ("mInverseViewProjMatrix", C.c_float * 16),
+                ("param", Parameters * 2), ("mJitterNdc", C.c_float * 4), ("mSinTime", C.c_float * 4),
+                ("splitScreen", C.c_uint32), ("splitX", C.c_int32), ("mUpsampling", C.c_uint32),
+                ("mBypassHistoryUpdate", C.c_uint32), ("mResetHistory", C.c_uint32), ("mCamNearPlane", C.c_float),
+                ("mCamFarPlane", C.c_float), ("pad1", C.c_float)]
+
+
+class SynthScene(C.Structure):
+    """taa_synth_scene_t (include/taa_synth.h)."""
+    _fields_ = [("struct_size", C.c_uint32), ("width", C.c_int32), ("height", C.c_int32), ("seed", C.c_uint64),
+                ("num_spheres", C.c_int32), ("radius_min", C.c_float), ("radius_max", C.c_float),
+                ("sphere_speed_max", C.c_float), ("spin_max", C.c_float), ("cam_v0", C.c_float * 2),
+                ("cam_accel", C.c_float * 2), ("checker_period", C.c_float), ("firefly_fraction", C.c_float),
+                ("firefly_max", C.c_float), ("jitter_phase", C.c_int32), ("jitter_enabled", C.c_int32)]
+
+
+assert C.sizeof(Parameters) == 176 and C.sizeof(Uniforms) == 544
+
+
+def default_parameters() -> Parameters:
+    p = Parameters()
+    lib = load()
+    lib.oracle_default_parameters.argtypes = [C.c_void_p]
+    lib.oracle_default_parameters(C.addressof(p))
+    return p
+
+
+def make_uniforms(p0: Parameters, jitter_ndc=(0.0, 0.0), **kw) -> Uniforms:
+    """The uniform block of a frame: identity matrices, both parameter sets p0,
+    the jitter, near 0.1 and far 1000, and any field given by name."""
+    u = Uniforms()
+    for m in (u.mHistoryViewProjMatrix, u.mInverseViewProjMatrix):
+        for i in range(4):
+            m[i * 5] = 1.0
+    u.param[0] = p0
+    u.param[1] = p0
+    u.mJitterNdc[0], u.mJitterNdc[1] = jitter_ndc
+    u.mCamNearPlane, u.mCamFarPlane = 0.1, 1000.0
+    for k, v in kw.items():
+        setattr(u, k, v)
+    return u
+
+
+def synth_scene(width, height, seed, **fields) -> SynthScene:
+    s = SynthScene()
+    lib = load()
+    lib.oracle_synth_default_scene.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_uint64]
+    lib.oracle_synth_default_scene(C.addressof(s), width, height, seed)
+    for k, v in fields.items():
+        if k in ("cam_v0", "cam_accel"):
+            getattr(s, k)[0], getattr(s, k)[1] = v
+        else:
+            setattr(s, k, v)
+    return s
+
+
+def synth_spheres(scene: SynthScene):
+    t = np.zeros((max(1, scene.num_spheres), 12), np.float32)
+    lib = load()
+    lib.oracle_synth_spheres.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
+    lib.oracle_synth_spheres(C.addressof(scene), _fp(t))
+    return t
+
+
+def synth_jitter(scene: SynthScene, frame: int):
+    """The frame's sub-pixel jitter in NDC."""
+    ndc = (C.c_float * 2)()
+    lib = load()
+    lib.oracle_synth_jitter.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_float)]
+    lib.oracle_synth_jitter(C.addressof(scene), frame, ndc)
+    return ndc[0], ndc[1]

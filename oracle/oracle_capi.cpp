@@ -115,6 +115,46 @@ long long oracle_check_div_const(float d, uint32_t lo_bits, uint32_t hi_bits, in
     return s;
 }
 
+// The reference's initial parameter values (source/taa.hpp:31-76), for the
+// benchmark's reference arm, which builds its inputs without the library.
+void oracle_default_parameters(taa_parameters_t* p) {
+    std::memset(p, 0, sizeof *p);
+    p->mAlpha = 0.05f;
+    p->mColorClampingOrClipping = 1;
+    p->mUnjitterFactor = 1.0f;
+    p->mVarClipGamma = 1.0f;
+    p->mMinAlpha = 1.0f - 0.97f;
+    p->mMaxAlpha = 1.0f - 0.88f;
+    p->mRejectionAlpha = 1.0f;
+    p->mUseVelocityVectors = 1;
+    p->mNoiseFactor = 1.f / 510.f;
+    p->mVelBasedAlphaMax = 0.2f;
+    p->mVelBasedAlphaFactor = 1.f / 40.f;
+    p->mRayTraceAugmentFlags = 0xffffffffu & ~(TAA_RTFLAG_ALL | TAA_RTFLAG_FXD);
+    p->mRayTraceAugment_WNrm = 0.5f;
+    p->mRayTraceAugment_WDpt = 0.015f;
+    p->mRayTraceAugment_WMId = 0.25f;
+    p->mRayTraceAugment_WLum = 0.5f;
+    p->mRayTraceAugment_Thresh = 0.5f;
+    p->mRayTraceHistoryCount = -1;
+    p->mDebugMask[0] = p->mDebugMask[1] = p->mDebugMask[2] = 1.0f;
+    p->mDebugScale = 1.0f;
+}
+
+// The analytic scene's defaults, its seeded sphere table and a frame's
+// sub-pixel jitter (include/taa_synth.h), from the scene header the oracle
+// shares with the renderer.
+void oracle_synth_default_scene(taa_synth_scene_t* s, int w, int h, uint64_t seed) {
+    taa_synth::default_scene(*s, w, h, seed);
+}
+void oracle_synth_spheres(const taa_synth_scene_t* s, float* table) { taa_synth::spheres(*s, table); }
+void oracle_synth_jitter(const taa_synth_scene_t* s, int frame, float ndc[2]) {
+    float jx, jy;
+    taa_synth::jitter_px(*s, frame, jx, jy);
+    ndc[0] = 2.0f * jx / (float)s->width;
+    ndc[1] = 2.0f * jy / (float)s->height;
+}
+
 // FP64 evaluation of the analytic scene (the scene's truth; the GPU renders
 // the same formulas in FP32).  Outputs: color RGBA (before the FP16 store),
 // depth, motion (4 channels, UV units, .w mover id), truth (64 spp).  Any

@@ -4,7 +4,7 @@ Every translation unit is compiled by nvcc in parallel and linked into
 ``taa-star_gb300/_build/libtaa_gb300.so``.  The FP32 resolve units are
 compiled with ``-fmad=false`` so that they round operation for operation like
 the FP32 oracle (their sources place explicit FMAs where the oracle has them);
-the FP16 form's unit may contract to FMA.
+the FP16 form's and the reassociating FP32 form's units may contract to FMA.
 
 Usage: ``python taa-star_gb300/build.py`` or ``build_library()`` from Python.
 """
@@ -32,6 +32,7 @@ UNITS = {
     "resolve_plain.cu": ["-fmad=false"],
     "resolve_fast.cu": ["-fmad=false"],
     "resolve_tiled.cu": ["-fmad=false"],
+    "resolve_fast32.cu": [],
     "resolve_half.cu": [],
     "resolve_half_guard.cu": [],
     "batch_tiled.cu": ["-fmad=false"],

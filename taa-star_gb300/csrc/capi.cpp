@@ -85,7 +85,7 @@ int check_desc(const taa_desc_t& d, const char* who) {
         return fail(TAA_E_INVAL, "%s: image sizes must be in 1..32768", who);
     if (d.history_format > TAA_HISTORY_RGBA16F) return fail(TAA_E_INVAL, "%s: history_format %u", who, d.history_format);
     if (d.motion_format > TAA_MOTION_RG16F) return fail(TAA_E_INVAL, "%s: motion_format %u", who, d.motion_format);
-    if (d.form > TAA_FORM_LEARNED) return fail(TAA_E_INVAL, "%s: form %u", who, d.form);
+    if (d.form > TAA_FORM_FAST) return fail(TAA_E_INVAL, "%s: form %u", who, d.form);
     if (d.sharpener > TAA_SHARPEN_CAS) return fail(TAA_E_INVAL, "%s: sharpener %u", who, d.sharpener);
     if (!finite(d.sharpen_factor)) return fail(TAA_E_INVAL, "%s: sharpen_factor not finite", who);
     if (d.flags & ~(TAA_FLAG_LEARNED_TCGEN05 | TAA_FLAG_FXAA | TAA_FLAG_FP16_GUARD | TAA_FLAG_FUSED_SHARPEN))
@@ -504,10 +504,11 @@ static bool fused_sharpen(const taa_desc_t& d) {
            d.form != TAA_FORM_PLAIN && d.form != TAA_FORM_LEARNED;
 }
 
-// AUTO picks the tiled FP32 form (bit-identical to the plain form); the FP16
-// form is used only when asked for, since its error contract is looser.
-// Parameters the tiled forms do not implement fall back to the plain form;
-// the FP16 form with a fused sharpener runs as the tiled FP32 form.
+// AUTO picks the reassociating FP32 form where it runs the parameters, else
+// the tiled FP32 form (bit-identical to the plain form); the FP16 form is used
+// only when asked for, since its error contract is looser.  Parameters the
+// tiled forms do not implement fall back to the plain form; the FP16 and fast
+// forms with a fused sharpener run as the tiled FP32 form.
 static int select_form(const taa_ctx* c, const taa_frame_io_t* io) {
     if (c->desc.form == TAA_FORM_PLAIN) return TAA_FORM_PLAIN;
     if (c->desc.form == TAA_FORM_LEARNED) return TAA_FORM_LEARNED;
@@ -524,6 +525,10 @@ static int select_form(const taa_ctx* c, const taa_frame_io_t* io) {
     // a debug binding: the tiled FP32 form writes it (the fused sharpener does not)
     if (io && io->debug) return fused ? TAA_FORM_PLAIN : TAA_FORM_TILED;
     if (d.form == TAA_FORM_FP16 && !fused) return TAA_FORM_FP16;
+    if ((d.form == TAA_FORM_AUTO || d.form == TAA_FORM_FAST) && !fused &&
+        taa_dev::fast32_supported(c->uniforms, (int)d.history_format, d.in_width, d.in_height, d.out_width,
+                                  d.out_height))
+        return TAA_FORM_FAST;
     return TAA_FORM_TILED;
 }
 
@@ -560,7 +565,10 @@ int taa_resolve(taa_ctx* c, void* stream, const taa_frame_io_t* io) {
         // without TAA_FLAG_FUSED_SHARPEN a sharpener reads the RGBA16F result
         // image the resolve writes (the caller's, or the context's)
         if (sharpen && !fused_sharpen(d) && !a.result.p) a.result = ImgW{(char*)c->scratch_screen, c->scratch_pitch};
-        if (form == TAA_FORM_FP16) {
+        if (form == TAA_FORM_FAST) {
+            e = taa_dev::launch_resolve_fast32(mc, U, a, s);
+            if (e == cudaSuccess && sharpen) e = taa_dev::launch_sharpen((int)d.sharpener, a, s);
+        } else if (form == TAA_FORM_FP16) {
             e = (d.flags & TAA_FLAG_FP16_GUARD)
                     ? taa_dev::launch_resolve_half_guarded((int)d.history_format, mc, U.param[0].mInterpolationMode, U, a, s)
                     : taa_dev::launch_resolve_half((int)d.history_format, mc, U.param[0].mInterpolationMode, U, a, s);
@@ -663,22 +671,7 @@ int taa_debug_set_window_wait(uint32_t first_wait_polls) {
 int taa_synth_default_scene(taa_synth_scene_t* o, int32_t w, int32_t h, uint64_t seed) {
     if (!o) return fail(TAA_E_INVAL, "taa_synth_default_scene: NULL");
     if (w <= 0 || h <= 0) return fail(TAA_E_INVAL, "taa_synth_default_scene: bad size");
-    std::memset(o, 0, sizeof *o);
-    o->struct_size = sizeof *o;
-    o->width = w;
-    o->height = h;
-    o->seed = seed;
-    o->num_spheres = 32;
-    o->radius_min = 20.f;
-    o->radius_max = 120.f;
-    o->sphere_speed_max = 6.f;
-    o->spin_max = 0.f;
-    o->cam_v0[0] = 3.f;
-    o->checker_period = 7.3f;
-    o->firefly_fraction = 0.01f;
-    o->firefly_max = 64.f;
-    o->jitter_phase = 0;
-    o->jitter_enabled = 1;
+    taa_synth::default_scene(*o, w, h, seed);
     return ok();
 }
 
@@ -695,26 +688,7 @@ int taa_synth_spheres(const taa_synth_scene_t* s, float* t, int32_t cap) {
     int rc = check_scene(s);
     if (rc) return rc;
     if (!t || cap < s->num_spheres) return fail(TAA_E_INVAL, "synth: sphere table too small");
-    uint64_t st = s->seed ^ 0xA0761D6478BD642Full;
-    auto uni = [&]() {
-        st += 0x9E3779B97F4A7C15ull;
-        return (double)(taa_synth::mix64(st) >> 11) * (1.0 / 9007199254740992.0);
-    };
-    for (int i = 0; i < s->num_spheres; ++i) {
-        float* p = t + i * TAA_SYNTH_SPHERE_FLOATS;
-        p[0] = (float)(uni() * s->width);
-        p[1] = (float)(uni() * s->height);
-        p[2] = (float)(s->radius_min + uni() * (s->radius_max - s->radius_min));
-        p[3] = (float)(50.0 + uni() * 350.0);
-        p[4] = (float)uni();
-        p[5] = (float)uni();
-        p[6] = (float)uni();
-        p[7] = (float)((2.0 * uni() - 1.0) * s->sphere_speed_max);
-        p[8] = (float)((2.0 * uni() - 1.0) * s->sphere_speed_max);
-        p[9] = (float)((2.0 * uni() - 1.0) * s->spin_max);
-        p[10] = p[2] / 3.0f;
-        p[11] = 0.f;
-    }
+    taa_synth::spheres(*s, t);
     return ok();
 }
 

@@ -36,6 +36,11 @@ bool fast_path_supported(const taa_uniforms_t& U, int in_w, int in_h, int out_w,
 // unjittered neighbourhood only with a zero jitter.
 bool up_path_supported(const taa_uniforms_t& U, int in_w, int in_h, int out_w, int out_h);
 
+// The reassociating FP32 resolve, TAA_FORM_FAST (resolve_fast32.cu): whether
+// it runs these parameters, sizes and history format, and its launch.
+bool fast32_supported(const taa_uniforms_t& U, int history_fmt, int in_w, int in_h, int out_w, int out_h);
+cudaError_t launch_resolve_fast32(int motion_ch, const taa_uniforms_t& U, const FrameArgs& a, cudaStream_t stream);
+
 // Tiled FP32 / FP16 resolve, optionally with the fused sharpen (resolve_fast.cu).
 cudaError_t launch_resolve_fast(const FastKey& key, const taa_uniforms_t& U, const FrameArgs& a,
                                 cudaStream_t stream);

@@ -1,0 +1,428 @@
+// resolve_fast32.cu - TAA_FORM_FAST: the resolve of the benchmark mode of the
+// parameter block (YCoCg variance clip toward the box centre, velocity for
+// every pixel, simple velocity sampling; Catmull-Rom or bilinear history;
+// optional depth culling and out-of-screen rejection; RGBA32F history) in
+// FP32 with the arithmetic reassociated for speed instead of rounded like
+// the shader:
+//
+//   * the 3x3 moments (taa.comp:266-277) come from row sums that a thread's
+//     two vertically adjacent pixels share (their boxes have two rows in
+//     common), with Cg and Cg^2 staged side by side so one packed add
+//     accumulates both, and mean = m1 * (1/9);
+//   * the standard deviation is the hardware square-root approximation, the
+//     clip's per-channel ratios (taa.comp:323-345) use the hardware
+//     reciprocal approximation; the box centre is the mean and its half
+//     extent gamma * sigma + 1e-7 (the shader's (max + min) / 2 and
+//     (max - min) / 2 + 1e-7 of mean -/+ gamma * sigma);
+//   * multiplies and adds contract into FMAs; uv is (x + 0.5) * (1 / size).
+//
+// Everything else is the exact forms' pipeline: a 32x16 tile per 256-thread
+// CTA, two pixels per thread; the colour tile with its 1-pixel halo staged in
+// shared memory as YCoCg; a history window per tile (the Catmull-Rom taps of
+// the tile's centre pixel widened by the tile and 3 pixels of motion
+// difference) copied by one TMA tensor copy on a bounded mbarrier wait, or by
+// cp.async with edge clamps where it crosses the image border; pixels whose
+// taps leave the window read global memory.  The window is placed by the
+// thread that owns the tile's centre pixel, from the velocity it has loaded
+// for its own pixel, so no extra load delays the copy.
+//
+// Precision: frame relative L2 within 1e-5 of the exact FP32 forms on the
+// benchmark scenes, and within the same distance of the FP64 oracle as they
+// are (tests/test_gpu_fast.py).
+#include <cuda.h>
+
+#include <cstring>
+
+#include "kernels.h"
+#include "tiled_skeleton.cuh"
+
+namespace taa_dev {
+namespace fast32 {
+
+using tiled::cp_async;
+using tiled::cp_async_commit;
+using tiled::cp_async_wait_all;
+using tiled::first_wait_polls;
+using tiled::mbar_expect_tx;
+using tiled::mbar_init;
+using tiled::mbar_wait_bounded;
+using tiled::tma_load_3d;
+
+constexpr int TX = 32, TY = 16, NT = 256;       // tile, threads (two pixels each)
+constexpr int SX = TX + 2, SY = TY + 2, NS = SX * SY;  // staged colour with its 1-pixel halo
+constexpr int MARGIN = tiled::WIN_MARGIN;
+constexpr int WW = TX + 3 + 2 * MARGIN, WH = TY + 3 + 2 * MARGIN;  // history window (texels)
+constexpr int REF_TID = (TY / 2 / 2) * 32 + TX / 2;  // the thread whose first pixel is the centre (16, 8)
+
+// Everything a launch reads, flattened: pointers, row pitches in bytes, the
+// few parameters the benchmark mode uses.
+struct Args {
+    const char* color;  // RGBA16F
+    const char* depth;  // D32F
+    const char* vel;    // RG16F or RGBA16F
+    const char* hist;   // RGBA32F, or null (reads zeros)
+    const char* hdepth; // D32F previous depth, or null
+    char* hout;         // RGBA32F
+    char* result;       // RGBA16F, or null
+    unsigned int* status;
+    uint32_t color_pitch, depth_pitch, vel_pitch, hist_pitch, hdepth_pitch, hout_pitch, result_pitch;
+    int W, H;
+    float inv_w, inv_h;
+    float alpha, rejection_alpha, gamma;
+    int reject_outside, depth_cull, reset;
+};
+
+struct Smem {
+    float4 col[NS];                    // staged (Y, Co, Cg, Cg^2)
+    alignas(128) float4 win[WW * WH];  // the history window
+    uint64_t bar;                      // completion of the window's TMA copy
+    int org[3];                        // window origin x, y; 1 TMA, 2 cp.async, 0 none
+};
+
+template <class T> __device__ __forceinline__ const T* at(const char* base, uint32_t pitch, int x, int y) {
+    return reinterpret_cast<const T*>(base + (size_t)(uint32_t)y * pitch) + x;
+}
+template <class T> __device__ __forceinline__ T* at_w(char* base, uint32_t pitch, int x, int y) {
+    return reinterpret_cast<T*>(base + (size_t)(uint32_t)y * pitch) + x;
+}
+
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ f2 mulp(f2 a, f2 b) {
+    f2 d;
+    asm("mul.f32x2 %0, %1, %2;" : "=l"(d.v) : "l"(a.v), "l"(b.v));
+    return d;
+}
+__device__ __forceinline__ f2 addp(f2 a, f2 b) {
+    f2 d;
+    asm("add.f32x2 %0, %1, %2;" : "=l"(d.v) : "l"(a.v), "l"(b.v));
+    return d;
+}
+__device__ __forceinline__ f2 fmap(f2 a, f2 b, f2 c) {
+    f2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+    return d;
+}
+
+// RGBA16F texel -> (Y, Co, Cg, Cg^2) (taa.comp:158-164)
+__device__ __forceinline__ float4 stage(uint2 raw) {
+    const float4 c = half4_to_float4(raw);
+    const float y = 0.25f * (c.x + c.z) + 0.5f * c.y;
+    const float co = 0.5f * (c.x - c.z);
+    const float cg = 0.5f * c.y - 0.25f * (c.x + c.z);
+    return make_float4(y, co, cg, cg * cg);
+}
+
+// The 3x3 moments of one staged row segment (three texels): the (Y, Co) sum,
+// the (Cg, Cg^2) sum and the (Y^2, Co^2) sum.
+struct Row {
+    f2 a, c, q;
+};
+__device__ __forceinline__ Row row_sums(const float4* p) {
+    f2 a0, c0, a1, c1, a2, c2;
+    load_pairs(p, a0, c0);
+    load_pairs(p + 1, a1, c1);
+    load_pairs(p + 2, a2, c2);
+    Row r;
+    r.a = addp(addp(a0, a1), a2);
+    r.c = addp(addp(c0, c1), c2);
+    r.q = fmap(a2, a2, fmap(a1, a1, mulp(a0, a0)));
+    return r;
+}
+__device__ __forceinline__ Row add(const Row& u, const Row& v) { return {addp(u.a, v.a), addp(u.c, v.c), addp(u.q, v.q)}; }
+
+// The variance box of one pixel: centre (the mean) and half extent gamma * sigma + 1e-7.
+struct Box {
+    float m[3], e[3];
+};
+__device__ __forceinline__ Box box_of(const Row& s, float gamma) {
+    const f2 n = dup(1.0f / 9.0f);
+    const f2 mean = mulp(s.a, n);  // (Y, Co)
+    const f2 cg = mulp(s.c, n);    // (mean Cg, m2 Cg / 9)
+    const f2 var = fmap(neg2(mean), mean, mulp(s.q, n));
+    const float var_cg = fmaf(-f2lo(cg), f2lo(cg), f2hi(cg));
+    Box b;
+    b.m[0] = f2lo(mean);
+    b.m[1] = f2hi(mean);
+    b.m[2] = f2lo(cg);
+    b.e[0] = fmaf(gamma, sqrt_approx(fmaxf(f2lo(var), 0.f)), 1e-7f);
+    b.e[1] = fmaf(gamma, sqrt_approx(fmaxf(f2hi(var), 0.f)), 1e-7f);
+    b.e[2] = fmaf(gamma, sqrt_approx(fmaxf(var_cg, 0.f)), 1e-7f);
+    return b;
+}
+
+// Catmull-Rom weights of both axes as (x, y) pairs (taa.comp:464-467, the
+// same polynomials in Horner form), and the first tap.
+struct Taps {
+    f2 w[4];
+    int ux, uy;
+};
+template <int INTERP>
+__device__ __forceinline__ Taps taps_of(float hu, float hv, const Args& a) {
+    Taps t;
+    const f2 it = mulp(pk(hu, hv), pk((float)a.W, (float)a.H));
+    const float bx = floorf(f2lo(it) - 0.5f), by = floorf(f2hi(it) - 0.5f);
+    const f2 f = addp(it, pk(-0.5f - bx, -0.5f - by));
+    if constexpr (INTERP == 2) {
+        const f2 one = dup(1.0f), half = dup(0.5f);
+        const f2 f2_ = mulp(f, f);
+        t.w[0] = mulp(f, fmap(f, fmap(dup(-0.5f), f, one), dup(-0.5f)));
+        t.w[1] = fmap(f2_, fmap(dup(1.5f), f, dup(-2.5f)), one);
+        t.w[2] = mulp(f, fmap(f, fmap(dup(-1.5f), f, dup(2.0f)), half));
+        t.w[3] = mulp(mulp(half, f2_), addp(f, dup(-1.0f)));
+        t.ux = trunc_index(bx) - 1;
+        t.uy = trunc_index(by) - 1;
+    } else {
+        // bilinear (taa.comp:546): weights (1 - f, f); a NaN fraction weights the first tap by 1
+        float fx = f2lo(f), fy = f2hi(f);
+        if (!(fx == fx)) fx = 0.f;
+        if (!(fy == fy)) fy = 0.f;
+        t.w[0] = pk(1.0f - fx, 1.0f - fy);
+        t.w[1] = pk(fx, fy);
+        t.ux = trunc_index(bx);
+        t.uy = trunc_index(by);
+    }
+    return t;
+}
+
+// The filter over N x N texels read through tex(i, j): rows of N taps
+// weighted by x, then the rows weighted by y; (R, G) as a pair, B alone.
+template <int N, class F> __device__ __forceinline__ float3 filter(const Taps& t, F&& tex) {
+    f2 acc = dup(0.f);
+    float accb = 0.f;
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        f2 r = dup(0.f);
+        float rb = 0.f;
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            const float4 s = tex(i, j);
+            const float wx = f2lo(t.w[i]);
+            r = fmap(dup(wx), pk(s.x, s.y), r);
+            rb = fmaf(wx, s.z, rb);
+        }
+        const float wy = f2hi(t.w[j]);
+        acc = fmap(dup(wy), r, acc);
+        accb = fmaf(wy, rb, accb);
+    }
+    return make_float3(f2lo(acc), f2hi(acc), accb);
+}
+
+template <int INTERP, int MC>
+__global__ void __launch_bounds__(NT, 4)
+    resolve_fast32(const Args a, const __grid_constant__ CUtensorMap hmap, const int tma_ok) {
+    using RawVel = typename std::conditional<MC == 4, uint2, uint32_t>::type;
+    constexpr int SPAN = INTERP == 2 ? 4 : 2;
+    __shared__ Smem sm;
+    const int tid = threadIdx.x, lx = tid & 31, ly = tid >> 5;
+    const int W = a.W, H = a.H;
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+    const int x = x0 + lx, cx = min(x, W - 1);
+    const int ya = y0 + 2 * ly;
+    const int cy0 = min(ya, H - 1), cy1 = min(ya + 1, H - 1);
+    const bool have_hist = a.hist != nullptr;
+
+    // 1. loads: the two pixels' depth and velocity, this thread's staged colour texels
+    const float d0 = __ldg(at<float>(a.depth, a.depth_pitch, cx, cy0));
+    const float d1 = __ldg(at<float>(a.depth, a.depth_pitch, cx, cy1));
+    const RawVel v0raw = __ldg(at<RawVel>(a.vel, a.vel_pitch, cx, cy0));
+    const RawVel v1raw = __ldg(at<RawVel>(a.vel, a.vel_pitch, cx, cy1));
+    uint2 st[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        const int i = tid + j * NT;
+        st[j] = make_uint2(0u, 0u);
+        if (j < 2 || i < NS) {
+            const int sy = i / SX, sx = i - sy * SX;
+            st[j] = __ldg(at<uint2>(a.color, a.color_pitch, clampi(x0 - 1 + sx, 0, W - 1), clampi(y0 - 1 + sy, 0, H - 1)));
+        }
+    }
+    // 2. history positions (uv - velocity), the previous depth under them
+    const float u = ((float)cx + 0.5f) * a.inv_w;
+    const float v0 = ((float)cy0 + 0.5f) * a.inv_h, v1 = ((float)cy1 + 0.5f) * a.inv_h;
+    const float4 vel0 = tiled::velocity_of<MC>(v0raw), vel1 = tiled::velocity_of<MC>(v1raw);
+    const float hu0 = u - vel0.x, hv0 = v0 - vel0.y, hu1 = u - vel1.x, hv1 = v1 - vel1.y;
+    float pd0 = 0.f, pd1 = 0.f;
+    if (a.depth_cull && a.hdepth) {
+        pd0 = __ldg(at<float>(a.hdepth, a.hdepth_pitch, clampi(trunc_index(hu0 * (float)W), 0, W - 1),
+                              clampi(trunc_index(hv0 * (float)H), 0, H - 1)));
+        pd1 = __ldg(at<float>(a.hdepth, a.hdepth_pitch, clampi(trunc_index(hu1 * (float)W), 0, W - 1),
+                              clampi(trunc_index(hv1 * (float)H), 0, H - 1)));
+    }
+    // 3. the thread owning the tile's centre pixel places the history window
+    //    (its own pixel's taps widened by the tile and MARGIN) and starts the copy
+    if (tid == REF_TID && have_hist) {
+        const int k0 = INTERP == 2 ? 1 : 0;
+        const int rux = trunc_index(floorf(hu0 * (float)W - 0.5f)) - k0;
+        const int ruy = trunc_index(floorf(hv0 * (float)H - 0.5f)) - k0;
+        const int wx0 = rux - (cx - x0) - MARGIN, wy0 = ruy - (cy0 - y0) - MARGIN;
+        const bool interior = wx0 >= 0 && wy0 >= 0 && wx0 <= W - WW && wy0 <= H - WH;
+        const int mode = tma_ok && interior ? 1 : 2;
+        sm.org[0] = wx0;
+        sm.org[1] = wy0;
+        sm.org[2] = mode;
+        if (mode == 1) {
+            mbar_init(&sm.bar, 1);
+            mbar_expect_tx(&sm.bar, (uint32_t)(sizeof(float4) * WW * WH));
+            tma_load_3d(sm.win, &hmap, 0, wx0, wy0, &sm.bar);
+        }
+    }
+    // 4. staged colour
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        const int i = tid + j * NT;
+        if (j < 2 || i < NS) sm.col[i] = stage(st[j]);
+    }
+    __syncthreads();
+    int wx0 = 0, wy0 = 0, mode = 0;
+    if (have_hist) {
+        wx0 = sm.org[0];
+        wy0 = sm.org[1];
+        mode = sm.org[2];
+    }
+    if (mode == 2) {
+        // a window across the image border: every texel edge-clamped
+        const int lane = tid & 31, warp = tid >> 5;
+        for (int r = warp; r < WH; r += NT / 32) {
+            const int gy = clampi(wy0 + r, 0, H - 1);
+            for (int c = lane; c < WW; c += 32)
+                cp_async<16>(&sm.win[r * WW + c], at<float4>(a.hist, a.hist_pitch, clampi(wx0 + c, 0, W - 1), gy));
+        }
+        cp_async_commit();
+    }
+    // rejection (taa.comp:787-823): out of the screen, or the previous depth
+    // under the history position too far from the expected one
+    bool rej[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const float hu = k ? hu1 : hu0, hv = k ? hv1 : hv0, pd = k ? pd1 : pd0;
+        const float ehd = (k ? d1 : d0) - (k ? vel1.z : vel0.z);
+        rej[k] = (a.reject_outside && (hu < 0.f || hv < 0.f || hu >= 1.f || hv >= 1.f)) ||
+                 (a.depth_cull && fabsf(pd - ehd) > 0.1f * (1.0f - pd));
+    }
+    // 5. the two boxes while the window is in flight: rows 2ly .. 2ly+3 of the
+    //    staged tile, columns lx .. lx+2; rows 1 and 2 are shared
+    const float4* sp = &sm.col[(2 * ly) * SX + lx];
+    const Row mid = add(row_sums(sp + SX), row_sums(sp + 2 * SX));
+    const Box b0 = box_of(add(row_sums(sp), mid), a.gamma);
+    const Box b1 = box_of(add(mid, row_sums(sp + 3 * SX)), a.gamma);
+
+    bool landed = true;
+    if (mode == 1) {
+        landed = mbar_wait_bounded(&sm.bar, 0u, first_wait_polls(a.status));
+        if (!landed) {
+            atomicOr(a.status, kStatusWindowTimeout);
+            mbar_wait_bounded(&sm.bar, 0u);  // the copy may still land in this CTA's memory
+        }
+    } else if (mode == 2) {
+        cp_async_wait_all();
+        __syncthreads();
+    }
+    // 6. per pixel: rejection, history sample, clip, blend, stores
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const int y = ya + k;
+        if (!(x < W && y < H && landed)) continue;
+        const Box& b = k ? b1 : b0;
+        const float hu = k ? hu1 : hu0, hv = k ? hv1 : hv0;
+        const bool rejected = rej[k];
+        float3 h = make_float3(0.f, 0.f, 0.f);
+        if (have_hist) {
+            const Taps t = taps_of<INTERP>(hu, hv, a);
+            const int bx = t.ux - wx0, by = t.uy - wy0;
+            if ((unsigned)bx <= (unsigned)(WW - SPAN) && (unsigned)by <= (unsigned)(WH - SPAN)) {
+                const float4* wp = &sm.win[by * WW + bx];
+                h = filter<SPAN>(t, [&](int i, int j) { return wp[j * WW + i]; });
+            } else {
+                h = filter<SPAN>(t, [&](int i, int j) {
+                    return __ldg(at<float4>(a.hist, a.hist_pitch, clampi(t.ux + i, 0, W - 1), clampi(t.uy + j, 0, H - 1)));
+                });
+            }
+        }
+        // history to YCoCg, clip toward the box centre (taa.comp:323-345)
+        float hc[3] = {0.25f * (h.x + h.z) + 0.5f * h.y, 0.5f * (h.x - h.z), 0.5f * h.y - 0.25f * (h.x + h.z)};
+        float dd[3], ma = 0.f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            dd[c] = hc[c] - b.m[c];
+            ma = fmaxf(ma, fabsf(dd[c]) * rcp_approx(b.e[c]));
+        }
+        const float s = ma > 1.0f ? rcp_approx(ma) : 1.0f;
+        // blend (taa.comp:848-900): mix(history, current, alpha)
+        const float alpha = a.reset ? 1.0f : (rejected ? a.rejection_alpha : a.alpha);
+        const float4 c0 = sm.col[(2 * ly + k + 1) * SX + lx + 1];
+        const float cur[3] = {c0.x, c0.y, c0.z};
+        float o[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float hcl = fmaf(dd[c], s, b.m[c]);
+            o[c] = fmaf(alpha, cur[c] - hcl, hcl);
+        }
+        const float tmp = o[0] - o[2];
+        const float r = tmp + o[1], g = o[0] + o[2], bl = tmp - o[1];
+        *at_w<float4>(a.hout, a.hout_pitch, x, y) = make_float4(r, g, bl, 0.f);
+        if (a.result) *at_w<uint2>(a.result, a.result_pitch, x, y) = float4_to_half4(make_float4(r, g, bl, 1.0f));
+    }
+}
+
+}  // namespace fast32
+
+bool fast32_supported(const taa_uniforms_t& U, int history_fmt, int in_w, int in_h, int out_w, int out_h) {
+    const taa_parameters_t& P = U.param[0];
+    return history_fmt == 0 && tiled::is_hot(P) && (P.mInterpolationMode == 0 || P.mInterpolationMode == 2) &&
+           fast_path_supported(U, in_w, in_h, out_w, out_h);
+}
+
+cudaError_t launch_resolve_fast32(int motion_ch, const taa_uniforms_t& U, const FrameArgs& f, cudaStream_t s) {
+    using namespace fast32;
+    const taa_parameters_t& P = U.param[0];
+    Args a;
+    a.color = f.color.p;
+    a.depth = f.depth.p;
+    a.vel = f.velocity.p;
+    a.hist = f.history.p;
+    a.hdepth = f.history_depth.p;
+    a.hout = f.history_out.p;
+    a.result = f.result.p;
+    a.status = f.status;
+    a.color_pitch = (uint32_t)f.color.pitch;
+    a.depth_pitch = (uint32_t)f.depth.pitch;
+    a.vel_pitch = (uint32_t)f.velocity.pitch;
+    a.hist_pitch = (uint32_t)f.history.pitch;
+    a.hdepth_pitch = (uint32_t)f.history_depth.pitch;
+    a.hout_pitch = (uint32_t)f.history_out.pitch;
+    a.result_pitch = (uint32_t)f.result.pitch;
+    a.W = f.out_w;
+    a.H = f.out_h;
+    a.inv_w = f.inv_out_w;
+    a.inv_h = f.inv_out_h;
+    a.alpha = P.mAlpha;
+    a.rejection_alpha = P.mRejectionAlpha;
+    a.gamma = P.mVarClipGamma;
+    a.reject_outside = P.mRejectOutside != 0;
+    a.depth_cull = P.mDepthCulling != 0;
+    a.reset = U.mResetHistory != 0;
+    CUtensorMap map;
+    std::memset(&map, 0, sizeof map);
+    const int tma_ok = a.hist && f.history.w >= WW && f.history.h >= WH &&
+                       encode_history_map(f.history, 0, WW, WH, &map);
+    const dim3 grid((a.W + TX - 1) / TX, (a.H + TY - 1) / TY);
+    if (P.mInterpolationMode == 2) {
+        if (motion_ch == 4) resolve_fast32<2, 4><<<grid, NT, 0, s>>>(a, map, tma_ok);
+        else resolve_fast32<2, 2><<<grid, NT, 0, s>>>(a, map, tma_ok);
+    } else {
+        if (motion_ch == 4) resolve_fast32<0, 4><<<grid, NT, 0, s>>>(a, map, tma_ok);
+        else resolve_fast32<0, 2><<<grid, NT, 0, s>>>(a, map, tma_ok);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace taa_dev

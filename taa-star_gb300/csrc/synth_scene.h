@@ -47,6 +47,50 @@ SYN_HD float halton_f(int i, int b) {
     return r;
 }
 
+// The scene's defaults for a w x h frame (the configurations' shared values).
+inline void default_scene(taa_synth_scene_t& o, int32_t w, int32_t h, uint64_t seed) {
+    o = taa_synth_scene_t{};
+    o.struct_size = sizeof o;
+    o.width = w;
+    o.height = h;
+    o.seed = seed;
+    o.num_spheres = 32;
+    o.radius_min = 20.f;
+    o.radius_max = 120.f;
+    o.sphere_speed_max = 6.f;
+    o.spin_max = 0.f;
+    o.cam_v0[0] = 3.f;
+    o.checker_period = 7.3f;
+    o.firefly_fraction = 0.01f;
+    o.firefly_max = 64.f;
+    o.jitter_phase = 0;
+    o.jitter_enabled = 1;
+}
+
+// The seeded sphere table: num_spheres rows of TAA_SYNTH_SPHERE_FLOATS.
+inline void spheres(const taa_synth_scene_t& s, float* t) {
+    uint64_t st = s.seed ^ 0xA0761D6478BD642Full;
+    auto uni = [&]() {
+        st += 0x9E3779B97F4A7C15ull;
+        return (double)(mix64(st) >> 11) * (1.0 / 9007199254740992.0);
+    };
+    for (int i = 0; i < s.num_spheres; ++i) {
+        float* p = t + i * TAA_SYNTH_SPHERE_FLOATS;
+        p[0] = (float)(uni() * s.width);
+        p[1] = (float)(uni() * s.height);
+        p[2] = (float)(s.radius_min + uni() * (s.radius_max - s.radius_min));
+        p[3] = (float)(50.0 + uni() * 350.0);
+        p[4] = (float)uni();
+        p[5] = (float)uni();
+        p[6] = (float)uni();
+        p[7] = (float)((2.0 * uni() - 1.0) * s.sphere_speed_max);
+        p[8] = (float)((2.0 * uni() - 1.0) * s.sphere_speed_max);
+        p[9] = (float)((2.0 * uni() - 1.0) * s.spin_max);
+        p[10] = p[2] / 3.0f;
+        p[11] = 0.f;
+    }
+}
+
 SYN_HD void jitter_px(const taa_synth_scene_t& s, int t, float& jx, float& jy) {
     if (!s.jitter_enabled) { jx = 0.f; jy = 0.f; return; }
     int idx = ((t + s.jitter_phase) % 8 + 8) % 8;

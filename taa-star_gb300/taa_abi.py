@@ -26,7 +26,7 @@ TAA_HISTORY_RGBA32F = 0
 TAA_HISTORY_RGBA16F = 1
 TAA_MOTION_RGBA16F = 0
 TAA_MOTION_RG16F = 1
-TAA_FORM_AUTO, TAA_FORM_PLAIN, TAA_FORM_TILED, TAA_FORM_FP16, TAA_FORM_LEARNED = 0, 1, 2, 3, 4
+TAA_FORM_AUTO, TAA_FORM_PLAIN, TAA_FORM_TILED, TAA_FORM_FP16, TAA_FORM_LEARNED, TAA_FORM_FAST = 0, 1, 2, 3, 4, 5
 TAA_FLAG_LEARNED_TCGEN05 = 0x1
 TAA_FLAG_FXAA = 0x2
 TAA_FLAG_FP16_GUARD = 0x4

@@ -25,6 +25,7 @@ pytestmark = pytest.mark.gpu
 CHECK = (16, 32, 48, 63)
 FORMS = {
     "tiled": (T.TAA_FORM_TILED, 0, 1e-4),
+    "fast": (T.TAA_FORM_FAST, 0, 1e-4),
     "fp16_guarded": (T.TAA_FORM_FP16, T.TAA_FLAG_FP16_GUARD, 1e-3),
 }
 

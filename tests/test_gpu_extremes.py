@@ -59,6 +59,14 @@ def test_fp32_forms_give_the_oracle_bits(cuda, extreme, form):
     assert T.device_status(clear=True) == 0
 
 
+def test_fast_form_within_its_contract(cuda, extreme):
+    w, h, fr, hist, u, ref = extreme
+    got, _ = resolve(cuda, T.TAA_FORM_FAST, w, h, fr, hist, u)
+    r = ref["history"][..., :3]
+    assert np.linalg.norm(got[..., :3] - r) <= 1e-5 * np.linalg.norm(r)
+    assert T.device_status(clear=True) == 0
+
+
 def test_fp16_form_within_its_contract(cuda, extreme):
     w, h, fr, hist, u, ref = extreme
     got, _ = resolve(cuda, T.TAA_FORM_FP16, w, h, fr, hist, u)

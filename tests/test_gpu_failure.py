@@ -71,7 +71,7 @@ def give_up(cuda):
     T.device_status(clear=True)
 
 
-@pytest.mark.parametrize("form", [T.TAA_FORM_TILED, T.TAA_FORM_FP16])
+@pytest.mark.parametrize("form", [T.TAA_FORM_TILED, T.TAA_FORM_FP16, T.TAA_FORM_FAST])
 def test_window_wait_gives_up_and_leaves_the_tile_unwritten(cuda, form):
     u, b = inputs(cuda)
     ctx = T.Taa(W, H, form=form)

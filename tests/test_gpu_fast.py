@@ -1,0 +1,130 @@
+"""TAA_FORM_FAST, the reassociating FP32 resolve (run with -m gpu).
+
+The form computes what the tiled FP32 form computes with the arithmetic
+reassociated (shared row sums for the 3x3 moments, contracted FMAs,
+hardware square-root and reciprocal approximations), so its contract is a
+distance, not bits: frame relative L2 within 1e-5 of the reference shader's
+own FP32 output (tests/golden) and of the exact tiled form, and within 1e-4
+relative L2 / 50 dB PSNR of the FP64 oracle on the benchmark sequences, as
+the exact forms are.  Parameters outside the benchmark mode run in the exact
+forms with their bits.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+import taa_abi as T
+import workloads as WL
+from helpers import cpu_frames, gpu_resolve, psnr, rel_l2, to_dev
+from test_gpu_golden import CASES, FIX, gpu
+
+pytestmark = pytest.mark.gpu
+
+FAST_RELL2 = 1e-5
+# fixture cases in the benchmark mode: the fast form runs them
+FAST_CASES = ("s:base", "s:c2_depth_reject", "s:bilinear", "s:gamma_1_5", "s:reset")
+
+
+@pytest.mark.parametrize("key", CASES)
+def test_fast_form_on_reference_fixtures(cuda, key):
+    used, hist, _ = gpu(key, T.TAA_FORM_FAST, cuda)
+    tused, thist, _ = gpu(key, T.TAA_FORM_TILED, cuda)
+    if key in FAST_CASES:
+        assert used == T.TAA_FORM_FAST
+    if used == T.TAA_FORM_FAST:
+        ref32 = FIX[f"{key}/ref32_history"].astype(np.float64)
+        assert rel_l2(hist[..., :3], ref32[..., :3]) <= FAST_RELL2
+        assert rel_l2(hist[..., :3], thist[..., :3]) <= FAST_RELL2
+        assert np.all(hist[..., 3] == 0.0)
+    else:
+        # parameters outside the benchmark mode: the exact forms, their bits
+        assert used == tused
+        np.testing.assert_array_equal(hist, thist)
+
+
+def test_auto_selects_the_fast_form_in_the_benchmark_mode(cuda):
+    ctx = T.Taa(64, 32)
+    for params, want in ((dict(), T.TAA_FORM_FAST), (dict(mDepthCulling=1, mRejectOutside=1), T.TAA_FORM_FAST),
+                         (dict(mInterpolationMode=0), T.TAA_FORM_FAST), (dict(mInterpolationMode=1), T.TAA_FORM_TILED),
+                         (dict(mToneMapLumaKaris=1), T.TAA_FORM_TILED),
+                         (dict(mColorClampingOrClipping=1), T.TAA_FORM_TILED)):
+        ctx.set_uniforms(T.make_uniforms(WL.base_parameters(**params)))
+        assert ctx.selected_form() == want, params
+    ctx.close()
+    ctx = T.Taa(64, 32, history_format=T.TAA_HISTORY_RGBA16F, form=T.TAA_FORM_FAST)
+    ctx.set_uniforms(T.make_uniforms(WL.base_parameters()))
+    assert ctx.selected_form() == T.TAA_FORM_TILED  # RGBA16F history: the exact form
+    ctx.close()
+
+
+@pytest.mark.parametrize("size", [(70, 41), (17, 9), (33, 31), (256, 144), (1, 1), (40, 1), (1, 40)])
+@pytest.mark.parametrize("mode", ["c2", "bilinear", "rgba16f_motion", "first_frame"])
+def test_fast_form_against_the_exact_form(cuda, size, mode):
+    w, h = size
+    params = dict(mDepthCulling=1, mRejectOutside=1) if mode == "c2" else \
+        dict(mInterpolationMode=0) if mode == "bilinear" else {}
+    mc = 4 if mode == "rgba16f_motion" else 2
+    wl = WL.small(w, h, frames=2, seed=w * 7 + h, params=params)
+    fr = cpu_frames(wl, range(2), motion_channels=mc)
+    hist = None if mode == "first_frame" else fr[0]["color"].astype(np.float32)
+    u = T.make_uniforms(wl.parameters(), jitter_ndc=fr[1]["jitter"], mResetHistory=1 if mode == "first_frame" else 0)
+    outs = {}
+    for form in (T.TAA_FORM_FAST, T.TAA_FORM_TILED):
+        ctx = T.Taa(w, h, form=form, motion_format=T.TAA_MOTION_RGBA16F if mc == 4 else T.TAA_MOTION_RG16F)
+        ctx.set_uniforms(u)
+        assert ctx.selected_form() == form
+        outs[form] = gpu_resolve(ctx, cuda, fr[1]["color"], fr[1]["depth"], fr[1]["motion"], hist, fr[0]["depth"])
+        ctx.close()
+    f, t = outs[T.TAA_FORM_FAST], outs[T.TAA_FORM_TILED]
+    assert np.all(np.isfinite(f["history_out"]))
+    assert rel_l2(f["history_out"][..., :3], t["history_out"][..., :3]) <= FAST_RELL2
+    assert rel_l2(f["result"][..., :3], t["result"][..., :3]) <= 1e-3  # after the RGBA16F store
+    assert np.all(f["result"][..., 3] == 1.0)
+    assert T.device_status(clear=True) == 0
+
+
+def render(wl, sc, f, dev):
+    H, W = wl.height, wl.width
+    col = torch.empty(H, W, 4, dtype=torch.float16, device=dev)
+    dep = torch.empty(H, W, dtype=torch.float32, device=dev)
+    mot = torch.empty(H, W, 2, dtype=torch.float16, device=dev)
+    T.synth_render(sc, f, color=col, depth=dep, motion=mot)
+    return col, dep, mot
+
+
+@pytest.mark.parametrize("name,frames,check", [("c1", 16, range(1, 16)), ("c2", 6, (1, 5)), ("c3", 6, (1, 5))])
+def test_fast_form_sequences_against_fp64(cuda, name, frames, check):
+    """Each checked frame against the FP64 oracle fed the same history: relative
+    L2 <= 1e-4 and PSNR >= 50 dB (the exact forms' bar); and within 1e-5 of
+    the exact FP32 oracle's resolve of the same frame."""
+    wl = {"c1": WL.c1, "c2": WL.c2, "c3": WL.c3}[name]()
+    sc = wl.scene()
+    H, W = wl.height, wl.width
+    ctx = T.Taa(W, H, form=T.TAA_FORM_FAST)
+    hist = torch.zeros(H, W, 4, device=cuda)
+    hout = torch.empty_like(hist)
+    prev = None
+    rep = []
+    for f in range(frames):
+        col, dep, mot = render(wl, sc, f, cuda)
+        u = T.make_uniforms(wl.parameters(), jitter_ndc=T.synth_jitter(sc, f)[1], mResetHistory=1 if f == 0 else 0)
+        ctx.set_uniforms(u)
+        assert ctx.selected_form() == T.TAA_FORM_FAST
+        pd = prev if prev is not None else dep
+        ctx.resolve(color=col, depth=dep, velocity=mot, history=hist, history_depth=pd, history_out=hout)
+        torch.cuda.synchronize()
+        if f in check:
+            args = (u, col.float().cpu().numpy(), dep.cpu().numpy(), mot.float().cpu().numpy())
+            kw = dict(history=hist.cpu().numpy(), history_depth=pd.cpu().numpy())
+            got = hout.cpu().numpy()[..., :3]
+            r32 = O.resolve(*args, **kw)["history"][..., :3]
+            r64 = O.resolve(*args, precision=64, **kw)["history"][..., :3]
+            rep.append((f, rel_l2(got, r32), rel_l2(got, r64), psnr(got, r64)))
+        hist, hout = hout, hist
+        prev = dep
+    ctx.close()
+    print(f"{name} fast form (frame, relL2 vs FP32 oracle, relL2 vs FP64, PSNR vs FP64):", rep)
+    assert max(r[1] for r in rep) <= FAST_RELL2
+    assert max(r[2] for r in rep) <= 1e-4
+    assert min(r[3] for r in rep) >= 50.0

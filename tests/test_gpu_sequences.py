@@ -172,7 +172,7 @@ def test_c3_1440p_cas_sequence(cuda, interp):
     wl = WL.c3(interp)
     sc = wl.scene()
     H, W = wl.height, wl.width
-    one = T.Taa(W, H, sharpener=T.TAA_SHARPEN_CAS, sharpen_factor=0.5)
+    one = T.Taa(W, H, form=T.TAA_FORM_TILED, sharpener=T.TAA_SHARPEN_CAS, sharpen_factor=0.5)
     two = T.Taa(W, H, form=T.TAA_FORM_FP16)
     _, c1 = O.cas_setup(0.5, W, H, W, H)
     hist = [torch.zeros(H, W, 4, dtype=torch.float32, device=cuda) for _ in range(2)]
