@@ -48,6 +48,16 @@ using tiled::mbar_init;
 using tiled::mbar_wait_bounded;
 using tiled::tma_load_3d;
 
+// Resident CTAs per SM the register budget is sized for (a tuning constant).
+#ifndef TAA_FAST_MIN_BLOCKS
+#define TAA_FAST_MIN_BLOCKS 4
+#endif
+// Whether a thread's two pixels read their Catmull-Rom rows once when their
+// footprints are one row apart (a tuning switch).
+#ifndef TAA_FAST_SHARED_TAPS
+#define TAA_FAST_SHARED_TAPS 1
+#endif
+
 constexpr int TX = 32, TY = 16, NT = 256;       // tile, threads (two pixels each)
 constexpr int SX = TX + 2, SY = TY + 2, NS = SX * SY;  // staged colour with its 1-pixel halo
 constexpr int MARGIN = tiled::WIN_MARGIN;
@@ -67,7 +77,7 @@ struct Args {
     unsigned int* status;
     uint32_t color_pitch, depth_pitch, vel_pitch, hist_pitch, hdepth_pitch, hout_pitch, result_pitch;
     int W, H;
-    float inv_w, inv_h;
+    float inv_w, inv_h;  // correctly rounded 1 / W, 1 / H
     float alpha, rejection_alpha, gamma;
     int reject_outside, depth_cull, reset;
 };
@@ -217,7 +227,7 @@ template <int N, class F> __device__ __forceinline__ float3 filter(const Taps& t
 }
 
 template <int INTERP, int MC>
-__global__ void __launch_bounds__(NT, 4)
+__global__ void __launch_bounds__(NT, TAA_FAST_MIN_BLOCKS)
     resolve_fast32(const Args a, const __grid_constant__ CUtensorMap hmap, const int tma_ok) {
     using RawVel = typename std::conditional<MC == 4, uint2, uint32_t>::type;
     constexpr int SPAN = INTERP == 2 ? 4 : 2;
@@ -245,9 +255,14 @@ __global__ void __launch_bounds__(NT, 4)
             st[j] = __ldg(at<uint2>(a.color, a.color_pitch, clampi(x0 - 1 + sx, 0, W - 1), clampi(y0 - 1 + sy, 0, H - 1)));
         }
     }
-    // 2. history positions (uv - velocity), the previous depth under them
-    const float u = ((float)cx + 0.5f) * a.inv_w;
-    const float v0 = ((float)cy0 + 0.5f) * a.inv_h, v1 = ((float)cy1 + 0.5f) * a.inv_h;
+    // the first window wait's poll limit, loaded with the inputs
+    const uint32_t polls = first_wait_polls(a.status);
+    // 2. history positions (uv - velocity; uv = (texel + 0.5) / size correctly
+    //    rounded: a sampling position one ulp off moves a 4K Catmull-Rom tap by
+    //    1e-4 texel), the previous depth under them
+    const float u = div_const_rn((float)cx + 0.5f, (float)W, a.inv_w);
+    const float v0 = div_const_rn((float)cy0 + 0.5f, (float)H, a.inv_h);
+    const float v1 = div_const_rn((float)cy1 + 0.5f, (float)H, a.inv_h);
     const float4 vel0 = tiled::velocity_of<MC>(v0raw), vel1 = tiled::velocity_of<MC>(v1raw);
     const float hu0 = u - vel0.x, hv0 = v0 - vel0.y, hu1 = u - vel1.x, hv1 = v1 - vel1.y;
     float pd0 = 0.f, pd1 = 0.f;
@@ -298,6 +313,12 @@ __global__ void __launch_bounds__(NT, 4)
         }
         cp_async_commit();
     }
+    // 5. the two boxes while the window is in flight: rows 2ly .. 2ly+3 of the
+    //    staged tile, columns lx .. lx+2; rows 1 and 2 are shared
+    const float4* sp = &sm.col[(2 * ly) * SX + lx];
+    const Row mid = add(row_sums(sp + SX), row_sums(sp + 2 * SX));
+    const Box b0 = box_of(add(row_sums(sp), mid), a.gamma);
+    const Box b1 = box_of(add(mid, row_sums(sp + 3 * SX)), a.gamma);
     // rejection (taa.comp:787-823): out of the screen, or the previous depth
     // under the history position too far from the expected one
     bool rej[2];
@@ -308,16 +329,10 @@ __global__ void __launch_bounds__(NT, 4)
         rej[k] = (a.reject_outside && (hu < 0.f || hv < 0.f || hu >= 1.f || hv >= 1.f)) ||
                  (a.depth_cull && fabsf(pd - ehd) > 0.1f * (1.0f - pd));
     }
-    // 5. the two boxes while the window is in flight: rows 2ly .. 2ly+3 of the
-    //    staged tile, columns lx .. lx+2; rows 1 and 2 are shared
-    const float4* sp = &sm.col[(2 * ly) * SX + lx];
-    const Row mid = add(row_sums(sp + SX), row_sums(sp + 2 * SX));
-    const Box b0 = box_of(add(row_sums(sp), mid), a.gamma);
-    const Box b1 = box_of(add(mid, row_sums(sp + 3 * SX)), a.gamma);
 
     bool landed = true;
     if (mode == 1) {
-        landed = mbar_wait_bounded(&sm.bar, 0u, first_wait_polls(a.status));
+        landed = mbar_wait_bounded(&sm.bar, 0u, polls);
         if (!landed) {
             atomicOr(a.status, kStatusWindowTimeout);
             mbar_wait_bounded(&sm.bar, 0u);  // the copy may still land in this CTA's memory
@@ -326,29 +341,73 @@ __global__ void __launch_bounds__(NT, 4)
         cp_async_wait_all();
         __syncthreads();
     }
-    // 6. per pixel: rejection, history sample, clip, blend, stores
+    // 6. the history samples of both pixels.  When their footprints are one
+    //    row apart (the same first column, as for coherent motion) the five
+    //    window rows they cover are read once for both (20 taps instead of 32).
+    float3 h[2] = {make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
+    if (have_hist && landed) {
+        const Taps t0 = taps_of<INTERP>(hu0, hv0, a), t1 = taps_of<INTERP>(hu1, hv1, a);
+        const int bx0 = t0.ux - wx0, by0 = t0.uy - wy0, bx1 = t1.ux - wx0, by1 = t1.uy - wy0;
+        const bool in0 = (unsigned)bx0 <= (unsigned)(WW - SPAN) && (unsigned)by0 <= (unsigned)(WH - SPAN);
+        const bool in1 = (unsigned)bx1 <= (unsigned)(WW - SPAN) && (unsigned)by1 <= (unsigned)(WH - SPAN);
+        if (TAA_FAST_SHARED_TAPS && in0 && in1 && bx1 == bx0 && by1 == by0 + 1) {
+            const float4* wp = &sm.win[by0 * WW + bx0];
+            f2 acc0 = dup(0.f), acc1 = dup(0.f);
+            float accb0 = 0.f, accb1 = 0.f;
+#pragma unroll
+            for (int j = 0; j <= SPAN; ++j) {
+                f2 r0 = dup(0.f), r1 = dup(0.f);
+                float rb0 = 0.f, rb1 = 0.f;
+#pragma unroll
+                for (int i = 0; i < SPAN; ++i) {
+                    const float4 tx = wp[j * WW + i];
+                    const f2 xy = pk(tx.x, tx.y);
+                    if (j < SPAN) {
+                        r0 = fmap(dup(f2lo(t0.w[i])), xy, r0);
+                        rb0 = fmaf(f2lo(t0.w[i]), tx.z, rb0);
+                    }
+                    if (j > 0) {
+                        r1 = fmap(dup(f2lo(t1.w[i])), xy, r1);
+                        rb1 = fmaf(f2lo(t1.w[i]), tx.z, rb1);
+                    }
+                }
+                if (j < SPAN) {
+                    acc0 = fmap(dup(f2hi(t0.w[j])), r0, acc0);
+                    accb0 = fmaf(f2hi(t0.w[j]), rb0, accb0);
+                }
+                if (j > 0) {
+                    acc1 = fmap(dup(f2hi(t1.w[j - 1])), r1, acc1);
+                    accb1 = fmaf(f2hi(t1.w[j - 1]), rb1, accb1);
+                }
+            }
+            h[0] = make_float3(f2lo(acc0), f2hi(acc0), accb0);
+            h[1] = make_float3(f2lo(acc1), f2hi(acc1), accb1);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const Taps& t = k ? t1 : t0;
+                const int bx = k ? bx1 : bx0, by = k ? by1 : by0;
+                if (k ? in1 : in0) {
+                    const float4* wp = &sm.win[by * WW + bx];
+                    h[k] = filter<SPAN>(t, [&](int i, int j) { return wp[j * WW + i]; });
+                } else {
+                    h[k] = filter<SPAN>(t, [&](int i, int j) {
+                        return __ldg(at<float4>(a.hist, a.hist_pitch, clampi(t.ux + i, 0, W - 1),
+                                                clampi(t.uy + j, 0, H - 1)));
+                    });
+                }
+            }
+        }
+    }
+    // 7. per pixel: clip, blend, stores
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
         const int y = ya + k;
         if (!(x < W && y < H && landed)) continue;
         const Box& b = k ? b1 : b0;
-        const float hu = k ? hu1 : hu0, hv = k ? hv1 : hv0;
-        const bool rejected = rej[k];
-        float3 h = make_float3(0.f, 0.f, 0.f);
-        if (have_hist) {
-            const Taps t = taps_of<INTERP>(hu, hv, a);
-            const int bx = t.ux - wx0, by = t.uy - wy0;
-            if ((unsigned)bx <= (unsigned)(WW - SPAN) && (unsigned)by <= (unsigned)(WH - SPAN)) {
-                const float4* wp = &sm.win[by * WW + bx];
-                h = filter<SPAN>(t, [&](int i, int j) { return wp[j * WW + i]; });
-            } else {
-                h = filter<SPAN>(t, [&](int i, int j) {
-                    return __ldg(at<float4>(a.hist, a.hist_pitch, clampi(t.ux + i, 0, W - 1), clampi(t.uy + j, 0, H - 1)));
-                });
-            }
-        }
         // history to YCoCg, clip toward the box centre (taa.comp:323-345)
-        float hc[3] = {0.25f * (h.x + h.z) + 0.5f * h.y, 0.5f * (h.x - h.z), 0.5f * h.y - 0.25f * (h.x + h.z)};
+        const float3 hk = h[k];
+        float hc[3] = {0.25f * (hk.x + hk.z) + 0.5f * hk.y, 0.5f * (hk.x - hk.z), 0.5f * hk.y - 0.25f * (hk.x + hk.z)};
         float dd[3], ma = 0.f;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
@@ -357,7 +416,7 @@ __global__ void __launch_bounds__(NT, 4)
         }
         const float s = ma > 1.0f ? rcp_approx(ma) : 1.0f;
         // blend (taa.comp:848-900): mix(history, current, alpha)
-        const float alpha = a.reset ? 1.0f : (rejected ? a.rejection_alpha : a.alpha);
+        const float alpha = a.reset ? 1.0f : (rej[k] ? a.rejection_alpha : a.alpha);
         const float4 c0 = sm.col[(2 * ly + k + 1) * SX + lx + 1];
         const float cur[3] = {c0.x, c0.y, c0.z};
         float o[3];
