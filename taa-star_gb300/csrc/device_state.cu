@@ -119,6 +119,18 @@ bool encode_history_map(const Img& h, int history_fmt, int box_w, int box_h, CUt
         r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<char*>(h.p), dim, stride, box, elem,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    } else if (history_fmt == 2) {
+        // RGBA32F as (float, y): a box row of box_w texels is one contiguous
+        // run of 16 * box_w bytes (the x coordinate, 4 floats per texel, is
+        // always a 16-byte multiple), fetched as a few wide requests instead
+        // of one 16-byte request per texel
+        if (4 * box_w > 256) return false;
+        const cuuint64_t dim[2] = {4 * (cuuint64_t)h.w, (cuuint64_t)h.h};
+        const cuuint64_t stride[1] = {(cuuint64_t)h.pitch};
+        const cuuint32_t box[2] = {(cuuint32_t)(4 * box_w), (cuuint32_t)box_h};
+        r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<char*>(h.p), dim, stride, box, elem,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     } else {
         // RGBA16F as (half, y): a box row of box_w texels is 8 * box_w bytes,
         // and the x coordinate (4 halves per texel) must be a multiple of 8

@@ -87,6 +87,8 @@ cudaError_t current_context_id(unsigned long long* id);
 
 // Tensor map of a history image for box_w x box_h texel window copies;
 // false when the image cannot be a TMA source (alignment, driver entry point).
+// history_fmt 0: RGBA32F as (channel, x, y); 1: RGBA16F as (half, y);
+// 2: RGBA32F as (float, y), rows of the box copied as contiguous runs.
 bool encode_history_map(const Img& history, int history_fmt, int box_w, int box_h, CUtensorMap* map);
 
 // The batched persistent resolve (batch_tiled.cu).

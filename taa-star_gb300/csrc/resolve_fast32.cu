@@ -50,7 +50,12 @@ using tiled::tma_load_3d;
 
 // Resident CTAs per SM the register budget is sized for (a tuning constant).
 #ifndef TAA_FAST_MIN_BLOCKS
-#define TAA_FAST_MIN_BLOCKS 4
+#define TAA_FAST_MIN_BLOCKS 5
+#endif
+// Whether the history window's TMA copy treats a row as one run of floats
+// (2-D tensor map) rather than one 16-byte texel per request (3-D map).
+#ifndef TAA_FAST_TMA2D
+#define TAA_FAST_TMA2D 1
 #endif
 // Whether a thread's two pixels read their Catmull-Rom rows once when their
 // footprints are one row apart (a tuning switch).
@@ -287,7 +292,8 @@ __global__ void __launch_bounds__(NT, TAA_FAST_MIN_BLOCKS)
         if (mode == 1) {
             mbar_init(&sm.bar, 1);
             mbar_expect_tx(&sm.bar, (uint32_t)(sizeof(float4) * WW * WH));
-            tma_load_3d(sm.win, &hmap, 0, wx0, wy0, &sm.bar);
+            if (TAA_FAST_TMA2D) tiled::tma_load_2d(sm.win, &hmap, 4 * wx0, wy0, &sm.bar);
+            else tma_load_3d(sm.win, &hmap, 0, wx0, wy0, &sm.bar);
         }
     }
     // 4. staged colour
@@ -472,7 +478,7 @@ cudaError_t launch_resolve_fast32(int motion_ch, const taa_uniforms_t& U, const 
     CUtensorMap map;
     std::memset(&map, 0, sizeof map);
     const int tma_ok = a.hist && f.history.w >= WW && f.history.h >= WH &&
-                       encode_history_map(f.history, 0, WW, WH, &map);
+                       encode_history_map(f.history, TAA_FAST_TMA2D ? 2 : 0, WW, WH, &map);
     const dim3 grid((a.W + TX - 1) / TX, (a.H + TY - 1) / TY);
     if (P.mInterpolationMode == 2) {
         if (motion_ch == 4) resolve_fast32<2, 4><<<grid, NT, 0, s>>>(a, map, tma_ok);

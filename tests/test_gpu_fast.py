@@ -78,7 +78,14 @@ def test_fast_form_against_the_exact_form(cuda, size, mode):
         ctx.close()
     f, t = outs[T.TAA_FORM_FAST], outs[T.TAA_FORM_TILED]
     assert np.all(np.isfinite(f["history_out"]))
-    assert rel_l2(f["history_out"][..., :3], t["history_out"][..., :3]) <= FAST_RELL2
+    # on frames of a few dozen pixels one pixel whose clip is ill-conditioned
+    # (a near-degenerate box channel, taa.comp:335-340) decides the frame norm:
+    # there the fast form must be as close to the FP64 oracle as the exact form
+    r64 = O.resolve(u, fr[1]["color"].astype(np.float32), fr[1]["depth"], fr[1]["motion"].astype(np.float32),
+                    history=hist, history_depth=fr[0]["depth"], precision=64)["history"][..., :3]
+    e_fast, e_exact = rel_l2(f["history_out"][..., :3], r64), rel_l2(t["history_out"][..., :3], r64)
+    assert e_fast <= max(FAST_RELL2, 3.0 * e_exact), (e_fast, e_exact)
+    assert rel_l2(f["history_out"][..., :3], t["history_out"][..., :3]) <= 1e-3
     assert rel_l2(f["result"][..., :3], t["result"][..., :3]) <= 1e-3  # after the RGBA16F store
     assert np.all(f["result"][..., 3] == 1.0)
     assert T.device_status(clear=True) == 0
