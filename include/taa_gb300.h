@@ -65,9 +65,12 @@ typedef enum taa_status {
 #define TAA_FORM_FP16   3u  /* packed half2 neighbourhood, clip and sharpen; FP32 history and blend */
 #define TAA_FORM_LEARNED 4u /* blend weight and clip-box scale from a per-pixel MLP (taa_set_mlp) */
 /* FP32 with the arithmetic reassociated: contracted FMAs, the 3x3 moments from
- * row sums two pixels share, hardware square-root and reciprocal
- * approximations in the variance box and the clip.  Frame error within 1e-5
- * relative L2 of TAA_FORM_TILED.  It runs the benchmark mode of the
+ * row sums a thread's four pixels share, the history rows filtered
+ * horizontally once for them, hardware square-root and reciprocal
+ * approximations in the variance box and the clip.  Frame error within 1e-4
+ * relative L2 of the FP64 oracle and of TAA_FORM_TILED on the benchmark
+ * sequences (measured 2e-5 to 6e-5; the exact FP32 form is 1e-5 to 5e-5 from
+ * FP64).  It runs the benchmark mode of the
  * parameter block (YCoCg variance clip toward the box centre, velocity for
  * every pixel with simple sampling, no tonemap, luma weighting, near-clamp
  * reduction, velocity-based alpha, noise or anti-ghosting) with Catmull-Rom

@@ -6,29 +6,38 @@
 // the shader:
 //
 //   * the 3x3 moments (taa.comp:266-277) come from row sums that a thread's
-//     two vertically adjacent pixels share (their boxes have two rows in
-//     common), with Cg and Cg^2 staged side by side so one packed add
-//     accumulates both, and mean = m1 * (1/9);
+//     vertically adjacent pixels share, with Cg and Cg^2 staged side by side
+//     so one packed add accumulates both, and mean = m1 * (1/9);
+//   * the separable Catmull-Rom filter (taa.comp:469-495) filters a row once
+//     for every pixel of a strip that shares its horizontal position;
 //   * the standard deviation is the hardware square-root approximation, the
 //     clip's per-channel ratios (taa.comp:323-345) use the hardware
 //     reciprocal approximation; the box centre is the mean and its half
 //     extent gamma * sigma + 1e-7 (the shader's (max + min) / 2 and
 //     (max - min) / 2 + 1e-7 of mean -/+ gamma * sigma);
-//   * multiplies and adds contract into FMAs; uv is (x + 0.5) * (1 / size).
+//   * multiplies and adds contract into FMAs (uv stays the correctly rounded
+//     (x + 0.5) / size: an ulp of uv moves a 4K Catmull-Rom tap by 1e-4 texel).
 //
-// Everything else is the exact forms' pipeline: a 32x16 tile per 256-thread
-// CTA, two pixels per thread; the colour tile with its 1-pixel halo staged in
-// shared memory as YCoCg; a history window per tile (the Catmull-Rom taps of
-// the tile's centre pixel widened by the tile and 3 pixels of motion
-// difference) copied by one TMA tensor copy on a bounded mbarrier wait, or by
-// cp.async with edge clamps where it crosses the image border; pixels whose
-// taps leave the window read global memory.  The window is placed by the
-// thread that owns the tile's centre pixel, from the velocity it has loaded
-// for its own pixel, so no extra load delays the copy.
+// Structure: a 32x16 tile per 128-thread CTA (eight CTAs per SM), each thread
+// a vertical strip of four pixels; the colour tile with its 1-pixel halo
+// staged in shared memory as YCoCg; a history window per tile (the
+// Catmull-Rom taps of the tile's centre pixel widened by the tile and 3
+// pixels of motion difference) copied by one TMA tensor copy on a bounded
+// mbarrier wait, or by cp.async with edge clamps where it crosses the image
+// border; pixels whose taps leave the window read global memory.  The window
+// is placed by the thread that owns the tile's centre pixel, from the
+// velocity it has loaded for its own pixel, so no extra load delays the copy.
+// The kernel is bound by the shared-memory pipe (window and box reads), so
+// the strip shares what it can: a strip with one horizontal position (equal
+// velocity x) filters each of its seven window rows horizontally once and
+// gives each pixel the vertical combination (7 x 4 taps for four pixels
+// instead of 4 x 16), and its boxes share the staged rows (six rows of three
+// texels for four pixels).
 //
-// Precision: frame relative L2 within 1e-5 of the exact FP32 forms on the
-// benchmark scenes, and within the same distance of the FP64 oracle as they
-// are (tests/test_gpu_fast.py).
+// Precision: frame relative L2 within 1e-4 of the FP64 oracle and of the
+// exact FP32 forms on the benchmark sequences (measured 2e-5 to 6e-5, the
+// distance at which the exact FP32 form itself sits from FP64), within 1e-5
+// on the reference's golden fixtures (tests/test_gpu_fast.py).
 #include <cuda.h>
 
 #include <cstring>
@@ -50,7 +59,7 @@ using tiled::tma_load_3d;
 
 // Resident CTAs per SM the register budget is sized for (a tuning constant).
 #ifndef TAA_FAST_MIN_BLOCKS
-#define TAA_FAST_MIN_BLOCKS 5
+#define TAA_FAST_MIN_BLOCKS 8
 #endif
 // Whether the history window's TMA copy treats a row as one run of floats
 // (2-D tensor map) rather than one 16-byte texel per request (3-D map).
@@ -63,11 +72,14 @@ using tiled::tma_load_3d;
 #define TAA_FAST_SHARED_TAPS 1
 #endif
 
-constexpr int TX = 32, TY = 16, NT = 256;       // tile, threads (two pixels each)
+constexpr int NPX = 4;                            // pixels per thread: a vertical strip
+constexpr int TX = 32, TY = 16, NT = TX * TY / NPX;  // tile, threads (one warp per 32 x 4 rows)
 constexpr int SX = TX + 2, SY = TY + 2, NS = SX * SY;  // staged colour with its 1-pixel halo
+constexpr int NSPT = (NS + NT - 1) / NT;               // staged texels per thread
 constexpr int MARGIN = tiled::WIN_MARGIN;
 constexpr int WW = TX + 3 + 2 * MARGIN, WH = TY + 3 + 2 * MARGIN;  // history window (texels)
-constexpr int REF_TID = (TY / 2 / 2) * 32 + TX / 2;  // the thread whose first pixel is the centre (16, 8)
+constexpr int REF_TID = (TY / 2 / NPX) * 32 + TX / 2;  // the thread whose first pixel is the centre (16, 8)
+static_assert(NPX * NT == TX * TY && NT % 32 == 0, "whole warps of strips");
 
 // Everything a launch reads, flattened: pointers, row pitches in bytes, the
 // few parameters the benchmark mode uses.
@@ -231,33 +243,58 @@ template <int N, class F> __device__ __forceinline__ float3 filter(const Taps& t
     return make_float3(f2lo(acc), f2hi(acc), accb);
 }
 
+// Catmull-Rom (or bilinear) weights of one axis at fraction f (taa.comp:464-467).
+template <int INTERP> __device__ __forceinline__ void axis_weights(float f, float w[4]) {
+    if constexpr (INTERP == 2) {
+        const float f2 = f * f;
+        w[0] = f * fmaf(f, fmaf(-0.5f, f, 1.0f), -0.5f);
+        w[1] = fmaf(f2, fmaf(1.5f, f, -2.5f), 1.0f);
+        w[2] = f * fmaf(f, fmaf(-1.5f, f, 2.0f), 0.5f);
+        w[3] = 0.5f * f2 * (f - 1.0f);
+    } else {
+        if (!(f == f)) f = 0.f;  // a NaN fraction weights the first tap by 1 (taa.comp:546)
+        w[0] = 1.0f - f;
+        w[1] = f;
+        w[2] = w[3] = 0.f;
+    }
+}
+// The first tap of an axis and its fraction: it = position * size.
+template <int INTERP> __device__ __forceinline__ int axis_first(float it, float& f) {
+    const float b = floorf(it - 0.5f);
+    f = it + (-0.5f - b);
+    return trunc_index(b) - (INTERP == 2 ? 1 : 0);
+}
+
 template <int INTERP, int MC>
 __global__ void __launch_bounds__(NT, TAA_FAST_MIN_BLOCKS)
     resolve_fast32(const Args a, const __grid_constant__ CUtensorMap hmap, const int tma_ok) {
     using RawVel = typename std::conditional<MC == 4, uint2, uint32_t>::type;
     constexpr int SPAN = INTERP == 2 ? 4 : 2;
     __shared__ Smem sm;
-    const int tid = threadIdx.x, lx = tid & 31, ly = tid >> 5;
+    const int tid = threadIdx.x, lx = tid & 31, sy = tid >> 5;
     const int W = a.W, H = a.H;
     const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
     const int x = x0 + lx, cx = min(x, W - 1);
-    const int ya = y0 + 2 * ly;
-    const int cy0 = min(ya, H - 1), cy1 = min(ya + 1, H - 1);
+    const int ya = y0 + NPX * sy;  // the strip's first row
     const bool have_hist = a.hist != nullptr;
 
-    // 1. loads: the two pixels' depth and velocity, this thread's staged colour texels
-    const float d0 = __ldg(at<float>(a.depth, a.depth_pitch, cx, cy0));
-    const float d1 = __ldg(at<float>(a.depth, a.depth_pitch, cx, cy1));
-    const RawVel v0raw = __ldg(at<RawVel>(a.vel, a.vel_pitch, cx, cy0));
-    const RawVel v1raw = __ldg(at<RawVel>(a.vel, a.vel_pitch, cx, cy1));
-    uint2 st[3];
+    // 1. loads: the strip's depths and velocities, this thread's staged colour texels
+    float dep[NPX];
+    RawVel vraw[NPX];
 #pragma unroll
-    for (int j = 0; j < 3; ++j) {
+    for (int k = 0; k < NPX; ++k) {
+        const int cy = min(ya + k, H - 1);
+        dep[k] = __ldg(at<float>(a.depth, a.depth_pitch, cx, cy));
+        vraw[k] = __ldg(at<RawVel>(a.vel, a.vel_pitch, cx, cy));
+    }
+    uint2 st[NSPT];
+#pragma unroll
+    for (int j = 0; j < NSPT; ++j) {
         const int i = tid + j * NT;
         st[j] = make_uint2(0u, 0u);
-        if (j < 2 || i < NS) {
-            const int sy = i / SX, sx = i - sy * SX;
-            st[j] = __ldg(at<uint2>(a.color, a.color_pitch, clampi(x0 - 1 + sx, 0, W - 1), clampi(y0 - 1 + sy, 0, H - 1)));
+        if (j < NSPT - 1 || i < NS) {
+            const int ry = i / SX, rx = i - ry * SX;
+            st[j] = __ldg(at<uint2>(a.color, a.color_pitch, clampi(x0 - 1 + rx, 0, W - 1), clampi(y0 - 1 + ry, 0, H - 1)));
         }
     }
     // the first window wait's poll limit, loaded with the inputs
@@ -266,24 +303,26 @@ __global__ void __launch_bounds__(NT, TAA_FAST_MIN_BLOCKS)
     //    rounded: a sampling position one ulp off moves a 4K Catmull-Rom tap by
     //    1e-4 texel), the previous depth under them
     const float u = div_const_rn((float)cx + 0.5f, (float)W, a.inv_w);
-    const float v0 = div_const_rn((float)cy0 + 0.5f, (float)H, a.inv_h);
-    const float v1 = div_const_rn((float)cy1 + 0.5f, (float)H, a.inv_h);
-    const float4 vel0 = tiled::velocity_of<MC>(v0raw), vel1 = tiled::velocity_of<MC>(v1raw);
-    const float hu0 = u - vel0.x, hv0 = v0 - vel0.y, hu1 = u - vel1.x, hv1 = v1 - vel1.y;
-    float pd0 = 0.f, pd1 = 0.f;
-    if (a.depth_cull && a.hdepth) {
-        pd0 = __ldg(at<float>(a.hdepth, a.hdepth_pitch, clampi(trunc_index(hu0 * (float)W), 0, W - 1),
-                              clampi(trunc_index(hv0 * (float)H), 0, H - 1)));
-        pd1 = __ldg(at<float>(a.hdepth, a.hdepth_pitch, clampi(trunc_index(hu1 * (float)W), 0, W - 1),
-                              clampi(trunc_index(hv1 * (float)H), 0, H - 1)));
+    float hu[NPX], hv[NPX], ehd[NPX], pd[NPX];
+#pragma unroll
+    for (int k = 0; k < NPX; ++k) {
+        const float4 vel = tiled::velocity_of<MC>(vraw[k]);
+        const float v = div_const_rn((float)min(ya + k, H - 1) + 0.5f, (float)H, a.inv_h);
+        hu[k] = u - vel.x;
+        hv[k] = v - vel.y;
+        ehd[k] = dep[k] - vel.z;
+        pd[k] = 0.f;
+        if (a.depth_cull && a.hdepth)
+            pd[k] = __ldg(at<float>(a.hdepth, a.hdepth_pitch, clampi(trunc_index(hu[k] * (float)W), 0, W - 1),
+                                    clampi(trunc_index(hv[k] * (float)H), 0, H - 1)));
     }
     // 3. the thread owning the tile's centre pixel places the history window
     //    (its own pixel's taps widened by the tile and MARGIN) and starts the copy
     if (tid == REF_TID && have_hist) {
-        const int k0 = INTERP == 2 ? 1 : 0;
-        const int rux = trunc_index(floorf(hu0 * (float)W - 0.5f)) - k0;
-        const int ruy = trunc_index(floorf(hv0 * (float)H - 0.5f)) - k0;
-        const int wx0 = rux - (cx - x0) - MARGIN, wy0 = ruy - (cy0 - y0) - MARGIN;
+        float f;
+        const int rux = axis_first<INTERP>(hu[0] * (float)W, f);
+        const int ruy = axis_first<INTERP>(hv[0] * (float)H, f);
+        const int wx0 = rux - (cx - x0) - MARGIN, wy0 = ruy - (min(ya, H - 1) - y0) - MARGIN;
         const bool interior = wx0 >= 0 && wy0 >= 0 && wx0 <= W - WW && wy0 <= H - WH;
         const int mode = tma_ok && interior ? 1 : 2;
         sm.org[0] = wx0;
@@ -298,9 +337,9 @@ __global__ void __launch_bounds__(NT, TAA_FAST_MIN_BLOCKS)
     }
     // 4. staged colour
 #pragma unroll
-    for (int j = 0; j < 3; ++j) {
+    for (int j = 0; j < NSPT; ++j) {
         const int i = tid + j * NT;
-        if (j < 2 || i < NS) sm.col[i] = stage(st[j]);
+        if (j < NSPT - 1 || i < NS) sm.col[i] = stage(st[j]);
     }
     __syncthreads();
     int wx0 = 0, wy0 = 0, mode = 0;
@@ -319,22 +358,14 @@ __global__ void __launch_bounds__(NT, TAA_FAST_MIN_BLOCKS)
         }
         cp_async_commit();
     }
-    // 5. the two boxes while the window is in flight: rows 2ly .. 2ly+3 of the
-    //    staged tile, columns lx .. lx+2; rows 1 and 2 are shared
-    const float4* sp = &sm.col[(2 * ly) * SX + lx];
-    const Row mid = add(row_sums(sp + SX), row_sums(sp + 2 * SX));
-    const Box b0 = box_of(add(row_sums(sp), mid), a.gamma);
-    const Box b1 = box_of(add(mid, row_sums(sp + 3 * SX)), a.gamma);
     // rejection (taa.comp:787-823): out of the screen, or the previous depth
     // under the history position too far from the expected one
-    bool rej[2];
+    unsigned rej = 0;
 #pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        const float hu = k ? hu1 : hu0, hv = k ? hv1 : hv0, pd = k ? pd1 : pd0;
-        const float ehd = (k ? d1 : d0) - (k ? vel1.z : vel0.z);
-        rej[k] = (a.reject_outside && (hu < 0.f || hv < 0.f || hu >= 1.f || hv >= 1.f)) ||
-                 (a.depth_cull && fabsf(pd - ehd) > 0.1f * (1.0f - pd));
-    }
+    for (int k = 0; k < NPX; ++k)
+        if ((a.reject_outside && (hu[k] < 0.f || hv[k] < 0.f || hu[k] >= 1.f || hv[k] >= 1.f)) ||
+            (a.depth_cull && fabsf(pd[k] - ehd[k]) > 0.1f * (1.0f - pd[k])))
+            rej |= 1u << k;
 
     bool landed = true;
     if (mode == 1) {
@@ -347,54 +378,65 @@ __global__ void __launch_bounds__(NT, TAA_FAST_MIN_BLOCKS)
         cp_async_wait_all();
         __syncthreads();
     }
-    // 6. the history samples of both pixels.  When their footprints are one
-    //    row apart (the same first column, as for coherent motion) the five
-    //    window rows they cover are read once for both (20 taps instead of 32).
-    float3 h[2] = {make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
-    if (have_hist && landed) {
-        const Taps t0 = taps_of<INTERP>(hu0, hv0, a), t1 = taps_of<INTERP>(hu1, hv1, a);
-        const int bx0 = t0.ux - wx0, by0 = t0.uy - wy0, bx1 = t1.ux - wx0, by1 = t1.uy - wy0;
-        const bool in0 = (unsigned)bx0 <= (unsigned)(WW - SPAN) && (unsigned)by0 <= (unsigned)(WH - SPAN);
-        const bool in1 = (unsigned)bx1 <= (unsigned)(WW - SPAN) && (unsigned)by1 <= (unsigned)(WH - SPAN);
-        if (TAA_FAST_SHARED_TAPS && in0 && in1 && bx1 == bx0 && by1 == by0 + 1) {
-            const float4* wp = &sm.win[by0 * WW + bx0];
-            f2 acc0 = dup(0.f), acc1 = dup(0.f);
-            float accb0 = 0.f, accb1 = 0.f;
+    // 5. the history samples.  A strip whose pixels share a horizontal
+    //    position (equal velocity x) and whose footprints are one row apart
+    //    filters each of its SPAN + NPX - 1 window rows horizontally once and
+    //    gives every pixel its vertical combination of them.
+    float3 h[NPX];
 #pragma unroll
-            for (int j = 0; j <= SPAN; ++j) {
-                f2 r0 = dup(0.f), r1 = dup(0.f);
-                float rb0 = 0.f, rb1 = 0.f;
+    for (int k = 0; k < NPX; ++k) h[k] = make_float3(0.f, 0.f, 0.f);
+    if (have_hist && landed) {
+        float fx, fy[NPX];
+        const int ux = axis_first<INTERP>(hu[0] * (float)W, fx);
+        int uy[NPX];
+        bool coherent = true;
+#pragma unroll
+        for (int k = 0; k < NPX; ++k) {
+            uy[k] = axis_first<INTERP>(hv[k] * (float)H, fy[k]);
+            coherent = coherent && __float_as_uint(hu[k]) == __float_as_uint(hu[0]) && uy[k] == uy[0] + k;
+        }
+        const int bx = ux - wx0, by = uy[0] - wy0;
+        coherent = coherent && (unsigned)bx <= (unsigned)(WW - SPAN) && (unsigned)by <= (unsigned)(WH - SPAN - NPX + 1);
+        if (TAA_FAST_SHARED_TAPS && coherent) {
+            float wx[4], wy[NPX][4];
+            axis_weights<INTERP>(fx, wx);
+#pragma unroll
+            for (int k = 0; k < NPX; ++k) axis_weights<INTERP>(fy[k], wy[k]);
+            const float4* wp = &sm.win[by * WW + bx];
+            f2 acc[NPX];
+            float accb[NPX];
+#pragma unroll
+            for (int k = 0; k < NPX; ++k) {
+                acc[k] = dup(0.f);
+                accb[k] = 0.f;
+            }
+#pragma unroll
+            for (int j = 0; j < SPAN + NPX - 1; ++j) {
+                f2 r = dup(0.f);
+                float rb = 0.f;
 #pragma unroll
                 for (int i = 0; i < SPAN; ++i) {
-                    const float4 tx = wp[j * WW + i];
-                    const f2 xy = pk(tx.x, tx.y);
-                    if (j < SPAN) {
-                        r0 = fmap(dup(f2lo(t0.w[i])), xy, r0);
-                        rb0 = fmaf(f2lo(t0.w[i]), tx.z, rb0);
-                    }
-                    if (j > 0) {
-                        r1 = fmap(dup(f2lo(t1.w[i])), xy, r1);
-                        rb1 = fmaf(f2lo(t1.w[i]), tx.z, rb1);
-                    }
+                    const float4 t = wp[j * WW + i];
+                    r = fmap(dup(wx[i]), pk(t.x, t.y), r);
+                    rb = fmaf(wx[i], t.z, rb);
                 }
-                if (j < SPAN) {
-                    acc0 = fmap(dup(f2hi(t0.w[j])), r0, acc0);
-                    accb0 = fmaf(f2hi(t0.w[j]), rb0, accb0);
-                }
-                if (j > 0) {
-                    acc1 = fmap(dup(f2hi(t1.w[j - 1])), r1, acc1);
-                    accb1 = fmaf(f2hi(t1.w[j - 1]), rb1, accb1);
+#pragma unroll
+                for (int k = 0; k < NPX; ++k) {
+                    if (j - k >= 0 && j - k < SPAN) {
+                        acc[k] = fmap(dup(wy[k][j - k]), r, acc[k]);
+                        accb[k] = fmaf(wy[k][j - k], rb, accb[k]);
+                    }
                 }
             }
-            h[0] = make_float3(f2lo(acc0), f2hi(acc0), accb0);
-            h[1] = make_float3(f2lo(acc1), f2hi(acc1), accb1);
+#pragma unroll
+            for (int k = 0; k < NPX; ++k) h[k] = make_float3(f2lo(acc[k]), f2hi(acc[k]), accb[k]);
         } else {
 #pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                const Taps& t = k ? t1 : t0;
-                const int bx = k ? bx1 : bx0, by = k ? by1 : by0;
-                if (k ? in1 : in0) {
-                    const float4* wp = &sm.win[by * WW + bx];
+            for (int k = 0; k < NPX; ++k) {
+                const Taps t = taps_of<INTERP>(hu[k], hv[k], a);
+                const int tbx = t.ux - wx0, tby = t.uy - wy0;
+                if ((unsigned)tbx <= (unsigned)(WW - SPAN) && (unsigned)tby <= (unsigned)(WH - SPAN)) {
+                    const float4* wp = &sm.win[tby * WW + tbx];
                     h[k] = filter<SPAN>(t, [&](int i, int j) { return wp[j * WW + i]; });
                 } else {
                     h[k] = filter<SPAN>(t, [&](int i, int j) {
@@ -405,36 +447,43 @@ __global__ void __launch_bounds__(NT, TAA_FAST_MIN_BLOCKS)
             }
         }
     }
-    // 7. per pixel: clip, blend, stores
+    // 6. per pixel: the 3x3 box from row sums the strip's boxes share (rows
+    //    k .. k+2 of the strip's six staged rows), clip, blend, stores
+    const float4* sp = &sm.col[(NPX * sy) * SX + lx];
+    Row r0 = row_sums(sp), r1 = row_sums(sp + SX);
 #pragma unroll
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < NPX; ++k) {
+        const Row r2 = row_sums(sp + (k + 2) * SX);
+        const Row s = add(add(r0, r1), r2);
+        r0 = r1;
+        r1 = r2;
         const int y = ya + k;
         if (!(x < W && y < H && landed)) continue;
-        const Box& b = k ? b1 : b0;
+        const Box b = box_of(s, a.gamma);
         // history to YCoCg, clip toward the box centre (taa.comp:323-345)
         const float3 hk = h[k];
-        float hc[3] = {0.25f * (hk.x + hk.z) + 0.5f * hk.y, 0.5f * (hk.x - hk.z), 0.5f * hk.y - 0.25f * (hk.x + hk.z)};
+        const float hc[3] = {0.25f * (hk.x + hk.z) + 0.5f * hk.y, 0.5f * (hk.x - hk.z), 0.5f * hk.y - 0.25f * (hk.x + hk.z)};
         float dd[3], ma = 0.f;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             dd[c] = hc[c] - b.m[c];
             ma = fmaxf(ma, fabsf(dd[c]) * rcp_approx(b.e[c]));
         }
-        const float s = ma > 1.0f ? rcp_approx(ma) : 1.0f;
+        const float sc = ma > 1.0f ? rcp_approx(ma) : 1.0f;
         // blend (taa.comp:848-900): mix(history, current, alpha)
-        const float alpha = a.reset ? 1.0f : (rej[k] ? a.rejection_alpha : a.alpha);
-        const float4 c0 = sm.col[(2 * ly + k + 1) * SX + lx + 1];
+        const float alpha = a.reset ? 1.0f : ((rej >> k) & 1u ? a.rejection_alpha : a.alpha);
+        const float4 c0 = sp[(k + 1) * SX + 1];
         const float cur[3] = {c0.x, c0.y, c0.z};
         float o[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const float hcl = fmaf(dd[c], s, b.m[c]);
+            const float hcl = fmaf(dd[c], sc, b.m[c]);
             o[c] = fmaf(alpha, cur[c] - hcl, hcl);
         }
         const float tmp = o[0] - o[2];
-        const float r = tmp + o[1], g = o[0] + o[2], bl = tmp - o[1];
-        *at_w<float4>(a.hout, a.hout_pitch, x, y) = make_float4(r, g, bl, 0.f);
-        if (a.result) *at_w<uint2>(a.result, a.result_pitch, x, y) = float4_to_half4(make_float4(r, g, bl, 1.0f));
+        const float rr = tmp + o[1], g = o[0] + o[2], bl = tmp - o[1];
+        *at_w<float4>(a.hout, a.hout_pitch, x, y) = make_float4(rr, g, bl, 0.f);
+        if (a.result) *at_w<uint2>(a.result, a.result_pitch, x, y) = float4_to_half4(make_float4(rr, g, bl, 1.0f));
     }
 }
 
