@@ -139,6 +139,19 @@ __device__ __forceinline__ f2 fmap(f2 a, f2 b, f2 c) {
     return d;
 }
 
+// One 16-byte shared-memory load.  A float4 whose fourth lane is unused would
+// otherwise be read as an 8-byte and a 4-byte load; at the 16-byte stride of
+// consecutive texels each of those occupies the shared-memory pipe as long as
+// the whole 16 bytes do.
+__device__ __forceinline__ float4 lds128(const float4* p) {
+    float4 v;
+    // volatile: kept in program order with the barrier waits that publish the data
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+        : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+        : "r"(tiled::smem_addr(p)));
+    return v;
+}
+
 // RGBA16F texel -> (Y, Co, Cg, Cg^2) (taa.comp:158-164)
 __device__ __forceinline__ float4 stage(uint2 raw) {
     const float4 c = half4_to_float4(raw);
@@ -416,7 +429,7 @@ __global__ void __launch_bounds__(NT, TAA_FAST_MIN_BLOCKS)
                 float rb = 0.f;
 #pragma unroll
                 for (int i = 0; i < SPAN; ++i) {
-                    const float4 t = wp[j * WW + i];
+                    const float4 t = lds128(&wp[j * WW + i]);
                     r = fmap(dup(wx[i]), pk(t.x, t.y), r);
                     rb = fmaf(wx[i], t.z, rb);
                 }
@@ -437,7 +450,7 @@ __global__ void __launch_bounds__(NT, TAA_FAST_MIN_BLOCKS)
                 const int tbx = t.ux - wx0, tby = t.uy - wy0;
                 if ((unsigned)tbx <= (unsigned)(WW - SPAN) && (unsigned)tby <= (unsigned)(WH - SPAN)) {
                     const float4* wp = &sm.win[tby * WW + tbx];
-                    h[k] = filter<SPAN>(t, [&](int i, int j) { return wp[j * WW + i]; });
+                    h[k] = filter<SPAN>(t, [&](int i, int j) { return lds128(&wp[j * WW + i]); });
                 } else {
                     h[k] = filter<SPAN>(t, [&](int i, int j) {
                         return __ldg(at<float4>(a.hist, a.hist_pitch, clampi(t.ux + i, 0, W - 1),
@@ -472,7 +485,7 @@ __global__ void __launch_bounds__(NT, TAA_FAST_MIN_BLOCKS)
         const float sc = ma > 1.0f ? rcp_approx(ma) : 1.0f;
         // blend (taa.comp:848-900): mix(history, current, alpha)
         const float alpha = a.reset ? 1.0f : ((rej >> k) & 1u ? a.rejection_alpha : a.alpha);
-        const float4 c0 = sp[(k + 1) * SX + 1];
+        const float4 c0 = lds128(&sp[(k + 1) * SX + 1]);
         const float cur[3] = {c0.x, c0.y, c0.z};
         float o[3];
 #pragma unroll
