@@ -359,7 +359,9 @@ int taa_settings_read_ini(taa_settings_t* settings, const char* text, size_t len
  * clip towards the box centre, velocity for every pixel - or all not); each
  * view keeps RGBA32F history, has equal source and target sizes and no
  * sharpener, and is resolved with the same bits as its own taa_resolve in
- * TAA_FORM_TILED.  Per-view arguments (uniform block, bindings, history
+ * the form of the batch's tile body (taa_batch_tuning_t.form: TAA_FORM_TILED,
+ * or TAA_FORM_FAST for benchmark-mode views of a batch created with
+ * TAA_FORM_AUTO or TAA_FORM_FAST).  Per-view arguments (uniform block, bindings, history
  * tensor maps) live in TAA_BATCH_SLOTS device slots: taa_batch_prepare fills
  * a slot, taa_batch_launch resolves every view of a prepared slot with one
  * launch (a persistent grid of SM count x CTAs per SM taking tiles from a job
@@ -374,11 +376,16 @@ typedef struct taa_batch taa_batch;
 #define TAA_SCHEDULE_INTERLEAVED   2  /* one tile of each view in turn */
 #define TAA_BATCH_CTA_PER_TILE    -1  /* taa_batch_tuning_t.ctas_per_sm: a grid of one CTA per tile */
 typedef struct taa_batch_tuning_t {
-    int32_t tile_w, tile_h;  /* 32x8, 16x16, 32x16, 16x8 or 8x8 pixels */
+    int32_t tile_w, tile_h;  /* TAA_FORM_TILED: 32x8, 16x16, 32x16, 16x8 or 8x8 pixels;
+                                TAA_FORM_FAST: 32x16 (four-pixel strips) */
     int32_t schedule;        /* TAA_SCHEDULE_* */
     int32_t ctas_per_sm;     /* persistent grid = SM count x this; 0 = as many as fit;
                                 TAA_BATCH_CTA_PER_TILE = one CTA per tile instead */
     float   ms;              /* one launch, as measured by taa_batch_autotune (0 otherwise) */
+    int32_t form;            /* the tile body: TAA_FORM_TILED (0 reads as TILED; each view gets the bits of its
+                                own taa_resolve in TAA_FORM_TILED) or TAA_FORM_FAST (views in the benchmark mode
+                                of a batch created with TAA_FORM_AUTO or TAA_FORM_FAST; the bits of taa_resolve
+                                in TAA_FORM_FAST) */
 } taa_batch_tuning_t;
 
 /* Create a batch for n views; allocates its device slots and job list. */
@@ -392,8 +399,9 @@ int taa_batch_set_uniforms(taa_batch* batch, int32_t view, const taa_uniforms_t*
 int taa_batch_prepare(taa_batch* batch, void* stream, int32_t slot, const taa_frame_io_t* ios);
 /* Resolve every view of a prepared slot on `stream` (one launch). */
 int taa_batch_launch(taa_batch* batch, void* stream, int32_t slot);
-/* Time every tile shape and job order, each with a persistent grid and with
- * one CTA per tile, on a prepared slot (reps launches each,
+/* Time every tile shape (the exact tiles, and the fast strips where the
+ * batch's form and parameters allow them) and job order, each with a
+ * persistent grid and with one CTA per tile, on a prepared slot (reps launches each,
  * which rewrite the slot's outputs with the same values), keep the fastest
  * and return it.  Synchronises the stream. */
 int taa_batch_autotune(taa_batch* batch, void* stream, int32_t slot, int32_t reps, taa_batch_tuning_t* best);

@@ -33,10 +33,13 @@ struct SlotLayout {
     }
 };
 
-const int kShapeDims[taa_dev::kBatchShapes][2] = {{32, 8}, {16, 16}, {32, 16}, {16, 8}, {8, 8}};
+const int kShapeDims[taa_dev::kBatchShapes][2] = {{32, 8}, {16, 16}, {32, 16}, {16, 8}, {8, 8}, {32, 16}};
 
-int shape_id(int w, int h) {
-    for (int i = 0; i < taa_dev::kBatchShapes; ++i)
+// The shape id of a tuning: the exact tiles by size, or the fast strips.
+int shape_id(int w, int h, int form) {
+    if (form == TAA_FORM_FAST) return w == 32 && h == 16 ? taa_dev::kBatchFastShape : -1;
+    if (form != 0 && form != TAA_FORM_TILED) return -1;
+    for (int i = 0; i < taa_dev::kBatchFastShape; ++i)
         if (kShapeDims[i][0] == w && kShapeDims[i][1] == h) return i;
     return -1;
 }
@@ -58,7 +61,8 @@ struct taa_batch {
     uint32_t* d_jobs = nullptr;              // the active job list
     size_t jobs_cap = 0;
     int njobs = 0;
-    taa_batch_tuning_t tuning{32, 8, TAA_SCHEDULE_LARGEST_FIRST, 0, 0.f};
+    taa_batch_tuning_t tuning{32, 8, TAA_SCHEDULE_LARGEST_FIRST, 0, 0.f, TAA_FORM_TILED};
+    bool fast_ok = false;                    // created with TAA_FORM_AUTO / TAA_FORM_FAST: the strips may run
 };
 
 namespace {
@@ -124,10 +128,14 @@ int upload_jobs(taa_batch& b, const taa_batch_tuning_t& t, cudaStream_t s) {
     return TAA_OK;
 }
 
-int check_tuning(const taa_batch_tuning_t& t) {
-    if (shape_id(t.tile_w, t.tile_h) < 0)
-        return fail(TAA_E_INVAL, "taa_batch: tile shape %dx%d is not one of 32x8, 16x16, 32x16, 16x8, 8x8", t.tile_w,
-                    t.tile_h);
+int check_tuning(const taa_batch& b, const taa_batch_tuning_t& t) {
+    if (shape_id(t.tile_w, t.tile_h, t.form) < 0)
+        return fail(TAA_E_INVAL,
+                    "taa_batch: tile shape %dx%d (form %d) is not one of 32x8, 16x16, 32x16, 16x8, 8x8 (TILED) or "
+                    "32x16 (FAST)",
+                    t.tile_w, t.tile_h, t.form);
+    if (t.form == TAA_FORM_FAST && !b.fast_ok)
+        return fail(TAA_E_UNSUPPORTED, "taa_batch: the batch was created with TAA_FORM_TILED");
     if (t.schedule < TAA_SCHEDULE_VIEW_ORDER || t.schedule > TAA_SCHEDULE_INTERLEAVED)
         return fail(TAA_E_INVAL, "taa_batch: schedule %d", t.schedule);
     if (t.ctas_per_sm < TAA_BATCH_CTA_PER_TILE || t.ctas_per_sm > 32)
@@ -147,7 +155,9 @@ int grid_of(const taa_batch& b, const BatchKey& k, int ctas_per_sm, int* grid) {
 
 int launch_slot(taa_batch& b, cudaStream_t s, int slot, const taa_batch_tuning_t& t) {
     BatchKey k = b.slot_key[slot];
-    k.shape = shape_id(t.tile_w, t.tile_h);
+    k.shape = shape_id(t.tile_w, t.tile_h, t.form);
+    if (k.shape == taa_dev::kBatchFastShape && !k.hot)
+        return fail(TAA_E_UNSUPPORTED, "taa_batch_launch: the fast strips run the benchmark mode only");
     int grid = 0;
     int rc = grid_of(b, k, t.ctas_per_sm, &grid);
     if (rc) return rc;
@@ -180,8 +190,10 @@ int taa_batch_create(const taa_desc_t* descs, int32_t n, taa_batch** out) {
             return fail(TAA_E_UNSUPPORTED, "taa_batch_create: view %d: upsampling runs with taa_resolve", v);
         if (d.sharpener != TAA_SHARPEN_OFF)
             return fail(TAA_E_UNSUPPORTED, "taa_batch_create: view %d: sharpening runs with taa_resolve", v);
-        if (d.form != TAA_FORM_AUTO && d.form != TAA_FORM_TILED)
-            return fail(TAA_E_UNSUPPORTED, "taa_batch_create: view %d: batches run the tiled FP32 form", v);
+        if (d.form != TAA_FORM_AUTO && d.form != TAA_FORM_TILED && d.form != TAA_FORM_FAST)
+            return fail(TAA_E_UNSUPPORTED, "taa_batch_create: view %d: batches run the tiled or fast FP32 forms", v);
+        if (d.form == TAA_FORM_TILED && descs[0].form != TAA_FORM_TILED)
+            return fail(TAA_E_UNSUPPORTED, "taa_batch_create: view %d: all views or none ask for TAA_FORM_TILED", v);
         if (d.flags) return fail(TAA_E_UNSUPPORTED, "taa_batch_create: view %d: flags 0x%x", v, d.flags);
         if ((d.out_width + 7) / 8 > 4096 || (d.out_height + 7) / 8 > 4096)
             return fail(TAA_E_INVAL, "taa_batch_create: view %d too large for the job encoding", v);
@@ -193,6 +205,7 @@ int taa_batch_create(const taa_desc_t* descs, int32_t n, taa_batch** out) {
     b->uniforms.resize(n);
     b->have_uniforms.assign(n, 0);
     b->layout = SlotLayout(n);
+    b->fast_ok = descs[0].form != TAA_FORM_TILED;
     cudaError_t e = cudaGetDevice(&b->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_slots, b->layout.total * TAA_BATCH_SLOTS);
@@ -278,8 +291,10 @@ int taa_batch_prepare(taa_batch* b, void* stream, int32_t slot, const taa_frame_
             const taa_dev::Img& hi = hv[v].a.history;
             CUtensorMap& m = hm[(size_t)s * n + v];
             std::memset(&m, 0, sizeof m);
+            // the fast strips copy rows as runs of floats (2-D map), the exact tiles texel by texel (3-D)
+            const int fmt = s == taa_dev::kBatchFastShape ? 2 : 0;
             hok[(size_t)s * n + v] = key.interp != 1 && hi.p && hi.w >= info.win_w && hi.h >= info.win_h &&
-                                     taa_dev::encode_history_map(hi, 0, info.win_w, info.win_h, &m);
+                                     taa_dev::encode_history_map(hi, fmt, info.win_w, info.win_h, &m);
         }
     }
     cudaStream_t s = (cudaStream_t)stream;
@@ -306,7 +321,7 @@ int taa_batch_get_tuning(const taa_batch* b, taa_batch_tuning_t* out) {
 
 int taa_batch_set_tuning(taa_batch* b, const taa_batch_tuning_t* t) {
     if (!b || !t) return fail(TAA_E_INVAL, "taa_batch_set_tuning: NULL argument");
-    int rc = check_tuning(*t);
+    int rc = check_tuning(*b, *t);
     if (rc) return rc;
     rc = upload_jobs(*b, *t, nullptr);
     if (rc) return rc;
@@ -328,9 +343,12 @@ int taa_batch_autotune(taa_batch* b, void* stream, int32_t slot, int32_t reps, t
     win.ms = -1.f;
     int rc = TAA_OK;
     for (int sh = 0; sh < taa_dev::kBatchShapes && rc == TAA_OK; ++sh) {
+        const bool fast = sh == taa_dev::kBatchFastShape;
+        if (fast && !(b->fast_ok && b->slot_key[slot].hot)) continue;
         for (int cand = 0; cand < 6 && rc == TAA_OK; ++cand) {
             const int sched = cand % 3, grid_mode = cand < 3 ? 0 : TAA_BATCH_CTA_PER_TILE;
-            taa_batch_tuning_t t{kShapeDims[sh][0], kShapeDims[sh][1], sched, grid_mode, 0.f};
+            taa_batch_tuning_t t{kShapeDims[sh][0], kShapeDims[sh][1], sched, grid_mode, 0.f,
+                                 fast ? (int32_t)TAA_FORM_FAST : (int32_t)TAA_FORM_TILED};
             if ((rc = upload_jobs(*b, t, s))) break;
             if ((rc = launch_slot(*b, s, slot, t))) break;  // warm-up
             e = cudaEventRecord(t0, s);

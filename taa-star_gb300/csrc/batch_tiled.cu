@@ -1,7 +1,9 @@
 // batch_tiled.cu - the batched resolve: many views of any size in one
 // persistent launch of the tiled FP32 form (tiled_skeleton.cuh, resolve_batch),
 // for each tile shape the autotuner chooses from.  Compiled with -fmad=false,
-// so every view gets the same bits as its own taa_resolve.
+// so every view gets the same bits as its own taa_resolve in TAA_FORM_TILED.
+// Shape 5 dispatches to TAA_FORM_FAST's strip body (resolve_fast32.cu), whose
+// views get the bits of their own taa_resolve in TAA_FORM_FAST.
 #include "kernels.h"
 #include "policy_f32.cuh"
 
@@ -56,6 +58,14 @@ bool with_kernel(const BatchKey& k, F&& f) {
 bool hot_parameters(const taa_parameters_t& P) { return tiled::is_hot(P); }
 
 bool batch_shape_info(int shape, int history_fmt, BatchShapeInfo* out) {
+    if (shape == kBatchFastShape) {
+        if (history_fmt != 0) return false;
+        out->tile_w = 32;
+        out->tile_h = 16;
+        out->threads = 128;
+        fast32_window(&out->win_w, &out->win_h);
+        return true;
+    }
     BatchKey k{shape, history_fmt, 2, 2, 1};
     return with_kernel(k, [&](auto s, const void*) {
         using S = decltype(s);
@@ -68,6 +78,10 @@ bool batch_shape_info(int shape, int history_fmt, BatchShapeInfo* out) {
 }
 
 cudaError_t batch_occupancy(const BatchKey& k, int* ctas_per_sm) {
+    if (k.shape == kBatchFastShape) {
+        if (k.history_fmt != 0 || !k.hot) return cudaErrorInvalidValue;
+        return fast32_batch_occupancy(k.interp, k.motion_ch, ctas_per_sm);
+    }
     cudaError_t e = cudaErrorInvalidValue;
     with_kernel(k, [&](auto s, const void* fn) {
         using S = decltype(s);
@@ -78,6 +92,10 @@ cudaError_t batch_occupancy(const BatchKey& k, int* ctas_per_sm) {
 
 cudaError_t launch_batch(const BatchKey& k, const BatchView* views, const CUtensorMap* maps, const int* tma_ok,
                          const uint32_t* jobs, int njobs, int grid, cudaStream_t stream) {
+    if (k.shape == kBatchFastShape) {
+        if (k.history_fmt != 0 || !k.hot) return cudaErrorInvalidValue;
+        return launch_fast32_batch(k.interp, k.motion_ch, views, maps, tma_ok, jobs, njobs, grid, stream);
+    }
     cudaError_t e = cudaErrorInvalidValue;
     with_kernel(k, [&](auto s, const void* fn) {
         using S = decltype(s);

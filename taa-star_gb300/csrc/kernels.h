@@ -40,6 +40,13 @@ bool up_path_supported(const taa_uniforms_t& U, int in_w, int in_h, int out_w, i
 // it runs these parameters, sizes and history format, and its launch.
 bool fast32_supported(const taa_uniforms_t& U, int history_fmt, int in_w, int in_h, int out_w, int out_h);
 cudaError_t launch_resolve_fast32(int motion_ch, const taa_uniforms_t& U, const FrameArgs& a, cudaStream_t stream);
+// The same tile body over many views (resolve_fast32.cu): the history window
+// (texels) its 2-D tensor maps cover, its occupancy and its launch (the batch
+// arguments as for launch_batch, one CTA of 128 threads per 32x16 tile).
+void fast32_window(int* w, int* h);
+cudaError_t fast32_batch_occupancy(int interp, int motion_ch, int* ctas_per_sm);
+cudaError_t launch_fast32_batch(int interp, int motion_ch, const BatchView* views, const CUtensorMap* maps,
+                                const int* tma_ok, const uint32_t* jobs, int njobs, int grid, cudaStream_t stream);
 
 // Tiled FP32 / FP16 resolve, optionally with the fused sharpen (resolve_fast.cu).
 cudaError_t launch_resolve_fast(const FastKey& key, const taa_uniforms_t& U, const FrameArgs& a,
@@ -93,7 +100,8 @@ bool encode_history_map(const Img& history, int history_fmt, int box_w, int box_
 
 // The batched persistent resolve (batch_tiled.cu).
 struct BatchKey {
-    int shape;        // tile shape id: 0 32x8, 1 16x16, 2 32x16, 3 16x8, 4 8x8
+    int shape;        // tile shape id: 0 32x8, 1 16x16, 2 32x16, 3 16x8, 4 8x8 (the exact FP32 tiles);
+                      // 5 32x16 in four-pixel strips (TAA_FORM_FAST's body)
     int history_fmt;  // 0 (RGBA32F) only
     int motion_ch;    // 2 or 4
     int interp;       // 0 bilinear or 2 Catmull-Rom
@@ -103,7 +111,8 @@ struct BatchShapeInfo {
     int tile_w, tile_h, threads;
     int win_w, win_h;  // history window (texels) = the TMA box
 };
-constexpr int kBatchShapes = 5;
+constexpr int kBatchShapes = 6;
+constexpr int kBatchFastShape = 5;
 bool batch_shape_info(int shape, int history_fmt, BatchShapeInfo* out);
 cudaError_t batch_occupancy(const BatchKey& k, int* ctas_per_sm);
 cudaError_t launch_batch(const BatchKey& k, const BatchView* views, const CUtensorMap* maps, const int* tma_ok,

@@ -99,11 +99,44 @@ struct Args {
     int reject_outside, depth_cull, reset;
 };
 
+// The arguments of a launch from a view's uniform block and bindings.
+__host__ __device__ inline Args make_args(const taa_uniforms_t& U, const FrameArgs& f) {
+    const taa_parameters_t& P = U.param[0];
+    Args a;
+    a.color = f.color.p;
+    a.depth = f.depth.p;
+    a.vel = f.velocity.p;
+    a.hist = f.history.p;
+    a.hdepth = f.history_depth.p;
+    a.hout = f.history_out.p;
+    a.result = f.result.p;
+    a.status = f.status;
+    a.color_pitch = (uint32_t)f.color.pitch;
+    a.depth_pitch = (uint32_t)f.depth.pitch;
+    a.vel_pitch = (uint32_t)f.velocity.pitch;
+    a.hist_pitch = (uint32_t)f.history.pitch;
+    a.hdepth_pitch = (uint32_t)f.history_depth.pitch;
+    a.hout_pitch = (uint32_t)f.history_out.pitch;
+    a.result_pitch = (uint32_t)f.result.pitch;
+    a.W = f.out_w;
+    a.H = f.out_h;
+    a.inv_w = f.inv_out_w;
+    a.inv_h = f.inv_out_h;
+    a.alpha = P.mAlpha;
+    a.rejection_alpha = P.mRejectionAlpha;
+    a.gamma = P.mVarClipGamma;
+    a.reject_outside = P.mRejectOutside != 0;
+    a.depth_cull = P.mDepthCulling != 0;
+    a.reset = U.mResetHistory != 0;
+    return a;
+}
+
 struct Smem {
     float4 col[NS];                    // staged (Y, Co, Cg, Cg^2)
     alignas(128) float4 win[WW * WH];  // the history window
     uint64_t bar;                      // completion of the window's TMA copy
     int org[3];                        // window origin x, y; 1 TMA, 2 cp.async, 0 none
+    int abort;                         // a persistent CTA stops after this tile (a window wait gave up)
 };
 
 template <class T> __device__ __forceinline__ const T* at(const char* base, uint32_t pitch, int x, int y) {
@@ -278,15 +311,20 @@ template <int INTERP> __device__ __forceinline__ int axis_first(float it, float&
     return trunc_index(b) - (INTERP == 2 ? 1 : 0);
 }
 
-template <int INTERP, int MC>
-__global__ void __launch_bounds__(NT, TAA_FAST_MIN_BLOCKS)
-    resolve_fast32(const Args a, const __grid_constant__ CUtensorMap hmap, const int tma_ok) {
+// One 32x16 tile (tile_x, tile_y) of a view; every thread of the CTA calls it.
+// `phase` is the parity the window barrier completes next (PERSIST: the CTA
+// takes several tiles with one barrier initialised by the caller; otherwise
+// the thread that starts the copy initialises it).  A wait that gives up sets
+// the status bit and leaves the tile unwritten; with PERSIST it also sets
+// sm.abort, which the caller reads after the barrier that separates tiles.
+template <int INTERP, int MC, bool PERSIST>
+__device__ __forceinline__ void strip_tile(const Args& a, const CUtensorMap* hmap, int tma_ok, int tile_x,
+                                           int tile_y, Smem& sm, uint32_t& phase) {
     using RawVel = typename std::conditional<MC == 4, uint2, uint32_t>::type;
     constexpr int SPAN = INTERP == 2 ? 4 : 2;
-    __shared__ Smem sm;
     const int tid = threadIdx.x, lx = tid & 31, sy = tid >> 5;
     const int W = a.W, H = a.H;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+    const int x0 = tile_x * TX, y0 = tile_y * TY;
     const int x = x0 + lx, cx = min(x, W - 1);
     const int ya = y0 + NPX * sy;  // the strip's first row
     const bool have_hist = a.hist != nullptr;
@@ -342,10 +380,10 @@ __global__ void __launch_bounds__(NT, TAA_FAST_MIN_BLOCKS)
         sm.org[1] = wy0;
         sm.org[2] = mode;
         if (mode == 1) {
-            mbar_init(&sm.bar, 1);
+            if (!PERSIST) mbar_init(&sm.bar, 1);
             mbar_expect_tx(&sm.bar, (uint32_t)(sizeof(float4) * WW * WH));
-            if (TAA_FAST_TMA2D) tiled::tma_load_2d(sm.win, &hmap, 4 * wx0, wy0, &sm.bar);
-            else tma_load_3d(sm.win, &hmap, 0, wx0, wy0, &sm.bar);
+            if (TAA_FAST_TMA2D) tiled::tma_load_2d(sm.win, hmap, 4 * wx0, wy0, &sm.bar);
+            else tma_load_3d(sm.win, hmap, 0, wx0, wy0, &sm.bar);
         }
     }
     // 4. staged colour
@@ -382,11 +420,13 @@ __global__ void __launch_bounds__(NT, TAA_FAST_MIN_BLOCKS)
 
     bool landed = true;
     if (mode == 1) {
-        landed = mbar_wait_bounded(&sm.bar, 0u, polls);
+        landed = mbar_wait_bounded(&sm.bar, phase & 1u, polls);
         if (!landed) {
             atomicOr(a.status, kStatusWindowTimeout);
-            mbar_wait_bounded(&sm.bar, 0u);  // the copy may still land in this CTA's memory
+            mbar_wait_bounded(&sm.bar, phase & 1u);  // the copy may still land in this CTA's memory
+            if (PERSIST) sm.abort = 1;
         }
+        phase ^= 1u;
     } else if (mode == 2) {
         cp_async_wait_all();
         __syncthreads();
@@ -500,6 +540,51 @@ __global__ void __launch_bounds__(NT, TAA_FAST_MIN_BLOCKS)
     }
 }
 
+// One view, one CTA per tile.
+template <int INTERP, int MC>
+__global__ void __launch_bounds__(NT, TAA_FAST_MIN_BLOCKS)
+    resolve_fast32(const Args a, const __grid_constant__ CUtensorMap hmap, const int tma_ok) {
+    __shared__ Smem sm;
+    uint32_t phase = 0;
+    strip_tile<INTERP, MC, false>(a, &hmap, tma_ok, blockIdx.x, blockIdx.y, sm, phase);
+}
+
+// Many views in one launch: each CTA takes jobs blockIdx.x, blockIdx.x +
+// gridDim.x, ... of the job list (view, tile x, tile y; common.cuh); a view's
+// arguments are rebuilt in shared memory when a CTA's job moves to another
+// view.  maps[v] is view v's 2-D history map for the 41x25 window, usable
+// when tma_ok[v].
+template <int INTERP, int MC>
+__global__ void __launch_bounds__(NT, TAA_FAST_MIN_BLOCKS)
+    resolve_fast32_batch(const BatchView* __restrict__ views, const CUtensorMap* __restrict__ maps,
+                         const int* __restrict__ tma_ok, const uint32_t* __restrict__ jobs, const int njobs) {
+    __shared__ Smem sm;
+    __shared__ Args s_args;
+    if (threadIdx.x == 0) {
+        mbar_init(&sm.bar, 1);
+        sm.abort = 0;
+    }
+    uint32_t phase = 0;
+    int cur_view = -1;
+    for (int j = blockIdx.x; j < njobs; j += gridDim.x) {
+        const uint32_t job = __ldg(jobs + j);
+        const int vi = job_view(job);
+        if (vi != cur_view) {
+            __syncthreads();  // every thread has read the previous view's arguments
+            if (threadIdx.x == 0) {
+                s_args = make_args(views[vi].U, views[vi].a);
+                asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;\n" ::"l"(maps + vi) : "memory");
+            }
+            cur_view = vi;
+            __syncthreads();
+        }
+        strip_tile<INTERP, MC, true>(s_args, maps + vi, __ldg(tma_ok + vi), job_tile_x(job), job_tile_y(job), sm,
+                                     phase);
+        __syncthreads();  // the next tile reuses the shared memory
+        if (sm.abort) return;
+    }
+}
+
 }  // namespace fast32
 
 bool fast32_supported(const taa_uniforms_t& U, int history_fmt, int in_w, int in_h, int out_w, int out_h) {
@@ -511,32 +596,7 @@ bool fast32_supported(const taa_uniforms_t& U, int history_fmt, int in_w, int in
 cudaError_t launch_resolve_fast32(int motion_ch, const taa_uniforms_t& U, const FrameArgs& f, cudaStream_t s) {
     using namespace fast32;
     const taa_parameters_t& P = U.param[0];
-    Args a;
-    a.color = f.color.p;
-    a.depth = f.depth.p;
-    a.vel = f.velocity.p;
-    a.hist = f.history.p;
-    a.hdepth = f.history_depth.p;
-    a.hout = f.history_out.p;
-    a.result = f.result.p;
-    a.status = f.status;
-    a.color_pitch = (uint32_t)f.color.pitch;
-    a.depth_pitch = (uint32_t)f.depth.pitch;
-    a.vel_pitch = (uint32_t)f.velocity.pitch;
-    a.hist_pitch = (uint32_t)f.history.pitch;
-    a.hdepth_pitch = (uint32_t)f.history_depth.pitch;
-    a.hout_pitch = (uint32_t)f.history_out.pitch;
-    a.result_pitch = (uint32_t)f.result.pitch;
-    a.W = f.out_w;
-    a.H = f.out_h;
-    a.inv_w = f.inv_out_w;
-    a.inv_h = f.inv_out_h;
-    a.alpha = P.mAlpha;
-    a.rejection_alpha = P.mRejectionAlpha;
-    a.gamma = P.mVarClipGamma;
-    a.reject_outside = P.mRejectOutside != 0;
-    a.depth_cull = P.mDepthCulling != 0;
-    a.reset = U.mResetHistory != 0;
+    const Args a = make_args(U, f);
     CUtensorMap map;
     std::memset(&map, 0, sizeof map);
     const int tma_ok = a.hist && f.history.w >= WW && f.history.h >= WH &&
@@ -550,6 +610,36 @@ cudaError_t launch_resolve_fast32(int motion_ch, const taa_uniforms_t& U, const 
         else resolve_fast32<0, 2><<<grid, NT, 0, s>>>(a, map, tma_ok);
     }
     return cudaGetLastError();
+}
+
+void fast32_window(int* w, int* h) {
+    *w = fast32::WW;
+    *h = fast32::WH;
+}
+
+namespace {
+template <int INTERP, int MC> const void* fast32_batch_kernel() {
+    return reinterpret_cast<const void*>(&fast32::resolve_fast32_batch<INTERP, MC>);
+}
+const void* fast32_batch_fn(int interp, int motion_ch) {
+    if (interp == 2) return motion_ch == 4 ? fast32_batch_kernel<2, 4>() : fast32_batch_kernel<2, 2>();
+    if (interp == 0) return motion_ch == 4 ? fast32_batch_kernel<0, 4>() : fast32_batch_kernel<0, 2>();
+    return nullptr;
+}
+}  // namespace
+
+cudaError_t fast32_batch_occupancy(int interp, int motion_ch, int* ctas_per_sm) {
+    const void* fn = fast32_batch_fn(interp, motion_ch);
+    if (!fn) return cudaErrorInvalidValue;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, fn, fast32::NT, 0);
+}
+
+cudaError_t launch_fast32_batch(int interp, int motion_ch, const BatchView* views, const CUtensorMap* maps,
+                                const int* tma_ok, const uint32_t* jobs, int njobs, int grid, cudaStream_t stream) {
+    const void* fn = fast32_batch_fn(interp, motion_ch);
+    if (!fn) return cudaErrorInvalidValue;
+    void* args[] = {(void*)&views, (void*)&maps, (void*)&tma_ok, (void*)&jobs, (void*)&njobs};
+    return cudaLaunchKernel(fn, dim3(grid), dim3(fast32::NT), args, 0, stream);
 }
 
 }  // namespace taa_dev

@@ -94,7 +94,7 @@ class JitterOpts(C.Structure):
 
 class BatchTuning(C.Structure):
     _fields_ = [("tile_w", C.c_int32), ("tile_h", C.c_int32), ("schedule", C.c_int32), ("ctas_per_sm", C.c_int32),
-                ("ms", C.c_float)]
+                ("ms", C.c_float), ("form", C.c_int32)]
 
 
 class MlpWeights(C.Structure):
@@ -460,12 +460,12 @@ def frame_io(**bindings) -> FrameIO:
 class Batch:
     """A batch of views resolved by one persistent launch (taa_batch_*)."""
 
-    def __init__(self, sizes, motion_format=TAA_MOTION_RG16F):
+    def __init__(self, sizes, motion_format=TAA_MOTION_RG16F, form=TAA_FORM_AUTO):
         self.lib = load()
         self.n = len(sizes)
         descs = (Desc * self.n)()
         for i, (w, h) in enumerate(sizes):
-            descs[i] = Desc(C.sizeof(Desc), w, h, w, h, TAA_HISTORY_RGBA32F, motion_format, TAA_FORM_AUTO,
+            descs[i] = Desc(C.sizeof(Desc), w, h, w, h, TAA_HISTORY_RGBA32F, motion_format, form,
                             TAA_SHARPEN_OFF, 0.5, 0)
         h = C.c_void_p()
         check(self.lib.taa_batch_create(descs, self.n, C.byref(h)))
@@ -502,8 +502,8 @@ class Batch:
         check(self.lib.taa_batch_get_tuning(self.handle, C.byref(t)))
         return t
 
-    def set_tuning(self, tile_w, tile_h, schedule, ctas_per_sm=0):
-        t = BatchTuning(tile_w, tile_h, schedule, ctas_per_sm, 0.0)
+    def set_tuning(self, tile_w, tile_h, schedule, ctas_per_sm=0, form=TAA_FORM_TILED):
+        t = BatchTuning(tile_w, tile_h, schedule, ctas_per_sm, 0.0, form)
         check(self.lib.taa_batch_set_tuning(self.handle, C.byref(t)))
 
 

@@ -1,10 +1,11 @@
 """The batched resolve (taa_batch_*) against per-view taa_resolve (run with -m gpu).
 
 A batch resolves views of different sizes in one persistent launch; every
-view must get exactly the bits its own taa_resolve gives in the tiled FP32
-form, whatever tile shape and job order the batch runs with, when the launch
-is replayed from a CUDA graph, and after taa_batch_autotune has picked its
-configuration.
+view must get exactly the bits its own taa_resolve gives in the form of the
+batch's tile body - the tiled FP32 form for the exact tile shapes, the fast
+form for the four-pixel strips - whatever tile shape and job order the batch
+runs with, when the launch is replayed from a CUDA graph, and after
+taa_batch_autotune has picked its configuration.
 """
 import ctypes as C
 
@@ -38,11 +39,11 @@ def make_views(dev, sizes, params=None, motion_channels=2):
     return views
 
 
-def reference(views, motion_format):
+def reference(views, motion_format, form=T.TAA_FORM_TILED):
     out = []
     for v in views:
         w, h = v["size"]
-        ctx = T.Taa(w, h, motion_format=motion_format, form=T.TAA_FORM_TILED)
+        ctx = T.Taa(w, h, motion_format=motion_format, form=form)
         ctx.set_uniforms(v["u"])
         b = dict(v["b"])
         b["history_out"] = torch.full_like(b["history_out"], float("nan"))
@@ -90,6 +91,42 @@ def test_batch_equals_per_view_resolve(cuda, shape, schedule):
     batch.close()
 
 
+@pytest.mark.parametrize("schedule", [T.TAA_SCHEDULE_VIEW_ORDER, T.TAA_SCHEDULE_LARGEST_FIRST,
+                                      T.TAA_SCHEDULE_INTERLEAVED])
+@pytest.mark.parametrize("params,mc", [({}, 2), (dict(mInterpolationMode=0, mDepthCulling=1, mRejectOutside=1), 2),
+                                       ({}, 4)], ids=["cr", "bilinear_c2", "rgba16f_motion"])
+def test_fast_strips_equal_per_view_fast_resolve(cuda, schedule, params, mc):
+    """The four-pixel strips (TAA_FORM_FAST's body) over many views: each view
+    gets the bits of its own taa_resolve in TAA_FORM_FAST, persistent or one
+    CTA per tile."""
+    mf = T.TAA_MOTION_RGBA16F if mc == 4 else T.TAA_MOTION_RG16F
+    views = make_views(cuda, SIZES, params=params, motion_channels=mc)
+    ref = reference(views, mf, form=T.TAA_FORM_FAST)
+    batch = make_batch(views, mf)
+    for grid_mode in (0, T.TAA_BATCH_CTA_PER_TILE, 1):
+        batch.set_tuning(32, 16, schedule, grid_mode, form=T.TAA_FORM_FAST)
+        reset_outputs(views)
+        batch.launch(0)
+        check_equal(views, ref)
+    batch.close()
+
+
+def test_fast_strips_need_a_fast_batch_and_the_benchmark_mode(cuda):
+    lib = T.load()
+    views = make_views(cuda, SIZES[:2])
+    tb = T.Batch([v["size"] for v in views], form=T.TAA_FORM_TILED)
+    bad = T.BatchTuning(32, 16, 0, 0, 0.0, T.TAA_FORM_FAST)
+    assert lib.taa_batch_set_tuning(tb.handle, C.byref(bad)) == T.TAA_E_UNSUPPORTED
+    tb.close()
+    views = make_views(cuda, SIZES[:2], params=dict(mColorClampingOrClipping=1))  # not the benchmark mode
+    batch = make_batch(views, T.TAA_MOTION_RG16F)
+    batch.set_tuning(32, 16, 0, 0, form=T.TAA_FORM_FAST)
+    assert lib.taa_batch_launch(batch.handle, None, 0) == T.TAA_E_UNSUPPORTED
+    best = batch.autotune(0, reps=1)
+    assert best.form in (0, T.TAA_FORM_TILED)  # the strips are not candidates
+    batch.close()
+
+
 @pytest.mark.parametrize("mode", ["bilinear_clamp", "rgba16f_motion"])
 def test_batch_other_modes(cuda, mode):
     params = dict(mInterpolationMode=0, mColorClampingOrClipping=1) if mode == "bilinear_clamp" else {}
@@ -107,12 +144,14 @@ def test_batch_other_modes(cuda, mode):
 
 def test_autotune_then_graph_replay(cuda):
     views = make_views(cuda, SIZES)
-    ref = reference(views, T.TAA_MOTION_RG16F)
     batch = make_batch(views, T.TAA_MOTION_RG16F)
     best = batch.autotune(0, reps=2)
-    assert (best.tile_w, best.tile_h) in SHAPES and best.ms > 0
+    assert best.ms > 0
+    assert ((best.tile_w, best.tile_h) in SHAPES and best.form in (0, T.TAA_FORM_TILED)) or \
+        ((best.tile_w, best.tile_h) == (32, 16) and best.form == T.TAA_FORM_FAST)
     t = batch.tuning()
-    assert (t.tile_w, t.tile_h, t.schedule) == (best.tile_w, best.tile_h, best.schedule)
+    assert (t.tile_w, t.tile_h, t.schedule, t.form) == (best.tile_w, best.tile_h, best.schedule, best.form)
+    ref = reference(views, T.TAA_MOTION_RG16F, form=T.TAA_FORM_FAST if best.form == T.TAA_FORM_FAST else T.TAA_FORM_TILED)
     reset_outputs(views)
     batch.launch(0)
     check_equal(views, ref)
@@ -176,7 +215,8 @@ def test_c4_views_from_a_graph_match_the_oracle(cuda):
         views.append(dict(size=(w, h), u=u, b=b))
     assert len(views) == 48
     batch = make_batch(views, T.TAA_MOTION_RG16F)
-    batch.autotune(0, reps=1)
+    # the exact tiles: the oracle's bits
+    batch.set_tuning(16, 16, T.TAA_SCHEDULE_LARGEST_FIRST)
     s = torch.cuda.Stream()
     g = torch.cuda.CUDAGraph()
     with torch.cuda.graph(g, stream=s):
@@ -203,4 +243,30 @@ def test_c4_views_from_a_graph_match_the_oracle(cuda):
     for (h_g, r_g), (h_r, r_r), v in zip(got, ref, views):
         np.testing.assert_array_equal(h_g, h_r, err_msg=str(v["size"]))
         np.testing.assert_array_equal(r_g, r_r, err_msg=str(v["size"]))
+    # the autotuned configuration (the fast strips where they win), from a graph:
+    # the bits of each view's own taa_resolve in that form, and within 1e-4
+    # relative L2 of the FP64 oracle on the checked views
+    best = batch.autotune(0, reps=1)
+    form = T.TAA_FORM_FAST if best.form == T.TAA_FORM_FAST else T.TAA_FORM_TILED
+    g2 = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g2, stream=s):
+        batch.launch(0, stream=torch.cuda.current_stream().cuda_stream)
+    reset_outputs(views)
+    torch.cuda.synchronize()
+    g2.replay()
+    torch.cuda.synchronize()
+    assert T.device_status(clear=True) == 0
+    got = [(v["b"]["history_out"].cpu().numpy(), v["b"]["result"].float().cpu().numpy()) for v in views]
+    ref = reference(views, T.TAA_MOTION_RG16F, form=form)
+    for (h_g, r_g), (h_r, r_r), v in zip(got, ref, views):
+        np.testing.assert_array_equal(h_g, h_r, err_msg=str(v["size"]))
+        np.testing.assert_array_equal(r_g, r_r, err_msg=str(v["size"]))
+    for i in order[:6] + order[-2:]:
+        v = views[i]
+        b = v["b"]
+        r64 = O.resolve(v["u"], b["color"].float().cpu().numpy(), b["depth"].cpu().numpy(),
+                        b["velocity"].float().cpu().numpy(), history=b["history"].cpu().numpy(),
+                        history_depth=b["history_depth"].cpu().numpy(), precision=64)["history"][..., :3]
+        h = got[i][0][..., :3]
+        assert np.linalg.norm(h - r64) <= 1e-4 * np.linalg.norm(r64), v["size"]
     batch.close()

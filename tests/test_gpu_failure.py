@@ -118,7 +118,7 @@ def test_upsampling_window_wait_gives_up(cuda, give_up):
     ctx.close()
 
 
-@pytest.mark.parametrize("shape", [(32, 16), (16, 8)])
+@pytest.mark.parametrize("shape", [(32, 16, T.TAA_FORM_TILED), (16, 8, T.TAA_FORM_TILED), (32, 16, T.TAA_FORM_FAST)])
 def test_batch_cta_stops_after_a_wait_gave_up(cuda, give_up, shape):
     sizes = [(W, H), (128, 64)]
     views = []
@@ -131,7 +131,7 @@ def test_batch_cta_stops_after_a_wait_gave_up(cuda, give_up, shape):
     outs = [outputs(cuda, *v["size"]) for v in views]
     batch.prepare(0, [dict(v["b"], **o) for v, o in zip(views, outs)])
     # one persistent CTA per SM: a CTA whose first tile gives up leaves its later tiles too
-    batch.set_tuning(shape[0], shape[1], T.TAA_SCHEDULE_VIEW_ORDER, 1)
+    batch.set_tuning(shape[0], shape[1], T.TAA_SCHEDULE_VIEW_ORDER, 1, form=shape[2])
     T.set_window_wait(None)
     batch.launch(0)
     torch.cuda.synchronize()
