@@ -90,10 +90,7 @@ typedef enum taa_status {
  * times narrower than its widest, as next to a firefly) is finished in FP32
  * from its source texels.  Frame error against the FP64 oracle below 1e-3
  * relative L2 on the benchmark scenes (up to 8.6e-3 without); the form runs
- * about 15 % slower.  In the benchmark mode of the parameter block (the
- * parameters TAA_FORM_FAST runs) the FP16 form always has its guard, on the
- * strip body (a box 16 times narrower in one channel than in another is
- * decided in FP32), and the flag changes nothing. */
+ * about 15 % slower. */
 #define TAA_FLAG_FP16_GUARD 0x4u
 /* taa_desc_t.flags, with a sharpener and the tiled FP32 form: one launch
  * resolves each tile and the 1-pixel ring around it (recomputing what the

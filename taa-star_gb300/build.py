@@ -33,7 +33,6 @@ UNITS = {
     "resolve_fast.cu": ["-fmad=false"],
     "resolve_tiled.cu": ["-fmad=false"],
     "resolve_fast32.cu": [],
-    "resolve_fast16.cu": [],
     "resolve_half.cu": [],
     "resolve_half_guard.cu": [],
     "batch_tiled.cu": ["-fmad=false"],

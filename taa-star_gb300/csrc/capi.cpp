@@ -568,11 +568,6 @@ int taa_resolve(taa_ctx* c, void* stream, const taa_frame_io_t* io) {
         if (form == TAA_FORM_FAST) {
             e = taa_dev::launch_resolve_fast32(mc, U, a, s);
             if (e == cudaSuccess && sharpen) e = taa_dev::launch_sharpen((int)d.sharpener, a, s);
-        } else if (form == TAA_FORM_FP16 && taa_dev::fast32_supported(U, (int)d.history_format, d.in_width,
-                                                                      d.in_height, d.out_width, d.out_height)) {
-            // the benchmark mode: the strip body, guarded whatever the flag says
-            e = taa_dev::launch_resolve_half_strips(mc, U, a, s);
-            if (e == cudaSuccess && sharpen) e = taa_dev::launch_sharpen((int)d.sharpener, a, s);
         } else if (form == TAA_FORM_FP16) {
             e = (d.flags & TAA_FLAG_FP16_GUARD)
                     ? taa_dev::launch_resolve_half_guarded((int)d.history_format, mc, U.param[0].mInterpolationMode, U, a, s)

@@ -58,10 +58,6 @@ cudaError_t launch_resolve_tiled(int history_fmt, int motion_ch, int interp, con
                                  const FrameArgs& a, cudaStream_t stream);
 cudaError_t launch_resolve_half(int history_fmt, int motion_ch, int interp, const taa_uniforms_t& U,
                                 const FrameArgs& a, cudaStream_t stream);
-// The FP16 form in the benchmark mode (the parameters fast32_supported
-// accepts): the strip body with half2 neighbourhood and clip arithmetic and
-// its FP32 guard (resolve_fast16.cu).
-cudaError_t launch_resolve_half_strips(int motion_ch, const taa_uniforms_t& U, const FrameArgs& a, cudaStream_t stream);
 // The FP16 form with TAA_FLAG_FP16_GUARD (resolve_half_guard.cu).
 cudaError_t launch_resolve_half_guarded(int history_fmt, int motion_ch, int interp, const taa_uniforms_t& U,
                                         const FrameArgs& a, cudaStream_t stream);
