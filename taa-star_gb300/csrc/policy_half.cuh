@@ -36,11 +36,12 @@ __device__ __forceinline__ __half2 u2h(uint32_t v) { return *reinterpret_cast<__
 __device__ __forceinline__ uint32_t h2u(__half2 v) { return *reinterpret_cast<uint32_t*>(&v); }
 
 // Width ratio of a box's widest to its tightest channel above which the
-// guarded variant finishes a clipped pixel in FP32 (a tuning constant: on the
-// benchmark scenes the frame error against FP64 falls from up to 8.6e-3 to
-// below 1e-3 relative L2 while the form stays above 40 Gpx/s at 4K).
+// guarded variant finishes a clipped pixel in FP32 (a tuning constant, by
+// measurement on the benchmark scenes: at 256 single frames stay below 1e-3
+// relative L2 against FP64 but a 64-frame C2 chain reaches 1.1e-3; at 16
+// single frames measure below 1e-4).
 #ifndef TAA_FP16_EXACT_RATIO
-#define TAA_FP16_EXACT_RATIO 256.0f
+#define TAA_FP16_EXACT_RATIO 16.0f
 #endif
 
 template <bool GUARD> struct HalfPol : tiled::HistoryFilter {
