@@ -258,7 +258,7 @@ def time_learned(T, WL, dev, stream, sid, args):
     learned, learned_max = LP.evaluate(wl, wl.frames, dev, T.TAA_FORM_LEARNED, weights=w, fr=fr)
     H, W = wl.height, wl.width
     cost = {}
-    for name, form in (("tiled", T.TAA_FORM_TILED), ("learned", T.TAA_FORM_LEARNED)):
+    for name, form in (("tiled", T.TAA_FORM_TILED), ("fast", T.TAA_FORM_FAST), ("learned", T.TAA_FORM_LEARNED)):
         ctx = T.Taa(W, H, form=form)
         if form == T.TAA_FORM_LEARNED:
             ctx.set_mlp(w)
@@ -279,11 +279,13 @@ def time_learned(T, WL, dev, stream, sid, args):
         ctx.close()
     return {"mpx_s": W * H / cost["learned"], "us_per_frame_1080p": cost["learned"],
             "plain_variance_clip_us_per_frame_1080p": cost["tiled"], "cost_vs_plain": cost["learned"] / cost["tiled"],
+            "fast_variance_clip_us_per_frame_1080p": cost["fast"], "cost_vs_fast": cost["learned"] / cost["fast"],
             "psnr_db_vs_64spp": float(np.mean(learned)), "plain_psnr_db_vs_64spp": float(np.mean(plain)),
             "gain_db": float(np.mean(learned) - np.mean(plain)), "max_abs_err": learned_max,
             "plain_max_abs_err": plain_max,
             "training": {"records": records, "steps": steps, "batch": batch, "loss_first": loss_first,
-                         "loss_last": loss_last, "seeds": [501, 502, 503, 504]},
+                         "loss_last": loss_last, "seeds": [501, 502, 503, 504],
+                         "deterministic": "records in key order, gradient sums added in CTA order"},
             "evaluation": f"{wl.name}, seed {wl.seed}, frames 8..{wl.frames - 1}, PSNR of the RGB history "
                           "against the 64-spp truth, peak = the frame's largest truth value"}
 

@@ -436,7 +436,7 @@ typedef struct taa_mlp_record_t {
     float truth[3];             /* RGB, 64-spp ground truth */
     float gamma, alpha_fixed;   /* mVarClipGamma; the blend weight when bit 0 of flags is set */
     uint32_t flags;             /* bit 0: rejected or reset (the network does not choose alpha) */
-    float pad[2];
+    uint32_t key[2];            /* the trainer's collection call (from 0), the pixel's index y * width + x */
 } taa_mlp_record_t;
 
 /* Random starting weights (uniform, Glorot scale; seeded) whose outputs
@@ -475,7 +475,11 @@ int taa_mlp_gradients(taa_mlp_trainer* tr, const taa_mlp_weights_t* w, int32_t f
  * run) on batches of `batch` records drawn
  * without replacement from a seeded shuffle, starting from *w; the trained
  * weights are written back to *w, and the mean loss of the first and last
- * batch to *loss_first / *loss_last.  Waits for the device. */
+ * batch to *loss_first / *loss_last.  Waits for the device.
+ * Deterministic: the shuffle runs over the records ordered by key (whatever
+ * order the collection appended them in) and the gradient sums are added in
+ * a fixed order, so the same collections (within the capacity), seed and
+ * starting weights give the same trained weights bit for bit. */
 int taa_mlp_train(taa_mlp_trainer* tr, taa_mlp_weights_t* w, int32_t steps, int32_t batch, float lr, uint64_t seed,
                   float* loss_first, float* loss_last);
 

@@ -128,14 +128,25 @@ cudaError_t launch_mlp_build_blob(const float* weights, char* blob, cudaStream_t
 cudaError_t launch_mlp_map_grads(float* grads, cudaStream_t s);
 cudaError_t launch_mlp_forward(const char* blob, const float* feat, float* out, int n, unsigned int* status,
                                cudaStream_t s);
+// Training over records [first, first + count) (in `order` when given): each of
+// the `grid` CTAs writes its gradient sums to its slab of `partial` (grid x
+// learned_grad_floats() floats), which are then added to `grads` in CTA order,
+// so the result does not depend on scheduling.
+int learned_grad_floats();
 cudaError_t launch_mlp_train(const char* blob, const void* records, const uint32_t* order, int first, int count,
-                             float* grads, unsigned int* status, int grid, cudaStream_t s);
+                             float* grads, float* partial, unsigned int* status, int grid, cudaStream_t s);
 cudaError_t launch_mlp_adam(float* weights, float* m, float* v, float* grads, int step, float lr, char* blob,
                             cudaStream_t s);
 cudaError_t launch_resolve_learned(int history_fmt, int motion_ch, bool collect, bool tcgen05, const taa_uniforms_t& U,
                                    const FrameArgs& a, const char* blob, void* records, uint32_t* count,
-                                   uint32_t capacity, uint32_t seed, float sample_fraction, const Img& truth,
+                                   uint32_t capacity, uint32_t seed, uint32_t call, float sample_fraction,
+                                   const Img& truth,
                                    cudaStream_t s);
+
+// The learned form's inference in the benchmark mode on the strip body
+// (resolve_learned_strips.cu); `blob` is the network's device blob.
+cudaError_t launch_resolve_learned_strips(int motion_ch, const taa_uniforms_t& U, const FrameArgs& a, const char* blob,
+                                          cudaStream_t s);
 
 // Synthetic renderer (synth.cu).
 cudaError_t launch_synth(const taa_synth_scene_t& s, const float* host_spheres, int frame,

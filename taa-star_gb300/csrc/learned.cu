@@ -27,7 +27,7 @@ struct __align__(16) Record {
     float gt[3];                          // RGB, 64-spp ground truth
     float gamma, alpha_fixed;             // mVarClipGamma; blend weight when the network does not choose it
     uint32_t flags;                       // 1: alpha is fixed (rejected or reset)
-    float pad[2];
+    uint32_t key[2];                      // collection call, pixel index: the canonical order of the records
 };
 static_assert(sizeof(Record) == 144, "record layout");
 
@@ -164,114 +164,6 @@ __device__ __forceinline__ bool forward(NetSmem<NB, BLOB>& s, int nblocks, uint3
 
 // ---------------------------------------------------------------- warp-level network
 
-// Inference without block barriers: each warp runs its own 32 pixels through
-// the network with warp-wide MMAs (mma.sync m16n8k16, FP16 in, FP32 out).  A
-// layer's accumulator fragments are, packed to FP16 after the ReLU, exactly
-// the next layer's A fragments, so the activations never leave registers.
-// Weights and the warp's feature rows sit in shared memory row-major with
-// 80-byte rows (conflict-free ldmatrix).
-constexpr int kPad = 40;  // halves per padded row
-struct WarpNet {
-    alignas(16) __half w1[kHid][kPad];
-    alignas(16) __half w2[kHid][kPad];
-    alignas(16) __half w3[8][kPad];
-    alignas(16) __half feat[8][32][kPad];  // one 32-row tile per warp
-};
-
-// The padded row-major weights from the canonical blob (all threads, then a barrier).
-__device__ __forceinline__ void load_warp_weights(WarpNet& s, const char* blob) {
-    for (int i = threadIdx.x; i < kHid * kIn; i += blockDim.x) {
-        const int r = i / kIn, k = i % kIn;
-        s.w1[r][k] = *reinterpret_cast<const __half*>(blob + Blob::W1 + tc::canon(r, k, kIn));
-        s.w2[r][k] = *reinterpret_cast<const __half*>(blob + Blob::W2 + tc::canon(r, k, kHid));
-        if (r < 8) s.w3[r][k] = *reinterpret_cast<const __half*>(blob + Blob::W3 + tc::canon(r, k, kHid));
-    }
-}
-
-__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void* p) {
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(tc::saddr(p)));
-}
-__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-__device__ __forceinline__ uint32_t pack_relu(float a, float b) {
-    __half2 h = __hmax2(__floats2half2_rn(a, b), __float2half2_rn(0.f));
-    return *reinterpret_cast<uint32_t*>(&h);
-}
-
-// One hidden layer of a 16-row m-tile: A (two k16 fragments) times W ([32][32]
-// padded) -> the ReLU'd FP16 A fragments of the next layer.
-__device__ __forceinline__ void warp_layer(const uint32_t (&a)[2][4], const __half (*w)[kPad], uint32_t (&h)[2][4]) {
-    const int lane = threadIdx.x & 31;
-    float acc[4][4];
-#pragma unroll
-    for (int nj = 0; nj < 4; ++nj) {
-        acc[nj][0] = acc[nj][1] = acc[nj][2] = acc[nj][3] = 0.f;
-        uint32_t b[4];  // (k 0-7, 8-15, 16-23, 24-31) of rows nj*8 .. nj*8+7
-        ldsm_x4(b, &w[nj * 8 + (lane & 7)][(lane >> 3) * 8]);
-        mma16816(acc[nj], a[0], b[0], b[1]);
-        mma16816(acc[nj], a[1], b[2], b[3]);
-    }
-#pragma unroll
-    for (int kj = 0; kj < 2; ++kj) {
-        h[kj][0] = pack_relu(acc[2 * kj][0], acc[2 * kj][1]);
-        h[kj][1] = pack_relu(acc[2 * kj][2], acc[2 * kj][3]);
-        h[kj][2] = pack_relu(acc[2 * kj + 1][0], acc[2 * kj + 1][1]);
-        h[kj][3] = pack_relu(acc[2 * kj + 1][2], acc[2 * kj + 1][3]);
-    }
-}
-
-// The network on this thread's 32 features; every thread of the warp calls it.
-__device__ __forceinline__ void forward_warp(WarpNet& s, const float (&f)[kIn], float& o0, float& o1) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    __half* row = s.feat[warp][lane];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        __half2 q0 = __floats2half2_rn(f[8 * j + 0], f[8 * j + 1]), q1 = __floats2half2_rn(f[8 * j + 2], f[8 * j + 3]);
-        __half2 q2 = __floats2half2_rn(f[8 * j + 4], f[8 * j + 5]), q3 = __floats2half2_rn(f[8 * j + 6], f[8 * j + 7]);
-        uint4 w;
-        w.x = *reinterpret_cast<uint32_t*>(&q0);
-        w.y = *reinterpret_cast<uint32_t*>(&q1);
-        w.z = *reinterpret_cast<uint32_t*>(&q2);
-        w.w = *reinterpret_cast<uint32_t*>(&q3);
-        *reinterpret_cast<uint4*>(row + 8 * j) = w;
-    }
-    __syncwarp();
-    float res[2][4];
-#pragma unroll
-    for (int mi = 0; mi < 2; ++mi) {
-        uint32_t a[2][4], h1[2][4], h2[2][4];
-#pragma unroll
-        for (int kj = 0; kj < 2; ++kj) ldsm_x4(a[kj], &s.feat[warp][mi * 16 + (lane & 15)][kj * 16 + (lane >> 4) * 8]);
-        warp_layer(a, s.w1, h1);
-        warp_layer(h1, s.w2, h2);
-        float o[4] = {0.f, 0.f, 0.f, 0.f};
-        uint32_t b[4];
-        ldsm_x4(b, &s.w3[lane & 7][(lane >> 3) * 8]);
-        mma16816(o, h2[0], b[0], b[1]);
-        mma16816(o, h2[1], b[2], b[3]);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) res[mi][i] = o[i];
-    }
-    __syncwarp();  // the feature rows are free for the next call
-    // pixel `lane` is row lane % 16 of m-tile lane / 16: its outputs (columns 0
-    // and 1) are in lane (lane % 8) * 4, registers 0-1 (rows 0-7) or 2-3 (8-15)
-    const int src = (lane & 7) * 4;
-    float v[2][4];
-#pragma unroll
-    for (int mi = 0; mi < 2; ++mi)
-#pragma unroll
-        for (int i = 0; i < 4; ++i) v[mi][i] = __shfl_sync(0xffffffffu, res[mi][i], src);
-    const int mi = lane >> 4, hi = (lane >> 3) & 1;
-    o0 = mi ? (hi ? v[1][2] : v[1][0]) : (hi ? v[0][2] : v[0][0]);
-    o1 = mi ? (hi ? v[1][3] : v[1][1]) : (hi ? v[0][3] : v[0][1]);
-}
-
 // ---------------------------------------------------------------- the finisher
 
 // Records are written for pixels whose hash falls below `sample_below`.
@@ -290,6 +182,7 @@ struct CollectArgs {
     uint32_t* count;
     uint32_t capacity;
     uint32_t seed;
+    uint32_t call;           // the trainer's count of collections before this one
     uint32_t sample_below;   // hash threshold: fraction * 2^32
     Img truth;               // RGBA32F ground truth
 };
@@ -362,6 +255,8 @@ template <bool COLLECT, bool TC> struct LearnedFinish {
                     r.gamma = g;
                     r.alpha_fixed = alpha_fixed;
                     r.flags = fixed_alpha ? 1u : 0u;
+                    r.key[0] = self.col.call;
+                    r.key[1] = (uint32_t)y * (uint32_t)a.out_w + (uint32_t)x;
                 }
             }
         } else {
@@ -547,8 +442,8 @@ struct TrainSmem {
     alignas(128) char g2[kRows * kHid * 2];    // dLoss/dH2 after the ReLU mask
     alignas(128) char at[128 * kRows * 2];     // a gradient, transposed: [128 (32 or 2 used)][128 pixels]
     alignas(128) char bt[kHid * kRows * 2];    // an activation, transposed: [32][128 pixels]
-    float loss;
-    float count;
+    float loss[4];   // per warp: summed in warp order, so every run adds them the same way
+    float count[4];
 };
 
 // Transposed copy of one pixel's n values into a [rows][128 pixels] canonical tile.
@@ -580,14 +475,18 @@ __device__ __forceinline__ bool weight_grad(TrainSmem& s, uint32_t cols, bool fi
 
 __global__ void __launch_bounds__(128) mlp_train(const char* __restrict__ blob, const Record* __restrict__ recs,
                                                  const uint32_t* __restrict__ order, int first, int count,
-                                                 float* __restrict__ grads, unsigned int* status) {
+                                                 float* __restrict__ partial, unsigned int* status) {
     extern __shared__ __align__(128) char dyn[];
     TrainSmem& s = *reinterpret_cast<TrainSmem*>(dyn);
     const int t = threadIdx.x, warp = t >> 5;
-    if (t == 0) {
-        tiled::mbar_init(&s.net.bar, 1);
-        s.loss = 0.f;
-        s.count = 0.f;
+    // this CTA's slab of gradient sums: written whole, then added up over the
+    // CTAs in a fixed order by mlp_sum_partials (no atomics: training repeats bit for bit)
+    float* const slab = partial + (size_t)blockIdx.x * kGradFloats;
+    for (int i = t; i < kGradFloats; i += 128) slab[i] = 0.f;
+    if (t == 0) tiled::mbar_init(&s.net.bar, 1);
+    if (t < 4) {
+        s.loss[t] = 0.f;
+        s.count[t] = 0.f;
     }
     copy_blob(s.net.blob, blob, Blob::BYTES);
     for (int w = t; w < (int)sizeof(s.at) / 16; w += 128) reinterpret_cast<uint4*>(s.at)[w] = make_uint4(0, 0, 0, 0);
@@ -665,8 +564,8 @@ __global__ void __launch_bounds__(128) mlp_train(const char* __restrict__ blob, 
         {
             const float l = warp_sum(loss), c = warp_sum(live ? 1.f : 0.f);
             if ((t & 31) == 0) {
-                atomicAdd(&s.loss, l);
-                atomicAdd(&s.count, c);
+                s.loss[warp] += l;
+                s.count[warp] += c;
             }
         }
         first_tile = false;
@@ -674,20 +573,21 @@ __global__ void __launch_bounds__(128) mlp_train(const char* __restrict__ blob, 
         __syncthreads();
     }
     // this CTA's weight gradients out of tensor memory (rows 0..31 are warp 0's lanes)
+    __syncthreads();  // the slab's zeros are in place
     if (!first_tile && warp == 0) {
         float acc[32];
         tc::ld32(s.net.tmem + 32, acc);
         if (t < kOut)
-            for (int i = 0; i < kHid; ++i) atomicAdd(&grads[offsetof(Weights, w3) / 4 + t * kHid + i], acc[i]);
+            for (int i = 0; i < kHid; ++i) slab[offsetof(Weights, w3) / 4 + t * kHid + i] = acc[i];
         tc::ld32(s.net.tmem + 64, acc);
-        for (int i = 0; i < kHid; ++i) atomicAdd(&grads[offsetof(Weights, w2) / 4 + t * kHid + i], acc[i]);
+        for (int i = 0; i < kHid; ++i) slab[offsetof(Weights, w2) / 4 + t * kHid + i] = acc[i];
         tc::ld32(s.net.tmem + 96, acc);
-        for (int i = 0; i < kIn; ++i) atomicAdd(&grads[offsetof(Weights, w1) / 4 + t * kIn + i], acc[i]);
+        for (int i = 0; i < kIn; ++i) slab[offsetof(Weights, w1) / 4 + t * kIn + i] = acc[i];
     }
     __syncthreads();
     if (t == 0) {
-        atomicAdd(&grads[kParams], s.loss);
-        atomicAdd(&grads[kParams + 1], s.count);
+        slab[kParams] = ((s.loss[0] + s.loss[1]) + s.loss[2]) + s.loss[3];
+        slab[kParams + 1] = ((s.count[0] + s.count[1]) + s.count[2]) + s.count[3];
         if (!ok) atomicOr(status, kStatusWindowTimeout);
     }
     tc::fence_before_sync();
@@ -748,6 +648,15 @@ __device__ __forceinline__ void map_grads(float* g, int t, int nt) {
     __syncthreads();
 }
 
+// grads[i] += the CTAs' slab values, added in CTA order.
+__global__ void mlp_sum_partials(const float* __restrict__ partial, int nslabs, float* __restrict__ grads) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kGradFloats) return;
+    float sum = 0.f;
+    for (int b = 0; b < nslabs; ++b) sum += partial[(size_t)b * kGradFloats + i];
+    grads[i] += sum;
+}
+
 __global__ void mlp_build_blob(const Weights* w, char* blob) { build_blob(*w, blob, threadIdx.x, blockDim.x); }
 __global__ void mlp_map_grads(float* grads) { map_grads(grads, threadIdx.x, blockDim.x); }
 
@@ -801,13 +710,17 @@ cudaError_t launch_mlp_forward(const char* blob, const float* feat, float* out, 
     return cudaGetLastError();
 }
 
+int learned_grad_floats() { return learned::kGradFloats; }
+
 cudaError_t launch_mlp_train(const char* blob, const void* records, const uint32_t* order, int first, int count,
-                             float* grads, unsigned int* status, int grid, cudaStream_t s) {
+                             float* grads, float* partial, unsigned int* status, int grid, cudaStream_t s) {
     const size_t smem = sizeof(learned::TrainSmem) + 128;
     cudaError_t e = cudaFuncSetAttribute(learned::mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     learned::mlp_train<<<grid, 128, smem, s>>>(blob, reinterpret_cast<const Record*>(records), order, first, count,
-                                                grads, status);
+                                                partial, status);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    learned::mlp_sum_partials<<<(learned::kGradFloats + 255) / 256, 256, 0, s>>>(partial, grid, grads);
     return cudaGetLastError();
 }
 
@@ -819,7 +732,8 @@ cudaError_t launch_mlp_adam(float* weights, float* m, float* v, float* grads, in
 
 cudaError_t launch_resolve_learned(int history_fmt, int motion_ch, bool collect, bool tcgen05, const taa_uniforms_t& U,
                                    const FrameArgs& a, const char* blob, void* records, uint32_t* count,
-                                   uint32_t capacity, uint32_t seed, float sample_fraction, const Img& truth,
+                                   uint32_t capacity, uint32_t seed, uint32_t call, float sample_fraction,
+                                   const Img& truth,
                                    cudaStream_t s) {
     using S = learned::S;
     dim3 grid((a.out_w + S::TX - 1) / S::TX, (a.out_h + S::TY - 1) / S::TY);
@@ -827,7 +741,7 @@ cudaError_t launch_resolve_learned(int history_fmt, int motion_ch, bool collect,
     std::memset(&map, 0, sizeof map);
     const int tma_ok = a.history.p && a.history.w >= tiled::Win<S, 0>::W && a.history.h >= S::WH &&
                        history_fmt == 0 && encode_history_map(a.history, 0, tiled::Win<S, 0>::W, S::WH, &map);
-    learned::CollectArgs col{reinterpret_cast<Record*>(records), count, capacity, seed,
+    learned::CollectArgs col{reinterpret_cast<Record*>(records), count, capacity, seed, call,
                              (uint32_t)fminf(fmaxf(sample_fraction, 0.f) * 4294967040.f, 4294967040.f), truth};
     if (history_fmt != 0) return cudaErrorInvalidValue;
     const int smem = collect ? 0 : (int)(tcgen05 ? sizeof(learned::InferSmem) : sizeof(learned::WarpNet));

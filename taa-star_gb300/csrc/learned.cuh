@@ -244,5 +244,118 @@ __device__ __forceinline__ bool layer(char* const* a_tiles, const char* w, int n
     return ok;
 }
 
+// ---------------------------------------------------------------- the network per warp
+
+// Inference without block barriers: each warp runs its own 32 pixels through
+// the network with warp-wide MMAs (mma.sync m16n8k16, FP16 in, FP32 out).  A
+// layer's accumulator fragments are, packed to FP16 after the ReLU, exactly
+// the next layer's A fragments, so the activations never leave registers.
+// Weights and the warp's feature rows sit in shared memory row-major with
+// 80-byte rows (conflict-free ldmatrix).
+constexpr int kPad = 40;  // halves per padded row
+template <int NW> struct WarpNetN {
+    alignas(16) __half w1[kHid][kPad];
+    alignas(16) __half w2[kHid][kPad];
+    alignas(16) __half w3[8][kPad];
+    alignas(16) __half feat[NW][32][kPad];  // one 32-row tile per warp of the CTA
+};
+using WarpNet = WarpNetN<8>;  // 256-thread CTAs
+
+// The padded row-major weights from the canonical blob (all threads, then a barrier).
+template <int NW> __device__ __forceinline__ void load_warp_weights(WarpNetN<NW>& s, const char* blob) {
+    for (int i = threadIdx.x; i < kHid * kIn; i += blockDim.x) {
+        const int r = i / kIn, k = i % kIn;
+        s.w1[r][k] = *reinterpret_cast<const __half*>(blob + Blob::W1 + tc::canon(r, k, kIn));
+        s.w2[r][k] = *reinterpret_cast<const __half*>(blob + Blob::W2 + tc::canon(r, k, kHid));
+        if (r < 8) s.w3[r][k] = *reinterpret_cast<const __half*>(blob + Blob::W3 + tc::canon(r, k, kHid));
+    }
+}
+
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void* p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(tc::saddr(p)));
+}
+__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+__device__ __forceinline__ uint32_t pack_relu(float a, float b) {
+    __half2 h = __hmax2(__floats2half2_rn(a, b), __float2half2_rn(0.f));
+    return *reinterpret_cast<uint32_t*>(&h);
+}
+
+// One hidden layer of a 16-row m-tile: A (two k16 fragments) times W ([32][32]
+// padded) -> the ReLU'd FP16 A fragments of the next layer.
+__device__ __forceinline__ void warp_layer(const uint32_t (&a)[2][4], const __half (*w)[kPad], uint32_t (&h)[2][4]) {
+    const int lane = threadIdx.x & 31;
+    float acc[4][4];
+#pragma unroll
+    for (int nj = 0; nj < 4; ++nj) {
+        acc[nj][0] = acc[nj][1] = acc[nj][2] = acc[nj][3] = 0.f;
+        uint32_t b[4];  // (k 0-7, 8-15, 16-23, 24-31) of rows nj*8 .. nj*8+7
+        ldsm_x4(b, &w[nj * 8 + (lane & 7)][(lane >> 3) * 8]);
+        mma16816(acc[nj], a[0], b[0], b[1]);
+        mma16816(acc[nj], a[1], b[2], b[3]);
+    }
+#pragma unroll
+    for (int kj = 0; kj < 2; ++kj) {
+        h[kj][0] = pack_relu(acc[2 * kj][0], acc[2 * kj][1]);
+        h[kj][1] = pack_relu(acc[2 * kj][2], acc[2 * kj][3]);
+        h[kj][2] = pack_relu(acc[2 * kj + 1][0], acc[2 * kj + 1][1]);
+        h[kj][3] = pack_relu(acc[2 * kj + 1][2], acc[2 * kj + 1][3]);
+    }
+}
+
+// The network on this thread's 32 features; every thread of the warp calls it.
+template <int NW>
+__device__ __forceinline__ void forward_warp(WarpNetN<NW>& s, const float (&f)[kIn], float& o0, float& o1) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __half* row = s.feat[warp][lane];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        __half2 q0 = __floats2half2_rn(f[8 * j + 0], f[8 * j + 1]), q1 = __floats2half2_rn(f[8 * j + 2], f[8 * j + 3]);
+        __half2 q2 = __floats2half2_rn(f[8 * j + 4], f[8 * j + 5]), q3 = __floats2half2_rn(f[8 * j + 6], f[8 * j + 7]);
+        uint4 w;
+        w.x = *reinterpret_cast<uint32_t*>(&q0);
+        w.y = *reinterpret_cast<uint32_t*>(&q1);
+        w.z = *reinterpret_cast<uint32_t*>(&q2);
+        w.w = *reinterpret_cast<uint32_t*>(&q3);
+        *reinterpret_cast<uint4*>(row + 8 * j) = w;
+    }
+    __syncwarp();
+    float res[2][4];
+#pragma unroll
+    for (int mi = 0; mi < 2; ++mi) {
+        uint32_t a[2][4], h1[2][4], h2[2][4];
+#pragma unroll
+        for (int kj = 0; kj < 2; ++kj) ldsm_x4(a[kj], &s.feat[warp][mi * 16 + (lane & 15)][kj * 16 + (lane >> 4) * 8]);
+        warp_layer(a, s.w1, h1);
+        warp_layer(h1, s.w2, h2);
+        float o[4] = {0.f, 0.f, 0.f, 0.f};
+        uint32_t b[4];
+        ldsm_x4(b, &s.w3[lane & 7][(lane >> 3) * 8]);
+        mma16816(o, h2[0], b[0], b[1]);
+        mma16816(o, h2[1], b[2], b[3]);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) res[mi][i] = o[i];
+    }
+    __syncwarp();  // the feature rows are free for the next call
+    // pixel `lane` is row lane % 16 of m-tile lane / 16: its outputs (columns 0
+    // and 1) are in lane (lane % 8) * 4, registers 0-1 (rows 0-7) or 2-3 (8-15)
+    const int src = (lane & 7) * 4;
+    float v[2][4];
+#pragma unroll
+    for (int mi = 0; mi < 2; ++mi)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) v[mi][i] = __shfl_sync(0xffffffffu, res[mi][i], src);
+    const int mi = lane >> 4, hi = (lane >> 3) & 1;
+    o0 = mi ? (hi ? v[1][2] : v[1][0]) : (hi ? v[0][2] : v[0][0]);
+    o1 = mi ? (hi ? v[1][3] : v[1][1]) : (hi ? v[0][3] : v[0][1]);
+}
+
+
 }  // namespace learned
 }  // namespace taa_dev

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 #include <new>
 #include <numeric>
@@ -26,8 +27,10 @@ struct taa_mlp_trainer {
     float* m = nullptr;          // Adam moments
     float* v = nullptr;
     float* grads = nullptr;      // gradient sums, then the loss sum and the record count
+    float* partial = nullptr;    // per-CTA slabs of the same, added in CTA order
     char* blob = nullptr;
     unsigned int* status = nullptr;
+    uint32_t calls = 0;          // collections so far: the first half of each record's key
 };
 
 namespace {
@@ -107,6 +110,8 @@ int taa_mlp_trainer_create(int32_t capacity, taa_mlp_trainer** out) {
     if (e == cudaSuccess) e = cudaMalloc(&tr->m, sizeof(float) * np);
     if (e == cudaSuccess) e = cudaMalloc(&tr->v, sizeof(float) * np);
     if (e == cudaSuccess) e = cudaMalloc(&tr->grads, sizeof(float) * (np + kGradExtra));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&tr->partial, sizeof(float) * (size_t)taa_dev::learned_grad_floats() * 2 * (size_t)tr->sms);
     if (e == cudaSuccess) e = cudaMalloc(&tr->blob, (size_t)taa_dev::learned_blob_bytes());
     if (e == cudaSuccess) e = taa_dev::device_status_word(&tr->status);
     if (e == cudaSuccess) e = cudaMemset(tr->count, 0, sizeof(uint32_t));
@@ -122,7 +127,7 @@ int taa_mlp_trainer_create(int32_t capacity, taa_mlp_trainer** out) {
 int taa_mlp_trainer_destroy(taa_mlp_trainer* tr) {
     if (!tr) return TAA_OK;
     for (void* p : {tr->records, (void*)tr->count, (void*)tr->order, (void*)tr->weights, (void*)tr->m, (void*)tr->v,
-                    (void*)tr->grads, (void*)tr->blob})
+                    (void*)tr->grads, (void*)tr->partial, (void*)tr->blob})
         if (p) cudaFree(p);
     delete tr;
     return TAA_OK;
@@ -143,7 +148,9 @@ int taa_mlp_collect(taa_mlp_trainer* tr, taa_ctx* c, void* stream, const taa_fra
     const taa_dev::Img t{(const char*)truth, truth_pitch, d.out_width, d.out_height};
     cudaError_t e = taa_dev::launch_resolve_learned((int)d.history_format, d.motion_format == TAA_MOTION_RGBA16F ? 4 : 2,
                                                     true, false, c->uniforms, a, nullptr, tr->records, tr->count,
-                                                    (uint32_t)tr->capacity, seed, fraction, t, (cudaStream_t)stream);
+                                                    (uint32_t)tr->capacity, seed, tr->calls, fraction, t,
+                                                    (cudaStream_t)stream);
+    if (e == cudaSuccess) ++tr->calls;
     if (e != cudaSuccess) return cuda_fail(e, "taa_mlp_collect");
     return TAA_OK;
 }
@@ -183,7 +190,8 @@ int taa_mlp_gradients(taa_mlp_trainer* tr, const taa_mlp_weights_t* w, int32_t f
     cudaError_t e = cudaMemset(tr->grads, 0, sizeof(float) * (np + kGradExtra));
     const int grid = std::max(1, std::min((count + 127) / 128, 2 * tr->sms));
     if (e == cudaSuccess)
-        e = taa_dev::launch_mlp_train(tr->blob, tr->records, nullptr, first, count, tr->grads, tr->status, grid, nullptr);
+        e = taa_dev::launch_mlp_train(tr->blob, tr->records, nullptr, first, count, tr->grads, tr->partial, tr->status,
+                                      grid, nullptr);
     if (e == cudaSuccess) e = taa_dev::launch_mlp_map_grads(tr->grads, nullptr);
     std::vector<float> g(np + kGradExtra);
     if (e == cudaSuccess) e = cudaMemcpy(g.data(), tr->grads, sizeof(float) * g.size(), cudaMemcpyDeviceToHost);
@@ -206,19 +214,33 @@ int taa_mlp_train(taa_mlp_trainer* tr, taa_mlp_weights_t* w, int32_t steps, int3
     cudaError_t e = cudaMemset(tr->m, 0, sizeof(float) * np);
     if (e == cudaSuccess) e = cudaMemset(tr->v, 0, sizeof(float) * np);
     if (e == cudaSuccess) e = cudaMemset(tr->grads, 0, sizeof(float) * (np + kGradExtra));
-    std::vector<uint32_t> order(n);
-    std::iota(order.begin(), order.end(), 0u);
+    // The collection appends records in whatever order its CTAs run; the
+    // epochs shuffle the records' canonical order (by key) instead, so that a
+    // training run repeats bit for bit on the same collections.
+    std::vector<uint32_t> keys(2 * (size_t)n), canon(n), order(n);
+    if (e == cudaSuccess)
+        e = cudaMemcpy2D(keys.data(), 2 * sizeof(uint32_t),
+                         (const char*)tr->records + offsetof(taa_mlp_record_t, key), sizeof(taa_mlp_record_t),
+                         2 * sizeof(uint32_t), (size_t)n, cudaMemcpyDeviceToHost);
+    std::iota(canon.begin(), canon.end(), 0u);
+    std::sort(canon.begin(), canon.end(), [&](uint32_t a, uint32_t b) {
+        return keys[2 * (size_t)a] != keys[2 * (size_t)b] ? keys[2 * (size_t)a] < keys[2 * (size_t)b]
+                                                        : keys[2 * (size_t)a + 1] < keys[2 * (size_t)b + 1];
+    });
     std::mt19937_64 rng(seed);
     int pos = n;  // forces a shuffle before the first batch
     const int grid = std::max(1, std::min((batch + 127) / 128, 2 * tr->sms));
     for (int step = 1; step <= steps && e == cudaSuccess; ++step) {
         if (pos + batch > n) {
+            std::iota(order.begin(), order.end(), 0u);
             std::shuffle(order.begin(), order.end(), rng);
+            for (uint32_t& o : order) o = canon[o];
             e = cudaMemcpy(tr->order, order.data(), sizeof(uint32_t) * (size_t)n, cudaMemcpyHostToDevice);
             pos = 0;
             if (e != cudaSuccess) break;
         }
-        e = taa_dev::launch_mlp_train(tr->blob, tr->records, tr->order, pos, batch, tr->grads, tr->status, grid, nullptr);
+        e = taa_dev::launch_mlp_train(tr->blob, tr->records, tr->order, pos, batch, tr->grads, tr->partial, tr->status,
+                                      grid, nullptr);
         pos += batch;
         if (e == cudaSuccess && (step == 1 || step == steps)) {
             float lc[2];

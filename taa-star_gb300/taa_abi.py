@@ -105,7 +105,7 @@ class MlpWeights(C.Structure):
 class MlpRecord(C.Structure):
     _fields_ = [("features", C.c_uint16 * 32), ("mean", C.c_float * 3), ("sigma", C.c_float * 3),
                 ("history", C.c_float * 3), ("current", C.c_float * 3), ("truth", C.c_float * 3),
-                ("gamma", C.c_float), ("alpha_fixed", C.c_float), ("flags", C.c_uint32), ("pad", C.c_float * 2)]
+                ("gamma", C.c_float), ("alpha_fixed", C.c_float), ("flags", C.c_uint32), ("key", C.c_uint32 * 2)]
 
 
 class FxaaParams(C.Structure):
@@ -561,7 +561,7 @@ class MlpTrainer:
                     mean=f32[:, 16:19].astype(np.float64), sigma=f32[:, 19:22].astype(np.float64),
                     history=f32[:, 22:25].astype(np.float64), current=f32[:, 25:28].astype(np.float64),
                     truth=f32[:, 28:31].astype(np.float64), gamma=f32[:, 31].astype(np.float64),
-                    alpha_fixed=f32[:, 32].astype(np.float64), flags=raw.view(np.uint32)[:, 33].copy())
+                    alpha_fixed=f32[:, 32].astype(np.float64), flags=raw.view(np.uint32)[:, 33].copy(), key=raw.view(np.uint32)[:, 34:36].copy())
 
     def gradients(self, w: MlpWeights, first: int, count: int):
         g = MlpWeights()

@@ -86,6 +86,41 @@ def test_gradients_match_oracle(collected):
     assert T.device_status(clear=True) == 0
 
 
+def test_records_carry_their_keys(collected):
+    tr, n, wl = collected
+    rec = tr.records(0, n)
+    key = rec["key"].astype(np.int64)
+    # frames 1..3 were the collections that recorded; keys are unique
+    assert set(np.unique(key[:, 0])) <= {1, 2, 3}
+    assert np.all(key[:, 1] < wl.width * wl.height)
+    assert len(np.unique(key[:, 0] * wl.width * wl.height + key[:, 1])) == n
+
+
+def test_gradient_sums_repeat_bit_for_bit(collected):
+    tr, n, _ = collected
+    w = random_weights(6)
+    g0, l0 = tr.gradients(w, 0, n)
+    for _ in range(3):
+        g1, l1 = tr.gradients(w, 0, n)
+        assert l1 == l0
+        assert bytes(g1) == bytes(g0)
+
+
+def test_training_repeats_bit_for_bit(cuda):
+    """Two trainers fed the same collections (appended in whatever order the
+    collection's CTAs ran) train to the same weights bit for bit."""
+    wl = WL.small(160, 96, frames=6, seed=11)
+    out = []
+    for _ in range(2):
+        tr = T.MlpTrainer(60000)
+        LP.collect(tr, wl, 6, cuda, 0.6, skip=1, seed=5)
+        w, first, last = LP.train(tr, seed=3, steps=40, batch=2048, lr=3e-3)
+        out.append((bytes(w), first, last))
+        tr.close()
+    assert out[0] == out[1]
+    assert T.device_status(clear=True) == 0
+
+
 def test_learned_form_beats_variance_clip_on_held_out_sequence(cuda):
     tr = T.MlpTrainer(1_200_000)
     for s in (601, 602, 603):
