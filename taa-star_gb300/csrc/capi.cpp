@@ -554,11 +554,11 @@ int taa_resolve(taa_ctx* c, void* stream, const taa_frame_io_t* io) {
     if (form == TAA_FORM_LEARNED) {
         if (!c->have_mlp) return fail(TAA_E_INVAL, "taa_resolve: the learned form has no weights (taa_set_mlp)");
         if ((rc = learned_supported(d, U, io, "taa_resolve"))) return rc;
-        if (!(d.flags & TAA_FLAG_LEARNED_TCGEN05) &&
-            taa_dev::fast32_supported(U, (int)d.history_format, d.in_width, d.in_height, d.out_width, d.out_height))
-            // the benchmark mode: the strip body with the network per warp
-            e = taa_dev::launch_resolve_learned_strips(d.motion_format == TAA_MOTION_RGBA16F ? 4 : 2, U, a,
-                                                       c->mlp_blob, s);
+        const int mc = d.motion_format == TAA_MOTION_RGBA16F ? 4 : 2;
+        if (taa_dev::fast32_supported(U, (int)d.history_format, d.in_width, d.in_height, d.out_width, d.out_height))
+            // the benchmark mode: the strip body, the network per warp or on tcgen05
+            e = (d.flags & TAA_FLAG_LEARNED_TCGEN05) ? taa_dev::launch_resolve_learned_strips_tc(mc, U, a, c->mlp_blob, s)
+                                                     : taa_dev::launch_resolve_learned_strips(mc, U, a, c->mlp_blob, s);
         else
             e = taa_dev::launch_resolve_learned((int)d.history_format, d.motion_format == TAA_MOTION_RGBA16F ? 4 : 2,
                                                 false, (d.flags & TAA_FLAG_LEARNED_TCGEN05) != 0, U, a, c->mlp_blob,

@@ -145,6 +145,8 @@ cudaError_t launch_resolve_learned(int history_fmt, int motion_ch, bool collect,
 
 // The learned form's inference in the benchmark mode on the strip body
 // (resolve_learned_strips.cu); `blob` is the network's device blob.
+cudaError_t launch_resolve_learned_strips_tc(int motion_ch, const taa_uniforms_t& U, const FrameArgs& f,
+                                             const char* blob, cudaStream_t s);
 cudaError_t launch_resolve_learned_strips(int motion_ch, const taa_uniforms_t& U, const FrameArgs& a, const char* blob,
                                           cudaStream_t s);
 

@@ -93,10 +93,6 @@ template <int NB, int BLOB> struct NetSmem {
 };
 using InferSmem = NetSmem<2, Blob::INFER_BYTES>;
 
-__device__ __forceinline__ void copy_blob(char* dst, const char* src, int bytes) {
-    for (int w = threadIdx.x; w < bytes / 16; w += blockDim.x)
-        reinterpret_cast<uint4*>(dst)[w] = __ldg(reinterpret_cast<const uint4*>(src) + w);
-}
 
 // The network on the features in a[0][*]; thread t (block t / 128, row t % 128)
 // ends with its outputs.  All threads of the CTA call it.  False if a wait

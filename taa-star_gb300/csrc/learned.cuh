@@ -126,6 +126,12 @@ __device__ __forceinline__ void rectify_blend(const float (&mean)[3], const floa
     }
 }
 
+// The first `bytes` of the device blob into shared memory (16-byte words).
+__device__ __forceinline__ void copy_blob(char* dst, const char* src, int bytes) {
+    for (int w = threadIdx.x; w < bytes / 16; w += blockDim.x)
+        reinterpret_cast<uint4*>(dst)[w] = __ldg(reinterpret_cast<const uint4*>(src) + w);
+}
+
 // Writes one pixel's 32 FP16 values as row r of a canonical [128][32] A tile.
 __device__ __forceinline__ void store_row(char* tile, int r, const float (&v)[32]) {
 #pragma unroll

@@ -140,15 +140,21 @@ def test_learned_form_beats_variance_clip_on_held_out_sequence(cuda):
     assert T.device_status(clear=True) == 0
 
 
-def test_learned_paths_agree_on_one_frame(cuda):
+# the benchmark-mode parameters run on the strip body, the others (here the
+# near-clamp blend reduction, which the learned weight replaces) on the tiled body
+@pytest.mark.parametrize("extra", [{}, {"mReduceBlendNearClamp": 1}], ids=["strips", "tiled"])
+def test_learned_paths_agree_on_one_frame(cuda, extra):
     wl = WL.small(96, 64, frames=2, seed=9)
     fr = LP.render(wl, 2, cuda)
     w = random_weights(5)
+    p = wl.parameters()
+    for k, v in extra.items():
+        setattr(p, k, v)
     outs = []
     for flags in (0, T.TAA_FLAG_LEARNED_TCGEN05):
         ctx = T.Taa(96, 64, form=T.TAA_FORM_LEARNED, flags=flags)
         ctx.set_mlp(w)
-        ctx.set_uniforms(T.make_uniforms(wl.parameters(), jitter_ndc=fr.jitter[1]))
+        ctx.set_uniforms(T.make_uniforms(p, jitter_ndc=fr.jitter[1]))
         h = torch.full((64, 96, 4), float("nan"), device=cuda)
         ctx.resolve(color=fr.color[1], depth=fr.depth[1], velocity=fr.motion[1], history=fr.color[0].float(),
                     history_depth=fr.depth[0], history_out=h)
