@@ -132,7 +132,13 @@ typedef struct taa_desc_t {
 
 /* Per-frame bindings; one field pair per descriptor binding of set 0 in
  * shaders/taa.comp:24-38 (bound at source/taa.hpp:1009-1025).  Optional
- * outputs may be NULL; a NULL history reads as zeros (first frame). */
+ * outputs may be NULL; a NULL history reads as zeros (first frame).
+ * Pointers are device-accessible memory.  An output the library only
+ * writes (sharpened, debug, and result unless a two-pass sharpener reads it
+ * back) may be pinned host memory (cudaHostAlloc, or cudaHostRegister with
+ * cudaHostRegisterMapped): the kernel's stores then cross the host link
+ * directly, which saves the caller a device image and a device-to-host copy
+ * (a frame's copy-in on another stream overlaps them). */
 typedef struct taa_frame_io_t {
     const void* color;         size_t color_pitch;          /* binding  1 uCurrentFrame    */
     const void* depth;         size_t depth_pitch;          /* binding  2 uCurrentDepth    */

@@ -140,3 +140,31 @@ def test_fast_form_sequences_against_fp64(cuda, name, frames, check):
     assert max(r[1] for r in rep) <= 1e-4
     assert max(r[2] for r in rep) <= 1e-4
     assert min(r[3] for r in rep) >= 50.0
+
+
+@pytest.mark.parametrize("form", [T.TAA_FORM_FAST, T.TAA_FORM_TILED], ids=["fast", "tiled"])
+def test_result_in_pinned_host_memory(cuda, form):
+    """The result binding may be pinned host memory: the kernel's stores cross
+    the host link and give the same bits as a device image."""
+    wl = WL.small(200, 120, frames=2, seed=21)
+    sc = wl.scene()
+    H, W = wl.height, wl.width
+    col = torch.empty(2, H, W, 4, dtype=torch.float16, device=cuda)
+    dep = torch.empty(2, H, W, device=cuda)
+    mot = torch.empty(2, H, W, 2, dtype=torch.float16, device=cuda)
+    for f in range(2):
+        T.synth_render(sc, f, color=col[f], depth=dep[f], motion=mot[f])
+    ctx = T.Taa(W, H, form=form)
+    ctx.set_uniforms(T.make_uniforms(wl.parameters(), jitter_ndc=T.synth_jitter(sc, 1)[1]))
+    hist = col[0].float()
+    host = torch.full((H, W, 4), float("nan"), dtype=torch.float16).pin_memory()
+    dev_res = torch.full((H, W, 4), float("nan"), dtype=torch.float16, device=cuda)
+    outs = []
+    for res in (host, dev_res):
+        h = torch.empty(H, W, 4, device=cuda)
+        ctx.resolve(color=col[1], depth=dep[1], velocity=mot[1], history=hist, history_depth=dep[0], history_out=h,
+                    result=res)
+        torch.cuda.synchronize()
+        outs.append(res.cpu())
+    ctx.close()
+    assert torch.equal(outs[0], outs[1]) and not torch.isnan(outs[0]).any()
