@@ -95,15 +95,19 @@ typedef enum taa_status {
  * relative L2 on the benchmark scenes, 64-frame chains included (up to
  * 8.6e-3 without); the form runs slower. */
 #define TAA_FLAG_FP16_GUARD 0x4u
-/* taa_desc_t.flags, with a sharpener and the tiled FP32 form: one launch
- * resolves each tile and the 1-pixel ring around it (recomputing what the
- * neighbouring tiles resolve, bit for bit) and sharpens the tile from shared
- * memory, so the unsharpened image never reaches device memory.  Without the
- * flag the tiled and FP16 forms launch the resolve, which writes the RGBA16F
- * result image, and then the sharpen pass on it, as the reference dispatches
- * taa.comp and then the sharpener (source/taa.hpp:1027, 1111-1139): the
- * resolve kernels are bound by instruction issue, not by memory, and the
- * ring's recomputation costs more than the result image's round trip. */
+/* taa_desc_t.flags, with a sharpener: one launch resolves each tile and the
+ * 1-pixel ring around it (recomputing what the neighbouring tiles resolve,
+ * bit for bit) and sharpens the tile from shared memory, so the unsharpened
+ * image never reaches device memory.  In TAA_FORM_FAST (and AUTO where it
+ * selects it) the tiles are 30x14 outputs of 32x16 strip-body regions, and
+ * the three images carry the two-pass fast form's bits; in TAA_FORM_TILED
+ * the exact form's.  Without the flag the forms launch the resolve, which
+ * writes the RGBA16F result image, and then the sharpen pass on it, as the
+ * reference dispatches taa.comp and then the sharpener (source/taa.hpp:1027,
+ * 1111-1139).  On 2560x1440 with CAS the fused fast form takes 58 us a frame
+ * with bilinear history (two passes: 61 us) and 74 us with Catmull-Rom (two
+ * passes: 71 us): the ring's 22% more resolves against the result image's
+ * round trip. */
 #define TAA_FLAG_FUSED_SHARPEN 0x8u
 /* Sharpener (taa<CF>::mSharpener, source/taa.hpp:1418). */
 #define TAA_SHARPEN_OFF     0u

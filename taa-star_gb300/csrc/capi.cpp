@@ -525,7 +525,7 @@ static int select_form(const taa_ctx* c, const taa_frame_io_t* io) {
     // a debug binding: the tiled FP32 form writes it (the fused sharpener does not)
     if (io && io->debug) return fused ? TAA_FORM_PLAIN : TAA_FORM_TILED;
     if (d.form == TAA_FORM_FP16 && !fused) return TAA_FORM_FP16;
-    if ((d.form == TAA_FORM_AUTO || d.form == TAA_FORM_FAST) && !fused &&
+    if ((d.form == TAA_FORM_AUTO || d.form == TAA_FORM_FAST) &&
         taa_dev::fast32_supported(c->uniforms, (int)d.history_format, d.in_width, d.in_height, d.out_width,
                                   d.out_height))
         return TAA_FORM_FAST;
@@ -572,7 +572,9 @@ int taa_resolve(taa_ctx* c, void* stream, const taa_frame_io_t* io) {
         // without TAA_FLAG_FUSED_SHARPEN a sharpener reads the RGBA16F result
         // image the resolve writes (the caller's, or the context's)
         if (sharpen && !fused_sharpen(d) && !a.result.p) a.result = ImgW{(char*)c->scratch_screen, c->scratch_pitch};
-        if (form == TAA_FORM_FAST) {
+        if (form == TAA_FORM_FAST && fused_sharpen(d)) {
+            e = taa_dev::launch_resolve_fast32_sharpen(mc, (int)d.sharpener, U, a, s);
+        } else if (form == TAA_FORM_FAST) {
             e = taa_dev::launch_resolve_fast32(mc, U, a, s);
             if (e == cudaSuccess && sharpen) e = taa_dev::launch_sharpen((int)d.sharpener, a, s);
         } else if (form == TAA_FORM_FP16) {

@@ -40,6 +40,10 @@ bool up_path_supported(const taa_uniforms_t& U, int in_w, int in_h, int out_w, i
 // it runs these parameters, sizes and history format, and its launch.
 bool fast32_supported(const taa_uniforms_t& U, int history_fmt, int in_w, int in_h, int out_w, int out_h);
 cudaError_t launch_resolve_fast32(int motion_ch, const taa_uniforms_t& U, const FrameArgs& a, cudaStream_t stream);
+// TAA_FORM_FAST and the sharpener (TAA_SHARPEN_SIMPLE or TAA_SHARPEN_CAS) in
+// one launch: result (if bound), history and sharpened as the two-pass form.
+cudaError_t launch_resolve_fast32_sharpen(int motion_ch, int sharpener, const taa_uniforms_t& U, const FrameArgs& f,
+                                          cudaStream_t s);
 // The same tile body over many views (resolve_fast32.cu): the history window
 // (texels) its 2-D tensor maps cover, its occupancy and its launch (the batch
 // arguments as for launch_batch, one CTA of 128 threads per 32x16 tile).

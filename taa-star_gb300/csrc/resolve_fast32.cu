@@ -1,5 +1,6 @@
 // resolve_fast32.cu - TAA_FORM_FAST: the strip body (strip_body.cuh) with the
-// FP32 policy, for one view (launch_resolve_fast32) and for many views in one
+// FP32 policy, for one view (launch_resolve_fast32), for one view with a
+// fused sharpener (launch_resolve_fast32_sharpen) and for many views in one
 // launch (launch_fast32_batch, the batch's tile shape 5).
 #include <cstring>
 
@@ -29,6 +30,36 @@ cudaError_t launch_resolve_fast32(int motion_ch, const taa_uniforms_t& U, const 
         else resolve_strips<F32Pol, 0, 2><<<grid, NT, 0, s>>>(a, map, tma_ok);
     }
     return cudaGetLastError();
+}
+
+cudaError_t launch_resolve_fast32_sharpen(int motion_ch, int sharpener, const taa_uniforms_t& U, const FrameArgs& f,
+                                          cudaStream_t s) {
+    using namespace fast32;
+    const taa_parameters_t& P = U.param[0];
+    const Args a = make_args(U, f);
+    CUtensorMap map;
+    std::memset(&map, 0, sizeof map);
+    const int tma_ok = a.hist && f.history.w >= WW && f.history.h >= WH &&
+                       encode_history_map(f.history, TAA_FAST_TMA2D ? 2 : 0, WW, WH, &map);
+    const bool cas = sharpener == TAA_SHARPEN_CAS;
+    float peak;
+    std::memcpy(&peak, &f.cas_peak_bits, sizeof peak);
+    const float k = cas ? peak : f.sharpen_factor;
+    char* const sp = f.sharpened.p;
+    const uint32_t pitch = (uint32_t)f.sharpened.pitch;
+    // 30x14 output tiles, each resolved with its 1-pixel ring
+    const dim3 grid((a.W + TX - 3) / (TX - 2), (a.H + TY - 3) / (TY - 2));
+    auto go = [&](auto kernel) {
+        kernel<<<grid, NT, 0, s>>>(a, map, tma_ok, sp, pitch, k);
+        return cudaGetLastError();
+    };
+    const bool cr = P.mInterpolationMode == 2, m4 = motion_ch == 4;
+    if (cas) {
+        if (cr) return m4 ? go(resolve_strips_sharpen<2, 2, 4>) : go(resolve_strips_sharpen<2, 2, 2>);
+        return m4 ? go(resolve_strips_sharpen<2, 0, 4>) : go(resolve_strips_sharpen<2, 0, 2>);
+    }
+    if (cr) return m4 ? go(resolve_strips_sharpen<1, 2, 4>) : go(resolve_strips_sharpen<1, 2, 2>);
+    return m4 ? go(resolve_strips_sharpen<1, 0, 4>) : go(resolve_strips_sharpen<1, 0, 2>);
 }
 
 void fast32_window(int* w, int* h) {

@@ -49,6 +49,7 @@
 #include <cstring>
 
 #include "kernels.h"
+#include "sharpen.cuh"
 #include "tiled_skeleton.cuh"
 
 namespace taa_dev {
@@ -202,8 +203,9 @@ __device__ __forceinline__ float3 ycocg(uint2 raw) {
 // history moves to m + (h - m) / ma when ma > 1), the blend with the current
 // colour (taa.comp:848-900: mix(history, current, alpha)), the conversion
 // back to RGB and the stores of the history (alpha 0) and the screen.
-__device__ __forceinline__ void clip_blend_store(const Args& a, int x, int y, const float hc[3], const float m[3],
-                                                 float ma, const float cur[3], float alpha) {
+// The clipped, blended colour in RGB: (r, g, b, 0).
+__device__ __forceinline__ float4 clip_blend(const float hc[3], const float m[3], float ma, const float cur[3],
+                                             float alpha) {
     const float sc = ma > 1.0f ? rcp_approx(ma) : 1.0f;
     float o[3];
 #pragma unroll
@@ -212,9 +214,15 @@ __device__ __forceinline__ void clip_blend_store(const Args& a, int x, int y, co
         o[c] = fmaf(alpha, cur[c] - hcl, hcl);
     }
     const float tmp = o[0] - o[2];
-    const float rr = tmp + o[1], g = o[0] + o[2], bl = tmp - o[1];
-    *at_w<float4>(a.hout, a.hout_pitch, x, y) = make_float4(rr, g, bl, 0.f);
-    if (a.result) *at_w<uint2>(a.result, a.result_pitch, x, y) = float4_to_half4(make_float4(rr, g, bl, 1.0f));
+    return make_float4(tmp + o[1], o[0] + o[2], tmp - o[1], 0.f);
+}
+__device__ __forceinline__ void store_out(const Args& a, int x, int y, float4 o) {
+    *at_w<float4>(a.hout, a.hout_pitch, x, y) = o;
+    if (a.result) *at_w<uint2>(a.result, a.result_pitch, x, y) = float4_to_half4(make_float4(o.x, o.y, o.z, 1.0f));
+}
+__device__ __forceinline__ void clip_blend_store(const Args& a, int x, int y, const float hc[3], const float m[3],
+                                                 float ma, const float cur[3], float alpha) {
+    store_out(a, x, y, clip_blend(hc, m, ma, cur, alpha));
 }
 // The history sample in YCoCg (taa.comp:158-164).
 __device__ __forceinline__ void hist_ycocg(float3 h, float hc[3]) {
@@ -334,6 +342,10 @@ template <int INTERP> __device__ __forceinline__ void axis_weights(float f, floa
     }
 }
 // The first tap of an axis and its fraction: it = position * size.
+// `it` is the texel-space position, a separately rounded product (__fmul_rn:
+// a product the compiler contracted into the subtraction below would round
+// the fraction differently from taps_of's, and a pixel's history sample would
+// depend on whether its strip takes the shared-row path).
 template <int INTERP> __device__ __forceinline__ int axis_first(float it, float& f) {
     const float b = floorf(it - 0.5f);
     f = it + (-0.5f - b);
@@ -353,7 +365,11 @@ struct PixelInfo {
     float u, v[NPX], hu[NPX], hv[NPX], ehd[NPX], pd[NPX];
 };
 
-template <class Pol, int INTERP, int MC, bool PERSIST>
+// ORIGIN: (tile_x, tile_y) is the pixel origin of the 32x16 region, which
+// may start at -1 (a fused sharpener resolves a ring around its output);
+// loads are then edge-clamped on every side and the policy chooses what it
+// stores.
+template <class Pol, int INTERP, int MC, bool PERSIST, bool ORIGIN = false>
 __device__ __forceinline__ void strip_tile(const Args& a, const CUtensorMap* hmap, int tma_ok, int tile_x,
                                            int tile_y, SmemT<typename Pol::Staged>& sm, uint32_t& phase,
                                            typename Pol::Ctx& ctx) {
@@ -361,8 +377,10 @@ __device__ __forceinline__ void strip_tile(const Args& a, const CUtensorMap* hma
     constexpr int SPAN = INTERP == 2 ? 4 : 2;
     const int tid = threadIdx.x, lx = tid & 31, sy = tid >> 5;
     const int W = a.W, H = a.H;
-    const int x0 = tile_x * TX, y0 = tile_y * TY;
-    const int x = x0 + lx, cx = min(x, W - 1);
+    const int x0 = ORIGIN ? tile_x : tile_x * TX, y0 = ORIGIN ? tile_y : tile_y * TY;
+    // a pixel's loads at edge-clamped coordinates
+    auto crow = [&](int y) { return ORIGIN ? clampi(y, 0, H - 1) : min(y, H - 1); };
+    const int x = x0 + lx, cx = ORIGIN ? clampi(x, 0, W - 1) : min(x, W - 1);
     const int ya = y0 + NPX * sy;  // the strip's first row
     const bool have_hist = a.hist != nullptr;
 
@@ -371,7 +389,7 @@ __device__ __forceinline__ void strip_tile(const Args& a, const CUtensorMap* hma
     RawVel vraw[NPX];
 #pragma unroll
     for (int k = 0; k < NPX; ++k) {
-        const int cy = min(ya + k, H - 1);
+        const int cy = crow(ya + k);
         dep[k] = __ldg(at<float>(a.depth, a.depth_pitch, cx, cy));
         vraw[k] = __ldg(at<RawVel>(a.vel, a.vel_pitch, cx, cy));
     }
@@ -396,7 +414,7 @@ __device__ __forceinline__ void strip_tile(const Args& a, const CUtensorMap* hma
 #pragma unroll
     for (int k = 0; k < NPX; ++k) {
         const float4 vel = tiled::velocity_of<MC>(vraw[k]);
-        px.v[k] = div_const_rn((float)min(ya + k, H - 1) + 0.5f, (float)H, a.inv_h);
+        px.v[k] = div_const_rn((float)crow(ya + k) + 0.5f, (float)H, a.inv_h);
         hu[k] = px.u - vel.x;
         hv[k] = px.v[k] - vel.y;
         ehd[k] = dep[k] - vel.z;
@@ -409,9 +427,9 @@ __device__ __forceinline__ void strip_tile(const Args& a, const CUtensorMap* hma
     //    (its own pixel's taps widened by the tile and MARGIN) and starts the copy
     if (tid == REF_TID && have_hist) {
         float f;
-        const int rux = axis_first<INTERP>(hu[0] * (float)W, f);
-        const int ruy = axis_first<INTERP>(hv[0] * (float)H, f);
-        const int wx0 = rux - (cx - x0) - MARGIN, wy0 = ruy - (min(ya, H - 1) - y0) - MARGIN;
+        const int rux = axis_first<INTERP>(__fmul_rn(hu[0], (float)W), f);
+        const int ruy = axis_first<INTERP>(__fmul_rn(hv[0], (float)H), f);
+        const int wx0 = rux - (cx - x0) - MARGIN, wy0 = ruy - (crow(ya) - y0) - MARGIN;
         const bool interior = wx0 >= 0 && wy0 >= 0 && wx0 <= W - WW && wy0 <= H - WH;
         const int mode = tma_ok && interior ? 1 : 2;
         sm.org[0] = wx0;
@@ -478,12 +496,12 @@ __device__ __forceinline__ void strip_tile(const Args& a, const CUtensorMap* hma
     for (int k = 0; k < NPX; ++k) h[k] = make_float3(0.f, 0.f, 0.f);
     if (have_hist && landed) {
         float fx, fy[NPX];
-        const int ux = axis_first<INTERP>(hu[0] * (float)W, fx);
+        const int ux = axis_first<INTERP>(__fmul_rn(hu[0], (float)W), fx);
         int uy[NPX];
         bool coherent = true;
 #pragma unroll
         for (int k = 0; k < NPX; ++k) {
-            uy[k] = axis_first<INTERP>(hv[k] * (float)H, fy[k]);
+            uy[k] = axis_first<INTERP>(__fmul_rn(hv[k], (float)H), fy[k]);
             coherent = coherent && __float_as_uint(hu[k]) == __float_as_uint(hu[0]) && uy[k] == uy[0] + k;
         }
         const int bx = ux - wx0, by = uy[0] - wy0;
@@ -564,19 +582,107 @@ struct F32Pol {
             r1 = r2;
             const int y = ya + k;
             if (!(x < a.W && y < a.H && landed)) continue;
-            const Box b = box_of(s, a.gamma);
-            float hc[3];
-            hist_ycocg(h[k], hc);
-            float ma = 0.f;
+            store_out(a, x, y, pixel(a, s, h[k], (rej >> k) & 1u, &sp[(k + 1) * SX + 1]));
+        }
+    }
+    // one pixel: the box from its 3x3 moments s, the clip of its history
+    // sample h, the blend with its staged colour at c
+    static __device__ __forceinline__ float4 pixel(const Args& a, const Row& s, float3 h, bool rejected,
+                                                   const float4* c) {
+        const Box b = box_of(s, a.gamma);
+        float hc[3];
+        hist_ycocg(h, hc);
+        float ma = 0.f;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) ma = fmaxf(ma, fabsf(hc[c] - b.m[c]) * rcp_approx(b.e[c]));
-            const float alpha = a.reset ? 1.0f : ((rej >> k) & 1u ? a.rejection_alpha : a.alpha);
-            const float4 c0 = lds128(&sp[(k + 1) * SX + 1]);
-            const float cur[3] = {c0.x, c0.y, c0.z};
-            clip_blend_store(a, x, y, hc, b.m, ma, cur, alpha);
+        for (int ch = 0; ch < 3; ++ch) ma = fmaxf(ma, fabsf(hc[ch] - b.m[ch]) * rcp_approx(b.e[ch]));
+        const float alpha = a.reset ? 1.0f : (rejected ? a.rejection_alpha : a.alpha);
+        const float4 c0 = lds128(c);
+        const float cur[3] = {c0.x, c0.y, c0.z};
+        return clip_blend(hc, b.m, ma, cur, alpha);
+    }
+};
+
+// TAA_FORM_FAST with a fused sharpener (TAA_FLAG_FUSED_SHARPEN): the strip
+// body in RING mode resolves a 32x16 region around a 30x14 output tile, keeps
+// the FP16-rounded screen colour of the whole region (what the two-pass form's
+// sharpen pass reads back from the result image) over the dead history
+// window, and sharpens the tile from there.  Each interior pixel is the value
+// the two-pass form computes for it (the same arithmetic on the same inputs;
+// the sharpeners round every operation), so the outputs are its bits.
+// The ring costs 512 / 420 = 1.22x the resolves.  A CTA that sweeps a column
+// of regions (each row resolved once, two rows carried in shared memory) cut
+// that to 1.07x but ran 13% slower: its steps serialise each region's loads
+// behind the previous region's arithmetic.
+template <int SHARPEN>  // TAA_SHARPEN_SIMPLE or TAA_SHARPEN_CAS
+struct FusedF32Pol {
+    using Staged = float4;
+    struct Ctx {
+        uint2* screen;   // [TY][TX] RGBA16F region colour, over the window
+        char* sharp;     // RGBA16F output
+        uint32_t sharp_pitch;
+        float k;         // CAS peak, or the simple sharpener's factor
+    };
+    static __device__ __forceinline__ float4 stage(uint2 raw) { return F32Pol::stage(raw); }
+    static __device__ __forceinline__ void finish(const Args& a, const float4* sp, int x, int ya, const float3 h[NPX],
+                                                  unsigned rej, bool landed, const PixelInfo&, Ctx& ctx) {
+        const int lx = threadIdx.x & 31, row0 = NPX * (threadIdx.x >> 5);
+        // x0 = x - lx >= -1: lx >= 1 puts x inside the image's left edge
+        const bool col_in = lx >= 1 && lx <= TX - 2 && x < a.W;
+        uint2 scr[NPX];
+        Row r0 = row_sums(sp), r1 = row_sums(sp + SX);
+#pragma unroll
+        for (int k = 0; k < NPX; ++k) {
+            const Row r2 = row_sums(sp + (k + 2) * SX);
+            const Row s = add(add(r0, r1), r2);
+            r0 = r1;
+            r1 = r2;
+            // every pixel of the region (ring and outside pixels from edge-clamped loads)
+            const float4 o = F32Pol::pixel(a, s, h[k], (rej >> k) & 1u, &sp[(k + 1) * SX + 1]);
+            scr[k] = float4_to_half4(make_float4(o.x, o.y, o.z, 1.0f));
+            const int row = row0 + k, y = ya + k;
+            if (col_in && row >= 1 && row <= TY - 2 && y < a.H && landed) store_out(a, x, y, o);
+        }
+        __syncthreads();  // every thread is done with the window the screen overlays
+#pragma unroll
+        for (int k = 0; k < NPX; ++k) ctx.screen[(row0 + k) * TX + lx] = scr[k];
+        __syncthreads();
+        if (!ctx.sharp || !col_in || !landed) return;
+        const int x0 = x - lx, y0 = ya - row0;
+        auto at = [&](int gx, int gy) {
+            const uint2 v = ctx.screen[(clampi(gy, 0, a.H - 1) - y0) * TX + (clampi(gx, 0, a.W - 1) - x0)];
+            const float4 c = half4_to_float4(v);
+            return make_float3(c.x, c.y, c.z);
+        };
+#pragma unroll
+        for (int k = 0; k < NPX; ++k) {
+            const int row = row0 + k, y = ya + k;
+            if (row < 1 || row > TY - 2 || y >= a.H) continue;
+            float3 r;
+            if (SHARPEN == 2)
+                r = cas_pixel(at(x, y - 1), at(x - 1, y), at(x, y), at(x + 1, y), at(x, y + 1), ctx.k);
+            else
+                r = simple_sharpen_pixel(at(x - 1, y), at(x + 1, y), at(x, y - 1), at(x, y + 1), at(x, y), ctx.k);
+            *at_w<uint2>(ctx.sharp, ctx.sharp_pitch, x, y) = float4_to_half4(make_float4(r.x, r.y, r.z, 1.0f));
         }
     }
 };
+static_assert(sizeof(float4) * WW * WH >= sizeof(uint2) * TX * TY, "the screen fits over the window");
+
+// Resident CTAs per SM the fused kernel's register budget is sized for (a tuning constant).
+#ifndef TAA_FUSED_MIN_BLOCKS
+#define TAA_FUSED_MIN_BLOCKS 7
+#endif
+template <int SHARPEN, int INTERP, int MC>
+__global__ void __launch_bounds__(NT, TAA_FUSED_MIN_BLOCKS)
+    resolve_strips_sharpen(const Args a, const __grid_constant__ CUtensorMap hmap, const int tma_ok, char* sharp,
+                           uint32_t sharp_pitch, float k) {
+    __shared__ SmemT<float4> sm;
+    uint32_t phase = 0;
+    typename FusedF32Pol<SHARPEN>::Ctx ctx{reinterpret_cast<uint2*>(sm.win), sharp, sharp_pitch, k};
+    strip_tile<FusedF32Pol<SHARPEN>, INTERP, MC, false, true>(a, &hmap, tma_ok, (int)blockIdx.x * (TX - 2) - 1,
+                                                              (int)blockIdx.y * (TY - 2) - 1, sm, phase, ctx);
+}
+
 
 // One view, one CTA per tile.
 template <class Pol, int INTERP, int MC>

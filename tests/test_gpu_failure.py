@@ -152,3 +152,35 @@ def test_batch_cta_stops_after_a_wait_gave_up(cuda, give_up, shape):
         np.testing.assert_array_equal(f[0][ok], n[0][ok])
         np.testing.assert_array_equal(f[1][ok], n[1][ok])
     batch.close()
+
+
+def test_fused_sharpen_window_wait_gives_up(cuda):
+    """The fast form's fused sharpener (30x14 tiles with their ring) leaves a
+    tile whose wait gave up unwritten in all three images."""
+    u, b = inputs(cuda)
+    ctx = T.Taa(W, H, form=T.TAA_FORM_FAST, sharpener=T.TAA_SHARPEN_CAS, flags=T.TAA_FLAG_FUSED_SHARPEN)
+    ctx.set_uniforms(u)
+    assert ctx.selected_form() == T.TAA_FORM_FAST
+
+    def go():
+        o = outputs(cuda)
+        o["sharpened"] = torch.full((H, W, 4), float("nan"), dtype=torch.float16, device=cuda)
+        ctx.resolve(**b, **o)
+        torch.cuda.synchronize()
+        return [o[k].float().cpu().numpy() for k in ("history_out", "result", "sharpened")]
+
+    T.device_status(clear=True)
+    normal = go()
+    assert T.device_status(clear=True) == 0 and not np.isnan(normal[2]).any()
+    T.set_window_wait(0)
+    try:
+        failed = go()
+        assert T.device_status(clear=True) & T.TAA_DEVICE_WINDOW_TIMEOUT
+    finally:
+        T.set_window_wait(None)
+    unwritten = np.isnan(failed[0][..., 0])
+    assert unwritten.any() and (~unwritten).any()
+    for n, f in zip(normal, failed):
+        assert np.all(np.isnan(f[unwritten]))
+        np.testing.assert_array_equal(f[~unwritten], n[~unwritten])
+    ctx.close()

@@ -168,3 +168,44 @@ def test_result_in_pinned_host_memory(cuda, form):
         outs.append(res.cpu())
     ctx.close()
     assert torch.equal(outs[0], outs[1]) and not torch.isnan(outs[0]).any()
+
+
+@pytest.mark.parametrize("size", [(200, 120), (61, 37), (256, 160)], ids=lambda s: f"{s[0]}x{s[1]}")
+@pytest.mark.parametrize("interp", [2, 0], ids=["catmull_rom", "bilinear"])
+@pytest.mark.parametrize("sharpener", [T.TAA_SHARPEN_CAS, T.TAA_SHARPEN_SIMPLE], ids=["cas", "simple"])
+def test_fused_sharpen_equals_two_passes(cuda, size, interp, sharpener):
+    """TAA_FLAG_FUSED_SHARPEN on the fast form (one launch, each 30x14 tile
+    resolved with its ring) gives the two-pass form's bits: history, result
+    and sharpened image, over a 4-frame chain."""
+    W, H = size
+    wl = WL.small(W, H, frames=4, seed=23, params=dict(mInterpolationMode=interp))
+    sc = wl.scene()
+    F = 4
+    col = torch.empty(F, H, W, 4, dtype=torch.float16, device=cuda)
+    dep = torch.empty(F, H, W, device=cuda)
+    mot = torch.empty(F, H, W, 2, dtype=torch.float16, device=cuda)
+    for f in range(F):
+        T.synth_render(sc, f, color=col[f], depth=dep[f], motion=mot[f])
+    outs = []
+    for flags in (0, T.TAA_FLAG_FUSED_SHARPEN):
+        ctx = T.Taa(W, H, form=T.TAA_FORM_AUTO, sharpener=sharpener, sharpen_factor=0.5, flags=flags)
+        hist = [torch.zeros(H, W, 4, device=cuda) for _ in range(2)]
+        frames = []
+        for f in range(F):
+            ctx.set_uniforms(T.make_uniforms(wl.parameters(), jitter_ndc=T.synth_jitter(sc, f)[1],
+                                             mResetHistory=1 if f == 0 else 0))
+            assert ctx.selected_form() == T.TAA_FORM_FAST
+            res = torch.full((H, W, 4), float("nan"), dtype=torch.float16, device=cuda)
+            shp = torch.full((H, W, 4), float("nan"), dtype=torch.float16, device=cuda)
+            ctx.resolve(color=col[f], depth=dep[f], velocity=mot[f], history=hist[f & 1],
+                        history_depth=dep[f - 1] if f else dep[0], history_out=hist[(f + 1) & 1], result=res,
+                        sharpened=shp)
+            torch.cuda.synchronize()
+            frames.append((hist[(f + 1) & 1][..., :3].clone(), res.clone(), shp.clone()))
+        outs.append(frames)
+        ctx.close()
+    for f in range(F):
+        for two, one, name in zip(outs[0][f], outs[1][f], ("history", "result", "sharpened")):
+            assert not torch.isnan(one).any(), (f, name)
+            assert torch.equal(two, one), (f, name, float((two.float() - one.float()).abs().max()))
+    assert T.device_status(clear=True) == 0
