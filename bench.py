@@ -500,11 +500,11 @@ def time_c3(T, WL, dev, stream, sid, args, peak):
     (2560x1440, 32 frames, spinning spheres), bilinear and Catmull-Rom history.
     Per history filter and form: the resolve followed by the sharpen pass on
     its RGBA16F result (the library's default, and the reference's structure
-    of two dispatches, taa.hpp:1027 and 1111-1139) in the FP16, tiled FP32 and
-    plain forms, and the tiled FP32 form's single launch that resolves each
-    tile with a 1-pixel ring and sharpens it from shared memory
-    (TAA_FLAG_FUSED_SHARPEN); last the tiled resolve alone (result image, no
-    sharpener), which prices the sharpen pass.  A step is the 32-frame sequence; 1 warm-up
+    of two dispatches, taa.hpp:1027 and 1111-1139) in the FP16, fast FP32,
+    exact tiled FP32 and plain forms, and the fast and exact forms' single
+    launch that resolves each tile with a 1-pixel ring and sharpens it from
+    shared memory (TAA_FLAG_FUSED_SHARPEN); last the fast resolve alone
+    (result image, no sharpener), which prices the sharpen pass.  A step is the 32-frame sequence; 1 warm-up
     step, 3 timed.  Bytes per pixel: 56 for one launch (colour 8, depth 4,
     motion 4, history 16 + 16, sharpened 8); two add the result image, written
     and read back (72)."""
@@ -535,11 +535,14 @@ def time_c3(T, WL, dev, stream, sid, args, peak):
                             history_depth=dep[f - 1] if f else dep[0], history_out=hist[(f + 1) & 1], **out_img)
 
         cas = dict(sharpener=T.TAA_SHARPEN_CAS, sharpen_factor=0.5)
+        fused = T.TAA_FLAG_FUSED_SHARPEN
         variants = (("fp16_then_cas", dict(form=T.TAA_FORM_FP16, **cas), 72),
-                    ("tiled_then_cas", dict(form=T.TAA_FORM_AUTO, **cas), 72),
-                    ("tiled_fused_cas", dict(form=T.TAA_FORM_AUTO, flags=T.TAA_FLAG_FUSED_SHARPEN, **cas), 56),
+                    ("fast_then_cas", dict(form=T.TAA_FORM_AUTO, **cas), 72),
+                    ("fast_fused_cas", dict(form=T.TAA_FORM_AUTO, flags=fused, **cas), 56),
+                    ("tiled_exact_then_cas", dict(form=T.TAA_FORM_TILED, **cas), 72),
+                    ("tiled_exact_fused_cas", dict(form=T.TAA_FORM_TILED, flags=fused, **cas), 56),
                     ("plain_then_cas", dict(form=T.TAA_FORM_PLAIN, **cas), 72),
-                    ("tiled_no_sharpener", dict(form=T.TAA_FORM_AUTO), 56))
+                    ("fast_no_sharpener", dict(form=T.TAA_FORM_AUTO), 56))
         res_i = {}
         for name, kw, bpp in variants:
             ctx = T.Taa(W, H, **kw)
@@ -648,7 +651,8 @@ def summarize(form_name, mpx, frac, forms, e2e, cpu):
         out["batch48_per_pixel_vs_single"] = b["per_pixel_vs_single_4k"]
     ln = f.get("learned")
     if ln:
-        out.update(learned_cost_vs_plain=ln["cost_vs_plain"], learned_gain_db=ln["gain_db"],
+        out.update(learned_cost_vs_plain=ln["cost_vs_plain"], learned_cost_vs_fast=ln.get("cost_vs_fast"),
+                   learned_gain_db=ln["gain_db"],
                    learned_max_abs_err=ln["max_abs_err"], plain_max_abs_err=ln["plain_max_abs_err"])
     c3 = f.get("c3_cas")
     if c3:
