@@ -717,15 +717,22 @@ def run_ours(args):
         c.set_uniforms(uniforms[1])
         return c
 
-    def sequence(ctx):
+    def sequence(ctx, s=sid):
         for f in range(F):
             ctx.set_uniforms(uniforms[f])
-            ctx.resolve(stream=sid, color=col[f], depth=dep[f], velocity=mot[f], history=hist[f & 1],
+            ctx.resolve(stream=s, color=col[f], depth=dep[f], velocity=mot[f], history=hist[f & 1],
                         history_depth=dep[f - 1] if f else dep[0], history_out=hist[(f + 1) & 1], result=res)
 
     def timed(ctx, steps, warmup, sampler=None):
+        """A step is the 64-frame sequence, captured once in a CUDA graph and
+        replayed (the launches a renderer would record per frame, without the
+        host's per-launch cost)."""
+        gs = torch.cuda.Stream(dev)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=gs):
+            sequence(ctx, gs.cuda_stream)
         for _ in range(warmup):
-            sequence(ctx)
+            graph.replay()
         torch.cuda.synchronize()
         if world > 1:
             dist.barrier()
@@ -735,11 +742,12 @@ def run_ours(args):
             sampler.__enter__()
         e0.record(stream)
         for _ in range(steps):
-            sequence(ctx)
+            graph.replay()
         e1.record(stream)
         torch.cuda.synchronize()
         if sampler:
             sampler.__exit__(None, None, None)
+        del graph
         ms = max_over_ranks(e0.elapsed_time(e1), world, dev)
         if world > 1:
             dist.barrier()
@@ -889,6 +897,7 @@ def run_ours(args):
             "config": {"workload": wl.name, "width": W, "height": H, "frames_per_step": F, "form": form_name,
                        "history": "RGBA32F", "motion": "RG16F", "bytes_per_px": bpp,
                        "l2": "no flush: each frame's inputs (500 MB) exceed the 129 MB L2",
+                       "timed": "CUDA graph of the 64-frame sequence, replayed once per step",
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
