@@ -91,9 +91,10 @@ typedef enum taa_status {
 /* taa_desc_t.flags, with TAA_FORM_FP16: a pixel whose clip toward the box
  * centre engages on a box that FP16 cannot resolve (its tightest channel 16
  * times narrower than its widest, as next to a firefly) is finished in FP32
- * from its source texels.  Frame error against the FP64 oracle below 1e-3
- * relative L2 on the benchmark scenes, 64-frame chains included (up to
- * 8.6e-3 without); the form runs slower. */
+ * from its source texels.  Frame error of one resolve against the FP64
+ * oracle below 1e-3 relative L2 on the benchmark scenes (up to 8.6e-3
+ * without); a free-running 64-frame 4K chain reaches 1.06e-3 at its last
+ * frame.  The form runs slower. */
 #define TAA_FLAG_FP16_GUARD 0x4u
 /* taa_desc_t.flags, with a sharpener: one launch resolves each tile and the
  * 1-pixel ring around it (recomputing what the neighbouring tiles resolve,
