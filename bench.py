@@ -155,6 +155,15 @@ C2_SCENE = dict(width=3840, height=2160, seed=2, num_spheres=128, cam_v0=(2.0, 0
 C2_NAME = "C2 3840x2160x64 depth+velocity rejection"
 
 
+def c2_config(world: int) -> dict:
+    """The workload both arms run (the same dict on both lines)."""
+    return {"workload": C2_NAME, "width": 3840, "height": 2160, "frames": 64,
+            "mode": "Catmull-Rom, YCoCg variance clip gamma 1, clip-fast, alpha 0.1, depth culling, reject outside",
+            "history": "RGBA32F", "motion": "RG16F", "bytes_per_px": 60,
+            "l2": "no flush: each frame's inputs (500 MB) exceed the 129 MB L2",
+            "parallelism": f"replicas x{world}"}
+
+
 def reference_c2():
     """The C2 workload (workloads.c2()) from the oracle's helpers: its scene and
     parameter block (Catmull-Rom, YCoCg variance clip gamma 1, clip-fast,
@@ -222,8 +231,8 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": mpx, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t / done * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded analytic scene, rendered on the host)",
-        "config": {"workload": C2_NAME, "width": sc.width, "height": sc.height, "frames_per_step": 1,
-                   "mode": "Catmull-Rom, YCoCg variance clip gamma 1, clip-fast, alpha 0.1, depth culling, reject outside"},
+        "config": c2_config(world), "frames_per_step": 1,
+        "timing": "wall clock over a bounded sample: one of the sequence's 4K frames per step",
         "cpu_baseline": {"value": mpx, "unit": UNIT, "cores": n, "kind": "port",
                          "sample": f"{done} consecutive 3840x2160 frames of the C2 scene, FP32 oracle restatement of taa.comp, {n} threads"},
         "e2e": {"value": mpx, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -363,9 +372,10 @@ def time_fxaa(T, WL, dev, stream, sid, args, peak, col, dep, mot, uniforms):
 def time_modes(T, WL, dev, stream, sid, args, peak):
     """The resolve modes outside the benchmark mode: the ray-trace-assist
     classification writing the segmentation mask (every test, history count 8)
-    TAAU upsampling (1920x1080 source, 3840x2160 target) and a debug output
-    (mode 2), each in the tiled form (the form selected by default) and in the
-    plain form (one thread per pixel).  Each on four rotating frames of the
+    TAAU upsampling (1920x1080 source, 3840x2160 target), a debug output
+    (mode 2) and the reference's default parameter block, each in the tiled
+    form (the form selected by default) and in the plain form (one thread per
+    pixel).  Each on four rotating frames of the
     C2 scene (every frame's bindings exceed the L2), CUDA events over 12
     launches after 3.  Material ids and uv/normals are seeded synthetic blocks
     (48 px materials, 8 px normals).  Last the post-process pass at 4K (split,
@@ -452,6 +462,16 @@ def time_modes(T, WL, dev, stream, sid, args, peak):
     ctx = T.Taa(W, H)
     run("debug_output", ctx, dm, lambda i: dict(base(i), debug=dbg), wl.bytes_per_pixel(16, 4) + 8, W * H)
     out["debug_output"]["form"] = "tiled"
+    ctx.close()
+    # the reference's default parameter block (taa.hpp:31-76: min/max clamp, bilinear
+    # history, velocity for movers only, no depth culling) on the same frames: AUTO runs
+    # it in the tiled form's general path (no benchmark-mode specialisation)
+    defaults = [T.make_uniforms(T.default_parameters(), jitter_ndc=T.synth_jitter(sc, 1 + i)[1]) for i in range(n)]
+    ctx = T.Taa(W, H)
+    run("reference_defaults", ctx, defaults, base, wl.bytes_per_pixel(16, 4) - 4, W * H)
+    ctx.close()
+    ctx = T.Taa(W, H, form=T.TAA_FORM_PLAIN)
+    run("reference_defaults_plain", ctx, defaults, base, wl.bytes_per_pixel(16, 4) - 4, W * H)
     ctx.close()
     del col, dep, mot, seg, mat, pmat, uvn, dbg
 
@@ -900,11 +920,8 @@ def run_ours(args):
             "metric": METRIC, "value": mpx, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded analytic scene rendered on the GPU)",
-            "config": {"workload": wl.name, "width": W, "height": H, "frames_per_step": F, "form": form_name,
-                       "history": "RGBA32F", "motion": "RG16F", "bytes_per_px": bpp,
-                       "l2": "no flush: each frame's inputs (500 MB) exceed the 129 MB L2",
-                       "timed": "CUDA graph of the 64-frame sequence, replayed once per step",
-                       "parallelism": f"replicas x{world}"},
+            "config": c2_config(world), "frames_per_step": F, "form": form_name,
+            "timing": "CUDA events around a CUDA graph of the 64-frame sequence, replayed once per step",
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "note": f"peak: {peak_kind}; achieved = {bpp} B/px x {W}x{H} / avg launch"},

@@ -30,6 +30,9 @@ def test_reference_inputs_equal_the_c2_workload(built):
     assert bytes(sc) == bytes(wl.scene())
     assert bytes(params) == bytes(wl.parameters())
     assert bench.C2_NAME == wl.name
+    cfg = bench.c2_config(1)
+    assert (cfg["width"], cfg["height"], cfg["frames"]) == (wl.width, wl.height, wl.frames)
+    assert cfg["bytes_per_px"] == wl.bytes_per_pixel(history_bytes=16, motion_bytes=4)
     np.testing.assert_array_equal(O.synth_spheres(sc)[:sc.num_spheres],
                                   np.asarray(T.synth_spheres(wl.scene()))[:sc.num_spheres])
     for f in (0, 3, 7, 63):
