@@ -102,7 +102,10 @@ typedef enum taa_status {
  * image never reaches device memory.  In TAA_FORM_FAST (and AUTO where it
  * selects it) the tiles are 30x14 outputs of 32x16 strip-body regions, and
  * the three images carry the two-pass fast form's bits; in TAA_FORM_TILED
- * the exact form's.  Without the flag the forms launch the resolve, which
+ * the exact form's.  TAA_FORM_FP16 with the flag runs the fast form's kernel
+ * where it runs the parameters (there is no FP16 one-launch kernel: on this
+ * GPU the fast FP32 form is the faster and the more precise), else the exact
+ * form's.  Without the flag the forms launch the resolve, which
  * writes the RGBA16F result image, and then the sharpen pass on it, as the
  * reference dispatches taa.comp and then the sharpener (source/taa.hpp:1027,
  * 1111-1139).  On 2560x1440 with CAS the fused fast form takes 58 us a frame

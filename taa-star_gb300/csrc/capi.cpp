@@ -525,7 +525,9 @@ static int select_form(const taa_ctx* c, const taa_frame_io_t* io) {
     // a debug binding: the tiled FP32 form writes it (the fused sharpener does not)
     if (io && io->debug) return fused ? TAA_FORM_PLAIN : TAA_FORM_TILED;
     if (d.form == TAA_FORM_FP16 && !fused) return TAA_FORM_FP16;
-    if ((d.form == TAA_FORM_AUTO || d.form == TAA_FORM_FAST) &&
+    // the one-launch sharpener exists for the fast and the exact FP32 forms; an FP16
+    // context asking for it gets the fast form's (faster than FP16 here, and within 1e-4)
+    if ((d.form == TAA_FORM_AUTO || d.form == TAA_FORM_FAST || (d.form == TAA_FORM_FP16 && fused)) &&
         taa_dev::fast32_supported(c->uniforms, (int)d.history_format, d.in_width, d.in_height, d.out_width,
                                   d.out_height))
         return TAA_FORM_FAST;

@@ -209,3 +209,28 @@ def test_fused_sharpen_equals_two_passes(cuda, size, interp, sharpener):
             assert not torch.isnan(one).any(), (f, name)
             assert torch.equal(two, one), (f, name, float((two.float() - one.float()).abs().max()))
     assert T.device_status(clear=True) == 0
+
+
+def test_fp16_context_with_fused_sharpener_runs_the_fast_one_launch_kernel(cuda):
+    W, H = 96, 64
+    wl = WL.small(W, H, frames=2, seed=29)
+    sc = wl.scene()
+    col = torch.empty(2, H, W, 4, dtype=torch.float16, device=cuda)
+    dep = torch.empty(2, H, W, device=cuda)
+    mot = torch.empty(2, H, W, 2, dtype=torch.float16, device=cuda)
+    for f in range(2):
+        T.synth_render(sc, f, color=col[f], depth=dep[f], motion=mot[f])
+    u = T.make_uniforms(wl.parameters(), jitter_ndc=T.synth_jitter(sc, 1)[1])
+    outs = []
+    for form in (T.TAA_FORM_FP16, T.TAA_FORM_FAST):
+        ctx = T.Taa(W, H, form=form, sharpener=T.TAA_SHARPEN_CAS, flags=T.TAA_FLAG_FUSED_SHARPEN)
+        ctx.set_uniforms(u)
+        assert ctx.selected_form() == T.TAA_FORM_FAST
+        h = torch.empty(H, W, 4, device=cuda)
+        shp = torch.empty(H, W, 4, dtype=torch.float16, device=cuda)
+        ctx.resolve(color=col[1], depth=dep[1], velocity=mot[1], history=col[0].float(), history_depth=dep[0],
+                    history_out=h, sharpened=shp)
+        torch.cuda.synchronize()
+        outs.append((h.clone(), shp.clone()))
+        ctx.close()
+    assert torch.equal(outs[0][0], outs[1][0]) and torch.equal(outs[0][1], outs[1][1])
