@@ -165,3 +165,29 @@ def test_learned_paths_agree_on_one_frame(cuda, extra):
     diff = np.abs(outs[0] - outs[1]) / np.maximum(1e-2, np.abs(outs[1]))
     # FP32 accumulation order only: equal but for pixels near a rounding of the FP16 activations
     assert np.mean(diff <= 1e-3) >= 0.99 and np.max(diff) <= 0.05
+
+
+def test_c5_gain_at_1080p_repeats(cuda):
+    """The C5 configuration at its own size: records from two other seeds of the
+    renderer at 1920x1080, 600 Adam steps, then the seed-5 sequence (24 frames,
+    judged from frame 8) against the 64-spp truth.  The learned form gains at
+    least 1 dB over the plain variance clip, and a second trainer fed the same
+    collections trains to the same weights bit for bit."""
+    weights = []
+    for _ in range(2):
+        tr = T.MlpTrainer(700_000)
+        for s in (501, 502):
+            LP.collect(tr, WL.Workload(f"C5 training seed {s}", 1920, 1080, 12, seed=s, num_spheres=32), 12, cuda,
+                       0.03, skip=4, seed=s)
+        w, first, last = LP.train(tr, seed=1, steps=600, batch=8192, lr=3e-3)
+        assert last < first
+        weights.append(w)
+        tr.close()
+    assert bytes(weights[0]) == bytes(weights[1])
+    wl = WL.Workload("C5 1920x1080 (24 frames)", 1920, 1080, 24, seed=5, num_spheres=32)
+    fr = LP.render(wl, 24, cuda)
+    plain, _ = LP.evaluate(wl, 24, cuda, T.TAA_FORM_TILED, fr=fr)
+    learned, _ = LP.evaluate(wl, 24, cuda, T.TAA_FORM_LEARNED, weights=weights[0], fr=fr)
+    gain = float(np.mean(learned) - np.mean(plain))
+    assert gain >= 1.0, (np.mean(plain), np.mean(learned))
+    assert T.device_status(clear=True) == 0
