@@ -70,11 +70,14 @@ typedef enum taa_status {
  * approximations in the variance box and the clip.  Frame error within 1e-4
  * relative L2 of the FP64 oracle and of TAA_FORM_TILED on the benchmark
  * sequences (measured 2e-5 to 6e-5; the exact FP32 form is 1e-5 to 5e-5 from
- * FP64).  It runs the benchmark mode of the
- * parameter block (YCoCg variance clip toward the box centre, velocity for
- * every pixel with simple sampling, no tonemap, luma weighting, near-clamp
- * reduction, velocity-based alpha, noise or anti-ghosting) with Catmull-Rom
- * or bilinear history, RGBA32F history, equal source and target sizes and no
+ * FP64).  It runs two modes of the parameter block: the benchmark mode
+ * (YCoCg variance clip toward the box centre, velocity for every pixel with
+ * simple sampling, no tonemap, luma weighting, near-clamp reduction,
+ * velocity-based alpha, noise or anti-ghosting) and the reference's default
+ * mode (RGB, 3x3 minimum/maximum box, clamp, velocity for every pixel, for
+ * movers only or reprojection through the matrices, none of those blend
+ * modifiers; without a fused sharpener or a batch), each with Catmull-Rom or
+ * bilinear history, RGBA32F history, equal source and target sizes and no
  * debug binding; other parameters run in TAA_FORM_TILED. */
 #define TAA_FORM_FAST   5u
 /* taa_desc_t.flags: run the learned form's network on tcgen05 through tensor

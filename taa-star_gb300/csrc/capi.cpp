@@ -531,6 +531,11 @@ static int select_form(const taa_ctx* c, const taa_frame_io_t* io) {
         taa_dev::fast32_supported(c->uniforms, (int)d.history_format, d.in_width, d.in_height, d.out_width,
                                   d.out_height))
         return TAA_FORM_FAST;
+    // the reference's default mode (clamp to the RGB min/max box) on the strip body, two-pass
+    if ((d.form == TAA_FORM_AUTO || d.form == TAA_FORM_FAST) && !fused &&
+        taa_dev::fast32_clamp_supported(c->uniforms, (int)d.history_format, d.in_width, d.in_height, d.out_width,
+                                        d.out_height))
+        return TAA_FORM_FAST;
     return TAA_FORM_TILED;
 }
 

@@ -13,6 +13,22 @@ bool fast32_supported(const taa_uniforms_t& U, int history_fmt, int in_w, int in
            fast_path_supported(U, in_w, in_h, out_w, out_h);
 }
 
+// The reference's default parameter block and its relatives: RGB, 3x3
+// minimum/maximum box, clamp; velocity for every pixel, for movers only, or
+// reprojection; nothing that changes the blend weight.
+static bool clamp_rgb_mode(const taa_parameters_t& P) {
+    return !P.mUseYCoCg && !P.mToneMapLumaKaris && !P.mVarianceClipping && !P.mShapedNeighbourhood &&
+           P.mColorClampingOrClipping == 1 && P.mUseVelocityVectors >= 0 && P.mUseVelocityVectors <= 2 &&
+           P.mVelocitySampleMode == 0 && !P.mVelBasedAlpha && !P.mLumaWeightingLottes && !P.mReduceBlendNearClamp &&
+           !P.mAddNoise && !P.mDynamicAntiGhosting && !P.mRayTraceAugment;
+}
+
+bool fast32_clamp_supported(const taa_uniforms_t& U, int history_fmt, int in_w, int in_h, int out_w, int out_h) {
+    const taa_parameters_t& P = U.param[0];
+    return history_fmt == 0 && clamp_rgb_mode(P) && (P.mInterpolationMode == 0 || P.mInterpolationMode == 2) &&
+           fast_path_supported(U, in_w, in_h, out_w, out_h);
+}
+
 cudaError_t launch_resolve_fast32(int motion_ch, const taa_uniforms_t& U, const FrameArgs& f, cudaStream_t s) {
     using namespace fast32;
     const taa_parameters_t& P = U.param[0];
@@ -22,14 +38,17 @@ cudaError_t launch_resolve_fast32(int motion_ch, const taa_uniforms_t& U, const 
     const int tma_ok = a.hist && f.history.w >= WW && f.history.h >= WH &&
                        encode_history_map(f.history, TAA_FAST_TMA2D ? 2 : 0, WW, WH, &map);
     const dim3 grid((a.W + TX - 1) / TX, (a.H + TY - 1) / TY);
-    if (P.mInterpolationMode == 2) {
-        if (motion_ch == 4) resolve_strips<F32Pol, 2, 4><<<grid, NT, 0, s>>>(a, map, tma_ok);
-        else resolve_strips<F32Pol, 2, 2><<<grid, NT, 0, s>>>(a, map, tma_ok);
-    } else {
-        if (motion_ch == 4) resolve_strips<F32Pol, 0, 4><<<grid, NT, 0, s>>>(a, map, tma_ok);
-        else resolve_strips<F32Pol, 0, 2><<<grid, NT, 0, s>>>(a, map, tma_ok);
+    auto go = [&](auto kernel) {
+        kernel<<<grid, NT, 0, s>>>(a, map, tma_ok);
+        return cudaGetLastError();
+    };
+    const bool cr = P.mInterpolationMode == 2, m4 = motion_ch == 4;
+    if (!tiled::is_hot(P)) {  // the clamp RGB mode (fast32_clamp_supported)
+        if (cr) return m4 ? go(resolve_strips<ClampRgbPol, 2, 4>) : go(resolve_strips<ClampRgbPol, 2, 2>);
+        return m4 ? go(resolve_strips<ClampRgbPol, 0, 4>) : go(resolve_strips<ClampRgbPol, 0, 2>);
     }
-    return cudaGetLastError();
+    if (cr) return m4 ? go(resolve_strips<F32Pol, 2, 4>) : go(resolve_strips<F32Pol, 2, 2>);
+    return m4 ? go(resolve_strips<F32Pol, 0, 4>) : go(resolve_strips<F32Pol, 0, 2>);
 }
 
 cudaError_t launch_resolve_fast32_sharpen(int motion_ch, int sharpener, const taa_uniforms_t& U, const FrameArgs& f,

@@ -33,16 +33,6 @@ namespace fast32 {
 constexpr int kLearnedWarps = NT / 32;
 using Net = learned::WarpNetN<kLearnedWarps>;
 
-// The 3x3 minimum and maximum of one staged row segment (three texels).
-struct RowMinMax {
-    float mn[3], mx[3];
-};
-__device__ __forceinline__ RowMinMax row_minmax(const float4* p) {
-    const float4 t0 = lds128(p), t1 = lds128(p + 1), t2 = lds128(p + 2);
-    return {{fminf(t0.x, fminf(t1.x, t2.x)), fminf(t0.y, fminf(t1.y, t2.y)), fminf(t0.z, fminf(t1.z, t2.z))},
-            {fmaxf(t0.x, fmaxf(t1.x, t2.x)), fmaxf(t0.y, fmaxf(t1.y, t2.y)), fmaxf(t0.z, fmaxf(t1.z, t2.z))}};
-}
-
 struct LearnedStripPol {
     using Staged = float4;
     struct Ctx {

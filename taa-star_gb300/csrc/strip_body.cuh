@@ -47,6 +47,7 @@
 #include <cuda.h>
 
 #include <cstring>
+#include <type_traits>
 
 #include "kernels.h"
 #include "sharpen.cuh"
@@ -104,6 +105,8 @@ struct Args {
     float inv_w, inv_h;  // correctly rounded 1 / W, 1 / H
     float alpha, rejection_alpha, gamma;
     int reject_outside, depth_cull, reset;
+    int vel_mode;                       // mUseVelocityVectors: 0 reproject, 1 velocity for movers, 2 for every pixel
+    float inv_vp[16], hist_vp[16];      // mInverseViewProjMatrix, mHistoryViewProjMatrix (column-major)
 };
 
 // The arguments of a launch from a view's uniform block and bindings.
@@ -135,6 +138,11 @@ __host__ __device__ inline Args make_args(const taa_uniforms_t& U, const FrameAr
     a.reject_outside = P.mRejectOutside != 0;
     a.depth_cull = P.mDepthCulling != 0;
     a.reset = U.mResetHistory != 0;
+    a.vel_mode = P.mUseVelocityVectors;
+    for (int i = 0; i < 16; ++i) {
+        a.inv_vp[i] = U.mInverseViewProjMatrix[i];
+        a.hist_vp[i] = U.mHistoryViewProjMatrix[i];
+    }
     return a;
 }
 
@@ -358,6 +366,30 @@ template <int INTERP> __device__ __forceinline__ int axis_first(float it, float&
 // the thread that starts the copy initialises it).  A wait that gives up sets
 // the status bit and leaves the tile unwritten; with PERSIST it also sets
 // sm.abort, which the caller reads after the barrier that separates tiles.
+// Whether a policy's parameter mode may reproject a pixel through the
+// matrices instead of its velocity (mUseVelocityVectors 0 or 1): its
+// `static constexpr bool kReproject`, false when it has none.
+template <class P, class = void> struct reprojects : std::false_type {};
+template <class P> struct reprojects<P, std::void_t<decltype(P::kReproject)>> : std::bool_constant<P::kReproject> {};
+
+// taa.comp:426-430: the pixel's history position and expected depth from the
+// depth and the two matrices (FP32; the fast forms' reassociated arithmetic).
+__device__ __forceinline__ void reproject(const Args& a, float u, float v, float depth, float& hu, float& hv,
+                                          float& ehd) {
+    const float c0 = fmaf(u, 2.0f, -1.0f), c1 = fmaf(v, 2.0f, -1.0f);
+    float ws[4], hs[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        ws[i] = fmaf(a.inv_vp[i], c0, fmaf(a.inv_vp[4 + i], c1, fmaf(a.inv_vp[8 + i], depth, a.inv_vp[12 + i])));
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        hs[i] = fmaf(a.hist_vp[i], ws[0], fmaf(a.hist_vp[4 + i], ws[1], fmaf(a.hist_vp[8 + i], ws[2], a.hist_vp[12 + i] * ws[3])));
+    const float rw = 1.0f / hs[3];
+    hu = fmaf(hs[0] * rw, 0.5f, 0.5f);
+    hv = fmaf(hs[1] * rw, 0.5f, 0.5f);
+    ehd = hs[2] * rw;
+}
+
 // What a policy's finisher may read of the strip's pixels besides their
 // boxes and history samples: uv, the history positions, the expected and the
 // previous depth (a finisher that reads none of it costs nothing for it).
@@ -415,9 +447,13 @@ __device__ __forceinline__ void strip_tile(const Args& a, const CUtensorMap* hma
     for (int k = 0; k < NPX; ++k) {
         const float4 vel = tiled::velocity_of<MC>(vraw[k]);
         px.v[k] = div_const_rn((float)crow(ya + k) + 0.5f, (float)H, a.inv_h);
-        hu[k] = px.u - vel.x;
-        hv[k] = px.v[k] - vel.y;
-        ehd[k] = dep[k] - vel.z;
+        if (reprojects<Pol>::value && (a.vel_mode == 0 || (a.vel_mode == 1 && vel.w < 0.5f))) {
+            reproject(a, px.u, px.v[k], dep[k], hu[k], hv[k], ehd[k]);
+        } else {
+            hu[k] = px.u - vel.x;
+            hv[k] = px.v[k] - vel.y;
+            ehd[k] = dep[k] - vel.z;
+        }
         pd[k] = 0.f;
         if (a.depth_cull && a.hdepth)
             pd[k] = __ldg(at<float>(a.hdepth, a.hdepth_pitch, clampi(trunc_index(hu[k] * (float)W), 0, W - 1),
@@ -599,6 +635,60 @@ struct F32Pol {
         const float4 c0 = lds128(c);
         const float cur[3] = {c0.x, c0.y, c0.z};
         return clip_blend(hc, b.m, ma, cur, alpha);
+    }
+};
+
+// The 3x3 minimum and maximum of one staged row segment (three texels).
+struct RowMinMax {
+    float mn[3], mx[3];
+};
+__device__ __forceinline__ RowMinMax row_minmax(const float4* p) {
+    const float4 t0 = lds128(p), t1 = lds128(p + 1), t2 = lds128(p + 2);
+    return {{fminf(t0.x, fminf(t1.x, t2.x)), fminf(t0.y, fminf(t1.y, t2.y)), fminf(t0.z, fminf(t1.z, t2.z))},
+            {fmaxf(t0.x, fmaxf(t1.x, t2.x)), fmaxf(t0.y, fmaxf(t1.y, t2.y)), fmaxf(t0.z, fmaxf(t1.z, t2.z))}};
+}
+
+// The policy of TAA_FORM_FAST for the reference's default parameter block
+// (taa.hpp:31-76): RGB, the 3x3 minimum/maximum box (taa.comp:288-291) from
+// row extrema the strip's pixels share, the history clamped to it
+// (taa.comp:831), velocity for movers only or for every pixel, or
+// reprojection through the matrices (taa.comp:393-431).
+struct ClampRgbPol {
+    using Staged = float4;
+    struct Ctx {};
+    static constexpr bool kReproject = true;
+    static __device__ __forceinline__ float4 stage(uint2 raw) {
+        const float4 c = half4_to_float4(raw);
+        return make_float4(c.x, c.y, c.z, 0.f);
+    }
+    static __device__ __forceinline__ void finish(const Args& a, const float4* sp, int x, int ya, const float3 h[NPX],
+                                                  unsigned rej, bool landed, const PixelInfo&, Ctx&) {
+        RowMinMax q0 = row_minmax(sp), q1 = row_minmax(sp + SX);
+#pragma unroll
+        for (int k = 0; k < NPX; ++k) {
+            const RowMinMax q2 = row_minmax(sp + (k + 2) * SX);
+            float mn[3], mx[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                mn[c] = fminf(q0.mn[c], fminf(q1.mn[c], q2.mn[c]));
+                mx[c] = fmaxf(q0.mx[c], fmaxf(q1.mx[c], q2.mx[c]));
+            }
+            q0 = q1;
+            q1 = q2;
+            const int y = ya + k;
+            if (!(x < a.W && y < a.H && landed)) continue;
+            const float hs[3] = {h[k].x, h[k].y, h[k].z};
+            const float4 c0 = lds128(&sp[(k + 1) * SX + 1]);
+            const float cur[3] = {c0.x, c0.y, c0.z};
+            const float alpha = a.reset ? 1.0f : ((rej >> k) & 1u ? a.rejection_alpha : a.alpha);
+            float o[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float hc = fminf(fmaxf(hs[c], mn[c]), mx[c]);
+                o[c] = fmaf(alpha, cur[c] - hc, hc);
+            }
+            store_out(a, x, y, make_float4(o[0], o[1], o[2], 0.f));
+        }
     }
 };
 

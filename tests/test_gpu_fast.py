@@ -234,3 +234,85 @@ def test_fp16_context_with_fused_sharpener_runs_the_fast_one_launch_kernel(cuda)
         outs.append((h.clone(), shp.clone()))
         ctx.close()
     assert torch.equal(outs[0][0], outs[1][0]) and torch.equal(outs[0][1], outs[1][1])
+
+
+def skew_matrices(u, seed):
+    """Non-trivial inverse view-projection and history view-projection matrices
+    (identity plus small seeded terms, w kept near 1) for the reprojection path."""
+    rng = np.random.default_rng(seed)
+    for name in ("mInverseViewProjMatrix", "mHistoryViewProjMatrix"):
+        m = np.eye(4) + rng.uniform(-0.03, 0.03, (4, 4))
+        m[3, 3] = 1.0
+        arr = getattr(u, name)
+        for i, v in enumerate(m.T.ravel()):  # column-major
+            arr[i] = float(v)
+    return u
+
+
+@pytest.mark.parametrize("size", [(70, 41), (33, 31), (256, 144)], ids=lambda s: f"{s[0]}x{s[1]}")
+@pytest.mark.parametrize("vel", [0, 1, 2], ids=["reproject", "movers", "velocity"])
+@pytest.mark.parametrize("interp,mc", [(0, 2), (2, 4), (0, 4)], ids=["bilinear-rg", "cr-rgba", "bilinear-rgba"])
+def test_fast_form_in_the_reference_default_mode(cuda, size, vel, interp, mc):
+    """The reference's default parameter block (RGB, 3x3 min/max box, clamp,
+    alpha 0.05) with each velocity use runs in the fast form (AUTO's choice)
+    and is as close to the FP64 oracle as the exact form (within 1e-5 relative
+    L2, or three times the exact form's distance on frames whose norm one
+    pixel decides), and within 1e-4 of the exact form."""
+    w, h = size
+    p = T.default_parameters()
+    p.mUseVelocityVectors, p.mInterpolationMode = vel, interp
+    wl = WL.small(w, h, frames=2, seed=w * 5 + h + vel)
+    fr = cpu_frames(wl, range(2), motion_channels=mc)
+    u = skew_matrices(T.make_uniforms(p, jitter_ndc=fr[1]["jitter"]), seed=vel + 3)
+    hist = fr[0]["color"].astype(np.float32)
+    outs = {}
+    for form in (T.TAA_FORM_AUTO, T.TAA_FORM_TILED):
+        ctx = T.Taa(w, h, form=form, motion_format=T.TAA_MOTION_RGBA16F if mc == 4 else T.TAA_MOTION_RG16F)
+        ctx.set_uniforms(u)
+        assert ctx.selected_form() == (T.TAA_FORM_FAST if form == T.TAA_FORM_AUTO else T.TAA_FORM_TILED)
+        outs[form] = gpu_resolve(ctx, cuda, fr[1]["color"], fr[1]["depth"], fr[1]["motion"], hist, fr[0]["depth"])
+        ctx.close()
+    f, t = outs[T.TAA_FORM_AUTO], outs[T.TAA_FORM_TILED]
+    assert np.all(np.isfinite(f["history_out"]))
+    r64 = O.resolve(u, fr[1]["color"].astype(np.float32), fr[1]["depth"], fr[1]["motion"].astype(np.float32),
+                    history=hist, history_depth=fr[0]["depth"], precision=64)["history"][..., :3]
+    e_fast, e_exact = rel_l2(f["history_out"][..., :3], r64), rel_l2(t["history_out"][..., :3], r64)
+    assert e_fast <= max(FAST_RELL2, 3.0 * e_exact), (e_fast, e_exact)
+    assert rel_l2(f["history_out"][..., :3], t["history_out"][..., :3]) <= 1e-4
+    assert np.all(f["history_out"][..., 3] == t["history_out"][..., 3])
+    assert T.device_status(clear=True) == 0
+
+
+def test_reference_default_mode_sequence_against_fp64(cuda):
+    """C1 (1280x720) with the reference's default parameter block, 8 frames:
+    every frame from frame 1 within 1e-4 relative L2 of the FP32 and the FP64
+    oracle fed the same history."""
+    wl = WL.c1()
+    sc = wl.scene()
+    H, W = wl.height, wl.width
+    p = T.default_parameters()
+    ctx = T.Taa(W, H)
+    hist = torch.zeros(H, W, 4, device=cuda)
+    hout = torch.empty_like(hist)
+    prev = None
+    rep = []
+    for f in range(8):
+        col, dep, mot = render(wl, sc, f, cuda)
+        u = T.make_uniforms(p, jitter_ndc=T.synth_jitter(sc, f)[1], mResetHistory=1 if f == 0 else 0)
+        ctx.set_uniforms(u)
+        assert ctx.selected_form() == T.TAA_FORM_FAST
+        pd = prev if prev is not None else dep
+        ctx.resolve(color=col, depth=dep, velocity=mot, history=hist, history_depth=pd, history_out=hout)
+        torch.cuda.synchronize()
+        if f >= 1:
+            args = (u, col.float().cpu().numpy(), dep.cpu().numpy(), mot.float().cpu().numpy())
+            kw = dict(history=hist.cpu().numpy(), history_depth=pd.cpu().numpy())
+            got = hout.cpu().numpy()[..., :3]
+            r32 = O.resolve(*args, **kw)["history"][..., :3]
+            r64 = O.resolve(*args, precision=64, **kw)["history"][..., :3]
+            rep.append((f, rel_l2(got, r32), rel_l2(got, r64)))
+        hist, hout = hout, hist
+        prev = dep
+    ctx.close()
+    print("C1 reference defaults, fast form (frame, relL2 vs FP32, vs FP64):", rep)
+    assert max(r[1] for r in rep) <= 1e-4 and max(r[2] for r in rep) <= 1e-4
