@@ -49,7 +49,8 @@ def parse():
     ap.add_argument("--no-modes", action="store_true")
     ap.add_argument("--no-c3", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--profile", choices=["fast", "tiled", "fp16", "plain", "batch48", "fxaa"],
+    ap.add_argument("--profile", choices=["fast", "tiled", "fp16", "plain", "batch48", "fxaa", "fused", "defaults",
+                                          "learned"],
                     help="a small case for ncu: a few launches of one form on 4K frames (no JSON line)")
     return ap.parse_args()
 
@@ -986,13 +987,25 @@ def run_profile_case(args):
         torch.cuda.synchronize()
         ctx.close()
         return 0
-    form = {"fast": T.TAA_FORM_FAST, "tiled": T.TAA_FORM_TILED, "fp16": T.TAA_FORM_FP16,
-            "plain": T.TAA_FORM_PLAIN}[args.profile]
-    ctx = T.Taa(W, H, form=form)
+    params = wl.parameters()
+    kw, bind = {}, {}
+    if args.profile == "fused":  # the fast form's one-launch resolve + CAS 0.5
+        kw = dict(sharpener=T.TAA_SHARPEN_CAS, sharpen_factor=0.5, flags=T.TAA_FLAG_FUSED_SHARPEN)
+        bind = dict(sharpened=torch.empty(H, W, 4, dtype=torch.float16, device=dev))
+    elif args.profile == "defaults":  # the reference's default parameter block in the fast form
+        params = T.default_parameters()
+    elif args.profile == "learned":  # the learned form's strip kernel (random weights)
+        kw = dict(form=T.TAA_FORM_LEARNED)
+    form = {"fast": T.TAA_FORM_FAST, "tiled": T.TAA_FORM_TILED, "fp16": T.TAA_FORM_FP16, "plain": T.TAA_FORM_PLAIN,
+            "fused": T.TAA_FORM_FAST, "defaults": T.TAA_FORM_FAST, "learned": T.TAA_FORM_LEARNED}[args.profile]
+    kw.setdefault("form", form)
+    ctx = T.Taa(W, H, **kw)
+    if args.profile == "learned":
+        ctx.set_mlp(T.mlp_init_weights(1, 0.1))
     for f in range(1, F):
-        ctx.set_uniforms(T.make_uniforms(wl.parameters(), jitter_ndc=T.synth_jitter(sc, f)[1]))
+        ctx.set_uniforms(T.make_uniforms(params, jitter_ndc=T.synth_jitter(sc, f)[1]))
         ctx.resolve(stream=sid, color=col[f], depth=dep[f], velocity=mot[f], history=hist[f & 1],
-                    history_depth=dep[f - 1], history_out=hist[(f + 1) & 1], result=res)
+                    history_depth=dep[f - 1], history_out=hist[(f + 1) & 1], result=res, **bind)
     torch.cuda.synchronize()
     ctx.close()
     return 0
