@@ -12,11 +12,13 @@
 // Cost at 1920x1080 (CUDA graph of 8 frames): 77 us a frame, against 44 us
 // for the tiled FP32 form and 31 us for TAA_FORM_FAST; without the network
 // the same kernel takes 44 us.  The network's 36 mma.sync per 32 pixels
-// (2 m-tiles x (8 + 8 + 2)) issue at one per 16 cycles per SM sub-partition,
-// 29.6 us for 2.07M pixels on 152 SMs at 2.07 GHz: the kernel is bound by
-// the legacy tensor pipe.  The tcgen05 variant (TAA_FLAG_LEARNED_TCGEN05,
-// below) has 8x the MMA rate but waits on six CTA-wide MMA round trips a
-// tile and measures 89 us.
+// (2 m-tiles x (8 + 8 + 2)) keep the tensor pipe 20 % busy (its peak is one
+// m16n8k16 per 2 cycles per SM: 15 us for 2.07M pixels); the kernel is bound
+// by latency at 20 warps per SM (5 CTAs of 96 registers and 42 KB), with the
+// layers' dependent MMA chains, the feature and activation round trips
+// through shared memory and instruction fetch (the unrolled network) in the
+// stall reasons.  The tcgen05 variant (TAA_FLAG_LEARNED_TCGEN05, below) waits
+// on six CTA-wide MMA round trips a tile and measures 89 us.
 //
 // The training records come from the tiled collection kernel of learned.cu;
 // the features here are the same functions of the same quantities (the box
