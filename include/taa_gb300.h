@@ -421,9 +421,10 @@ int taa_batch_prepare(taa_batch* batch, void* stream, int32_t slot, const taa_fr
 int taa_batch_launch(taa_batch* batch, void* stream, int32_t slot);
 /* Time every tile shape (the exact tiles, and the fast strips where the
  * batch's form and parameters allow them) and job order, each with a
- * persistent grid and with one CTA per tile, on a prepared slot (reps launches each,
- * which rewrite the slot's outputs with the same values), keep the fastest
- * and return it.  Synchronises the stream. */
+ * persistent grid and with one CTA per tile, on a prepared slot (three
+ * interleaved rounds of a warm-up and reps launches each, which rewrite the
+ * slot's outputs with the same values; a candidate's time is its best round),
+ * keep the fastest and return it.  Synchronises the stream. */
 int taa_batch_autotune(taa_batch* batch, void* stream, int32_t slot, int32_t reps, taa_batch_tuning_t* best);
 int taa_batch_get_tuning(const taa_batch* batch, taa_batch_tuning_t* out);
 int taa_batch_set_tuning(taa_batch* batch, const taa_batch_tuning_t* tuning);

@@ -339,16 +339,23 @@ int taa_batch_autotune(taa_batch* b, void* stream, int32_t slot, int32_t reps, t
     cudaError_t e = cudaEventCreate(&t0);
     if (e == cudaSuccess) e = cudaEventCreate(&t1);
     if (e != cudaSuccess) return cuda_fail(e, "taa_batch_autotune: events");
-    taa_batch_tuning_t win{};
-    win.ms = -1.f;
-    int rc = TAA_OK;
-    for (int sh = 0; sh < taa_dev::kBatchShapes && rc == TAA_OK; ++sh) {
+    // every candidate (tile shape x job order x grid), timed in three interleaved
+    // rounds; a candidate's time is its best round (a round disturbed by a clock
+    // change or another job on the device does not decide the choice)
+    std::vector<taa_batch_tuning_t> cands;
+    for (int sh = 0; sh < taa_dev::kBatchShapes; ++sh) {
         const bool fast = sh == taa_dev::kBatchFastShape;
         if (fast && !(b->fast_ok && b->slot_key[slot].hot)) continue;
-        for (int cand = 0; cand < 6 && rc == TAA_OK; ++cand) {
+        for (int cand = 0; cand < 6; ++cand) {
             const int sched = cand % 3, grid_mode = cand < 3 ? 0 : TAA_BATCH_CTA_PER_TILE;
-            taa_batch_tuning_t t{kShapeDims[sh][0], kShapeDims[sh][1], sched, grid_mode, 0.f,
-                                 fast ? (int32_t)TAA_FORM_FAST : (int32_t)TAA_FORM_TILED};
+            cands.push_back(taa_batch_tuning_t{kShapeDims[sh][0], kShapeDims[sh][1], sched, grid_mode, -1.f,
+                                               fast ? (int32_t)TAA_FORM_FAST : (int32_t)TAA_FORM_TILED});
+        }
+    }
+    constexpr int kRounds = 3;
+    int rc = TAA_OK;
+    for (int round = 0; round < kRounds && rc == TAA_OK; ++round) {
+        for (taa_batch_tuning_t& t : cands) {
             if ((rc = upload_jobs(*b, t, s))) break;
             if ((rc = launch_slot(*b, s, slot, t))) break;  // warm-up
             e = cudaEventRecord(t0, s);
@@ -361,10 +368,15 @@ int taa_batch_autotune(taa_batch* b, void* stream, int32_t slot, int32_t reps, t
                 rc = cuda_fail(e, "taa_batch_autotune: timing");
                 break;
             }
-            t.ms = ms / (float)reps;
-            if (win.ms < 0.f || t.ms < win.ms) win = t;
+            const float per = ms / (float)reps;
+            if (t.ms < 0.f || per < t.ms) t.ms = per;
         }
     }
+    taa_batch_tuning_t win{};
+    win.ms = -1.f;
+    for (const taa_batch_tuning_t& t : cands)
+        if (t.ms >= 0.f && (win.ms < 0.f || t.ms < win.ms)) win = t;
+    if (rc == TAA_OK && win.ms < 0.f) rc = fail(TAA_E_INVAL, "taa_batch_autotune: no candidate ran");
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
     if (rc == TAA_OK) rc = upload_jobs(*b, win, s);

@@ -170,7 +170,8 @@ def test_result_in_pinned_host_memory(cuda, form):
     assert torch.equal(outs[0], outs[1]) and not torch.isnan(outs[0]).any()
 
 
-@pytest.mark.parametrize("size", [(200, 120), (61, 37), (256, 160)], ids=lambda s: f"{s[0]}x{s[1]}")
+@pytest.mark.parametrize("size", [(200, 120), (61, 37), (256, 160), (1, 1), (40, 1), (1, 40), (31, 15)],
+                         ids=lambda s: f"{s[0]}x{s[1]}")
 @pytest.mark.parametrize("interp", [2, 0], ids=["catmull_rom", "bilinear"])
 @pytest.mark.parametrize("sharpener", [T.TAA_SHARPEN_CAS, T.TAA_SHARPEN_SIMPLE], ids=["cas", "simple"])
 def test_fused_sharpen_equals_two_passes(cuda, size, interp, sharpener):
@@ -249,7 +250,8 @@ def skew_matrices(u, seed):
     return u
 
 
-@pytest.mark.parametrize("size", [(70, 41), (33, 31), (256, 144)], ids=lambda s: f"{s[0]}x{s[1]}")
+@pytest.mark.parametrize("size", [(70, 41), (33, 31), (256, 144), (1, 1), (40, 1), (1, 40)],
+                         ids=lambda s: f"{s[0]}x{s[1]}")
 @pytest.mark.parametrize("vel", [0, 1, 2], ids=["reproject", "movers", "velocity"])
 @pytest.mark.parametrize("interp,mc", [(0, 2), (2, 4), (0, 4)], ids=["bilinear-rg", "cr-rgba", "bilinear-rgba"])
 def test_fast_form_in_the_reference_default_mode(cuda, size, vel, interp, mc):

@@ -175,10 +175,11 @@ def test_c5_gain_at_1080p_repeats(cuda):
     collections trains to the same weights bit for bit."""
     weights = []
     for _ in range(2):
-        tr = T.MlpTrainer(700_000)
+        tr = T.MlpTrainer(1_100_000)  # holds every record (about 1.0M): the kept set does not depend on timing
         for s in (501, 502):
             LP.collect(tr, WL.Workload(f"C5 training seed {s}", 1920, 1080, 12, seed=s, num_spheres=32), 12, cuda,
                        0.03, skip=4, seed=s)
+        assert tr.count() < 1_100_000
         w, first, last = LP.train(tr, seed=1, steps=600, batch=8192, lr=3e-3)
         assert last < first
         weights.append(w)
