@@ -732,6 +732,14 @@ def run_ours(args):
     hist = [torch.zeros(H, W, 4, dtype=torch.float32, device=dev) for _ in range(2)]
     res = torch.empty(H, W, 4, dtype=torch.float16, device=dev)
     torch.cuda.synchronize()
+    # the end-to-end run's pinned host images, taken while the process is young: taken
+    # after the rest of the run's allocations, the same buffers measured 5 Gpx/s end to
+    # end against 9.6-12.3 here
+    if not args.no_e2e:
+        h_col = col.cpu().pin_memory()
+        h_dep = dep.cpu().pin_memory()
+        h_mot = mot.cpu().pin_memory()
+        h_out = torch.empty(F, H, W, 4, dtype=torch.float16).pin_memory()
 
     def make_ctx(form, flags=0):
         c = T.Taa(W, H, form=form, flags=flags)
@@ -827,10 +835,6 @@ def run_ours(args):
     e2e = None
     if not args.no_e2e:
         nbuf = 3
-        h_col = col.cpu().pin_memory()
-        h_dep = dep.cpu().pin_memory()
-        h_mot = mot.cpu().pin_memory()
-        h_out = torch.empty(F, H, W, 4, dtype=torch.float16).pin_memory()
         d_col = [torch.empty(H, W, 4, dtype=torch.float16, device=dev) for _ in range(nbuf)]
         d_dep = [torch.empty(H, W, dtype=torch.float32, device=dev) for _ in range(nbuf)]
         d_mot = [torch.empty(H, W, 2, dtype=torch.float16, device=dev) for _ in range(nbuf)]

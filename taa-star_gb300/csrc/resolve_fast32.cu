@@ -44,8 +44,13 @@ cudaError_t launch_resolve_fast32(int motion_ch, const taa_uniforms_t& U, const 
     };
     const bool cr = P.mInterpolationMode == 2, m4 = motion_ch == 4;
     if (!tiled::is_hot(P)) {  // the clamp RGB mode (fast32_clamp_supported)
-        if (cr) return m4 ? go(resolve_strips<ClampRgbPol, 2, 4>) : go(resolve_strips<ClampRgbPol, 2, 2>);
-        return m4 ? go(resolve_strips<ClampRgbPol, 0, 4>) : go(resolve_strips<ClampRgbPol, 0, 2>);
+        const Reproj rp = make_reproj(U);
+        auto go_rp = [&](auto kernel) {
+            kernel<<<grid, NT, 0, s>>>(a, map, tma_ok, rp);
+            return cudaGetLastError();
+        };
+        if (cr) return m4 ? go_rp(resolve_strips_reproj<ClampRgbPol, 2, 4>) : go_rp(resolve_strips_reproj<ClampRgbPol, 2, 2>);
+        return m4 ? go_rp(resolve_strips_reproj<ClampRgbPol, 0, 4>) : go_rp(resolve_strips_reproj<ClampRgbPol, 0, 2>);
     }
     if (cr) return m4 ? go(resolve_strips<F32Pol, 2, 4>) : go(resolve_strips<F32Pol, 2, 2>);
     return m4 ? go(resolve_strips<F32Pol, 0, 4>) : go(resolve_strips<F32Pol, 0, 2>);

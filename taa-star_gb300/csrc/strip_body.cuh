@@ -105,9 +105,23 @@ struct Args {
     float inv_w, inv_h;  // correctly rounded 1 / W, 1 / H
     float alpha, rejection_alpha, gamma;
     int reject_outside, depth_cull, reset;
-    int vel_mode;                       // mUseVelocityVectors: 0 reproject, 1 velocity for movers, 2 for every pixel
-    float inv_vp[16], hist_vp[16];      // mInverseViewProjMatrix, mHistoryViewProjMatrix (column-major)
 };
+
+// What a policy that may reproject reads besides Args (a kernel parameter of
+// its own, so that the other kernels' arguments stay small).
+struct Reproj {
+    int vel_mode;                   // mUseVelocityVectors: 0 reproject, 1 velocity for movers, 2 for every pixel
+    float inv_vp[16], hist_vp[16];  // mInverseViewProjMatrix, mHistoryViewProjMatrix (column-major)
+};
+inline Reproj make_reproj(const taa_uniforms_t& U) {
+    Reproj r;
+    r.vel_mode = U.param[0].mUseVelocityVectors;
+    for (int i = 0; i < 16; ++i) {
+        r.inv_vp[i] = U.mInverseViewProjMatrix[i];
+        r.hist_vp[i] = U.mHistoryViewProjMatrix[i];
+    }
+    return r;
+}
 
 // The arguments of a launch from a view's uniform block and bindings.
 __host__ __device__ inline Args make_args(const taa_uniforms_t& U, const FrameArgs& f) {
@@ -138,11 +152,6 @@ __host__ __device__ inline Args make_args(const taa_uniforms_t& U, const FrameAr
     a.reject_outside = P.mRejectOutside != 0;
     a.depth_cull = P.mDepthCulling != 0;
     a.reset = U.mResetHistory != 0;
-    a.vel_mode = P.mUseVelocityVectors;
-    for (int i = 0; i < 16; ++i) {
-        a.inv_vp[i] = U.mInverseViewProjMatrix[i];
-        a.hist_vp[i] = U.mHistoryViewProjMatrix[i];
-    }
     return a;
 }
 
@@ -368,13 +377,14 @@ template <int INTERP> __device__ __forceinline__ int axis_first(float it, float&
 // sm.abort, which the caller reads after the barrier that separates tiles.
 // Whether a policy's parameter mode may reproject a pixel through the
 // matrices instead of its velocity (mUseVelocityVectors 0 or 1): its
-// `static constexpr bool kReproject`, false when it has none.
+// `static constexpr bool kReproject`, false when it has none; such a policy's
+// Ctx holds `const Reproj* rp`.
 template <class P, class = void> struct reprojects : std::false_type {};
 template <class P> struct reprojects<P, std::void_t<decltype(P::kReproject)>> : std::bool_constant<P::kReproject> {};
 
 // taa.comp:426-430: the pixel's history position and expected depth from the
 // depth and the two matrices (FP32; the fast forms' reassociated arithmetic).
-__device__ __forceinline__ void reproject(const Args& a, float u, float v, float depth, float& hu, float& hv,
+__device__ __forceinline__ void reproject(const Reproj& a, float u, float v, float depth, float& hu, float& hv,
                                           float& ehd) {
     const float c0 = fmaf(u, 2.0f, -1.0f), c1 = fmaf(v, 2.0f, -1.0f);
     float ws[4], hs[4];
@@ -447,9 +457,13 @@ __device__ __forceinline__ void strip_tile(const Args& a, const CUtensorMap* hma
     for (int k = 0; k < NPX; ++k) {
         const float4 vel = tiled::velocity_of<MC>(vraw[k]);
         px.v[k] = div_const_rn((float)crow(ya + k) + 0.5f, (float)H, a.inv_h);
-        if (reprojects<Pol>::value && (a.vel_mode == 0 || (a.vel_mode == 1 && vel.w < 0.5f))) {
-            reproject(a, px.u, px.v[k], dep[k], hu[k], hv[k], ehd[k]);
-        } else {
+        bool use_velocity = true;
+        if constexpr (reprojects<Pol>::value) {
+            const int vm = ctx.rp->vel_mode;
+            use_velocity = vm == 2 || (vm == 1 && vel.w >= 0.5f);
+            if (!use_velocity) reproject(*ctx.rp, px.u, px.v[k], dep[k], hu[k], hv[k], ehd[k]);
+        }
+        if (use_velocity) {
             hu[k] = px.u - vel.x;
             hv[k] = px.v[k] - vel.y;
             ehd[k] = dep[k] - vel.z;
@@ -655,7 +669,9 @@ __device__ __forceinline__ RowMinMax row_minmax(const float4* p) {
 // reprojection through the matrices (taa.comp:393-431).
 struct ClampRgbPol {
     using Staged = float4;
-    struct Ctx {};
+    struct Ctx {
+        const Reproj* rp;
+    };
     static constexpr bool kReproject = true;
     static __device__ __forceinline__ float4 stage(uint2 raw) {
         const float4 c = half4_to_float4(raw);
@@ -781,6 +797,17 @@ __global__ void __launch_bounds__(NT, TAA_FAST_MIN_BLOCKS)
     __shared__ SmemT<typename Pol::Staged> sm;
     uint32_t phase = 0;
     typename Pol::Ctx ctx;
+    strip_tile<Pol, INTERP, MC, false>(a, &hmap, tma_ok, blockIdx.x, blockIdx.y, sm, phase, ctx);
+}
+
+// One view with a policy that may reproject (its Reproj a kernel parameter).
+template <class Pol, int INTERP, int MC>
+__global__ void __launch_bounds__(NT, TAA_FAST_MIN_BLOCKS)
+    resolve_strips_reproj(const Args a, const __grid_constant__ CUtensorMap hmap, const int tma_ok,
+                          const __grid_constant__ Reproj rp) {
+    __shared__ SmemT<typename Pol::Staged> sm;
+    uint32_t phase = 0;
+    typename Pol::Ctx ctx{&rp};
     strip_tile<Pol, INTERP, MC, false>(a, &hmap, tma_ok, blockIdx.x, blockIdx.y, sm, phase, ctx);
 }
 
