@@ -19,7 +19,7 @@ present (they are not built on the GPU machine).
     and are written beside the shader so that its includes find them.
 
 The reference tree is read from $TAA_REFERENCE_ROOT, by default
-/root/reference (where this build's container mounts it).
+/root/reference.
   * libfxaa_ref32.so / libfxaa_ref64.so - shaders/antialias_fxaa_prepare.comp
     and shaders/antialias_fxaa.comp (which includes shaders/Fxaa3_11_mod.h
     from the reference tree as it lies) through the same shim, with the

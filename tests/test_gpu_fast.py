@@ -6,7 +6,7 @@ hardware square-root and reciprocal approximations), so its contract is a
 distance, not bits: frame relative L2 within 1e-5 of the reference shader's
 own FP32 output on the golden fixtures (tests/golden) and of the exact tiled
 form there, and within 1e-4 relative L2 / 50 dB PSNR of the FP64 oracle on
-the benchmark sequences (the north star's "within 1e-4 relative").  On those
+the benchmark sequences (the benchmark's "within 1e-4 relative").  On those
 full frames the form is 2e-5 to 6e-5 from both the FP64 oracle and the FP32
 oracle: the algorithm amplifies FP32 rounding (the variance of a flat
 neighbourhood, taa.comp:270; the clip toward a near-degenerate box,

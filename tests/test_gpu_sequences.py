@@ -130,9 +130,9 @@ def test_4k_constant_image_is_a_fixed_point(cuda):
 
 
 # With TAA_FLAG_FP16_GUARD a pixel whose clip engages on a box FP16 cannot
-# resolve (its tightest channel 256 times narrower than its widest: the tight
+# resolve (its tightest channel 16 times narrower than its widest: the tight
 # chroma box next to a firefly) is finished in FP32, and the frame error falls
-# below the spec bar of 1e-3 relative L2 against FP64.
+# below 1e-3 relative L2 against FP64.
 FP16_GUARD_RELL2 = 1e-3
 
 
