@@ -810,6 +810,33 @@ def run_ours(args):
             g = launch_bytes / (m2 / 1e3 / (k * F)) / 1e9
             forms[name] = {"mpx_s": v, "gb_s": g, "frac_of_hbm": g / peak}
             c2.close()
+        # RGBA16F history (the reference's storage format) in the fast form: 44 B/px
+        hist16 = [torch.zeros(H, W, 4, dtype=torch.float16, device=dev) for _ in range(2)]
+        c2 = T.Taa(W, H, form=T.TAA_FORM_AUTO, history_format=T.TAA_HISTORY_RGBA16F)
+        gs = torch.cuda.Stream(dev)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=gs):
+            for f in range(F):
+                c2.set_uniforms(uniforms[f])
+                c2.resolve(stream=gs.cuda_stream, color=col[f], depth=dep[f], velocity=mot[f], history=hist16[f & 1],
+                           history_depth=dep[f - 1] if f else dep[0], history_out=hist16[(f + 1) & 1], result=res)
+        graph.replay()
+        torch.cuda.synchronize()
+        k = max(2, args.steps // 4)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            graph.replay()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        m2 = max_over_ranks(e0.elapsed_time(e1), world, dev)
+        b16 = bpp - 16
+        v = job_throughput(W * H * F * k, world, m2 / 1e3) / 1e6
+        g = b16 * W * H / (m2 / 1e3 / (k * F)) / 1e9
+        forms["fast_rgba16f_history"] = {"mpx_s": v, "gb_s": g, "frac_of_hbm": g / peak, "bytes_per_px": b16,
+                                         "form": {5: "fast", 2: "tiled"}.get(c2.selected_form(), "other")}
+        c2.close()
+        del graph, hist16
 
     # the 48-view batch (C4 sizes, log-uniform 320x180 .. 3840x2160): one launch per step
     if not args.no_batch:

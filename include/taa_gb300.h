@@ -77,8 +77,10 @@ typedef enum taa_status {
  * mode (RGB, 3x3 minimum/maximum box, clamp, velocity for every pixel, for
  * movers only or reprojection through the matrices, none of those blend
  * modifiers; without a fused sharpener or a batch), each with Catmull-Rom or
- * bilinear history, RGBA32F history, equal source and target sizes and no
- * debug binding; other parameters run in TAA_FORM_TILED. */
+ * bilinear history, equal source and target sizes and no debug binding;
+ * other parameters run in TAA_FORM_TILED.  RGBA32F history, or RGBA16F (the
+ * reference's storage; one resolve within 5e-4 of the exact form after the
+ * FP16 store) for one view without the one-launch sharpener. */
 #define TAA_FORM_FAST   5u
 /* taa_desc_t.flags: run the learned form's network on tcgen05 through tensor
  * memory (128-row blocks, one thread issuing per CTA, a CTA-wide barrier per

@@ -39,10 +39,12 @@ bool up_path_supported(const taa_uniforms_t& U, int in_w, int in_h, int out_w, i
 // The reassociating FP32 resolve, TAA_FORM_FAST (resolve_fast32.cu): whether
 // it runs these parameters, sizes and history format, and its launch.
 bool fast32_supported(const taa_uniforms_t& U, int history_fmt, int in_w, int in_h, int out_w, int out_h);
-// TAA_FORM_FAST in the reference's default parameter mode (RGB, minimum/maximum
-// box, clamp, any velocity use): one view, no fused sharpener, no batch.
-bool fast32_clamp_supported(const taa_uniforms_t& U, int history_fmt, int in_w, int in_h, int out_w, int out_h);
-cudaError_t launch_resolve_fast32(int motion_ch, const taa_uniforms_t& U, const FrameArgs& a, cudaStream_t stream);
+// TAA_FORM_FAST for one view without a fused sharpener: the benchmark mode or
+// the reference's default mode (RGB, minimum/maximum box, clamp, any velocity
+// use), RGBA32F or RGBA16F history.
+bool fast32_single_supported(const taa_uniforms_t& U, int history_fmt, int in_w, int in_h, int out_w, int out_h);
+cudaError_t launch_resolve_fast32(int motion_ch, int history_fmt, const taa_uniforms_t& U, const FrameArgs& f,
+                                  cudaStream_t s);
 // TAA_FORM_FAST and the sharpener (TAA_SHARPEN_SIMPLE or TAA_SHARPEN_CAS) in
 // one launch: result (if bound), history and sharpened as the two-pass form.
 cudaError_t launch_resolve_fast32_sharpen(int motion_ch, int sharpener, const taa_uniforms_t& U, const FrameArgs& f,

@@ -23,37 +23,54 @@ static bool clamp_rgb_mode(const taa_parameters_t& P) {
            !P.mAddNoise && !P.mDynamicAntiGhosting && !P.mRayTraceAugment;
 }
 
-bool fast32_clamp_supported(const taa_uniforms_t& U, int history_fmt, int in_w, int in_h, int out_w, int out_h) {
+bool fast32_single_supported(const taa_uniforms_t& U, int history_fmt, int in_w, int in_h, int out_w, int out_h) {
     const taa_parameters_t& P = U.param[0];
-    return history_fmt == 0 && clamp_rgb_mode(P) && (P.mInterpolationMode == 0 || P.mInterpolationMode == 2) &&
-           fast_path_supported(U, in_w, in_h, out_w, out_h);
+    return (history_fmt == 0 || history_fmt == 1) && (tiled::is_hot(P) || clamp_rgb_mode(P)) &&
+           (P.mInterpolationMode == 0 || P.mInterpolationMode == 2) && fast_path_supported(U, in_w, in_h, out_w, out_h);
 }
 
-cudaError_t launch_resolve_fast32(int motion_ch, const taa_uniforms_t& U, const FrameArgs& f, cudaStream_t s) {
+namespace {
+// The kernel for the mode, filter, velocity channels and history format.
+template <int HF>
+cudaError_t launch_single(const taa_parameters_t& P, const taa_uniforms_t& U, const fast32::Args& a,
+                          const CUtensorMap& map, int tma_ok, int motion_ch, cudaStream_t s) {
     using namespace fast32;
-    const taa_parameters_t& P = U.param[0];
-    const Args a = make_args(U, f);
-    CUtensorMap map;
-    std::memset(&map, 0, sizeof map);
-    const int tma_ok = a.hist && f.history.w >= WW && f.history.h >= WH &&
-                       encode_history_map(f.history, TAA_FAST_TMA2D ? 2 : 0, WW, WH, &map);
     const dim3 grid((a.W + TX - 1) / TX, (a.H + TY - 1) / TY);
     auto go = [&](auto kernel) {
         kernel<<<grid, NT, 0, s>>>(a, map, tma_ok);
         return cudaGetLastError();
     };
     const bool cr = P.mInterpolationMode == 2, m4 = motion_ch == 4;
-    if (!tiled::is_hot(P)) {  // the clamp RGB mode (fast32_clamp_supported)
+    if (!tiled::is_hot(P)) {  // the clamp RGB mode
         const Reproj rp = make_reproj(U);
         auto go_rp = [&](auto kernel) {
             kernel<<<grid, NT, 0, s>>>(a, map, tma_ok, rp);
             return cudaGetLastError();
         };
-        if (cr) return m4 ? go_rp(resolve_strips_reproj<ClampRgbPol, 2, 4>) : go_rp(resolve_strips_reproj<ClampRgbPol, 2, 2>);
-        return m4 ? go_rp(resolve_strips_reproj<ClampRgbPol, 0, 4>) : go_rp(resolve_strips_reproj<ClampRgbPol, 0, 2>);
+        if (cr)
+            return m4 ? go_rp(resolve_strips_reproj<ClampRgbPol, 2, 4, HF>)
+                      : go_rp(resolve_strips_reproj<ClampRgbPol, 2, 2, HF>);
+        return m4 ? go_rp(resolve_strips_reproj<ClampRgbPol, 0, 4, HF>)
+                  : go_rp(resolve_strips_reproj<ClampRgbPol, 0, 2, HF>);
     }
-    if (cr) return m4 ? go(resolve_strips<F32Pol, 2, 4>) : go(resolve_strips<F32Pol, 2, 2>);
-    return m4 ? go(resolve_strips<F32Pol, 0, 4>) : go(resolve_strips<F32Pol, 0, 2>);
+    if (cr) return m4 ? go(resolve_strips<F32Pol, 2, 4, HF>) : go(resolve_strips<F32Pol, 2, 2, HF>);
+    return m4 ? go(resolve_strips<F32Pol, 0, 4, HF>) : go(resolve_strips<F32Pol, 0, 2, HF>);
+}
+}  // namespace
+
+cudaError_t launch_resolve_fast32(int motion_ch, int history_fmt, const taa_uniforms_t& U, const FrameArgs& f,
+                                  cudaStream_t s) {
+    using namespace fast32;
+    const taa_parameters_t& P = U.param[0];
+    Args a = make_args(U, f);
+    a.hout_half = history_fmt == 1;
+    CUtensorMap map;
+    std::memset(&map, 0, sizeof map);
+    const int ww = history_fmt == 1 ? WinOf<1>::W : WW;
+    const int tma_ok = a.hist && f.history.w >= ww && f.history.h >= WH &&
+                       encode_history_map(f.history, history_fmt == 1 ? 1 : (TAA_FAST_TMA2D ? 2 : 0), ww, WH, &map);
+    if (history_fmt == 1) return launch_single<1>(P, U, a, map, tma_ok, motion_ch, s);
+    return launch_single<0>(P, U, a, map, tma_ok, motion_ch, s);
 }
 
 cudaError_t launch_resolve_fast32_sharpen(int motion_ch, int sharpener, const taa_uniforms_t& U, const FrameArgs& f,

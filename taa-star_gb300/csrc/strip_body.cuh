@@ -105,6 +105,7 @@ struct Args {
     float inv_w, inv_h;  // correctly rounded 1 / W, 1 / H
     float alpha, rejection_alpha, gamma;
     int reject_outside, depth_cull, reset;
+    int hout_half;       // history_out is RGBA16F (the history window then holds RGBA16F texels too)
 };
 
 // What a policy that may reproject reads besides Args (a kernel parameter of
@@ -152,15 +153,28 @@ __host__ __device__ inline Args make_args(const taa_uniforms_t& U, const FrameAr
     a.reject_outside = P.mRejectOutside != 0;
     a.depth_cull = P.mDepthCulling != 0;
     a.reset = U.mResetHistory != 0;
+    a.hout_half = 0;
     return a;
 }
 
-template <class Staged> struct SmemT {
-    Staged col[NS];                    // the staged colour tile in the policy's format
-    alignas(128) float4 win[WW * WH];  // the history window
-    uint64_t bar;                      // completion of the window's TMA copy
-    int org[3];                        // window origin x, y; 1 TMA, 2 cp.async, 0 none
-    int abort;                         // a persistent CTA stops after this tile (a window wait gave up)
+// The history window's texel type and row length: RGBA32F texels, or (HF 1)
+// RGBA16F texels in a row one texel longer, its origin on an even texel (a
+// TMA coordinate is a multiple of 16 bytes).
+template <int HF> struct WinOf {
+    using T = float4;
+    static constexpr int W = WW;
+};
+template <> struct WinOf<1> {
+    using T = uint2;
+    static constexpr int W = WW + 1;
+};
+
+template <class Staged, int HF = 0> struct SmemT {
+    Staged col[NS];                                       // the staged colour tile in the policy's format
+    alignas(128) typename WinOf<HF>::T win[WinOf<HF>::W * WH];  // the history window
+    uint64_t bar;                                         // completion of the window's TMA copy
+    int org[3];                                           // window origin x, y; 1 TMA, 2 cp.async, 0 none
+    int abort;                                            // a persistent CTA stops after this tile (a window wait gave up)
 };
 
 template <class T> __device__ __forceinline__ const T* at(const char* base, uint32_t pitch, int x, int y) {
@@ -200,6 +214,11 @@ __device__ __forceinline__ f2 fmap(f2 a, f2 b, f2 c) {
 // otherwise be read as an 8-byte and a 4-byte load; at the 16-byte stride of
 // consecutive texels each of those occupies the shared-memory pipe as long as
 // the whole 16 bytes do.
+__device__ __forceinline__ uint2 lds64(const uint2* p) {
+    uint2 v;
+    asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(tiled::smem_addr(p)));
+    return v;
+}
 __device__ __forceinline__ float4 lds128(const float4* p) {
     float4 v;
     // volatile: kept in program order with the barrier waits that publish the data
@@ -208,6 +227,9 @@ __device__ __forceinline__ float4 lds128(const float4* p) {
         : "r"(tiled::smem_addr(p)));
     return v;
 }
+// A history texel of the window as FP32 (RGBA16F texels widened).
+__device__ __forceinline__ float4 win_texel(const float4* p) { return lds128(p); }
+__device__ __forceinline__ float4 win_texel(const uint2* p) { return half4_to_float4(lds64(p)); }
 
 // RGBA16F texel -> YCoCg in FP32 (taa.comp:158-164)
 __device__ __forceinline__ float3 ycocg(uint2 raw) {
@@ -234,7 +256,8 @@ __device__ __forceinline__ float4 clip_blend(const float hc[3], const float m[3]
     return make_float4(tmp + o[1], o[0] + o[2], tmp - o[1], 0.f);
 }
 __device__ __forceinline__ void store_out(const Args& a, int x, int y, float4 o) {
-    *at_w<float4>(a.hout, a.hout_pitch, x, y) = o;
+    if (a.hout_half) *at_w<uint2>(a.hout, a.hout_pitch, x, y) = float4_to_half4(o);
+    else *at_w<float4>(a.hout, a.hout_pitch, x, y) = o;
     if (a.result) *at_w<uint2>(a.result, a.result_pitch, x, y) = float4_to_half4(make_float4(o.x, o.y, o.z, 1.0f));
 }
 __device__ __forceinline__ void clip_blend_store(const Args& a, int x, int y, const float hc[3], const float m[3],
@@ -411,10 +434,12 @@ struct PixelInfo {
 // may start at -1 (a fused sharpener resolves a ring around its output);
 // loads are then edge-clamped on every side and the policy chooses what it
 // stores.
-template <class Pol, int INTERP, int MC, bool PERSIST, bool ORIGIN = false>
+template <class Pol, int INTERP, int MC, bool PERSIST, bool ORIGIN = false, int HF = 0>
 __device__ __forceinline__ void strip_tile(const Args& a, const CUtensorMap* hmap, int tma_ok, int tile_x,
-                                           int tile_y, SmemT<typename Pol::Staged>& sm, uint32_t& phase,
+                                           int tile_y, SmemT<typename Pol::Staged, HF>& sm, uint32_t& phase,
                                            typename Pol::Ctx& ctx) {
+    using HistT = typename WinOf<HF>::T;
+    constexpr int WWS = WinOf<HF>::W;  // the window's row length in texels
     using RawVel = typename std::conditional<MC == 4, uint2, uint32_t>::type;
     constexpr int SPAN = INTERP == 2 ? 4 : 2;
     const int tid = threadIdx.x, lx = tid & 31, sy = tid >> 5;
@@ -479,15 +504,17 @@ __device__ __forceinline__ void strip_tile(const Args& a, const CUtensorMap* hma
         float f;
         const int rux = axis_first<INTERP>(__fmul_rn(hu[0], (float)W), f);
         const int ruy = axis_first<INTERP>(__fmul_rn(hv[0], (float)H), f);
-        const int wx0 = rux - (cx - x0) - MARGIN, wy0 = ruy - (crow(ya) - y0) - MARGIN;
-        const bool interior = wx0 >= 0 && wy0 >= 0 && wx0 <= W - WW && wy0 <= H - WH;
+        int wx0 = rux - (cx - x0) - MARGIN;
+        if (HF == 1) wx0 -= wx0 & 1;  // an even texel: its TMA coordinate is a multiple of 16 bytes
+        const int wy0 = ruy - (crow(ya) - y0) - MARGIN;
+        const bool interior = wx0 >= 0 && wy0 >= 0 && wx0 <= W - WWS && wy0 <= H - WH;
         const int mode = tma_ok && interior ? 1 : 2;
         sm.org[0] = wx0;
         sm.org[1] = wy0;
         sm.org[2] = mode;
         if (mode == 1) {
             if (!PERSIST) mbar_init(&sm.bar, 1);
-            mbar_expect_tx(&sm.bar, (uint32_t)(sizeof(float4) * WW * WH));
+            mbar_expect_tx(&sm.bar, (uint32_t)(sizeof(HistT) * WWS * WH));
             if (TAA_FAST_TMA2D) tiled::tma_load_2d(sm.win, hmap, 4 * wx0, wy0, &sm.bar);
             else tma_load_3d(sm.win, hmap, 0, wx0, wy0, &sm.bar);
         }
@@ -510,8 +537,9 @@ __device__ __forceinline__ void strip_tile(const Args& a, const CUtensorMap* hma
         const int lane = tid & 31, warp = tid >> 5;
         for (int r = warp; r < WH; r += NT / 32) {
             const int gy = clampi(wy0 + r, 0, H - 1);
-            for (int c = lane; c < WW; c += 32)
-                cp_async<16>(&sm.win[r * WW + c], at<float4>(a.hist, a.hist_pitch, clampi(wx0 + c, 0, W - 1), gy));
+            for (int c = lane; c < WWS; c += 32)
+                cp_async<sizeof(HistT)>(&sm.win[r * WWS + c],
+                                        at<HistT>(a.hist, a.hist_pitch, clampi(wx0 + c, 0, W - 1), gy));
         }
         cp_async_commit();
     }
@@ -555,13 +583,13 @@ __device__ __forceinline__ void strip_tile(const Args& a, const CUtensorMap* hma
             coherent = coherent && __float_as_uint(hu[k]) == __float_as_uint(hu[0]) && uy[k] == uy[0] + k;
         }
         const int bx = ux - wx0, by = uy[0] - wy0;
-        coherent = coherent && (unsigned)bx <= (unsigned)(WW - SPAN) && (unsigned)by <= (unsigned)(WH - SPAN - NPX + 1);
+        coherent = coherent && (unsigned)bx <= (unsigned)(WWS - SPAN) && (unsigned)by <= (unsigned)(WH - SPAN - NPX + 1);
         if (TAA_FAST_SHARED_TAPS && coherent) {
             float wx[4], wy[NPX][4];
             axis_weights<INTERP>(fx, wx);
 #pragma unroll
             for (int k = 0; k < NPX; ++k) axis_weights<INTERP>(fy[k], wy[k]);
-            const float4* wp = &sm.win[by * WW + bx];
+            const HistT* wp = &sm.win[by * WWS + bx];
             f2 acc[NPX];
             float accb[NPX];
 #pragma unroll
@@ -575,7 +603,7 @@ __device__ __forceinline__ void strip_tile(const Args& a, const CUtensorMap* hma
                 float rb = 0.f;
 #pragma unroll
                 for (int i = 0; i < SPAN; ++i) {
-                    const float4 t = lds128(&wp[j * WW + i]);
+                    const float4 t = win_texel(&wp[j * WWS + i]);
                     r = fmap(dup(wx[i]), pk(t.x, t.y), r);
                     rb = fmaf(wx[i], t.z, rb);
                 }
@@ -594,13 +622,15 @@ __device__ __forceinline__ void strip_tile(const Args& a, const CUtensorMap* hma
             for (int k = 0; k < NPX; ++k) {
                 const Taps t = taps_of<INTERP>(hu[k], hv[k], a);
                 const int tbx = t.ux - wx0, tby = t.uy - wy0;
-                if ((unsigned)tbx <= (unsigned)(WW - SPAN) && (unsigned)tby <= (unsigned)(WH - SPAN)) {
-                    const float4* wp = &sm.win[tby * WW + tbx];
-                    h[k] = filter<SPAN>(t, [&](int i, int j) { return lds128(&wp[j * WW + i]); });
+                if ((unsigned)tbx <= (unsigned)(WWS - SPAN) && (unsigned)tby <= (unsigned)(WH - SPAN)) {
+                    const HistT* wp = &sm.win[tby * WWS + tbx];
+                    h[k] = filter<SPAN>(t, [&](int i, int j) { return win_texel(&wp[j * WWS + i]); });
                 } else {
                     h[k] = filter<SPAN>(t, [&](int i, int j) {
-                        return __ldg(at<float4>(a.hist, a.hist_pitch, clampi(t.ux + i, 0, W - 1),
-                                                clampi(t.uy + j, 0, H - 1)));
+                        const HistT* g = at<HistT>(a.hist, a.hist_pitch, clampi(t.ux + i, 0, W - 1),
+                                                   clampi(t.uy + j, 0, H - 1));
+                        if constexpr (HF == 1) return half4_to_float4(__ldg(g));
+                        else return __ldg(g);
                     });
                 }
             }
@@ -790,25 +820,25 @@ __global__ void __launch_bounds__(NT, TAA_FUSED_MIN_BLOCKS)
 }
 
 
-// One view, one CTA per tile.
-template <class Pol, int INTERP, int MC>
+// One view, one CTA per tile; HF 1: RGBA16F history (a.hout_half set).
+template <class Pol, int INTERP, int MC, int HF = 0>
 __global__ void __launch_bounds__(NT, TAA_FAST_MIN_BLOCKS)
     resolve_strips(const Args a, const __grid_constant__ CUtensorMap hmap, const int tma_ok) {
-    __shared__ SmemT<typename Pol::Staged> sm;
+    __shared__ SmemT<typename Pol::Staged, HF> sm;
     uint32_t phase = 0;
     typename Pol::Ctx ctx;
-    strip_tile<Pol, INTERP, MC, false>(a, &hmap, tma_ok, blockIdx.x, blockIdx.y, sm, phase, ctx);
+    strip_tile<Pol, INTERP, MC, false, false, HF>(a, &hmap, tma_ok, blockIdx.x, blockIdx.y, sm, phase, ctx);
 }
 
 // One view with a policy that may reproject (its Reproj a kernel parameter).
-template <class Pol, int INTERP, int MC>
+template <class Pol, int INTERP, int MC, int HF = 0>
 __global__ void __launch_bounds__(NT, TAA_FAST_MIN_BLOCKS)
     resolve_strips_reproj(const Args a, const __grid_constant__ CUtensorMap hmap, const int tma_ok,
                           const __grid_constant__ Reproj rp) {
-    __shared__ SmemT<typename Pol::Staged> sm;
+    __shared__ SmemT<typename Pol::Staged, HF> sm;
     uint32_t phase = 0;
     typename Pol::Ctx ctx{&rp};
-    strip_tile<Pol, INTERP, MC, false>(a, &hmap, tma_ok, blockIdx.x, blockIdx.y, sm, phase, ctx);
+    strip_tile<Pol, INTERP, MC, false, false, HF>(a, &hmap, tma_ok, blockIdx.x, blockIdx.y, sm, phase, ctx);
 }
 
 // Many views in one launch: each CTA takes jobs blockIdx.x, blockIdx.x +

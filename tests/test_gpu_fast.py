@@ -57,9 +57,16 @@ def test_auto_selects_the_fast_form_in_the_benchmark_mode(cuda):
         ctx.set_uniforms(T.make_uniforms(WL.base_parameters(**params)))
         assert ctx.selected_form() == want, params
     ctx.close()
+    # RGBA16F history (the reference's own storage) runs in the fast form too, but not
+    # with the one-launch sharpener
     ctx = T.Taa(64, 32, history_format=T.TAA_HISTORY_RGBA16F, form=T.TAA_FORM_FAST)
     ctx.set_uniforms(T.make_uniforms(WL.base_parameters()))
-    assert ctx.selected_form() == T.TAA_FORM_TILED  # RGBA16F history: the exact form
+    assert ctx.selected_form() == T.TAA_FORM_FAST
+    ctx.close()
+    ctx = T.Taa(64, 32, history_format=T.TAA_HISTORY_RGBA16F, sharpener=T.TAA_SHARPEN_CAS,
+                flags=T.TAA_FLAG_FUSED_SHARPEN)
+    ctx.set_uniforms(T.make_uniforms(WL.base_parameters()))
+    assert ctx.selected_form() == T.TAA_FORM_TILED
     ctx.close()
 
 
@@ -318,3 +325,75 @@ def test_reference_default_mode_sequence_against_fp64(cuda):
     ctx.close()
     print("C1 reference defaults, fast form (frame, relL2 vs FP32, vs FP64):", rep)
     assert max(r[1] for r in rep) <= 1e-4 and max(r[2] for r in rep) <= 1e-4
+
+
+@pytest.mark.parametrize("size", [(70, 41), (256, 144), (33, 31), (1, 1), (40, 1)], ids=lambda s: f"{s[0]}x{s[1]}")
+@pytest.mark.parametrize("mode", ["benchmark", "defaults"])
+def test_fast_form_with_rgba16f_history(cuda, size, mode):
+    """RGBA16F history (the reference's TAA_IMAGE_FORMAT_RGB) in the fast form: the
+    window holds RGBA16F texels, the history is stored as RGBA16F.  Against the
+    exact form with the same storage: most pixels round to the same FP16 value,
+    the rest one FP16 step apart (frame relative L2 within 5e-4); against the
+    FP64 oracle fed the same FP16 history, within 5e-4 after the store as well."""
+    w, h = size
+    if mode == "defaults":
+        p = T.default_parameters()
+        wl = WL.small(w, h, frames=2, seed=w + 3 * h)
+    else:
+        wl = WL.small(w, h, frames=2, seed=w + 3 * h, params=dict(mDepthCulling=1, mRejectOutside=1))
+        p = wl.parameters()
+    fr = cpu_frames(wl, range(2))
+    hist = fr[0]["color"].astype(np.float16).astype(np.float32)
+    u = T.make_uniforms(p, jitter_ndc=fr[1]["jitter"])
+    outs = {}
+    for form in (T.TAA_FORM_AUTO, T.TAA_FORM_TILED):
+        ctx = T.Taa(w, h, form=form, history_format=T.TAA_HISTORY_RGBA16F)
+        ctx.set_uniforms(u)
+        assert ctx.selected_form() == (T.TAA_FORM_FAST if form == T.TAA_FORM_AUTO else T.TAA_FORM_TILED)
+        outs[form] = gpu_resolve(ctx, cuda, fr[1]["color"], fr[1]["depth"], fr[1]["motion"], hist, fr[0]["depth"],
+                                 history_fp16=True)
+        ctx.close()
+    f, t = outs[T.TAA_FORM_AUTO]["history_out"], outs[T.TAA_FORM_TILED]["history_out"]
+    assert np.all(np.isfinite(f))
+    assert rel_l2(f[..., :3], t[..., :3]) <= 5e-4
+    r64 = O.resolve(u, fr[1]["color"].astype(np.float32), fr[1]["depth"], fr[1]["motion"].astype(np.float32),
+                    history=hist, history_depth=fr[0]["depth"], precision=64)["history"][..., :3]
+    r64h = r64.astype(np.float16).astype(np.float64)
+    assert rel_l2(f[..., :3], r64h) <= max(5e-4, 3.0 * rel_l2(t[..., :3], r64h))
+    assert T.device_status(clear=True) == 0
+
+
+def test_rgba16f_history_chain_at_4k(cuda):
+    """The C2 workload's first 16 frames with RGBA16F history, fast form against the
+    exact form, each on its own history.  FP16 storage has a dead band: a blend step
+    smaller than half an FP16 step of the history (|alpha (c - h)| < 2^-12 |h|) does
+    not move it, so two chains whose arithmetic differs by a rounding settle up to
+    about 2^-12 / alpha = 2.4e-3 relative apart per pixel (measured frame relative
+    L2 1.2e-3 at frame 8, 2.2e-3 at frame 15).  Bar 5e-3; each single resolve from
+    the same history is within 5e-4 (the test above)."""
+    wl = WL.c2()
+    sc = wl.scene()
+    H, W = wl.height, wl.width
+    ctxs = {f: T.Taa(W, H, form=f, history_format=T.TAA_HISTORY_RGBA16F) for f in (T.TAA_FORM_AUTO, T.TAA_FORM_TILED)}
+    hists = {f: [torch.zeros(H, W, 4, dtype=torch.float16, device=cuda) for _ in range(2)] for f in ctxs}
+    prev = None
+    rep = []
+    for fi in range(16):
+        col, dep, mot = render(wl, sc, fi, cuda)
+        u = T.make_uniforms(wl.parameters(), jitter_ndc=T.synth_jitter(sc, fi)[1], mResetHistory=1 if fi == 0 else 0)
+        for f, ctx in ctxs.items():
+            ctx.set_uniforms(u)
+            hb = hists[f]
+            ctx.resolve(color=col, depth=dep, velocity=mot, history=hb[fi & 1], history_depth=prev if prev is not None else dep,
+                        history_out=hb[(fi + 1) & 1])
+        torch.cuda.synchronize()
+        if fi in (8, 15):
+            a = hists[T.TAA_FORM_AUTO][(fi + 1) & 1][..., :3].float().cpu().numpy()
+            b = hists[T.TAA_FORM_TILED][(fi + 1) & 1][..., :3].float().cpu().numpy()
+            rep.append((fi, rel_l2(a, b)))
+        prev = dep
+    assert ctxs[T.TAA_FORM_AUTO].selected_form() == T.TAA_FORM_FAST
+    for ctx in ctxs.values():
+        ctx.close()
+    print("C2 RGBA16F history, fast vs exact (frame, relL2):", rep)
+    assert all(e <= 5e-3 for _, e in rep), rep
