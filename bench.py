@@ -666,6 +666,12 @@ def summarize(form_name, mpx, frac, forms, e2e, cpu):
                 out[f"{k}_vs_tiled"] = g(k) / tiled
     if g("plain"):
         out["value_vs_plain"] = mpx / g("plain")
+    if g("fast_rgba16f_history"):
+        out["fast_rgba16f_history_mpx_s"] = g("fast_rgba16f_history")
+    m = (f.get("modes") or {}).get("reference_defaults")
+    if m:
+        out["reference_defaults_us"] = m["us_per_frame"]
+        out["reference_defaults_form"] = m["form"]
     b = f.get("batch48")
     if b:
         out["batch48_mpx_s"] = b["mpx_s"]
