@@ -738,9 +738,7 @@ def run_ours(args):
     hist = [torch.zeros(H, W, 4, dtype=torch.float32, device=dev) for _ in range(2)]
     res = torch.empty(H, W, 4, dtype=torch.float16, device=dev)
     torch.cuda.synchronize()
-    # the end-to-end run's pinned host images, taken while the process is young: taken
-    # after the rest of the run's allocations, the same buffers measured 5 Gpx/s end to
-    # end against 9.6-12.3 here
+    # the end-to-end run's pinned host images, taken while the process is young
     if not args.no_e2e:
         h_col = col.cpu().pin_memory()
         h_dep = dep.cpu().pin_memory()
@@ -803,68 +801,8 @@ def run_ours(args):
     achieved = launch_bytes / avg_launch_s / 1e9
     traffic, traffic_src = load_traffic(form_name)
 
-    forms = {form_name: {"mpx_s": mpx, "gb_s": achieved, "frac_of_hbm": achieved / peak}}
-    if not args.no_forms:
-        for fid, name, fl in ((T.TAA_FORM_TILED, "tiled", 0), (T.TAA_FORM_PLAIN, "plain", 0),
-                              (T.TAA_FORM_FP16, "fp16", 0), (T.TAA_FORM_FP16, "fp16_guarded", T.TAA_FLAG_FP16_GUARD)):
-            if name in forms:
-                continue
-            c2 = make_ctx(fid, fl)
-            k = max(2, args.steps // 4)
-            m2 = timed(c2, k, 1)
-            v = job_throughput(W * H * F * k, world, m2 / 1e3) / 1e6
-            g = launch_bytes / (m2 / 1e3 / (k * F)) / 1e9
-            forms[name] = {"mpx_s": v, "gb_s": g, "frac_of_hbm": g / peak}
-            c2.close()
-        # RGBA16F history (the reference's storage format) in the fast form: 44 B/px
-        hist16 = [torch.zeros(H, W, 4, dtype=torch.float16, device=dev) for _ in range(2)]
-        c2 = T.Taa(W, H, form=T.TAA_FORM_AUTO, history_format=T.TAA_HISTORY_RGBA16F)
-        gs = torch.cuda.Stream(dev)
-        graph = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(graph, stream=gs):
-            for f in range(F):
-                c2.set_uniforms(uniforms[f])
-                c2.resolve(stream=gs.cuda_stream, color=col[f], depth=dep[f], velocity=mot[f], history=hist16[f & 1],
-                           history_depth=dep[f - 1] if f else dep[0], history_out=hist16[(f + 1) & 1], result=res)
-        graph.replay()
-        torch.cuda.synchronize()
-        k = max(2, args.steps // 4)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(k):
-            graph.replay()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        m2 = max_over_ranks(e0.elapsed_time(e1), world, dev)
-        b16 = bpp - 16
-        v = job_throughput(W * H * F * k, world, m2 / 1e3) / 1e6
-        g = b16 * W * H / (m2 / 1e3 / (k * F)) / 1e9
-        forms["fast_rgba16f_history"] = {"mpx_s": v, "gb_s": g, "frac_of_hbm": g / peak, "bytes_per_px": b16,
-                                         "form": {5: "fast", 2: "tiled"}.get(c2.selected_form(), "other")}
-        c2.close()
-        del graph, hist16
-
-    # the 48-view batch (C4 sizes, log-uniform 320x180 .. 3840x2160): one launch per step
-    if not args.no_batch:
-        forms["batch48"] = time_batch(T, WL, dev, stream, sid, world, args, peak, mpx / world)
-
-    # the ray-trace-assist classification (tiled and plain), TAAU and debug output (plain form), post-process
-    if not args.no_modes and rank == 0:
-        forms["modes"] = time_modes(T, WL, dev, stream, sid, args, peak)
-
-    # the resolve with the CAS sharpener (C3: 2560x1440), one pass against two dispatches
-    if not args.no_c3 and rank == 0:
-        forms["c3_cas"] = time_c3(T, WL, dev, stream, sid, args, peak)
-
-    # the FXAA pass on the segmentation mask (ray-trace-assist path) at 4K
-    if not args.no_fxaa and rank == 0:
-        forms["fxaa"] = time_fxaa(T, WL, dev, stream, sid, args, peak, col, dep, mot, uniforms)
-
-    # the learned rectifier (C5: 1920x1080): trained here, judged against the 64-spp truth
-    if not args.no_learned and rank == 0:
-        forms["learned"] = time_learned(T, WL, dev, stream, sid, args)
-
-    # end to end through the C ABI with host buffers (pinned), copies inside the timed region
+    # end to end right after the headline (the rest of the run allocates much more: placed
+    # after it, the same measurement gave 5 Gpx/s; here 11.2-12.4, the host link's rate)
     e2e = None
     if not args.no_e2e:
         nbuf = 3
@@ -933,6 +871,68 @@ def run_ours(args):
         torch.cuda.synchronize()
         e2e["result_matches_device_resolve"] = bool(torch.equal(ref.cpu(), h_out[F - 1]))
         ectx.close()
+
+
+    forms = {form_name: {"mpx_s": mpx, "gb_s": achieved, "frac_of_hbm": achieved / peak}}
+    if not args.no_forms:
+        for fid, name, fl in ((T.TAA_FORM_TILED, "tiled", 0), (T.TAA_FORM_PLAIN, "plain", 0),
+                              (T.TAA_FORM_FP16, "fp16", 0), (T.TAA_FORM_FP16, "fp16_guarded", T.TAA_FLAG_FP16_GUARD)):
+            if name in forms:
+                continue
+            c2 = make_ctx(fid, fl)
+            k = max(2, args.steps // 4)
+            m2 = timed(c2, k, 1)
+            v = job_throughput(W * H * F * k, world, m2 / 1e3) / 1e6
+            g = launch_bytes / (m2 / 1e3 / (k * F)) / 1e9
+            forms[name] = {"mpx_s": v, "gb_s": g, "frac_of_hbm": g / peak}
+            c2.close()
+        # RGBA16F history (the reference's storage format) in the fast form: 44 B/px
+        hist16 = [torch.zeros(H, W, 4, dtype=torch.float16, device=dev) for _ in range(2)]
+        c2 = T.Taa(W, H, form=T.TAA_FORM_AUTO, history_format=T.TAA_HISTORY_RGBA16F)
+        gs = torch.cuda.Stream(dev)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=gs):
+            for f in range(F):
+                c2.set_uniforms(uniforms[f])
+                c2.resolve(stream=gs.cuda_stream, color=col[f], depth=dep[f], velocity=mot[f], history=hist16[f & 1],
+                           history_depth=dep[f - 1] if f else dep[0], history_out=hist16[(f + 1) & 1], result=res)
+        graph.replay()
+        torch.cuda.synchronize()
+        k = max(2, args.steps // 4)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            graph.replay()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        m2 = max_over_ranks(e0.elapsed_time(e1), world, dev)
+        b16 = bpp - 16
+        v = job_throughput(W * H * F * k, world, m2 / 1e3) / 1e6
+        g = b16 * W * H / (m2 / 1e3 / (k * F)) / 1e9
+        forms["fast_rgba16f_history"] = {"mpx_s": v, "gb_s": g, "frac_of_hbm": g / peak, "bytes_per_px": b16,
+                                         "form": {5: "fast", 2: "tiled"}.get(c2.selected_form(), "other")}
+        c2.close()
+        del graph, hist16
+
+    # the 48-view batch (C4 sizes, log-uniform 320x180 .. 3840x2160): one launch per step
+    if not args.no_batch:
+        forms["batch48"] = time_batch(T, WL, dev, stream, sid, world, args, peak, mpx / world)
+
+    # the ray-trace-assist classification (tiled and plain), TAAU and debug output (plain form), post-process
+    if not args.no_modes and rank == 0:
+        forms["modes"] = time_modes(T, WL, dev, stream, sid, args, peak)
+
+    # the resolve with the CAS sharpener (C3: 2560x1440), one pass against two dispatches
+    if not args.no_c3 and rank == 0:
+        forms["c3_cas"] = time_c3(T, WL, dev, stream, sid, args, peak)
+
+    # the FXAA pass on the segmentation mask (ray-trace-assist path) at 4K
+    if not args.no_fxaa and rank == 0:
+        forms["fxaa"] = time_fxaa(T, WL, dev, stream, sid, args, peak, col, dep, mot, uniforms)
+
+    # the learned rectifier (C5: 1920x1080): trained here, judged against the 64-spp truth
+    if not args.no_learned and rank == 0:
+        forms["learned"] = time_learned(T, WL, dev, stream, sid, args)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
