@@ -77,8 +77,10 @@ typedef enum taa_status {
  * mode (RGB, 3x3 minimum/maximum box, clamp, velocity for every pixel, for
  * movers only or reprojection through the matrices, none of those blend
  * modifiers; without a fused sharpener or a batch), each with Catmull-Rom or
- * bilinear history, equal source and target sizes and no debug binding;
- * other parameters run in TAA_FORM_TILED.  RGBA32F history, or RGBA16F (the
+ * bilinear history and no debug binding, equal source and target sizes, or
+ * (the benchmark mode, RGBA32F history) upsampling (taa_uniforms_t
+ * mUpsampling, a source no larger than the target on either axis); other
+ * parameters run in TAA_FORM_TILED.  RGBA32F history, or RGBA16F (the
  * reference's storage; one resolve within 5e-4 of the exact form after the
  * FP16 store) for one view without the one-launch sharpener. */
 #define TAA_FORM_FAST   5u

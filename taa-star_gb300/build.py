@@ -33,6 +33,7 @@ UNITS = {
     "resolve_fast.cu": ["-fmad=false"],
     "resolve_tiled.cu": ["-fmad=false"],
     "resolve_fast32.cu": [],
+    "resolve_up32.cu": [],
     "resolve_learned_strips.cu": [],
     "resolve_half.cu": [],
     "resolve_half_guard.cu": [],

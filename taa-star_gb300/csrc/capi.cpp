@@ -516,7 +516,11 @@ static int select_form(const taa_ctx* c, const taa_frame_io_t* io) {
     const bool fused = fused_sharpen(d);
     if (!taa_dev::fast_path_supported(c->uniforms, d.in_width, d.in_height, d.out_width, d.out_height, !fused,
                                       !fused)) {
-        // upsampling: the tiled FP32 form's path for it
+        // upsampling: the fast form's path for it in the benchmark mode, else the tiled FP32 form's
+        if (!fused && !(io && io->debug) && (d.form == TAA_FORM_AUTO || d.form == TAA_FORM_FAST) &&
+            taa_dev::fast32_up_supported(c->uniforms, (int)d.history_format, d.in_width, d.in_height, d.out_width,
+                                         d.out_height))
+            return TAA_FORM_FAST;
         if (!fused && !(io && io->debug) &&
             taa_dev::up_path_supported(c->uniforms, d.in_width, d.in_height, d.out_width, d.out_height))
             return TAA_FORM_TILED;
@@ -582,6 +586,9 @@ int taa_resolve(taa_ctx* c, void* stream, const taa_frame_io_t* io) {
         if (sharpen && !fused_sharpen(d) && !a.result.p) a.result = ImgW{(char*)c->scratch_screen, c->scratch_pitch};
         if (form == TAA_FORM_FAST && fused_sharpen(d)) {
             e = taa_dev::launch_resolve_fast32_sharpen(mc, (int)d.sharpener, U, a, s);
+        } else if (form == TAA_FORM_FAST && (d.in_width != d.out_width || d.in_height != d.out_height)) {
+            e = taa_dev::launch_resolve_fast32_up(mc, U, a, s);
+            if (e == cudaSuccess && sharpen) e = taa_dev::launch_sharpen((int)d.sharpener, a, s);
         } else if (form == TAA_FORM_FAST) {
             e = taa_dev::launch_resolve_fast32(mc, (int)d.history_format, U, a, s);
             if (e == cudaSuccess && sharpen) e = taa_dev::launch_sharpen((int)d.sharpener, a, s);

@@ -188,7 +188,7 @@ __device__ __forceinline__ UpAxis upsample_axis(int t, int hi, int lo, float tj,
     return r;
 }
 // The jitter of an axis in source texels (taa.comp:225-227) and the axis scale.
-__device__ __forceinline__ float upsample_jitter(float jitter_ndc, float unjitter_factor, int lo) {
+__host__ __device__ __forceinline__ float upsample_jitter(float jitter_ndc, float unjitter_factor, int lo) {
     return jitter_ndc * 0.5f * unjitter_factor * (float)lo * -1.0f;
 }
 // True (beta = 1) with the source texel (fx, fy) when a sample lands.

@@ -43,6 +43,9 @@ bool fast32_supported(const taa_uniforms_t& U, int history_fmt, int in_w, int in
 // the reference's default mode (RGB, minimum/maximum box, clamp, any velocity
 // use), RGBA32F or RGBA16F history.
 bool fast32_single_supported(const taa_uniforms_t& U, int history_fmt, int in_w, int in_h, int out_w, int out_h);
+// TAA_FORM_FAST for upsampling (TAAU) in the benchmark mode, RGBA32F history.
+bool fast32_up_supported(const taa_uniforms_t& U, int history_fmt, int in_w, int in_h, int out_w, int out_h);
+cudaError_t launch_resolve_fast32_up(int motion_ch, const taa_uniforms_t& U, const FrameArgs& f, cudaStream_t s);
 cudaError_t launch_resolve_fast32(int motion_ch, int history_fmt, const taa_uniforms_t& U, const FrameArgs& f,
                                   cudaStream_t s);
 // TAA_FORM_FAST and the sharpener (TAA_SHARPEN_SIMPLE or TAA_SHARPEN_CAS) in

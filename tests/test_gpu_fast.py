@@ -397,3 +397,40 @@ def test_rgba16f_history_chain_at_4k(cuda):
         ctx.close()
     print("C2 RGBA16F history, fast vs exact (frame, relL2):", rep)
     assert all(e <= 5e-3 for _, e in rep), rep
+
+
+@pytest.mark.parametrize("sizes", [((48, 32), (96, 64)), ((64, 40), (96, 60)), ((80, 45), (97, 61)),
+                                   ((40, 40), (40, 72)), ((960, 540), (1920, 1080)), ((7, 5), (13, 9))],
+                         ids=["2x", "1.5x", "odd", "one_axis", "1080p", "tiny"])
+@pytest.mark.parametrize("mode", ["base", "c2", "bilinear", "rgba16f_motion", "first_frame"])
+def test_fast_upsampling(cuda, sizes, mode):
+    """TAAU in the fast form (AUTO's choice in the benchmark mode): as close to the
+    FP64 oracle as the exact tiled form's upsampling path (within 1e-5 relative L2,
+    or three times the exact form's distance on frames a few pixels decide), and
+    within 1e-4 of it."""
+    (w, h), (ow, oh) = sizes
+    params = dict(mDepthCulling=1, mRejectOutside=1) if mode == "c2" else \
+        dict(mInterpolationMode=0) if mode == "bilinear" else {}
+    mc = 4 if mode == "rgba16f_motion" else 2
+    wl = WL.small(w, h, frames=2, seed=ow + 7 * oh, params=params)
+    fr = cpu_frames(wl, range(2), motion_channels=mc)
+    rng = np.random.default_rng(ow)
+    hist = None if mode == "first_frame" else np.ascontiguousarray(rng.uniform(0.0, 2.0, (oh, ow, 4)).astype(np.float32))
+    u = T.make_uniforms(wl.parameters(), jitter_ndc=fr[1]["jitter"], mUpsampling=1,
+                        mResetHistory=1 if mode == "first_frame" else 0)
+    outs = {}
+    for form in (T.TAA_FORM_AUTO, T.TAA_FORM_TILED):
+        ctx = T.Taa(w, h, ow, oh, form=form, motion_format=T.TAA_MOTION_RGBA16F if mc == 4 else T.TAA_MOTION_RG16F)
+        ctx.set_uniforms(u)
+        assert ctx.selected_form() == (T.TAA_FORM_FAST if form == T.TAA_FORM_AUTO else T.TAA_FORM_TILED)
+        outs[form] = gpu_resolve(ctx, cuda, fr[1]["color"], fr[1]["depth"], fr[1]["motion"], hist, fr[0]["depth"])
+        ctx.close()
+    f, t = outs[T.TAA_FORM_AUTO], outs[T.TAA_FORM_TILED]
+    assert np.all(np.isfinite(f["history_out"]))
+    r64 = O.resolve(u, fr[1]["color"].astype(np.float32), fr[1]["depth"], fr[1]["motion"].astype(np.float32),
+                    history=hist, history_depth=fr[0]["depth"], out_size=(ow, oh), precision=64)["history"][..., :3]
+    e_fast, e_exact = rel_l2(f["history_out"][..., :3], r64), rel_l2(t["history_out"][..., :3], r64)
+    assert e_fast <= max(FAST_RELL2, 3.0 * e_exact), (e_fast, e_exact)
+    assert rel_l2(f["history_out"][..., :3], t["history_out"][..., :3]) <= 1e-4
+    assert np.all(f["history_out"][..., 3] == 0.0)
+    assert T.device_status(clear=True) == 0

@@ -395,7 +395,7 @@ def test_upsampling_runs_in_the_tiled_form(cuda, mode, sizes):
     hist = np.ascontiguousarray(rng.uniform(0.0, 2.0, (oh, ow, 4)).astype(np.float32))
     u = T.make_uniforms(wl.parameters(), jitter_ndc=fr[1]["jitter"], mUpsampling=1)
     outs = {}
-    for form in (T.TAA_FORM_PLAIN, T.TAA_FORM_AUTO):
+    for form in (T.TAA_FORM_PLAIN, T.TAA_FORM_TILED):
         ctx = T.Taa(w, h, ow, oh, form=form)
         ctx.set_uniforms(u)
         outs[ctx.selected_form()] = gpu_resolve(ctx, cuda, fr[1]["color"], fr[1]["depth"], fr[1]["motion"], hist,
