@@ -374,9 +374,10 @@ def time_modes(T, WL, dev, stream, sid, args, peak):
     """The resolve modes outside the benchmark mode: the ray-trace-assist
     classification writing the segmentation mask (every test, history count 8)
     TAAU upsampling (1920x1080 source, 3840x2160 target), a debug output
-    (mode 2) and the reference's default parameter block, each in the tiled
-    form (the form selected by default) and in the plain form (one thread per
-    pixel).  Each on four rotating frames of the
+    (mode 2) and the reference's default parameter block, each in the form
+    AUTO selects (recorded per entry: the fast form for TAAU and the default
+    block, the tiled form for the others) and in the plain form (one thread
+    per pixel).  Each on four rotating frames of the
     C2 scene (every frame's bindings exceed the L2), CUDA events over 12
     launches after 3.  Material ids and uv/normals are seeded synthetic blocks
     (48 px materials, 8 px normals).  Last the post-process pass at 4K (split,
@@ -483,7 +484,8 @@ def time_modes(T, WL, dev, stream, sid, args, peak):
     up = [T.make_uniforms(lo.parameters(), jitter_ndc=T.synth_jitter(sc, 1 + i)[1], mUpsampling=1) for i in range(n)]
     # per target pixel history in/out 16 + 16 and screen 8; per source pixel colour 8, depth 4, motion 4, previous depth 4
     up_bpp = 40 + 20 * (lo.width * lo.height) / (W * H)
-    for name, form in (("upsample_2x", T.TAA_FORM_AUTO), ("upsample_2x_plain", T.TAA_FORM_PLAIN)):
+    for name, form in (("upsample_2x", T.TAA_FORM_AUTO), ("upsample_2x_tiled", T.TAA_FORM_TILED),
+                       ("upsample_2x_plain", T.TAA_FORM_PLAIN)):
         ctx = T.Taa(lo.width, lo.height, W, H, form=form)
         run(name, ctx, up, base, up_bpp, W * H)
         out[name]["source"] = [lo.width, lo.height]
