@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--no-c3", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--profile", choices=["fast", "tiled", "fp16", "plain", "batch48", "fxaa", "fused", "defaults",
-                                          "learned"],
+                                          "learned", "up"],
                     help="a small case for ncu: a few launches of one form on 4K frames (no JSON line)")
     return ap.parse_args()
 
@@ -1023,6 +1023,23 @@ def run_profile_case(args):
         for i in range(4):
             T.fxaa(res, out, seg if i < 3 else None, stream=sid, ctx=fctx)
         fctx.close()
+        torch.cuda.synchronize()
+        ctx.close()
+        return 0
+    if args.profile == "up":  # TAAU 1920x1080 -> 3840x2160 in the fast form, two resolves
+        lo = WL.Workload("C2 scene at 1920x1080", 1920, 1080, F, seed=wl.seed, num_spheres=wl.num_spheres,
+                         cam_v0=(1.0, 0.0), cam_accel=(19.0 / 63.0, 0.0), radius=(10.0, 60.0), params=dict(wl.params))
+        lsc = lo.scene()
+        lc = torch.empty(F, 1080, 1920, 4, dtype=torch.float16, device=dev)
+        ld = torch.empty(F, 1080, 1920, dtype=torch.float32, device=dev)
+        lm = torch.empty(F, 1080, 1920, 2, dtype=torch.float16, device=dev)
+        for f in range(F):
+            T.synth_render(lsc, f, stream=sid, color=lc[f], depth=ld[f], motion=lm[f])
+        ctx = T.Taa(1920, 1080, W, H)
+        for f in range(1, F):
+            ctx.set_uniforms(T.make_uniforms(lo.parameters(), jitter_ndc=T.synth_jitter(lsc, f)[1], mUpsampling=1))
+            ctx.resolve(stream=sid, color=lc[f], depth=ld[f], velocity=lm[f], history=hist[f & 1],
+                        history_depth=ld[f - 1], history_out=hist[(f + 1) & 1], result=res)
         torch.cuda.synchronize()
         ctx.close()
         return 0
