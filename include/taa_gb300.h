@@ -70,17 +70,18 @@ typedef enum taa_status {
  * approximations in the variance box and the clip.  Frame error within 1e-4
  * relative L2 of the FP64 oracle and of TAA_FORM_TILED on the benchmark
  * sequences (measured 2e-5 to 6e-5; the exact FP32 form is 1e-5 to 5e-5 from
- * FP64).  It runs two modes of the parameter block: the benchmark mode
- * (YCoCg variance clip toward the box centre, velocity for every pixel with
- * simple sampling, no tonemap, luma weighting, near-clamp reduction,
- * velocity-based alpha, noise or anti-ghosting) and the reference's default
- * mode (RGB, 3x3 minimum/maximum box, clamp, velocity for every pixel, for
- * movers only or reprojection through the matrices, none of those blend
- * modifiers; without a fused sharpener or a batch), each with Catmull-Rom or
- * bilinear history and no debug binding, equal source and target sizes, or
- * (the benchmark mode, RGBA32F history) upsampling (taa_uniforms_t
- * mUpsampling, a source no larger than the target on either axis); other
- * parameters run in TAA_FORM_TILED.  RGBA32F history, or RGBA16F (the
+ * FP64).  It runs the parameter block's rectification modes without a
+ * tonemap, shaped neighbourhood, chroma-axis shrinking or blend modifiers
+ * (luma weighting, near-clamp reduction, velocity-based alpha, noise,
+ * anti-ghosting, ray-trace assist): YCoCg or RGB, the variance or the 3x3
+ * minimum/maximum box, clamp or the clip toward the box centre, velocity for
+ * every pixel, for movers only or reprojection through the matrices, simple
+ * velocity sampling, Catmull-Rom or bilinear history, no debug binding.  The
+ * benchmark mode (YCoCg, variance, clip, velocity for every pixel) also runs
+ * with a fused sharpener, in a batch and with upsampling (taa_uniforms_t
+ * mUpsampling, a source no larger than the target on either axis); the other
+ * modes run for one view of equal source and target sizes.  Other parameters
+ * run in TAA_FORM_TILED.  RGBA32F history, or RGBA16F (the
  * reference's storage; one resolve within 5e-4 of the exact form after the
  * FP16 store) for one view without the one-launch sharpener. */
 #define TAA_FORM_FAST   5u

@@ -34,6 +34,7 @@ UNITS = {
     "resolve_tiled.cu": ["-fmad=false"],
     "resolve_fast32.cu": [],
     "resolve_up32.cu": [],
+    "resolve_gen32.cu": [],
     "resolve_learned_strips.cu": [],
     "resolve_half.cu": [],
     "resolve_half_guard.cu": [],

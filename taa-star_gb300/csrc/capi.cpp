@@ -538,8 +538,10 @@ static int select_form(const taa_ctx* c, const taa_frame_io_t* io) {
     // one view without the one-launch sharpener: also the reference's default mode (clamp to
     // the RGB min/max box) and RGBA16F history on the strip body
     if ((d.form == TAA_FORM_AUTO || d.form == TAA_FORM_FAST) && !fused &&
-        taa_dev::fast32_single_supported(c->uniforms, (int)d.history_format, d.in_width, d.in_height, d.out_width,
-                                         d.out_height))
+        (taa_dev::fast32_single_supported(c->uniforms, (int)d.history_format, d.in_width, d.in_height, d.out_width,
+                                          d.out_height) ||
+         taa_dev::fast32_gen_supported(c->uniforms, (int)d.history_format, d.in_width, d.in_height, d.out_width,
+                                       d.out_height)))
         return TAA_FORM_FAST;
     return TAA_FORM_TILED;
 }
@@ -590,7 +592,10 @@ int taa_resolve(taa_ctx* c, void* stream, const taa_frame_io_t* io) {
             e = taa_dev::launch_resolve_fast32_up(mc, U, a, s);
             if (e == cudaSuccess && sharpen) e = taa_dev::launch_sharpen((int)d.sharpener, a, s);
         } else if (form == TAA_FORM_FAST) {
-            e = taa_dev::launch_resolve_fast32(mc, (int)d.history_format, U, a, s);
+            e = taa_dev::fast32_single_supported(U, (int)d.history_format, d.in_width, d.in_height, d.out_width,
+                                                 d.out_height)
+                    ? taa_dev::launch_resolve_fast32(mc, (int)d.history_format, U, a, s)
+                    : taa_dev::launch_resolve_fast32_gen(mc, U, a, s);
             if (e == cudaSuccess && sharpen) e = taa_dev::launch_sharpen((int)d.sharpener, a, s);
         } else if (form == TAA_FORM_FP16) {
             e = (d.flags & TAA_FLAG_FP16_GUARD)

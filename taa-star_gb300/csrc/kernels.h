@@ -46,6 +46,12 @@ bool fast32_single_supported(const taa_uniforms_t& U, int history_fmt, int in_w,
 // TAA_FORM_FAST for upsampling (TAAU) in the benchmark mode, RGBA32F history.
 bool fast32_up_supported(const taa_uniforms_t& U, int history_fmt, int in_w, int in_h, int out_w, int out_h);
 cudaError_t launch_resolve_fast32_up(int motion_ch, const taa_uniforms_t& U, const FrameArgs& f, cudaStream_t s);
+// TAA_FORM_FAST for the other rectification modes (YCoCg or RGB, variance or
+// min/max box, clamp or clip toward the centre, any velocity use), one view,
+// RGBA32F history, no fused sharpener.
+bool fast32_gen_mode(const taa_parameters_t& P);
+bool fast32_gen_supported(const taa_uniforms_t& U, int history_fmt, int in_w, int in_h, int out_w, int out_h);
+cudaError_t launch_resolve_fast32_gen(int motion_ch, const taa_uniforms_t& U, const FrameArgs& f, cudaStream_t s);
 cudaError_t launch_resolve_fast32(int motion_ch, int history_fmt, const taa_uniforms_t& U, const FrameArgs& f,
                                   cudaStream_t s);
 // TAA_FORM_FAST and the sharpener (TAA_SHARPEN_SIMPLE or TAA_SHARPEN_CAS) in

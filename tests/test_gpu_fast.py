@@ -53,7 +53,9 @@ def test_auto_selects_the_fast_form_in_the_benchmark_mode(cuda):
     for params, want in ((dict(), T.TAA_FORM_FAST), (dict(mDepthCulling=1, mRejectOutside=1), T.TAA_FORM_FAST),
                          (dict(mInterpolationMode=0), T.TAA_FORM_FAST), (dict(mInterpolationMode=1), T.TAA_FORM_TILED),
                          (dict(mToneMapLumaKaris=1), T.TAA_FORM_TILED),
-                         (dict(mColorClampingOrClipping=1), T.TAA_FORM_TILED)):
+                         (dict(mColorClampingOrClipping=1), T.TAA_FORM_FAST),
+                         (dict(mColorClampingOrClipping=3), T.TAA_FORM_TILED),
+                         (dict(mShapedNeighbourhood=1, mVarianceClipping=0), T.TAA_FORM_TILED)):
         ctx.set_uniforms(T.make_uniforms(WL.base_parameters(**params)))
         assert ctx.selected_form() == want, params
     ctx.close()
@@ -433,4 +435,43 @@ def test_fast_upsampling(cuda, sizes, mode):
     assert e_fast <= max(FAST_RELL2, 3.0 * e_exact), (e_fast, e_exact)
     assert rel_l2(f["history_out"][..., :3], t["history_out"][..., :3]) <= 1e-4
     assert np.all(f["history_out"][..., 3] == 0.0)
+    assert T.device_status(clear=True) == 0
+
+
+GEN_MODES = {f"{'ycocg' if yc else 'rgb'}-{'var' if var else 'minmax'}-{'clamp' if rect == 1 else 'clip'}":
+             dict(mUseYCoCg=yc, mVarianceClipping=var, mColorClampingOrClipping=rect)
+             for yc in (0, 1) for var in (0, 1) for rect in (1, 2)}
+
+
+@pytest.mark.parametrize("mode", list(GEN_MODES))
+@pytest.mark.parametrize("vel", [0, 2], ids=["reproject", "velocity"])
+@pytest.mark.parametrize("interp", [2, 0], ids=["catmull_rom", "bilinear"])
+def test_fast_form_in_every_rectification_mode(cuda, mode, vel, interp):
+    """Every combination of colour space (YCoCg, RGB), box (variance, min/max)
+    and rectification (clamp, clip toward the centre) with either velocity use
+    runs in the fast form (AUTO's choice), as close to the FP64 oracle as the
+    exact form and within 1e-4 of it."""
+    w, h = 96, 56
+    p = T.default_parameters()
+    for k, v in GEN_MODES[mode].items():
+        setattr(p, k, v)
+    p.mUseVelocityVectors, p.mInterpolationMode, p.mAlpha = vel, interp, 0.1
+    wl = WL.small(w, h, frames=2, seed=len(mode) * 7 + vel + interp)
+    fr = cpu_frames(wl, range(2), motion_channels=2)
+    u = skew_matrices(T.make_uniforms(p, jitter_ndc=fr[1]["jitter"]), seed=vel + interp)
+    hist = fr[0]["color"].astype(np.float32)
+    outs = {}
+    for form in (T.TAA_FORM_AUTO, T.TAA_FORM_TILED):
+        ctx = T.Taa(w, h, form=form)
+        ctx.set_uniforms(u)
+        assert ctx.selected_form() == (T.TAA_FORM_FAST if form == T.TAA_FORM_AUTO else T.TAA_FORM_TILED)
+        outs[form] = gpu_resolve(ctx, cuda, fr[1]["color"], fr[1]["depth"], fr[1]["motion"], hist, fr[0]["depth"])
+        ctx.close()
+    f, t = outs[T.TAA_FORM_AUTO], outs[T.TAA_FORM_TILED]
+    assert np.all(np.isfinite(f["history_out"]))
+    r64 = O.resolve(u, fr[1]["color"].astype(np.float32), fr[1]["depth"], fr[1]["motion"].astype(np.float32),
+                    history=hist, history_depth=fr[0]["depth"], precision=64)["history"][..., :3]
+    e_fast, e_exact = rel_l2(f["history_out"][..., :3], r64), rel_l2(t["history_out"][..., :3], r64)
+    assert e_fast <= max(FAST_RELL2, 3.0 * e_exact), (e_fast, e_exact)
+    assert rel_l2(f["history_out"][..., :3], t["history_out"][..., :3]) <= 1e-4
     assert T.device_status(clear=True) == 0
