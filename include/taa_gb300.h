@@ -71,12 +71,13 @@ typedef enum taa_status {
  * relative L2 of the FP64 oracle and of TAA_FORM_TILED on the benchmark
  * sequences (measured 2e-5 to 6e-5; the exact FP32 form is 1e-5 to 5e-5 from
  * FP64).  It runs the parameter block's rectification modes without a
- * tonemap, shaped neighbourhood, chroma-axis shrinking or blend modifiers
- * (luma weighting, near-clamp reduction, velocity-based alpha, noise,
- * anti-ghosting, ray-trace assist): YCoCg or RGB, the variance or the 3x3
- * minimum/maximum box, clamp or the clip toward the box centre, velocity for
- * every pixel, for movers only or reprojection through the matrices, simple
- * velocity sampling, Catmull-Rom or bilinear history, no debug binding.  The
+ * tonemap, shaped neighbourhood, noise, anti-ghosting or ray-trace assist:
+ * YCoCg (with or without chroma-axis shrinking) or RGB, the variance or the
+ * 3x3 minimum/maximum box, clamp or the clip toward the box centre, the
+ * velocity-based alpha, luma weighting and near-clamp reduction of the blend
+ * weight, velocity for every pixel, for movers only or reprojection through
+ * the matrices, simple velocity sampling, Catmull-Rom or bilinear history, no
+ * debug binding.  The
  * benchmark mode (YCoCg, variance, clip, velocity for every pixel) also runs
  * with a fused sharpener, in a batch and with upsampling (taa_uniforms_t
  * mUpsampling, a source no larger than the target on either axis); the other

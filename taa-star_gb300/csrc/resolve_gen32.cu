@@ -32,7 +32,10 @@ struct GenPol {
         }
     }
     static __device__ __forceinline__ void finish(const Args& a, const float4* sp, int x, int ya, const float3 h[NPX],
-                                                  unsigned rej, bool landed, const PixelInfo&, Ctx&) {
+                                                  unsigned rej, bool landed, const PixelInfo& px, Ctx& ctx) {
+        const Reproj& md = *ctx.rp;
+        // a colour's luma in the working space (taa.comp:855-893)
+        auto lum = [](const float c[3]) { return YC ? c[0] : 0.25f * c[0] + 0.5f * c[1] + 0.25f * c[2]; };
         Row r0, r1;
         RowMinMax q0, q1;
         if constexpr (VAR) {
@@ -76,6 +79,16 @@ struct GenPol {
                 q0 = q1;
                 q1 = q2;
             }
+            if (YC && md.shrink) {  // taa.comp:297-311: chroma half extents halved about the box centre
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float half = (c == 0 ? 0.5f : 0.25f) * (hi[c] - lo[c]), ce = (lo[c] + hi[c]) * 0.5f;
+                    lo[c] = ce - half;
+                    hi[c] = ce + half;
+                    p[c] = ce;
+                    e[c] = half + 1e-7f;
+                }
+            }
             const int y = ya + k;
             if (!(x < a.W && y < a.H && landed)) continue;
             float hc[3];
@@ -86,6 +99,7 @@ struct GenPol {
                 hc[1] = h[k].y;
                 hc[2] = h[k].z;
             }
+            const float orig[3] = {hc[0], hc[1], hc[2]};
             if constexpr (RECT == 1) {
 #pragma unroll
                 for (int c = 0; c < 3; ++c) hc[c] = fminf(fmaxf(hc[c], lo[c]), hi[c]);
@@ -97,9 +111,30 @@ struct GenPol {
 #pragma unroll
                 for (int c = 0; c < 3; ++c) hc[c] = fmaf(hc[c] - p[c], sc, p[c]);
             }
-            const float alpha = a.reset ? 1.0f : ((rej >> k) & 1u ? a.rejection_alpha : a.alpha);
             const float4 c0 = lds128(&sp[(k + 1) * SX + 1]);
             const float cur[3] = {c0.x, c0.y, c0.z};
+            float alpha = a.alpha;
+            if ((rej >> k) & 1u) {
+                alpha = a.rejection_alpha;
+            } else {
+                if (md.vel_alpha) {  // taa.comp:856-860
+                    const float du = px.u - px.hu[k], dv = px.v[k] - px.hv[k];
+                    const float t = fminf(fmaxf(sqrt_approx(du * du + dv * dv) * md.vel_alpha_factor, 0.f), 1.f);
+                    alpha = fmaxf(alpha, fmaf(t, md.vel_alpha_max - alpha, alpha));
+                }
+                if (md.lottes) {  // taa.comp:863-870
+                    const float lc = lum(cur), lh = lum(hc);
+                    const float wl = 1.0f - fabsf(lc - lh) * rcp_approx(fmaxf(fmaxf(lc, lh), 0.2f));
+                    alpha = fmaf(wl * wl, md.min_alpha - md.max_alpha, md.max_alpha);
+                }
+                if (md.near_clamp) {  // taa.comp:873-892
+                    const float lmn = lum(lo), lmx = lum(hi), lh = lum(orig);
+                    float dist = 2.0f * fabsf(fminf(lh - lmn, lmx - lh)) * rcp_approx(lmx - lmn);
+                    if (lmx - lmn < 0.001f) dist = 1.0f;
+                    alpha *= fminf(fmaxf(4.0f * dist, 0.f), 1.f);
+                }
+            }
+            if (a.reset) alpha = 1.0f;
             float o[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) o[c] = fmaf(alpha, cur[c] - hc[c], hc[c]);
@@ -116,14 +151,14 @@ struct GenPol {
 }  // namespace fast32
 
 // The parameter modes this unit runs: clamp or clip toward the centre on the
-// variance or min/max box, YCoCg (without chroma-axis shrinking) or RGB, any
-// velocity use with simple sampling, no tonemap, shaped neighbourhood or blend
-// modifiers.
+// variance or min/max box, YCoCg (with or without chroma-axis shrinking) or
+// RGB, any velocity use with simple sampling, the velocity-based alpha, the
+// luma weighting and the near-clamp reduction of the blend weight; no
+// tonemap, shaped neighbourhood, noise, anti-ghosting or ray-trace assist.
 bool fast32_gen_mode(const taa_parameters_t& P) {
-    return !P.mToneMapLumaKaris && !P.mShapedNeighbourhood && !(P.mUseYCoCg && P.mShrinkChromaAxis) &&
+    return !P.mToneMapLumaKaris && !P.mShapedNeighbourhood &&
            (P.mColorClampingOrClipping == 1 || P.mColorClampingOrClipping == 2) && P.mUseVelocityVectors >= 0 &&
-           P.mUseVelocityVectors <= 2 && P.mVelocitySampleMode == 0 && !P.mVelBasedAlpha &&
-           !P.mLumaWeightingLottes && !P.mReduceBlendNearClamp && !P.mAddNoise && !P.mDynamicAntiGhosting &&
+           P.mUseVelocityVectors <= 2 && P.mVelocitySampleMode == 0 && !P.mAddNoise && !P.mDynamicAntiGhosting &&
            !P.mRayTraceAugment && (P.mInterpolationMode == 0 || P.mInterpolationMode == 2);
 }
 

@@ -113,14 +113,27 @@ struct Args {
 struct Reproj {
     int vel_mode;                   // mUseVelocityVectors: 0 reproject, 1 velocity for movers, 2 for every pixel
     float inv_vp[16], hist_vp[16];  // mInverseViewProjMatrix, mHistoryViewProjMatrix (column-major)
+    // the blend-weight modifiers and the chroma-axis shrink (taa.comp:283-311, 855-895),
+    // read by the policies that run them
+    int shrink, vel_alpha, lottes, near_clamp;
+    float vel_alpha_max, vel_alpha_factor, min_alpha, max_alpha;
 };
 inline Reproj make_reproj(const taa_uniforms_t& U) {
+    const taa_parameters_t& P = U.param[0];
     Reproj r;
-    r.vel_mode = U.param[0].mUseVelocityVectors;
+    r.vel_mode = P.mUseVelocityVectors;
     for (int i = 0; i < 16; ++i) {
         r.inv_vp[i] = U.mInverseViewProjMatrix[i];
         r.hist_vp[i] = U.mHistoryViewProjMatrix[i];
     }
+    r.shrink = P.mUseYCoCg && P.mShrinkChromaAxis;
+    r.vel_alpha = P.mVelBasedAlpha != 0;
+    r.lottes = P.mLumaWeightingLottes != 0;
+    r.near_clamp = P.mReduceBlendNearClamp != 0;
+    r.vel_alpha_max = P.mVelBasedAlphaMax;
+    r.vel_alpha_factor = P.mVelBasedAlphaFactor;
+    r.min_alpha = P.mMinAlpha;
+    r.max_alpha = P.mMaxAlpha;
     return r;
 }
 

@@ -475,3 +475,35 @@ def test_fast_form_in_every_rectification_mode(cuda, mode, vel, interp):
     assert e_fast <= max(FAST_RELL2, 3.0 * e_exact), (e_fast, e_exact)
     assert rel_l2(f["history_out"][..., :3], t["history_out"][..., :3]) <= 1e-4
     assert T.device_status(clear=True) == 0
+
+
+@pytest.mark.parametrize("extra", [dict(mVelBasedAlpha=1), dict(mLumaWeightingLottes=1), dict(mReduceBlendNearClamp=1),
+                                   dict(mShrinkChromaAxis=1), dict(mVelBasedAlpha=1, mLumaWeightingLottes=1,
+                                                                   mReduceBlendNearClamp=1, mShrinkChromaAxis=1)],
+                         ids=["vel_alpha", "lottes", "near_clamp", "shrink_chroma", "all"])
+@pytest.mark.parametrize("mode", ["ycocg-var-clip", "ycocg-minmax-clamp", "rgb-minmax-clamp", "rgb-var-clip"])
+def test_fast_form_with_blend_modifiers(cuda, extra, mode):
+    """The blend-weight modifiers (velocity-based alpha, luma weighting, near-clamp
+    reduction) and the chroma-axis shrink in the fast form, against the exact form
+    and FP64 as above."""
+    w, h = 96, 56
+    p = WL.base_parameters(**GEN_MODES[mode], **extra)
+    wl = WL.small(w, h, frames=2, seed=len(mode) + len(extra))
+    fr = cpu_frames(wl, range(2), motion_channels=2)
+    u = T.make_uniforms(p, jitter_ndc=fr[1]["jitter"])
+    hist = fr[0]["color"].astype(np.float32)
+    outs = {}
+    for form in (T.TAA_FORM_AUTO, T.TAA_FORM_TILED):
+        ctx = T.Taa(w, h, form=form)
+        ctx.set_uniforms(u)
+        assert ctx.selected_form() == (T.TAA_FORM_FAST if form == T.TAA_FORM_AUTO else T.TAA_FORM_TILED)
+        outs[form] = gpu_resolve(ctx, cuda, fr[1]["color"], fr[1]["depth"], fr[1]["motion"], hist, fr[0]["depth"])
+        ctx.close()
+    f, t = outs[T.TAA_FORM_AUTO], outs[T.TAA_FORM_TILED]
+    assert np.all(np.isfinite(f["history_out"]))
+    r64 = O.resolve(u, fr[1]["color"].astype(np.float32), fr[1]["depth"], fr[1]["motion"].astype(np.float32),
+                    history=hist, history_depth=fr[0]["depth"], precision=64)["history"][..., :3]
+    e_fast, e_exact = rel_l2(f["history_out"][..., :3], r64), rel_l2(t["history_out"][..., :3], r64)
+    assert e_fast <= max(FAST_RELL2, 3.0 * e_exact), (e_fast, e_exact)
+    assert rel_l2(f["history_out"][..., :3], t["history_out"][..., :3]) <= 1e-4
+    assert T.device_status(clear=True) == 0
