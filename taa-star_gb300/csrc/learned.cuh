@@ -182,15 +182,26 @@ __device__ __forceinline__ void load_row(const char* tile, int r, float (&v)[32]
 // suspends the thread in hardware until the phase completes or kPollNs pass,
 // so a waiting warp issues a handful of instructions, not a spin loop.
 constexpr uint32_t kMmaPolls = 1u << 16;
-constexpr uint32_t kPollNs = 20000;
+#ifndef TAA_MMA_POLL_NS
+#define TAA_MMA_POLL_NS 20000
+#endif
+constexpr uint32_t kPollNs = TAA_MMA_POLL_NS;
 __device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity) {
     for (uint32_t i = 0; i < kMmaPolls; ++i) {
         uint32_t done;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(tc::saddr(bar)), "r"(parity), "r"(kPollNs)
-            : "memory");
+        if constexpr (kPollNs > 0) {
+            asm volatile(
+                "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+                : "=r"(done)
+                : "r"(tc::saddr(bar)), "r"(parity), "r"(kPollNs)
+                : "memory");
+        } else {
+            asm volatile(
+                "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                : "=r"(done)
+                : "r"(tc::saddr(bar)), "r"(parity)
+                : "memory");
+        }
         if (done) return true;
     }
     return false;

@@ -2,23 +2,28 @@
 // (TAA_FORM_LEARNED, learned.cuh) on the strip body of the fast forms
 // (strip_body.cuh): the colour tile staged in FP32 YCoCg, each thread a
 // vertical strip of four pixels whose 3x3 boxes (mean, standard deviation,
-// minimum, maximum) come from staged rows the strip shares; the history
-// sample from the tile's TMA window; then for each of the strip's four
-// pixels in turn, every warp runs its 32 lanes' features through the network
-// with warp-wide MMAs (mma.sync m16n8k16, FP16 in, FP32 out, activations in
-// registers) and clips and blends with the predicted weight and box scale
-// (the plain variance clip where the scale leaves [0.5, 2]).
+// minimum, maximum) come from staged rows the strip shares, each row read
+// once for its sums and extrema; the history sample from the tile's TMA
+// window.  Then the strip's pixels go through the network two at a time:
+// every warp writes its 64 pixels' FP16 feature rows over the history window
+// (dead once every warp has its samples), loads the three layers' weight
+// fragments into registers and runs its four 16-row m-tiles through the
+// layers with warp-wide MMAs (mma.sync m16n8k16, FP16 in, FP32 out, the
+// activations rounded and clamped by one cvt.rn.relu per pair and kept in
+// registers); each pixel then clips and blends with its predicted weight and
+// box scale (the plain variance clip where the scale leaves [0.5, 2]).
 //
-// Cost at 1920x1080 (CUDA graph of 8 frames): 77 us a frame, against 44 us
-// for the tiled FP32 form and 31 us for TAA_FORM_FAST; without the network
-// the same kernel takes 44 us.  The network's 36 mma.sync per 32 pixels
-// (2 m-tiles x (8 + 8 + 2)) keep the tensor pipe 20 % busy (its peak is one
-// m16n8k16 per 2 cycles per SM: 15 us for 2.07M pixels); the kernel is bound
-// by latency at 20 warps per SM (5 CTAs of 96 registers and 42 KB), with the
-// layers' dependent MMA chains, the feature and activation round trips
-// through shared memory and instruction fetch (the unrolled network) in the
-// stall reasons.  The tcgen05 variant (TAA_FLAG_LEARNED_TCGEN05, below) waits
-// on six CTA-wide MMA round trips a tile and measures 89 us.
+// Cost at 1920x1080 (20 launches on one frame): 80-82 us, against 47 us for
+// the exact tiled FP32 form and 33 us for TAA_FORM_FAST.  A 4K launch under
+// ncu: 711 issue slots per pixel (the fast form 295), issue active 50 % at
+// 19 warps per SM (5 CTAs of 96 registers and 34 KB), stalls per issue
+// long-scoreboard 3.2 (the strip body's input and gather latency), wait 1.7;
+// the tensor pipe 20 % busy.  Structure does not move it: the network per
+// pixel of the strip with weights reloaded per m-tile, two or four m-tiles
+// per weight load, 4 or 5 CTAs per SM all measure within 1 %, the same
+// bits.  The tcgen05 variant (TAA_FLAG_LEARNED_TCGEN05, below) waits on six
+// CTA-wide MMA round trips a tile and measures 93 us (one round of four
+// blocks, or waits without a suspend hint: the same).
 //
 // The training records come from the tiled collection kernel of learned.cu;
 // the features here are the same functions of the same quantities (the box
@@ -33,86 +38,227 @@ namespace taa_dev {
 namespace fast32 {
 
 constexpr int kLearnedWarps = NT / 32;
-using Net = learned::WarpNetN<kLearnedWarps>;
+
+// Pixels of a strip that go through the network together: the warp's rows
+// are KB x 32 (KB m-tile pairs), so a layer's weight fragments, held in
+// registers for the whole strip, meet 2 x KB independent m-tiles.
+#ifndef TAA_LEARNED_BATCH
+#define TAA_LEARNED_BATCH 2
+#endif
+constexpr int KB = TAA_LEARNED_BATCH;
+static_assert(NPX % KB == 0, "the strip splits into whole batches");
+constexpr int kFeatRow = learned::kIn * 2;  // bytes of one FP16 feature row
+static_assert(NT / 32 * KB * 32 * kFeatRow <= (int)sizeof(float4) * WW * WH,
+              "every warp's feature rows fit over the history window");
+
+// The network's weights (padded rows: conflict-free ldmatrix) and one output
+// pair per feature row of a batch.
+struct NetSmem {
+    alignas(16) __half w1[learned::kHid][learned::kPad];
+    alignas(16) __half w2[learned::kHid][learned::kPad];
+    alignas(16) __half w3[8][learned::kPad];
+    float2 out[kLearnedWarps][KB * 32];
+};
+
+// Byte offset of 16-byte chunk c (features 8c .. 8c+7) of feature row r: the
+// chunks of rows 2i and 2i+1 are rotated by i, so the eight rows an ldmatrix
+// phase reads (and the eight a store phase writes) fall in distinct banks.
+__device__ __forceinline__ uint32_t feat_off(int r, int c) { return (uint32_t)(r * kFeatRow + ((c ^ ((r >> 1) & 3)) << 4)); }
+
+// Two FP32 activations rounded to FP16 and clamped at zero, packed (a low,
+// b high) in one conversion: learned::pack_relu's values.
+__device__ __forceinline__ uint32_t cvt_relu(float a, float b) {
+    uint32_t d;
+    asm("cvt.rn.relu.f16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(b), "f"(a));
+    return d;
+}
+
+// One hidden layer of a 16-row m-tile with the B fragments in registers: the
+// arithmetic of learned::warp_layer.
+__device__ __forceinline__ void layer_rb(const uint32_t (&a)[2][4], const uint32_t (&b)[4][4], uint32_t (&h)[2][4]) {
+    float acc[4][4];
+#pragma unroll
+    for (int nj = 0; nj < 4; ++nj) {
+        acc[nj][0] = acc[nj][1] = acc[nj][2] = acc[nj][3] = 0.f;
+        learned::mma16816(acc[nj], a[0], b[nj][0], b[nj][1]);
+        learned::mma16816(acc[nj], a[1], b[nj][2], b[nj][3]);
+    }
+#pragma unroll
+    for (int kj = 0; kj < 2; ++kj) {
+        h[kj][0] = cvt_relu(acc[2 * kj][0], acc[2 * kj][1]);
+        h[kj][1] = cvt_relu(acc[2 * kj][2], acc[2 * kj][3]);
+        h[kj][2] = cvt_relu(acc[2 * kj + 1][0], acc[2 * kj + 1][1]);
+        h[kj][3] = cvt_relu(acc[2 * kj + 1][2], acc[2 * kj + 1][3]);
+    }
+}
+
+// The 3x3 sums and extrema of one staged row segment from one read of its texels.
+__device__ __forceinline__ void row_stats(const float4* p, Row& r, RowMinMax& q) {
+    const float4 t0 = lds128(p), t1 = lds128(p + 1), t2 = lds128(p + 2);
+    const f2 a0 = pk(t0.x, t0.y), a1 = pk(t1.x, t1.y), a2 = pk(t2.x, t2.y);
+    r.a = addp(addp(a0, a1), a2);
+    r.c = addp(addp(pk(t0.z, t0.w), pk(t1.z, t1.w)), pk(t2.z, t2.w));
+    r.q = fmap(a2, a2, fmap(a1, a1, mulp(a0, a0)));
+    q = {{fminf(t0.x, fminf(t1.x, t2.x)), fminf(t0.y, fminf(t1.y, t2.y)), fminf(t0.z, fminf(t1.z, t2.z))},
+         {fmaxf(t0.x, fmaxf(t1.x, t2.x)), fmaxf(t0.y, fmaxf(t1.y, t2.y)), fmaxf(t0.z, fmaxf(t1.z, t2.z))}};
+}
 
 struct LearnedStripPol {
     using Staged = float4;
     struct Ctx {
-        Net* net;
+        NetSmem* net;
+        char* feat;  // the feature rows, over the history window (dead once the samples are taken)
     };
     static __device__ __forceinline__ float4 stage(uint2 raw) { return F32Pol::stage(raw); }
 
     static __device__ __forceinline__ void finish(const Args& a, const float4* sp, int x, int ya, const float3 h[NPX],
                                                   unsigned rej, bool landed, const PixelInfo& px, Ctx& ctx) {
-        Row r0 = row_sums(sp), r1 = row_sums(sp + SX);
-        RowMinMax q0 = row_minmax(sp), q1 = row_minmax(sp + SX);
+        using namespace learned;
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        NetSmem& net = *ctx.net;
+        char* const ft = ctx.feat + warp * (KB * 32 * kFeatRow);
+        // the motion features of the strip's pixels (the rest of PixelInfo dies here)
+        float vel_px[NPX], depth_rel[NPX];
 #pragma unroll
         for (int k = 0; k < NPX; ++k) {
-            const Row r2 = row_sums(sp + (k + 2) * SX);
-            const RowMinMax q2 = row_minmax(sp + (k + 2) * SX);
-            const Row s = add(add(r0, r1), r2);
-            learned::FeatureIn fi;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                fi.mn[c] = fminf(q0.mn[c], fminf(q1.mn[c], q2.mn[c]));
-                fi.mx[c] = fmaxf(q0.mx[c], fmaxf(q1.mx[c], q2.mx[c]));
-            }
-            r0 = r1;
-            r1 = r2;
-            q0 = q1;
-            q1 = q2;
-            const int y = ya + k;
-            const bool valid = x < a.W && y < a.H && landed;
-            // mean and standard deviation of the box (taa.comp:266-277)
-            const f2 n = dup(1.0f / 9.0f);
-            const f2 mean = mulp(s.a, n), cg = mulp(s.c, n);
-            const f2 var = fmap(neg2(mean), mean, mulp(s.q, n));
-            fi.mean[0] = f2lo(mean);
-            fi.mean[1] = f2hi(mean);
-            fi.mean[2] = f2lo(cg);
-            fi.sigma[0] = learned::sqrt_approx(fmaxf(f2lo(var), 0.f));
-            fi.sigma[1] = learned::sqrt_approx(fmaxf(f2hi(var), 0.f));
-            fi.sigma[2] = learned::sqrt_approx(fmaxf(fmaf(-f2lo(cg), f2lo(cg), f2hi(cg)), 0.f));
-            hist_ycocg(h[k], fi.hist);
-            const float4 c0 = lds128(&sp[(k + 1) * SX + 1]);
-            fi.cur[0] = c0.x;
-            fi.cur[1] = c0.y;
-            fi.cur[2] = c0.z;
             const float du = (px.u - px.hu[k]) * (float)a.W, dv = (px.v[k] - px.hv[k]) * (float)a.H;
-            fi.vel_px = learned::sqrt_approx(du * du + dv * dv);
-            fi.depth_rel = a.depth_cull ? __fdividef(px.pd[k] - px.ehd[k], 0.1f * (1.0f - px.pd[k]) + 1e-6f) : 0.f;
-            const bool rejected = (rej >> k) & 1u;
-            fi.rejected = rejected;
-            float f[learned::kIn];
-            if (valid) {
-                learned::features(fi, f);
-            } else {
+            vel_px[k] = learned::sqrt_approx(du * du + dv * dv);
+            depth_rel[k] = a.depth_cull ? __fdividef(px.pd[k] - px.ehd[k], 0.1f * (1.0f - px.pd[k]) + 1e-6f) : 0.f;
+        }
+        __syncthreads();  // every warp has taken its history samples: the window is free
+        Row r0, r1;
+        RowMinMax q0, q1;
+        row_stats(sp, r0, q0);
+        row_stats(sp + SX, r1, q1);
 #pragma unroll
-                for (int i = 0; i < learned::kIn; ++i) f[i] = 0.f;
-            }
-            // every lane of the warp takes part in the network
-            float o0, o1;
-            learned::forward_warp(*ctx.net, f, o0, o1);
-            if (!valid) continue;
-            float alpha = learned::out_alpha(o0), scale = learned::out_scale(o1);
-            if (!(scale >= 0.5f && scale <= 2.0f)) {  // outside the trusted range: the plain variance clip
-                scale = 1.f;
-                alpha = a.alpha;
-            }
-            if (a.reset) alpha = 1.0f;
-            else if (rejected) alpha = a.rejection_alpha;
-            float e[3], o[3];
+        for (int hb = 0; hb < NPX / KB; ++hb) {
+            float mean[KB][3], sigma[KB][3];
+            // features of the batch's pixels: FP16 row kk * 32 + lane
 #pragma unroll
-            for (int c = 0; c < 3; ++c) e[c] = scale * a.gamma * fi.sigma[c] + 1e-7f;
-            learned::rectify_blend(fi.mean, e, fi.hist, fi.cur, alpha, o);
-            const float tmp = o[0] - o[2];
-            const float rr = tmp + o[1], g = o[0] + o[2], bl = tmp - o[1];
-            *at_w<float4>(a.hout, a.hout_pitch, x, y) = make_float4(rr, g, bl, 0.f);
-            if (a.result)
-                *at_w<uint2>(a.result, a.result_pitch, x, y) = float4_to_half4(make_float4(rr, g, bl, 1.0f));
+            for (int kk = 0; kk < KB; ++kk) {
+                const int k = hb * KB + kk;
+                Row r2;
+                RowMinMax q2;
+                row_stats(sp + (k + 2) * SX, r2, q2);
+                const Row s = add(add(r0, r1), r2);
+                FeatureIn fi;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    fi.mn[c] = fminf(q0.mn[c], fminf(q1.mn[c], q2.mn[c]));
+                    fi.mx[c] = fmaxf(q0.mx[c], fmaxf(q1.mx[c], q2.mx[c]));
+                }
+                r0 = r1;
+                r1 = r2;
+                q0 = q1;
+                q1 = q2;
+                const bool valid = x < a.W && ya + k < a.H && landed;
+                // mean and standard deviation of the box (taa.comp:266-277)
+                const f2 n = dup(1.0f / 9.0f);
+                const f2 m = mulp(s.a, n), cg = mulp(s.c, n);
+                const f2 var = fmap(neg2(m), m, mulp(s.q, n));
+                fi.mean[0] = f2lo(m);
+                fi.mean[1] = f2hi(m);
+                fi.mean[2] = f2lo(cg);
+                fi.sigma[0] = learned::sqrt_approx(fmaxf(f2lo(var), 0.f));
+                fi.sigma[1] = learned::sqrt_approx(fmaxf(f2hi(var), 0.f));
+                fi.sigma[2] = learned::sqrt_approx(fmaxf(fmaf(-f2lo(cg), f2lo(cg), f2hi(cg)), 0.f));
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    mean[kk][c] = fi.mean[c];
+                    sigma[kk][c] = fi.sigma[c];
+                }
+                hist_ycocg(h[k], fi.hist);
+                const float4 c0 = lds128(&sp[(k + 1) * SX + 1]);
+                fi.cur[0] = c0.x;
+                fi.cur[1] = c0.y;
+                fi.cur[2] = c0.z;
+                fi.vel_px = vel_px[k];
+                fi.depth_rel = depth_rel[k];
+                fi.rejected = (rej >> k) & 1u;
+                float f[kIn];
+                if (valid) {
+                    features(fi, f);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < kIn; ++i) f[i] = 0.f;
+                }
+                const int row = kk * 32 + lane;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    __half2 q[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) q[e] = __floats2half2_rn(f[8 * j + 2 * e], f[8 * j + 2 * e + 1]);
+                    uint4 wv;
+                    wv.x = *reinterpret_cast<uint32_t*>(&q[0]);
+                    wv.y = *reinterpret_cast<uint32_t*>(&q[1]);
+                    wv.z = *reinterpret_cast<uint32_t*>(&q[2]);
+                    wv.w = *reinterpret_cast<uint32_t*>(&q[3]);
+                    *reinterpret_cast<uint4*>(ft + feat_off(row, j)) = wv;
+                }
+            }
+            __syncwarp();
+            // the three layers' B fragments, held for the batch's 2 x KB m-tiles
+            uint32_t b1[4][4], b2[4][4], b3[4];
+#pragma unroll
+            for (int nj = 0; nj < 4; ++nj) {
+                ldsm_x4(b1[nj], &net.w1[nj * 8 + (lane & 7)][(lane >> 3) * 8]);
+                ldsm_x4(b2[nj], &net.w2[nj * 8 + (lane & 7)][(lane >> 3) * 8]);
+            }
+            ldsm_x4(b3, &net.w3[lane & 7][(lane >> 3) * 8]);
+            // the network on the batch's m-tiles (m-tile mt: rows 16 mt .. 16 mt + 15)
+#pragma unroll
+            for (int mt = 0; mt < 2 * KB; ++mt) {
+                uint32_t a0[2][4], a1[2][4], a2[2][4];
+#pragma unroll
+                for (int kj = 0; kj < 2; ++kj) ldsm_x4(a0[kj], ft + feat_off(mt * 16 + (lane & 15), 2 * kj + (lane >> 4)));
+                layer_rb(a0, b1, a1);
+                layer_rb(a1, b2, a2);
+                float o[4] = {0.f, 0.f, 0.f, 0.f};
+                mma16816(o, a2[0], b3[0], b3[1]);
+                mma16816(o, a2[1], b3[2], b3[3]);
+                // outputs 0 and 1 of rows g and g + 8 sit in lane 4 g
+                if ((lane & 3) == 0) {
+                    net.out[warp][mt * 16 + (lane >> 2)] = make_float2(o[0], o[1]);
+                    net.out[warp][mt * 16 + (lane >> 2) + 8] = make_float2(o[2], o[3]);
+                }
+            }
+            __syncwarp();
+            // clip and blend with the predicted weight and box scale
+#pragma unroll
+            for (int kk = 0; kk < KB; ++kk) {
+                const int k = hb * KB + kk, y = ya + k;
+                const float2 oo = net.out[warp][kk * 32 + lane];
+                if (!(x < a.W && y < a.H && landed)) continue;
+                float alpha = out_alpha(oo.x), scale = out_scale(oo.y);
+                if (!(scale >= 0.5f && scale <= 2.0f)) {  // outside the trusted range: the plain variance clip
+                    scale = 1.f;
+                    alpha = a.alpha;
+                }
+                if (a.reset) alpha = 1.0f;
+                else if ((rej >> k) & 1u) alpha = a.rejection_alpha;
+                float hy[3], cur[3], e[3], o[3];
+                hist_ycocg(h[k], hy);
+                const float4 c0 = lds128(&sp[(k + 1) * SX + 1]);
+                cur[0] = c0.x;
+                cur[1] = c0.y;
+                cur[2] = c0.z;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) e[c] = scale * a.gamma * sigma[kk][c] + 1e-7f;
+                rectify_blend(mean[kk], e, hy, cur, alpha, o);
+                const float tmp = o[0] - o[2];
+                const float rr = tmp + o[1], g = o[0] + o[2], bl = tmp - o[1];
+                *at_w<float4>(a.hout, a.hout_pitch, x, y) = make_float4(rr, g, bl, 0.f);
+                if (a.result)
+                    *at_w<uint2>(a.result, a.result_pitch, x, y) = float4_to_half4(make_float4(rr, g, bl, 1.0f));
+            }
+            __syncwarp();  // the batch's feature rows and outputs are free
         }
     }
 };
+
+#ifndef TAA_LEARNED_TC_NB
+#define TAA_LEARNED_TC_NB 2
+#endif
 
 // The same inference with the network on the 5th-generation tensor cores:
 // the CTA's 512 pixels go through it in two rounds of 256 (pixels 0-1, then
@@ -125,9 +271,10 @@ struct LearnedStripPol {
 struct LearnedTcPol {
     using Staged = float4;
     static constexpr int kTile = learned::kRows * learned::kIn * 2;  // one 128-row activation tile
-    static constexpr int NB = 2;  // 128-row blocks per round
+    static constexpr int NB = TAA_LEARNED_TC_NB;  // 128-row blocks per round
     struct Ctx {
-        char* tiles;       // the two activation tiles (over the history window)
+        char* tiles;       // the first two activation tiles (over the history window)
+        char* tiles2;      // the others (NB = 4)
         const char* w;     // the blob's inference matrices in shared memory
         uint64_t* bar;     // MMA completion
         uint32_t tmem;     // one 32-column accumulator per block
@@ -141,7 +288,9 @@ struct LearnedTcPol {
         using namespace learned;
         const int t = threadIdx.x;
         const uint32_t lane_cols = ctx.tmem + ((uint32_t)((t >> 5) & 3) * 32u << 16);
-        char* const tiles[NB] = {ctx.tiles, ctx.tiles + kTile};
+        char* tiles[NB];
+#pragma unroll
+        for (int b = 0; b < NB; ++b) tiles[b] = b < 2 ? ctx.tiles + b * kTile : ctx.tiles2 + (b - 2) * kTile;
         __syncthreads();  // every thread is done with the history window the tiles overlay
         Row r0 = row_sums(sp), r1 = row_sums(sp + SX);
         RowMinMax q0 = row_minmax(sp), q1 = row_minmax(sp + SX);
@@ -267,11 +416,16 @@ __global__ void __launch_bounds__(NT, TAA_LEARNED_STRIP_MIN_BLOCKS)
     resolve_strips_learned(const Args a, const __grid_constant__ CUtensorMap hmap, const int tma_ok,
                            const char* __restrict__ blob) {
     __shared__ SmemT<float4> sm;
-    __shared__ Net net;
-    learned::load_warp_weights(net, blob);
+    __shared__ NetSmem net;
+    for (int i = threadIdx.x; i < learned::kHid * learned::kIn; i += NT) {
+        const int r = i / learned::kIn, k = i % learned::kIn;
+        net.w1[r][k] = *reinterpret_cast<const __half*>(blob + learned::Blob::W1 + tc::canon(r, k, learned::kIn));
+        net.w2[r][k] = *reinterpret_cast<const __half*>(blob + learned::Blob::W2 + tc::canon(r, k, learned::kHid));
+        if (r < 8) net.w3[r][k] = *reinterpret_cast<const __half*>(blob + learned::Blob::W3 + tc::canon(r, k, learned::kHid));
+    }
     __syncthreads();
     uint32_t phase = 0;
-    LearnedStripPol::Ctx ctx{&net};
+    LearnedStripPol::Ctx ctx{&net, reinterpret_cast<char*>(sm.win)};
     strip_tile<LearnedStripPol, 2, MC, false>(a, &hmap, tma_ok, blockIdx.x, blockIdx.y, sm, phase, ctx);
 }
 
@@ -283,6 +437,7 @@ __global__ void __launch_bounds__(NT, TAA_LEARNED_STRIP_MIN_BLOCKS)
 // inference matrices, the MMA barrier and the tensor-memory base.
 struct TcNetSmem {
     alignas(128) char w[learned::Blob::INFER_BYTES];
+    alignas(128) char tiles2[LearnedTcPol::NB > 2 ? (LearnedTcPol::NB - 2) * LearnedTcPol::kTile : 16];
     uint64_t bar;
     uint32_t tmem;
 };
@@ -302,7 +457,7 @@ __global__ void __launch_bounds__(NT, TAA_LEARNED_TC_STRIP_MIN_BLOCKS)
     __syncthreads();
     tc::fence_after_sync();
     uint32_t phase = 0;
-    LearnedTcPol::Ctx ctx{reinterpret_cast<char*>(sm.win), net.w, &net.bar, net.tmem, 0u, true};
+    LearnedTcPol::Ctx ctx{reinterpret_cast<char*>(sm.win), net.tiles2, net.w, &net.bar, net.tmem, 0u, true};
     strip_tile<LearnedTcPol, 2, MC, false>(a, &hmap, tma_ok, blockIdx.x, blockIdx.y, sm, phase, ctx);
     if (!ctx.ok && threadIdx.x == 0) atomicOr(a.status, kStatusWindowTimeout);
     tc::fence_before_sync();
