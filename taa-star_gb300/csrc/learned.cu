@@ -611,16 +611,28 @@ __device__ __forceinline__ void build_blob(const Weights& w, char* blob, int t, 
     auto put = [&](int base, int r, int k, int K, float v) {
         *reinterpret_cast<__half*>(blob + base + tc::canon(r, k, K)) = __float2half_rn(v);
     };
+    // the warp network's padded row-major image: w1, w2 [32][40], w3 [8][40]
+    auto put_row = [&](int mat, int r, int k, float v) {
+        *reinterpret_cast<__half*>(blob + Blob::WARP + ((mat * 32 + r) * 40 + k) * 2) = __float2half_rn(v);
+    };
     for (int i = t; i < kHid * kIn; i += nt) {
         const int h = i / kIn, x = i % kIn;
         put(Blob::W1, h, x, kIn, eff1(w, h, x));
         put(Blob::W2, h, x, kHid, eff2(w, h, x));
         put(Blob::W2T, x, h, kHid, eff2(w, h, x));
+        put_row(0, h, x, eff1(w, h, x));
+        put_row(1, h, x, eff2(w, h, x));
     }
     for (int i = t; i < kOutPad * kHid; i += nt) {
         const int o = i / kHid, h = i % kHid;
         put(Blob::W3, o, h, kHid, eff3(w, o, h));
         put(Blob::W3T, h, o, kOutPad, eff3(w, o, h));
+        if (o < 8) put_row(2, o, h, eff3(w, o, h));
+    }
+    // the image's padding columns (never read) written too, so the blob is fully defined
+    for (int i = t; i < 72 * 8; i += nt) {
+        const int r = i / 8, k = 32 + i % 8;
+        *reinterpret_cast<__half*>(blob + Blob::WARP + (r * 40 + k) * 2) = __float2half_rn(0.f);
     }
 }
 
@@ -684,7 +696,7 @@ using learned::Record;
 
 size_t learned_record_bytes() { return sizeof(Record); }
 int learned_param_count() { return learned::kParams; }
-int learned_blob_bytes() { return learned::Blob::BYTES; }
+int learned_blob_bytes() { return learned::Blob::ALL_BYTES; }
 
 cudaError_t launch_mlp_map_grads(float* grads, cudaStream_t s) {
     learned::mlp_map_grads<<<1, 256, 0, s>>>(grads);

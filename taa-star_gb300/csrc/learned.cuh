@@ -15,6 +15,7 @@
 // a scale outside [0.5, 2] falls back to the plain variance clip and alpha.
 #pragma once
 #include <cuda_fp16.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include "tcgen05.cuh"
@@ -47,9 +48,16 @@ struct Blob {
     static constexpr int INFER_BYTES = W3 + kOutPad * kHid * 2;
     static constexpr int W3T = INFER_BYTES;               // [32 hid][16 out (2 used)]
     static constexpr int W2T = W3T + kHid * kOutPad * 2;  // [32 in of layer 2][32 out of layer 2]
-    static constexpr int BYTES = W2T + kHid * kHid * 2;
+    static constexpr int BYTES = W2T + kHid * kHid * 2;   // what the training kernels copy
+    // the inference matrices once more as the warp network's padded row-major
+    // image (WarpNetN's w1, w2, w3: [32][40], [32][40], [8][40] halves), which a
+    // CTA copies in 16-byte words
+    static constexpr int WARP = BYTES;
+    static constexpr int WARP_BYTES = (2 * 32 + 8) * 40 * 2;
+    static constexpr int ALL_BYTES = WARP + WARP_BYTES;  // the allocation
 };
-static_assert(Blob::BYTES % 16 == 0 && Blob::INFER_BYTES % 16 == 0, "blob copied as 16-byte words");
+static_assert(Blob::BYTES % 16 == 0 && Blob::INFER_BYTES % 16 == 0 && Blob::WARP_BYTES % 16 == 0,
+              "blob copied as 16-byte words");
 
 // Features of one pixel (see the file comment).  All colours YCoCg.
 struct FeatureIn {
@@ -278,14 +286,16 @@ template <int NW> struct WarpNetN {
 };
 using WarpNet = WarpNetN<8>;  // 256-thread CTAs
 
-// The padded row-major weights from the canonical blob (all threads, then a barrier).
+// The padded row-major weights (w1, w2, w3 laid out back to back from w1)
+// from the blob's image of them (all threads, then a barrier).
+__device__ __forceinline__ void copy_warp_weights(__half* w1, const char* blob) {
+    copy_blob(reinterpret_cast<char*>(w1), blob + Blob::WARP, Blob::WARP_BYTES);
+}
 template <int NW> __device__ __forceinline__ void load_warp_weights(WarpNetN<NW>& s, const char* blob) {
-    for (int i = threadIdx.x; i < kHid * kIn; i += blockDim.x) {
-        const int r = i / kIn, k = i % kIn;
-        s.w1[r][k] = *reinterpret_cast<const __half*>(blob + Blob::W1 + tc::canon(r, k, kIn));
-        s.w2[r][k] = *reinterpret_cast<const __half*>(blob + Blob::W2 + tc::canon(r, k, kHid));
-        if (r < 8) s.w3[r][k] = *reinterpret_cast<const __half*>(blob + Blob::W3 + tc::canon(r, k, kHid));
-    }
+    static_assert(offsetof(WarpNetN<NW>, w2) == offsetof(WarpNetN<NW>, w1) + 2560 &&
+                      offsetof(WarpNetN<NW>, w3) == offsetof(WarpNetN<NW>, w1) + 5120,
+                  "w1, w2, w3 back to back as in the blob's image");
+    copy_warp_weights(&s.w1[0][0], blob);
 }
 
 __device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void* p) {

@@ -13,17 +13,16 @@
 // registers); each pixel then clips and blends with its predicted weight and
 // box scale (the plain variance clip where the scale leaves [0.5, 2]).
 //
-// Cost at 1920x1080 (20 launches on one frame): 80-82 us, against 47 us for
-// the exact tiled FP32 form and 33 us for TAA_FORM_FAST.  A 4K launch under
-// ncu: 711 issue slots per pixel (the fast form 295), issue active 50 % at
-// 19 warps per SM (5 CTAs of 96 registers and 34 KB), stalls per issue
-// long-scoreboard 3.2 (the strip body's input and gather latency), wait 1.7;
-// the tensor pipe 20 % busy.  Structure does not move it: the network per
-// pixel of the strip with weights reloaded per m-tile, two or four m-tiles
-// per weight load, 4 or 5 CTAs per SM all measure within 1 %, the same
-// bits.  The tcgen05 variant (TAA_FLAG_LEARNED_TCGEN05, below) waits on six
-// CTA-wide MMA round trips a tile and measures 93 us (one round of four
-// blocks, or waits without a suspend hint: the same).
+// Cost at 1920x1080 (20 launches on one frame): 68 us, against 48 us for
+// the exact tiled FP32 form and 34 us for TAA_FORM_FAST.  Measured by parts
+// (variants with a part removed): the network 16 us, the features 6 us; the
+// rest is the strip body at 128 registers (4 CTAs per SM: fewer registers
+// spill and measure slower, 5 CTAs 73 us).  The weights reach shared memory
+// by cp.async from the blob's row-major image while the strip's inputs load
+// (a per-element copy from the canonical layout at the start of every CTA
+// cost 11 us).  The tcgen05 variants (TAA_FLAG_LEARNED_TCGEN05, below) run
+// the same network with the same bits: with the activations in tensor memory
+// 79 us, through shared memory 93 us.
 //
 // The training records come from the tiled collection kernel of learned.cu;
 // the features here are the same functions of the same quantities (the box
@@ -45,6 +44,12 @@ constexpr int kLearnedWarps = NT / 32;
 #ifndef TAA_LEARNED_BATCH
 #define TAA_LEARNED_BATCH 2
 #endif
+// Whether a batch reads its first two staged rows again instead of holding
+// the previous batch's across the network (spill-free at 126 registers: 68.4
+// against 69.2 us per 1080p frame).
+#ifndef TAA_LEARNED_RECOMPUTE_ROWS
+#define TAA_LEARNED_RECOMPUTE_ROWS 1
+#endif
 constexpr int KB = TAA_LEARNED_BATCH;
 static_assert(NPX % KB == 0, "the strip splits into whole batches");
 constexpr int kFeatRow = learned::kIn * 2;  // bytes of one FP16 feature row
@@ -52,13 +57,16 @@ static_assert(NT / 32 * KB * 32 * kFeatRow <= (int)sizeof(float4) * WW * WH,
               "every warp's feature rows fit over the history window");
 
 // The network's weights (padded rows: conflict-free ldmatrix) and one output
-// pair per feature row of a batch.
+// pair per feature row of a batch (the feature rows overlay the history
+// window, free once every warp has its samples).
 struct NetSmem {
     alignas(16) __half w1[learned::kHid][learned::kPad];
     alignas(16) __half w2[learned::kHid][learned::kPad];
     alignas(16) __half w3[8][learned::kPad];
     float2 out[kLearnedWarps][KB * 32];
 };
+static_assert(offsetof(NetSmem, w2) == 2560 && offsetof(NetSmem, w3) == 5120,
+              "w1, w2, w3 back to back as in the blob's image");
 
 // Byte offset of 16-byte chunk c (features 8c .. 8c+7) of feature row r: the
 // chunks of rows 2i and 2i+1 are rotated by i, so the eight rows an ldmatrix
@@ -125,13 +133,19 @@ struct LearnedStripPol {
             vel_px[k] = learned::sqrt_approx(du * du + dv * dv);
             depth_rel[k] = a.depth_cull ? __fdividef(px.pd[k] - px.ehd[k], 0.1f * (1.0f - px.pd[k]) + 1e-6f) : 0.f;
         }
-        __syncthreads();  // every warp has taken its history samples: the window is free
+        // every warp has its history samples (the window is free) and its share of the weights
+        cp_async_wait_all();
+        __syncthreads();
         Row r0, r1;
         RowMinMax q0, q1;
-        row_stats(sp, r0, q0);
-        row_stats(sp + SX, r1, q1);
 #pragma unroll
         for (int hb = 0; hb < NPX / KB; ++hb) {
+            // the batch's first two staged rows (read again rather than held
+            // across the network: fewer live registers)
+            if (TAA_LEARNED_RECOMPUTE_ROWS || hb == 0) {
+                row_stats(sp + (hb * KB) * SX, r0, q0);
+                row_stats(sp + (hb * KB + 1) * SX, r1, q1);
+            }
             float mean[KB][3], sigma[KB][3];
             // features of the batch's pixels: FP16 row kk * 32 + lane
 #pragma unroll
@@ -258,6 +272,11 @@ struct LearnedStripPol {
 
 #ifndef TAA_LEARNED_TC_NB
 #define TAA_LEARNED_TC_NB 2
+#endif
+// Whether TAA_FLAG_LEARNED_TCGEN05 runs the variant with its activations in
+// shared memory instead of the tensor-memory-resident one.
+#ifndef TAA_LEARNED_TC_SMEM_A
+#define TAA_LEARNED_TC_SMEM_A 0
 #endif
 
 // The same inference with the network on the 5th-generation tensor cores:
@@ -405,10 +424,10 @@ struct LearnedTcPol {
     }
 };
 
-// Resident CTAs per SM (42 KB of shared memory each: the strip tile and the
-// network's weights and feature rows).
+// Resident CTAs per SM the register budget is sized for (34 KB of shared
+// memory each: the strip tile, the network's weights and outputs).
 #ifndef TAA_LEARNED_STRIP_MIN_BLOCKS
-#define TAA_LEARNED_STRIP_MIN_BLOCKS 5
+#define TAA_LEARNED_STRIP_MIN_BLOCKS 4
 #endif
 
 template <int MC>
@@ -417,13 +436,12 @@ __global__ void __launch_bounds__(NT, TAA_LEARNED_STRIP_MIN_BLOCKS)
                            const char* __restrict__ blob) {
     __shared__ SmemT<float4> sm;
     __shared__ NetSmem net;
-    for (int i = threadIdx.x; i < learned::kHid * learned::kIn; i += NT) {
-        const int r = i / learned::kIn, k = i % learned::kIn;
-        net.w1[r][k] = *reinterpret_cast<const __half*>(blob + learned::Blob::W1 + tc::canon(r, k, learned::kIn));
-        net.w2[r][k] = *reinterpret_cast<const __half*>(blob + learned::Blob::W2 + tc::canon(r, k, learned::kHid));
-        if (r < 8) net.w3[r][k] = *reinterpret_cast<const __half*>(blob + learned::Blob::W3 + tc::canon(r, k, learned::kHid));
-    }
-    __syncthreads();
+    // the weights' image copied asynchronously: the strip body's loads go out
+    // first; the copies complete (cp.async.wait_group 0) before the barrier in
+    // front of the network
+    for (int w = threadIdx.x; w < learned::Blob::WARP_BYTES / 16; w += NT)
+        cp_async<16>(reinterpret_cast<char*>(&net.w1[0][0]) + 16 * w, blob + learned::Blob::WARP + 16 * w);
+    cp_async_commit();
     uint32_t phase = 0;
     LearnedStripPol::Ctx ctx{&net, reinterpret_cast<char*>(sm.win)};
     strip_tile<LearnedStripPol, 2, MC, false>(a, &hmap, tma_ok, blockIdx.x, blockIdx.y, sm, phase, ctx);
@@ -465,6 +483,215 @@ __global__ void __launch_bounds__(NT, TAA_LEARNED_TC_STRIP_MIN_BLOCKS)
     if (threadIdx.x < 32) tc::tmem_free(net.tmem, kCols);
 }
 
+// The network on the 5th-generation tensor cores with every activation in
+// tensor memory: each thread (one TMEM lane, row = thread) stores its pixel's
+// 32 FP16 features as 16 packed columns (tcgen05.st); per layer one thread
+// issues, for each of the round's NBT 128-row blocks, two MMAs that read A
+// from those columns and B (the weights) from shared memory and accumulate
+// 32 FP32 columns; every thread reads its row back (tcgen05.ld), rounds and
+// clamps it to FP16 pairs (cvt.rn.relu) and stores it as the next layer's A.
+// No activation passes through shared memory.  Columns: D of block b at
+// 32 b, A of block b at 32 NBT + 16 b.
+#ifndef TAA_LEARNED_TM_NB
+#define TAA_LEARNED_TM_NB 2
+#endif
+#ifndef TAA_LEARNED_TM_STRIP_MIN_BLOCKS
+#define TAA_LEARNED_TM_STRIP_MIN_BLOCKS 4
+#endif
+template <int NBT> struct LearnedTmemPol {
+    using Staged = float4;
+    static constexpr int NB = NBT;
+    static constexpr uint32_t kCols = NB == 1 ? 64u : NB == 2 ? 128u : 256u;
+    static_assert(NPX % NB == 0 && 48 * NB <= (int)kCols, "whole rounds in the allocation");
+    struct Ctx {
+        const char* w;   // the blob's inference matrices in shared memory
+        uint64_t* bar;   // MMA completion
+        uint32_t tmem;
+        uint32_t phase;
+        bool ok;
+    };
+    static __device__ __forceinline__ float4 stage(uint2 raw) { return F32Pol::stage(raw); }
+
+    // One layer for the round's blocks: A from TMEM, B = w (K 32), N = n.
+    static __device__ __forceinline__ bool layer(Ctx& ctx, const char* w, int n) {
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        if (threadIdx.x == 0) {
+            const uint32_t idesc = tc::idesc_f16(128, n);
+#pragma unroll
+            for (int b = 0; b < NB; ++b)
+#pragma unroll
+                for (int ks = 0; ks < 2; ++ks)
+                    tc::mma_f16_ta(ctx.tmem + (uint32_t)(32 * b), ctx.tmem + (uint32_t)(32 * NB + 16 * b + 8 * ks),
+                                   tc::smem_desc(w + ks * 256, 128, 512), idesc, ks > 0);
+            tc::commit(ctx.bar);
+        }
+        const bool ok = learned::wait_bar(ctx.bar, ctx.phase);
+        ctx.phase ^= 1u;
+        tc::fence_after_sync();
+        return ok;
+    }
+
+    static __device__ __forceinline__ void finish(const Args& a, const float4* sp, int x, int ya, const float3 h[NPX],
+                                                  unsigned rej, bool landed, const PixelInfo& px, Ctx& ctx) {
+        using namespace learned;
+        const int t = threadIdx.x;
+        const uint32_t lane_base = ((uint32_t)((t >> 5) & 3) * 32u) << 16;
+        const uint32_t d0 = ctx.tmem + lane_base, a0 = ctx.tmem + lane_base + (uint32_t)(32 * NB);
+        float vel_px[NPX], depth_rel[NPX];
+#pragma unroll
+        for (int k = 0; k < NPX; ++k) {
+            const float du = (px.u - px.hu[k]) * (float)a.W, dv = (px.v[k] - px.hv[k]) * (float)a.H;
+            vel_px[k] = sqrt_approx(du * du + dv * dv);
+            depth_rel[k] = a.depth_cull ? __fdividef(px.pd[k] - px.ehd[k], 0.1f * (1.0f - px.pd[k]) + 1e-6f) : 0.f;
+        }
+        Row r0, r1;
+        RowMinMax q0, q1;
+        row_stats(sp, r0, q0);
+        row_stats(sp + SX, r1, q1);
+#pragma unroll
+        for (int rd = 0; rd < NPX / NB; ++rd) {
+            float mean[NB][3], sigma[NB][3];
+#pragma unroll
+            for (int kk = 0; kk < NB; ++kk) {
+                const int k = NB * rd + kk;
+                Row r2;
+                RowMinMax q2;
+                row_stats(sp + (k + 2) * SX, r2, q2);
+                const Row s = add(add(r0, r1), r2);
+                FeatureIn fi;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    fi.mn[c] = fminf(q0.mn[c], fminf(q1.mn[c], q2.mn[c]));
+                    fi.mx[c] = fmaxf(q0.mx[c], fmaxf(q1.mx[c], q2.mx[c]));
+                }
+                r0 = r1;
+                r1 = r2;
+                q0 = q1;
+                q1 = q2;
+                const bool valid = x < a.W && ya + k < a.H && landed;
+                const f2 n = dup(1.0f / 9.0f);
+                const f2 m = mulp(s.a, n), cg = mulp(s.c, n);
+                const f2 var = fmap(neg2(m), m, mulp(s.q, n));
+                fi.mean[0] = f2lo(m);
+                fi.mean[1] = f2hi(m);
+                fi.mean[2] = f2lo(cg);
+                fi.sigma[0] = sqrt_approx(fmaxf(f2lo(var), 0.f));
+                fi.sigma[1] = sqrt_approx(fmaxf(f2hi(var), 0.f));
+                fi.sigma[2] = sqrt_approx(fmaxf(fmaf(-f2lo(cg), f2lo(cg), f2hi(cg)), 0.f));
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    mean[kk][c] = fi.mean[c];
+                    sigma[kk][c] = fi.sigma[c];
+                }
+                hist_ycocg(h[k], fi.hist);
+                const float4 c0 = lds128(&sp[(k + 1) * SX + 1]);
+                fi.cur[0] = c0.x;
+                fi.cur[1] = c0.y;
+                fi.cur[2] = c0.z;
+                fi.vel_px = vel_px[k];
+                fi.depth_rel = depth_rel[k];
+                fi.rejected = (rej >> k) & 1u;
+                float f[kIn];
+                if (valid) {
+                    features(fi, f);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < kIn; ++i) f[i] = 0.f;
+                }
+                uint32_t q[16];
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    __half2 hh = __floats2half2_rn(f[2 * i], f[2 * i + 1]);
+                    q[i] = *reinterpret_cast<uint32_t*>(&hh);
+                }
+                tc::st16(a0 + (uint32_t)(16 * kk), q);
+            }
+            tc::wait_st();
+            // hidden layers: D -> ReLU'd FP16 -> the next A, in tensor memory
+#pragma unroll
+            for (int l = 0; l < 2; ++l) {
+                ctx.ok &= layer(ctx, ctx.w + (l == 0 ? Blob::W1 : Blob::W2), kHid);
+#pragma unroll
+                for (int kk = 0; kk < NB; ++kk) {
+                    float acc[32];
+                    tc::ld32(d0 + (uint32_t)(32 * kk), acc);
+                    uint32_t q[16];
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) q[i] = cvt_relu(acc[2 * i], acc[2 * i + 1]);
+                    tc::st16(a0 + (uint32_t)(16 * kk), q);
+                }
+                tc::wait_st();
+            }
+            ctx.ok &= layer(ctx, ctx.w + Blob::W3, kOutPad);
+            float o[NB][2];
+#pragma unroll
+            for (int kk = 0; kk < NB; ++kk) {
+                float v[16];
+                tc::ld16(d0 + (uint32_t)(32 * kk), v);
+                o[kk][0] = v[0];
+                o[kk][1] = v[1];
+            }
+#pragma unroll
+            for (int kk = 0; kk < NB; ++kk) {
+                const int k = NB * rd + kk, y = ya + k;
+                if (!(x < a.W && y < a.H && landed)) continue;
+                float alpha = out_alpha(o[kk][0]), scale = out_scale(o[kk][1]);
+                if (!(scale >= 0.5f && scale <= 2.0f)) {  // outside the trusted range: the plain variance clip
+                    scale = 1.f;
+                    alpha = a.alpha;
+                }
+                if (a.reset) alpha = 1.0f;
+                else if ((rej >> k) & 1u) alpha = a.rejection_alpha;
+                float hy[3], cur[3], e[3], out[3];
+                hist_ycocg(h[k], hy);
+                const float4 c0 = lds128(&sp[(k + 1) * SX + 1]);
+                cur[0] = c0.x;
+                cur[1] = c0.y;
+                cur[2] = c0.z;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) e[c] = scale * a.gamma * sigma[kk][c] + 1e-7f;
+                rectify_blend(mean[kk], e, hy, cur, alpha, out);
+                const float tmp = out[0] - out[2];
+                const float rr = tmp + out[1], g = out[0] + out[2], bl = tmp - out[1];
+                *at_w<float4>(a.hout, a.hout_pitch, x, y) = make_float4(rr, g, bl, 0.f);
+                if (a.result)
+                    *at_w<uint2>(a.result, a.result_pitch, x, y) = float4_to_half4(make_float4(rr, g, bl, 1.0f));
+            }
+        }
+    }
+};
+using TmPol = LearnedTmemPol<TAA_LEARNED_TM_NB>;
+
+struct TmNetSmem {
+    alignas(128) char w[learned::Blob::INFER_BYTES];
+    uint64_t bar;
+    uint32_t tmem;
+};
+
+template <int MC>
+__global__ void __launch_bounds__(NT, TAA_LEARNED_TM_STRIP_MIN_BLOCKS)
+    resolve_strips_learned_tm(const Args a, const __grid_constant__ CUtensorMap hmap, const int tma_ok,
+                              const char* __restrict__ blob) {
+    __shared__ SmemT<float4> sm;
+    __shared__ TmNetSmem net;
+    if (threadIdx.x == 0) mbar_init(&net.bar, 1);
+    learned::copy_blob(net.w, blob, learned::Blob::INFER_BYTES);
+    if (threadIdx.x < 32) tc::tmem_alloc(&net.tmem, TmPol::kCols);
+    tc::fence_smem_to_async();  // the weights, written here, are read by the tensor core
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    uint32_t phase = 0;
+    TmPol::Ctx ctx{net.w, &net.bar, net.tmem, 0u, true};
+    strip_tile<TmPol, 2, MC, false>(a, &hmap, tma_ok, blockIdx.x, blockIdx.y, sm, phase, ctx);
+    if (!ctx.ok && threadIdx.x == 0) atomicOr(a.status, kStatusWindowTimeout);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x < 32) tc::tmem_free(net.tmem, TmPol::kCols);
+}
+
 }  // namespace fast32
 
 cudaError_t launch_resolve_learned_strips_tc(int motion_ch, const taa_uniforms_t& U, const FrameArgs& f,
@@ -476,8 +703,13 @@ cudaError_t launch_resolve_learned_strips_tc(int motion_ch, const taa_uniforms_t
     const int tma_ok = a.hist && f.history.w >= WW && f.history.h >= WH &&
                        encode_history_map(f.history, TAA_FAST_TMA2D ? 2 : 0, WW, WH, &map);
     const dim3 grid((a.W + TX - 1) / TX, (a.H + TY - 1) / TY);
+#if TAA_LEARNED_TC_SMEM_A
     if (motion_ch == 4) resolve_strips_learned_tc<4><<<grid, NT, 0, s>>>(a, map, tma_ok, blob);
     else resolve_strips_learned_tc<2><<<grid, NT, 0, s>>>(a, map, tma_ok, blob);
+#else
+    if (motion_ch == 4) resolve_strips_learned_tm<4><<<grid, NT, 0, s>>>(a, map, tma_ok, blob);
+    else resolve_strips_learned_tm<2><<<grid, NT, 0, s>>>(a, map, tma_ok, blob);
+#endif
     return cudaGetLastError();
 }
 
