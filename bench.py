@@ -264,8 +264,9 @@ def time_learned(T, WL, dev, stream, sid, args):
     tr.close()
     wl = WL.c5()
     fr = LP.render(wl, wl.frames, dev)
-    plain, plain_max = LP.evaluate(wl, wl.frames, dev, T.TAA_FORM_TILED, fr=fr)
-    learned, learned_max = LP.evaluate(wl, wl.frames, dev, T.TAA_FORM_LEARNED, weights=w, fr=fr)
+    ps, ls = {}, {}
+    plain, plain_max = LP.evaluate(wl, wl.frames, dev, T.TAA_FORM_TILED, fr=fr, stats=ps)
+    learned, learned_max = LP.evaluate(wl, wl.frames, dev, T.TAA_FORM_LEARNED, weights=w, fr=fr, stats=ls)
     H, W = wl.height, wl.width
     cost = {}
     for name, form in (("tiled", T.TAA_FORM_TILED), ("fast", T.TAA_FORM_FAST), ("learned", T.TAA_FORM_LEARNED)):
@@ -293,6 +294,8 @@ def time_learned(T, WL, dev, stream, sid, args):
             "psnr_db_vs_64spp": float(np.mean(learned)), "plain_psnr_db_vs_64spp": float(np.mean(plain)),
             "gain_db": float(np.mean(learned) - np.mean(plain)), "max_abs_err": learned_max,
             "plain_max_abs_err": plain_max,
+            "q9999_abs_err": float(np.median(ls["q9999"])), "plain_q9999_abs_err": float(np.median(ps["q9999"])),
+            "frames_q9999_below_plain": int(np.sum(np.array(ls["q9999"]) < np.array(ps["q9999"]))),
             "training": {"records": records, "steps": steps, "batch": batch, "loss_first": loss_first,
                          "loss_last": loss_last, "seeds": [501, 502, 503, 504],
                          "deterministic": "records in key order, gradient sums added in CTA order"},
@@ -682,7 +685,8 @@ def summarize(form_name, mpx, frac, forms, e2e, cpu):
     if ln:
         out.update(learned_cost_vs_plain=ln["cost_vs_plain"], learned_cost_vs_fast=ln.get("cost_vs_fast"),
                    learned_gain_db=ln["gain_db"],
-                   learned_max_abs_err=ln["max_abs_err"], plain_max_abs_err=ln["plain_max_abs_err"])
+                   learned_max_abs_err=ln["max_abs_err"], plain_max_abs_err=ln["plain_max_abs_err"],
+                   learned_q9999_abs_err=ln.get("q9999_abs_err"), plain_q9999_abs_err=ln.get("plain_q9999_abs_err"))
     c3 = f.get("c3_cas")
     if c3:
         for interp, entries in c3.items():

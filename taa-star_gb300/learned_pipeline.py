@@ -84,9 +84,11 @@ def psnr(a, ref) -> float:
 
 
 def evaluate(wl: WL.Workload, frames: int, dev, form: int, weights: T.MlpWeights | None = None,
-             fr: Frames | None = None, skip: int = 8, flags: int = 0):
+             fr: Frames | None = None, skip: int = 8, flags: int = 0, stats: dict | None = None):
     """Per-frame PSNR (frames >= skip) of the resolved history against the
-    ground truth, and the largest absolute error."""
+    ground truth, and the largest absolute error.  With `stats`, its "q9999"
+    entry receives each frame's 99.99th percentile of the per-pixel error (the
+    largest channel's absolute error)."""
     import torch
     fr = fr or render(wl, frames, dev)
     H, W = wl.height, wl.width
@@ -104,5 +106,7 @@ def evaluate(wl: WL.Workload, frames: int, dev, form: int, weights: T.MlpWeights
             ref = fr.truth[f][..., :3].cpu().numpy()
             out.append(psnr(res, ref))
             maxerr = max(maxerr, float(np.max(np.abs(res - ref))))
+            if stats is not None:
+                stats.setdefault("q9999", []).append(float(np.quantile(np.max(np.abs(res - ref), axis=-1), 0.9999)))
     ctx.close()
     return out, maxerr
