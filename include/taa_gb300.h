@@ -86,12 +86,12 @@ typedef enum taa_status {
  * reference's storage; one resolve within 5e-4 of the exact form after the
  * FP16 store) for one view without the one-launch sharpener. */
 #define TAA_FORM_FAST   5u
-/* taa_desc_t.flags: run the learned form's network on tcgen05 through tensor
- * memory (128-row blocks, one thread issuing per CTA, a CTA-wide barrier per
- * layer) instead of per warp with warp-wide MMAs (the default: no block
- * barriers; at 1080p 77 us a frame against 89 us for tcgen05).  Both run the
- * parameters of TAA_FORM_FAST's benchmark mode on its strip body, others on
- * the tiled body. */
+/* taa_desc_t.flags: run the learned form's network on tcgen05 (128-row blocks
+ * whose features and activations stay in tensor memory, one thread issuing
+ * per CTA, a CTA-wide barrier per layer) instead of per warp with warp-wide
+ * MMAs (the default: no block barriers; at 1080p 68 us a frame against 79 us
+ * for tcgen05; the same output bits).  Both run the parameters of
+ * TAA_FORM_FAST's benchmark mode on its strip body, others on the tiled body. */
 #define TAA_FLAG_LEARNED_TCGEN05 0x1u
 /* taa_desc_t.flags: taa_create also sets aside the work list of the FXAA pass
  * (taa_fxaa), 4 bytes per output pixel, so that the pass needs one read of
