@@ -13,8 +13,9 @@
 //   3. per target pixel: the 3x3 variance box around its source texel from
 //      staged row sums (a strip's pixels on one source row share it: the
 //      test is the same for every lane of a warp), the jittered source sample
-//      that lands in it (upsample_axis / upsampled_pick, as the exact forms;
-//      beta 0 when none does), the clip toward the box centre, the blend
+//      that lands in it (upsample_axis / upsampled_pick, as the exact forms,
+//      the row axis once per tile row in shared memory; beta 0 when none
+//      does), the clip toward the box centre, the blend
 //      mix(history, current, alpha * beta).
 // The arithmetic is the fast form's (contracted FMAs, hardware square root
 // and reciprocal approximations): within 1e-4 relative L2 of the FP64 oracle
@@ -39,7 +40,11 @@ constexpr int UNSPT = (UNS + NT - 1) / NT;
 // Resident CTAs per SM the register budget is sized for (a tuning constant:
 // 8 measured 167 us per 1080p -> 4K frame, 7 177 us, 6 183 us; staging the
 // source velocity in shared memory for the bilinear taps cost an eighth CTA
-// and measured 175 us).
+// and measured 175 us).  Measured by parts (variants with a part removed,
+// 170 us in all): the history filter 53 us, the landing-sample search and
+// the current colour 30 us (the rows' candidates once per tile row in
+// shared memory: 170 -> 166.5 us, the same bits), the bilinear velocity
+// 9 us, the previous-depth gather 10 us; the rest 78 us.
 #ifndef TAA_FAST_UP_MIN_BLOCKS
 #define TAA_FAST_UP_MIN_BLOCKS 8
 #endif
@@ -47,9 +52,19 @@ constexpr int UNSPT = (UNS + NT - 1) / NT;
 struct UpSmem {
     float4 col[UNS];                   // staged source texels (Y, Co, Cg, Cg^2), row length rw
     alignas(128) float4 win[WW * WH];  // the target-size history window
+    UpAxis yaxis[TY];                  // the landing-sample candidates of the tile's target rows
     uint64_t bar;
     int org[3];
 };
+
+// The staged source texel (ix, iy) of the tile, or - never for a sample that
+// lands within a texel of its target pixel, which the staged ring covers -
+// the texel read and converted from global memory.
+__device__ __forceinline__ float4 staged_or_global(const Args& a, const float4* col, int rw, int rh, int ix, int iy,
+                                                 int gx, int gy, int loW, int loH) {
+    if (ix >= 0 && iy >= 0 && ix < rw && iy < rh) return col[iy * rw + ix];
+    return F32Pol::stage(__ldg(at<uint2>(a.color, a.color_pitch, clampi(gx, 0, loW - 1), clampi(gy, 0, loH - 1))));
+}
 
 
 template <int INTERP, int MC>
@@ -128,6 +143,8 @@ __global__ void __launch_bounds__(NT, TAA_FAST_UP_MIN_BLOCKS)
         const int i = tid + j * NT;
         if (i < rw * rh) sm.col[i] = F32Pol::stage(st[j]);
     }
+    // the tile's rows' landing-sample candidates, once per row (the shader's arithmetic per axis)
+    if (tid < TY) sm.yaxis[tid] = upsample_axis(min(y0 + tid, H - 1), H, loH, up.jy, up.scy);
     __syncthreads();
     int wx0 = 0, wy0 = 0, mode = 0;
     if (have_hist) {
@@ -243,13 +260,9 @@ __global__ void __launch_bounds__(NT, TAA_FAST_UP_MIN_BLOCKS)
         int fxs, fys;
         float cur[3] = {0.f, 0.f, 0.f};
         float beta = 0.f;
-        if (upsampled_pick(uxa, upsample_axis(min(y, H - 1), H, loH, up.jy, up.scy), fxs, fys)) {
+        if (upsampled_pick(uxa, sm.yaxis[y - y0], fxs, fys)) {
             beta = 1.f;
-            const int ix = fxs - rx0, iy = fys - ry0;
-            const float4 c = ix >= 0 && iy >= 0 && ix < rw && iy < rh
-                                 ? sm.col[iy * rw + ix]
-                                 : F32Pol::stage(__ldg(at<uint2>(a.color, a.color_pitch, clampi(fxs, 0, loW - 1),
-                                                                 clampi(fys, 0, loH - 1))));
+            const float4 c = staged_or_global(a, sm.col, rw, rh, fxs - rx0, fys - ry0, fxs, fys, loW, loH);
             cur[0] = c.x;
             cur[1] = c.y;
             cur[2] = c.z;
