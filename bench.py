@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--no-modes", action="store_true")
     ap.add_argument("--no-c3", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--isa-rates", action="store_true",
+                    help="build and run the FMA issue-rate measurement (taa-star_gb300/csrc/isa_rates.cu; no JSON "
+                         "benchmark line)")
     ap.add_argument("--profile", choices=["fast", "tiled", "fp16", "plain", "batch48", "fxaa", "fused", "defaults",
                                           "learned", "up"],
                     help="a small case for ncu: a few launches of one form on 4K frames (no JSON line)")
@@ -1071,8 +1074,21 @@ def run_profile_case(args):
     return 0
 
 
+def run_isa_rates():
+    """Packed FP32, packed FP16 and scalar FP32 FMA issue rates on this GPU: the
+    stand-alone program in taa-star_gb300/csrc/isa_rates.cu, built with nvcc."""
+    sys.path.insert(0, str(ROOT / "taa-star_gb300"))
+    import build as B
+    B.OUT.mkdir(exist_ok=True)
+    exe = B.OUT / "isa_rates"
+    subprocess.run([B.nvcc(), *B.ARCH, "-O3", "-o", str(exe), str(B.CSRC / "isa_rates.cu")], check=True)
+    return subprocess.run([str(exe)]).returncode
+
+
 def main():
     args = parse()
+    if args.isa_rates:
+        return run_isa_rates()
     if args.profile:
         return run_profile_case(args)
     if args.impl == "reference":
