@@ -24,6 +24,7 @@ import numpy as np
 
 LN2 = 0.69314718055994531
 PENALTY = 1.0  # weight of the pull on a log2 box scale outside [-1, 1] (learned.cu kPenalty)
+OUTLIER_K = 2.0  # a current sample beyond K * gamma * sigma of the box mean caps the blend weight (learned.cuh)
 
 
 def half(x):
@@ -100,9 +101,14 @@ def loss_and_output_grad(rec, o):
     fixed = (rec["flags"] & 1) != 0
     s = np.exp2(o1)
     s_in = (s >= 0.5) & (s <= 2.0)
-    alpha = np.where(fixed | ~s_in, rec["alpha_fixed"], 1.0 / (1.0 + np.exp(-o0)))
-    sc = np.where(s_in, s, 1.0)
     mean, sigma, hist, cur, gt = rec["mean"], rec["sigma"], rec["history"], rec["current"], rec["truth"]
+    a_net = 1.0 / (1.0 + np.exp(-o0))
+    # a current sample farther from the box mean in luma than twice gamma * sigma: the blend
+    # weight no more than the plain one (learned.cuh current_outlier)
+    outlier = np.abs(cur[:, 0] - mean[:, 0]) > OUTLIER_K * rec["gamma"] * sigma[:, 0] + 1e-7
+    capped = ~fixed & s_in & outlier & (a_net > rec["alpha_fixed"])
+    alpha = np.where(fixed | ~s_in | capped, rec["alpha_fixed"], a_net)
+    sc = np.where(s_in, s, 1.0)
     g = rec["gamma"][:, None]
     e = sc[:, None] * g * sigma + 1e-7
     d = hist - mean
@@ -124,7 +130,7 @@ def loss_and_output_grad(rec, o):
     sk = sigma[np.arange(len(k)), k]
     dsc = np.where(clipped, np.sum(dout * (1.0 - alpha[:, None]) * d, axis=1) * (rec["gamma"] * sk /
                                                                                    np.where(clipped, dk, 1.0)), 0.0)
-    d0 = np.where(fixed | ~s_in, 0.0, dalpha * alpha * (1.0 - alpha))
+    d0 = np.where(fixed | ~s_in | capped, 0.0, dalpha * alpha * (1.0 - alpha))
     d1 = np.where(s_in, dsc * s * LN2, 0.0)
     # outside the trusted scale range: the plain result and a penalty pulling o1 back
     over = np.abs(o1) - 1.0

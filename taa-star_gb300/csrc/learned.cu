@@ -271,6 +271,7 @@ template <bool COLLECT, bool TC> struct LearnedFinish {
                 scale = 1.f;
                 alpha = P.mAlpha;
             }
+            if (current_outlier(mean, sigma, cur, g)) alpha = fminf(alpha, P.mAlpha);
             if (fixed_alpha) alpha = alpha_fixed;
         }
         if (!valid) return;
@@ -387,7 +388,10 @@ __device__ __forceinline__ float record_loss(const Record& r, float o0, float o1
     const bool fixed_alpha = r.flags & 1u;
     const float s = out_scale(o1);
     const bool s_in = s >= 0.5f && s <= 2.0f;
-    const float alpha = (fixed_alpha || !s_in) ? r.alpha_fixed : out_alpha(o0);
+    // an outlier current sample: the blend weight no more than the plain one (current_outlier)
+    const bool capped = !fixed_alpha && s_in && current_outlier(r.mean, r.sigma, r.cur, r.gamma) &&
+                        out_alpha(o0) > r.alpha_fixed;
+    const float alpha = (fixed_alpha || !s_in || capped) ? r.alpha_fixed : out_alpha(o0);
     const float sc = s_in ? s : 1.0f;
     float e[3], dd[3], ma = 0.f;
     int k = 0;
@@ -422,7 +426,7 @@ __device__ __forceinline__ float record_loss(const Record& r, float o0, float o1
         // hc = mean + d * e_k / |d_k| when clipped: d(hc)/d(sc) = d * gamma * sigma_k / |d_k|
         if (clipped) dsc += dout[c] * (1.f - alpha) * dd[c] * (r.gamma * r.sigma[k] / fabsf(dd[k]));
     }
-    d0 = (fixed_alpha || !s_in) ? 0.f : dalpha * alpha * (1.f - alpha);
+    d0 = (fixed_alpha || !s_in || capped) ? 0.f : dalpha * alpha * (1.f - alpha);
     d1 = s_in ? dsc * s * 0.69314718055994531f : 0.f;
     if (!s_in) {
         const float over = fabsf(o1) - 1.f;

@@ -248,14 +248,15 @@ struct LearnedStripPol {
                     scale = 1.f;
                     alpha = a.alpha;
                 }
-                if (a.reset) alpha = 1.0f;
-                else if ((rej >> k) & 1u) alpha = a.rejection_alpha;
                 float hy[3], cur[3], e[3], o[3];
                 hist_ycocg(h[k], hy);
                 const float4 c0 = lds128(&sp[(k + 1) * SX + 1]);
                 cur[0] = c0.x;
                 cur[1] = c0.y;
                 cur[2] = c0.z;
+                if (current_outlier(mean[kk], sigma[kk], cur, a.gamma)) alpha = fminf(alpha, a.alpha);
+                if (a.reset) alpha = 1.0f;
+                else if ((rej >> k) & 1u) alpha = a.rejection_alpha;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) e[c] = scale * a.gamma * sigma[kk][c] + 1e-7f;
                 rectify_blend(mean[kk], e, hy, cur, alpha, o);
@@ -403,14 +404,15 @@ struct LearnedTcPol {
                     scale = 1.f;
                     alpha = a.alpha;
                 }
-                if (a.reset) alpha = 1.0f;
-                else if (rejected) alpha = a.rejection_alpha;
                 float hy[3], cur[3], e[3], out[3];
                 hist_ycocg(h[k], hy);
                 const float4 c0 = lds128(&sp[(k + 1) * SX + 1]);
                 cur[0] = c0.x;
                 cur[1] = c0.y;
                 cur[2] = c0.z;
+                if (current_outlier(mean[kk], sigma[kk], cur, a.gamma)) alpha = fminf(alpha, a.alpha);
+                if (a.reset) alpha = 1.0f;
+                else if (rejected) alpha = a.rejection_alpha;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) e[c] = scale * a.gamma * sigma[kk][c] + 1e-7f;
                 rectify_blend(mean[kk], e, hy, cur, alpha, out);
@@ -642,14 +644,15 @@ template <int NBT> struct LearnedTmemPol {
                     scale = 1.f;
                     alpha = a.alpha;
                 }
-                if (a.reset) alpha = 1.0f;
-                else if ((rej >> k) & 1u) alpha = a.rejection_alpha;
                 float hy[3], cur[3], e[3], out[3];
                 hist_ycocg(h[k], hy);
                 const float4 c0 = lds128(&sp[(k + 1) * SX + 1]);
                 cur[0] = c0.x;
                 cur[1] = c0.y;
                 cur[2] = c0.z;
+                if (current_outlier(mean[kk], sigma[kk], cur, a.gamma)) alpha = fminf(alpha, a.alpha);
+                if (a.reset) alpha = 1.0f;
+                else if ((rej >> k) & 1u) alpha = a.rejection_alpha;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) e[c] = scale * a.gamma * sigma[kk][c] + 1e-7f;
                 rectify_blend(mean[kk], e, hy, cur, alpha, out);

@@ -82,3 +82,24 @@ def test_features_scale_invariant():
     assert f1.shape == (8, 32) and np.all(f1[:, 31] == 1.0)
     # deviation features are in units of sigma: hist = mean + sigma gives about 1/4
     np.testing.assert_allclose(f1[:, 18:21], 0.25, atol=0.01)
+
+
+def test_outlier_current_sample_caps_the_blend_weight():
+    """A current sample farther from the box mean (luma) than twice the plain box's half
+    extent: the network's blend weight is held to the plain one and passes no gradient;
+    just inside that distance it is the network's own."""
+    n = 4
+    mean = np.tile([1.0, 0.0, 0.0], (n, 1))
+    sigma = np.full((n, 3), 0.2)
+    cur = mean.copy()
+    cur[:, 0] += np.array([0.5, 0.39, -0.45, 0.5])   # 2.5, 1.95, 2.25 and 2.5 sigma from the mean
+    rec = dict(mean=mean, sigma=sigma, history=mean + 0.05, current=cur, truth=cur.copy(), gamma=np.full(n, 1.0),
+               alpha_fixed=np.full(n, 0.1), flags=np.zeros(n, dtype=np.uint32))
+    o = np.zeros((n, 2))
+    o[:, 0] = [2.0, 2.0, 2.0, -4.0]   # network weights 0.88, 0.88, 0.88 and 0.018
+    loss, d = M.loss_and_output_grad(rec, o)
+    loss_plain, _ = M.loss_and_output_grad(rec, np.where(np.arange(2) == 0, np.log(0.1 / 0.9), 0.0) * np.ones((n, 2)))
+    assert d[0, 0] == 0.0 and d[2, 0] == 0.0           # capped: the plain weight, no gradient
+    assert abs(loss[0] - loss_plain[0]) < 1e-12 and abs(loss[2] - loss_plain[2]) < 1e-12
+    assert d[1, 0] != 0.0                               # inside 2 sigma: the network's weight
+    assert d[3, 0] != 0.0                               # below the plain weight: not capped
