@@ -849,10 +849,10 @@ def run_ours(args):
         torch.cuda.synchronize()
         if world > 1:
             dist.barrier()
-        # the host link is shared with the machine's other GPUs: three timed runs, the median reported
+        # the host link is shared with the machine's other GPUs: five timed runs, the median reported
         k = max(2, args.steps // 4)
         runs = []
-        for _ in range(3):
+        for _ in range(5):
             t0 = torch.cuda.Event(enable_timing=True)
             t1 = torch.cuda.Event(enable_timing=True)
             t0.record(s_in)
@@ -864,10 +864,10 @@ def run_ours(args):
             torch.cuda.synchronize()
             ms_e = max_over_ranks(t0.elapsed_time(t1), world, dev)
             runs.append(job_throughput(W * H * F * k, world, ms_e / 1e3) / 1e6)
-        e2e = {"value": sorted(runs)[1], "unit": UNIT,
+        e2e = {"value": sorted(runs)[len(runs) // 2], "unit": UNIT,
                "h2d_bytes_per_step": F * H * W * (8 + 4 + 4), "d2h_bytes_per_step": F * H * W * 8,
                "runs": runs,
-               "note": f"median of 3 runs of {k} steps; pinned host buffers; inputs copied 3 slots ahead on a "
+               "note": f"median of {len(runs)} runs of {k} steps; pinned host buffers; inputs copied 3 slots ahead on a "
                        "copy stream; the resolve stores its RGBA16F result straight into the frame's pinned "
                        "host image"}
         # the last frame's result against the same frame resolved into device memory
