@@ -251,8 +251,9 @@ def time_learned(T, WL, dev, stream, sid, args):
     seeds of the renderer (about 2M pixels, resolved with the plain variance
     clip), Adam on the library's tensor-core training kernels, then the 64-frame
     seed-5 sequence resolved by the plain variance clip and by the learned form,
-    each against the renderer's 64-spp ground truth; and the cost of one 1080p
-    resolve of each (CUDA events, 20 launches after 3)."""
+    each against the renderer's 64-spp ground truth; and the cost per 1080p
+    frame of each over that sequence replayed from a CUDA graph (CUDA events,
+    5 replays after 3), beside the cost of one frame resolved 20 times."""
     import numpy as np
     import torch
     import learned_pipeline as LP
@@ -271,29 +272,54 @@ def time_learned(T, WL, dev, stream, sid, args):
     plain, plain_max = LP.evaluate(wl, wl.frames, dev, T.TAA_FORM_TILED, fr=fr, stats=ps)
     learned, learned_max = LP.evaluate(wl, wl.frames, dev, T.TAA_FORM_LEARNED, weights=w, fr=fr, stats=ls)
     H, W = wl.height, wl.width
-    cost = {}
+    # the cost of each form on the C5 sequence itself: the 64 frames (history chained, each
+    # frame's inputs read once) captured in a CUDA graph, replayed as the 4K forms are; and on
+    # one frame resolved 20 times in a row (its 124 MB of inputs stay in the 129 MB L2)
+    cost, cost_one = {}, {}
+    uni = [T.make_uniforms(wl.parameters(), jitter_ndc=fr.jitter[f], mResetHistory=1 if f == 0 else 0)
+           for f in range(wl.frames)]
     for name, form in (("tiled", T.TAA_FORM_TILED), ("fast", T.TAA_FORM_FAST), ("learned", T.TAA_FORM_LEARNED)):
         ctx = T.Taa(W, H, form=form)
         if form == T.TAA_FORM_LEARNED:
             ctx.set_mlp(w)
-        ctx.set_uniforms(T.make_uniforms(wl.parameters(), jitter_ndc=fr.jitter[5]))
         h = [torch.zeros(H, W, 4, device=dev) for _ in range(2)]
+        gs = torch.cuda.Stream(dev)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=gs):
+            for f in range(wl.frames):
+                ctx.set_uniforms(uni[f])
+                ctx.resolve(stream=gs.cuda_stream, color=fr.color[f], depth=fr.depth[f], velocity=fr.motion[f],
+                            history=h[f & 1], history_depth=fr.depth[f - 1] if f else fr.depth[0],
+                            history_out=h[(f + 1) & 1])
+        for _ in range(3):
+            graph.replay()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(5):
+            graph.replay()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        cost[name] = e0.elapsed_time(e1) * 1000 / (5 * wl.frames)
+        del graph
+        ctx.set_uniforms(uni[5])
         b = dict(color=fr.color[5], depth=fr.depth[5], velocity=fr.motion[5], history=h[0],
                  history_depth=fr.depth[4], history_out=h[1])
         for _ in range(3):
             ctx.resolve(stream=sid, **b)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         e0.record(stream)
         for _ in range(20):
             ctx.resolve(stream=sid, **b)
         e1.record(stream)
         torch.cuda.synchronize()
-        cost[name] = e0.elapsed_time(e1) * 1000 / 20
+        cost_one[name] = e0.elapsed_time(e1) * 1000 / 20
         ctx.close()
     return {"mpx_s": W * H / cost["learned"], "us_per_frame_1080p": cost["learned"],
             "plain_variance_clip_us_per_frame_1080p": cost["tiled"], "cost_vs_plain": cost["learned"] / cost["tiled"],
             "fast_variance_clip_us_per_frame_1080p": cost["fast"], "cost_vs_fast": cost["learned"] / cost["fast"],
+            "cost_timing": "the 64-frame C5 sequence from a CUDA graph (5 replays after 3)",
+            "one_frame_us": cost_one, "one_frame_cost_vs_plain": cost_one["learned"] / cost_one["tiled"],
             "psnr_db_vs_64spp": float(np.mean(learned)), "plain_psnr_db_vs_64spp": float(np.mean(plain)),
             "gain_db": float(np.mean(learned) - np.mean(plain)), "max_abs_err": learned_max,
             "plain_max_abs_err": plain_max,
