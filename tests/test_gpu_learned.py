@@ -162,6 +162,9 @@ def test_learned_paths_agree_on_one_frame(cuda, extra):
         outs.append(h[..., :3].cpu().numpy())
         ctx.close()
     assert np.all(np.isfinite(outs[0])) and np.all(np.isfinite(outs[1]))
+    if not extra:
+        # the strip body: the warp MMAs and tcgen05 (activations in tensor memory) give the same bits
+        np.testing.assert_array_equal(outs[0], outs[1])
     diff = np.abs(outs[0] - outs[1]) / np.maximum(1e-2, np.abs(outs[1]))
     # FP32 accumulation order only: equal but for pixels near a rounding of the FP16 activations
     assert np.mean(diff <= 1e-3) >= 0.99 and np.max(diff) <= 0.05
