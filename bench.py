@@ -53,7 +53,7 @@ def parse():
                     help="build and run the FMA issue-rate measurement (taa-star_gb300/csrc/isa_rates.cu; no JSON "
                          "benchmark line)")
     ap.add_argument("--profile", choices=["fast", "tiled", "fp16", "plain", "batch48", "fxaa", "fused", "defaults",
-                                          "learned", "up"],
+                                          "learned", "learned_tc", "up"],
                     help="a small case for ncu: a few launches of one form on 4K frames (no JSON line)")
     return ap.parse_args()
 
@@ -1085,11 +1085,14 @@ def run_profile_case(args):
         params = T.default_parameters()
     elif args.profile == "learned":  # the learned form's strip kernel (random weights)
         kw = dict(form=T.TAA_FORM_LEARNED)
+    elif args.profile == "learned_tc":  # the same on tcgen05, activations in tensor memory
+        kw = dict(form=T.TAA_FORM_LEARNED, flags=T.TAA_FLAG_LEARNED_TCGEN05)
     form = {"fast": T.TAA_FORM_FAST, "tiled": T.TAA_FORM_TILED, "fp16": T.TAA_FORM_FP16, "plain": T.TAA_FORM_PLAIN,
-            "fused": T.TAA_FORM_FAST, "defaults": T.TAA_FORM_FAST, "learned": T.TAA_FORM_LEARNED}[args.profile]
+            "fused": T.TAA_FORM_FAST, "defaults": T.TAA_FORM_FAST, "learned": T.TAA_FORM_LEARNED,
+            "learned_tc": T.TAA_FORM_LEARNED}[args.profile]
     kw.setdefault("form", form)
     ctx = T.Taa(W, H, **kw)
-    if args.profile == "learned":
+    if args.profile in ("learned", "learned_tc"):
         ctx.set_mlp(T.mlp_init_weights(1, 0.1))
     for f in range(1, F):
         ctx.set_uniforms(T.make_uniforms(params, jitter_ndc=T.synth_jitter(sc, f)[1]))
