@@ -150,6 +150,69 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
+class NvmlClockSampler:
+    """The same record as ClockSampler from NVML itself (libnvidia-ml, read-only
+    queries), every 10 ms: the GPU is found by the CUDA device's PCI bus id, so
+    a short timed region still gets a dozen samples.  make() falls back to
+    ClockSampler where NVML cannot be loaded."""
+
+    SM = 1  # NVML_CLOCK_SM
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
+
+    def __init__(self, nvml, handle):
+        self.nvml, self.handle = nvml, handle
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    @classmethod
+    def make(cls, device: int):
+        import ctypes
+        import ctypes.util
+        try:
+            nvml = ctypes.CDLL("libnvidia-ml.so.1")
+            rt = ctypes.CDLL(ctypes.util.find_library("cudart") or "libcudart.so")
+            bus = ctypes.create_string_buffer(64)
+            if rt.cudaDeviceGetPCIBusId(bus, 64, device) != 0 or nvml.nvmlInit_v2() != 0:
+                raise OSError("no bus id or NVML")
+            handle = ctypes.c_void_p()
+            if nvml.nvmlDeviceGetHandleByPciBusId_v2(bus, ctypes.byref(handle)) != 0:
+                raise OSError("no NVML handle")
+            return cls(nvml, handle)
+        except (OSError, AttributeError):
+            return ClockSampler(device)
+
+    def _run(self):
+        import ctypes
+        sm, mx, reasons = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+        get_reasons = getattr(self.nvml, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.nvml.nvmlDeviceGetCurrentClocksThrottleReasons
+        while not self._stop.is_set():
+            if (self.nvml.nvmlDeviceGetClockInfo(self.handle, self.SM, ctypes.byref(sm)) == 0 and
+                    self.nvml.nvmlDeviceGetMaxClockInfo(self.handle, self.SM, ctypes.byref(mx)) == 0 and
+                    get_reasons(self.handle, ctypes.byref(reasons)) == 0):
+                self.samples.append((sm.value, mx.value, reasons.value))
+            self._stop.wait(0.01)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["NVML returned no sample"]}
+        import statistics
+        reasons = sorted({name for _, _, r in self.samples for bit, name in self.REASONS.items() if r & bit})
+        return {"sm_mhz": statistics.median(s[0] for s in self.samples), "sm_max_mhz": max(s[1] for s in self.samples),
+                "reasons": reasons, "samples": len(self.samples), "source": "NVML, every 10 ms"}
+
+
 # ------------------------------------------------------------------ reference arm
 # The reference's path on the host cores is the oracle's FP32 restatement of
 # taa.comp (the shader itself needs Vulkan).  This arm builds its inputs from
@@ -828,7 +891,7 @@ def run_ours(args):
     ctx = make_ctx(T.TAA_FORM_AUTO)
     form_used = ctx.selected_form()
     form_name = {1: "plain", 2: "tiled", 3: "fp16", 5: "fast"}[form_used]
-    sampler = ClockSampler(local)
+    sampler = NvmlClockSampler.make(local)
     ms = timed(ctx, args.steps, args.warmup, sampler)
     launches = args.steps * F
     mpx = job_throughput(W * H * F * args.steps, world, ms / 1e3) / 1e6
